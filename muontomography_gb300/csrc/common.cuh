@@ -1,0 +1,180 @@
+// Shared device helpers and the kernel-launch interface between the handle
+// (handle.cu) and the kernel files (setup.cu, em.cu, poca.cu, scan.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include "geometry.cuh"
+
+namespace muto {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// Precision traits: Real is the storage/accumulation type of the per-pair
+// data (float in the mixed form, double in the plain FP64 form).
+// ---------------------------------------------------------------------------
+template <typename Real> struct Vec4;
+template <> struct Vec4<float> { using type = float4; };
+template <> struct Vec4<double> { using type = double4; };
+
+// Order-preserving integer keys for the per-voxel selection.
+__device__ __forceinline__ uint32_t to_key(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float from_key(uint32_t k) {
+    const uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(u);
+}
+__device__ __forceinline__ unsigned long long to_key(double f) {
+    const unsigned long long u = static_cast<unsigned long long>(__double_as_longlong(f));
+    return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double from_key(unsigned long long k) {
+    const unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+    return __longlong_as_double(static_cast<long long>(u));
+}
+template <typename Real> struct KeyOf;
+template <> struct KeyOf<float> { using type = uint32_t; static constexpr int bits = 32; };
+template <> struct KeyOf<double> { using type = unsigned long long; static constexpr int bits = 64; };
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+// Warp-aggregated increment of a global counter by the number of lanes with pred.
+__device__ __forceinline__ void warp_count(unsigned long long* ctr, bool pred) {
+    const unsigned b = __ballot_sync(__activemask(), pred);
+    const unsigned lead = __ffs(__activemask()) - 1;
+    if ((threadIdx.x & 31) == lead && b) atomicAdd(ctr, static_cast<unsigned long long>(__popc(b)));
+}
+
+// Device-side counters shared by all kernels of a handle.
+struct Counters {
+    unsigned long long singular;
+    unsigned long long nonconverged;
+    unsigned long long bounds;
+    unsigned long long overflow;
+    unsigned long long not_parallel;
+    unsigned long long in_grid;
+    unsigned long long iteration;   // device iteration index (graph replays)
+    unsigned long long pad;
+    double cost_sum;                // cost of the current iteration
+    double cost_last;               // mean cost of the last finished iteration
+    double cost_prev;               // mean cost of the one before
+    double pad2;
+};
+
+// ---------------------------------------------------------------------------
+// Kernel launch wrappers (all asynchronous on `s`)
+// ---------------------------------------------------------------------------
+// scan.cu: out[i] = sum_{k<i} in[k] (exclusive), out has n+1 entries
+// (out[n] = total).  scratch must hold scan_scratch_bytes(n) bytes.
+size_t scan_scratch_bytes(uint64_t n);
+void scan_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, void* scratch, cudaStream_t s);
+
+// setup.cu
+void launch_keep_flags(const muto_ray* rays, uint64_t n_total, muto_grid g, double eps, uint32_t* flags,
+                       cudaStream_t s);
+void launch_compact(const uint32_t* flags, const uint64_t* pos, uint64_t n, uint32_t* kept, cudaStream_t s);
+template <typename Real>
+void launch_muon_info(const muto_ray* rays, const uint32_t* kept, uint64_t n, muto_grid g, double eps, int has_energy,
+                      typename Vec4<Real>::type* sd, Real* pr2, double* scat, double* pr_out, cudaStream_t s);
+void launch_path_count(const muto_ray* rays, const uint32_t* kept, const double* scat, uint64_t n, muto_grid g,
+                       int straight, uint32_t* counts, Counters* ctr, cudaStream_t s);
+template <typename Real>
+void launch_path_fill(const muto_ray* rays, const uint32_t* kept, const double* scat, const uint64_t* off, uint64_t n,
+                      muto_grid g, int straight, uint32_t* vidx, double* l64, Real* L, Real* T, cudaStream_t s);
+void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* mult, Counters* ctr, cudaStream_t s);
+void launch_assign_slots(const uint32_t* vidx, uint64_t P, uint32_t V, const uint64_t* start, uint32_t* cursor,
+                         uint32_t* slot, cudaStream_t s);
+void launch_siddon_batch(muto_grid g, const double* p1, const double* p2, uint64_t n, uint32_t cap, uint32_t* xyz,
+                         double* len, uint32_t* counts, cudaStream_t s);
+
+// poca.cu
+struct PocaArgs {
+    const muto_ray* rays;
+    uint64_t n;
+    muto_grid g;
+    double eps, mag;
+    int has_energy, straight, length_weighted;
+    double* img;
+    double* weight;
+    long long* assign;  // 3 per ray, optional
+    Counters* ctr;
+};
+void launch_poca(const PocaArgs& a, cudaStream_t s);
+void launch_poca_normalize(double* img, const double* weight, uint64_t V, double eps, cudaStream_t s);
+
+// em.cu
+enum EmMode { kEmMedian = 0, kEmMean = 1, kEmCostOnly = 2 };
+
+template <typename Real>
+struct EmArgs {
+    const uint64_t* off;         // N+1 pair offsets
+    const uint32_t* tile_mb;     // ntiles+1 first muon of each tile
+    uint32_t ntiles;
+    const uint32_t* vidx;        // P
+    const Real* L;               // P
+    const Real* T;               // P
+    const uint32_t* slot;        // P (median)
+    const typename Vec4<Real>::type* sd;  // N: Sx, Dx, Sy, Dy
+    const Real* pr2;             // N
+    const Real* lam;             // V: lambda gathered by the muons
+    Real* S;                     // P (median)
+    Real* G;                     // V (mean / gradient), += sum_i pr^2 g_ij
+    uint32_t V;
+    double E00, E01, E11;
+    int mode;
+    int compute_cost;
+    Counters* ctr;
+};
+template <typename Real>
+void launch_em_tile(const EmArgs<Real>& a, int tile_pairs, int tile_muons, int blocks, int group, cudaStream_t s);
+template <typename Real>
+size_t em_tile_smem_bytes(int tile_pairs, int tile_muons);
+// sets the dynamic shared-memory limit of every k_em_tile variant (call outside graph capture)
+template <typename Real>
+cudaError_t em_tile_configure(int tile_pairs, int tile_muons);
+
+template <typename Real, typename OutT>
+void launch_select(const Real* S, const uint64_t* start, const uint32_t* mult, uint32_t V, int use_mean,
+                   int percentile, OutT* out, cudaStream_t s);
+template <typename Real, typename OutT>
+void launch_voxel_mean(const Real* lam, Real* G, const uint32_t* mult, uint32_t V, OutT* out, cudaStream_t s);
+void launch_finalize_cost(Counters* ctr, double n_muons, double* hist, uint32_t hist_cap, cudaStream_t s);
+
+struct MapParams {
+    double beta, p, delta, eps;
+    int all_neighbours, add_object_prior, newton_max_iter;
+};
+template <typename LamT>
+void launch_map_voxel(const LamT* last, double* ml_inout, const uint32_t* mult, DevGrid g, MapParams mp,
+                      Counters* ctr, cudaStream_t s);
+template <typename LamT>
+void launch_copy_to(const double* in, LamT* out, uint64_t n, cudaStream_t s);
+
+// adjoint.cu
+template <typename Real>
+void launch_exp_lambda(const double* loglam, const uint32_t* mult, uint32_t V, Real* lam, cudaStream_t s);
+template <typename Real>
+void launch_grad_finish(Real* G, const double* lam64, const uint32_t* mult, uint32_t V, double* grad,
+                        cudaStream_t s);
+// adds d prior / d log(lambda) to grad and the prior's value to *value;
+// dl_scratch: V doubles, zero on entry and on return
+void launch_prior(const double* lam64, const uint32_t* mult, DevGrid g, MapParams mp, double* dl_scratch, double* grad,
+                  double* value, cudaStream_t s);
+
+// gen.cu
+void launch_generate(const muto_grid& g, const double* lambda, const muto_gen_params& p, uint64_t first, uint64_t n,
+                     muto_ray* out, cudaStream_t s);
+
+// Kernel launches issued by the library (all handles), for the launch count.
+void count_launches(unsigned long long n);
+unsigned long long launches_so_far();
+
+}  // namespace muto

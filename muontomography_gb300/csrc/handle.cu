@@ -1,0 +1,1173 @@
+// C ABI of the reconstruction library (include/muto_gb300.h): handle state,
+// configuration, device memory, the setup pipeline and the EM / MAP
+// iteration, captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/muto_gb300.h"
+#include "common.cuh"
+#include "gen.h"
+#include "json.hpp"
+
+namespace muto {
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launches(unsigned long long n) { g_launches += n; }
+unsigned long long launches_so_far() { return g_launches.load(); }
+
+namespace {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(call)                                                                                       \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            throw Error(e_ == cudaErrorMemoryAllocation ? MUTO_ERR_NOMEM : MUTO_ERR_CUDA,              \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                           \
+    } while (0)
+
+// Owned device allocation.
+class DevMem {
+public:
+    DevMem() = default;
+    DevMem(const DevMem&) = delete;
+    DevMem& operator=(const DevMem&) = delete;
+    ~DevMem() { release(); }
+    void alloc(size_t bytes, std::atomic<uint64_t>* tally) {
+        release();
+        if (bytes == 0) bytes = 16;
+        CK(cudaMalloc(&p_, bytes));
+        bytes_ = bytes;
+        tally_ = tally;
+        if (tally_) *tally_ += bytes_;
+    }
+    void release() {
+        if (p_) {
+            cudaFree(p_);
+            if (tally_) *tally_ -= bytes_;
+        }
+        p_ = nullptr;
+        bytes_ = 0;
+    }
+    template <typename T> T* as() const { return static_cast<T*>(p_); }
+    size_t bytes() const { return bytes_; }
+    bool empty() const { return p_ == nullptr; }
+
+private:
+    void* p_ = nullptr;
+    size_t bytes_ = 0;
+    std::atomic<uint64_t>* tally_ = nullptr;
+};
+
+enum Method { kPoca, kMlsd, kMap };
+
+struct Params {
+    muto_grid grid{};
+    // MLSD / MAP keys, src/MutoMLSD.cpp:47-84 and src/MutoMAP.cpp:75-82
+    bool update_with_mean = false;
+    int mean_percentile = 100;
+    bool straight_line = false, has_energy = false, early_stop = false, log_results = false;
+    int64_t total_num_rays = 0;
+    int num_iteration = 10;
+    int initialize_method = 0;
+    double initialize_value = 1.0e-7;
+    std::string initial_image_file;
+    double error_xy = 1.0, error_dz_outer = 1000.0, error_dz_inner = 1000.0;
+    double angle_unit_mag = 1.0, eps = 1.0e-8;
+    double beta = 1.0, p = 1.0, delta = 0.1;
+    bool add_object_prior = false, all_neighbours = false;
+    // PoCA, src/MutoPoCA.cpp:74-97
+    bool length_weighted = false;
+    // this library
+    int precision = 0;  // 0 mixed, 1 fp64
+    bool use_graph = true;
+    bool seed_set = false;
+    uint64_t random_seed = 0;
+    int compute_cost = -1;
+    int newton_max_iter = 200;
+    int tile_pairs = 0;
+};
+
+Params parse_params(Method m, const std::string& text) {
+    Params P;
+    P.grid = muto_grid{100, 100, 100, 0, 0.0, 0.0, 0.0, 10.0, 10.0, 10.0};
+    json cfg;
+    try {
+        cfg = text.empty() ? json::parse("{}") : json::parse(text);
+    } catch (const std::exception& e) {
+        throw Error(MUTO_ERR_CONFIG, std::string("config JSON: ") + e.what());
+    }
+    if (!cfg.is_object()) throw Error(MUTO_ERR_CONFIG, "config must be a JSON object");
+    try {
+        if (cfg.contains("grid")) {  // a missing "grid" keeps the defaults (src/MutoMLSD.cpp:60)
+            const json& g = cfg.at("grid");
+            const int64_t nx = g.value("nx", int64_t(100)), ny = g.value("ny", int64_t(100)),
+                          nz = g.value("nz", int64_t(100));
+            if (nx <= 0 || ny <= 0 || nz <= 0 || nx * ny * nz > 0xffffffffLL)
+                throw Error(MUTO_ERR_CONFIG, "grid nx, ny, nz must be positive and nx*ny*nz < 2^32");
+            P.grid.nx = static_cast<uint32_t>(nx);
+            P.grid.ny = static_cast<uint32_t>(ny);
+            P.grid.nz = static_cast<uint32_t>(nz);
+            P.grid.x_min = g.value("x_min", 0.0);
+            P.grid.y_min = g.value("y_min", 0.0);
+            P.grid.z_min = g.value("z_min", 0.0);
+            P.grid.dx = g.value("dx", 10.0);
+            P.grid.dy = g.value("dy", 10.0);
+            P.grid.dz = g.value("dz", 10.0);
+            if (!(P.grid.dx > 0 && P.grid.dy > 0 && P.grid.dz > 0))
+                throw Error(MUTO_ERR_CONFIG, "grid dx, dy, dz must be positive");
+        }
+        P.straight_line = cfg.value("straight_line", false);
+        P.has_energy = cfg.value("has_energy", false);
+        P.log_results = cfg.value("log_results", false);
+        P.total_num_rays = cfg.value("total_num_rays", int64_t(0));
+        P.angle_unit_mag = cfg.value("angle_unit_mag", 1.0);
+        P.eps = cfg.value("eps", 1.0e-8);
+        if (m == kPoca) {
+            P.length_weighted = cfg.value("length_weighted", false);
+        } else {
+            P.update_with_mean = cfg.value("update_with_mean", false);
+            P.early_stop = cfg.value("early_stop", false);
+            P.mean_percentile = cfg.value("mean_percentile", 100);
+            P.num_iteration = cfg.value("num_iteration", 10);
+            P.initialize_method = cfg.value("initialize_method", 0);
+            P.initialize_value = cfg.value("initialize_value", 1.0e-7);
+            P.initial_image_file = cfg.value("initial_image_file", "");
+            P.error_xy = cfg.value("error_xy", 1.0);
+            P.error_dz_outer = cfg.value("error_dz_outer", 1000.0);
+            P.error_dz_inner = cfg.value("error_dz_inner", 1000.0);
+            if (m == kMap) {
+                P.beta = cfg.value("beta", 1.0);
+                P.p = cfg.value("p", 1.0);
+                P.delta = cfg.value("delta", 0.1);
+                P.add_object_prior = cfg.value("add_object_prior", false);
+                P.all_neighbours = cfg.value("all_neighbours", false);
+            }
+            if (P.mean_percentile <= 0) throw Error(MUTO_ERR_CONFIG, "mean_percentile must be positive");
+            if (P.num_iteration < 0) throw Error(MUTO_ERR_CONFIG, "num_iteration must be >= 0");
+        }
+        const std::string prec = cfg.value("precision", "mixed");
+        if (prec == "mixed") P.precision = 0;
+        else if (prec == "fp64") P.precision = 1;
+        else throw Error(MUTO_ERR_CONFIG, "precision must be \"mixed\" or \"fp64\"");
+        P.use_graph = cfg.value("use_graph", true);
+        if (cfg.contains("random_seed")) {
+            P.seed_set = true;
+            P.random_seed = static_cast<uint64_t>(cfg.value("random_seed", int64_t(0)));
+        }
+        if (cfg.contains("compute_cost")) P.compute_cost = cfg.value("compute_cost", false) ? 1 : 0;
+        P.newton_max_iter = cfg.value("newton_max_iter", 200);
+        P.tile_pairs = cfg.value("tile_pairs", 0);
+        if (P.newton_max_iter < 1) throw Error(MUTO_ERR_CONFIG, "newton_max_iter must be >= 1");
+    } catch (const json::type_error& e) {
+        throw Error(MUTO_ERR_CONFIG, std::string("config value of the wrong type: ") + e.what());
+    } catch (const json::out_of_range& e) {
+        throw Error(MUTO_ERR_CONFIG, e.what());
+    }
+    return P;
+}
+
+// CUDA-event timing of launches, also inside captured graphs (external event nodes)
+class Profiler {
+public:
+    bool on = false;
+    struct Rec {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> pool;   // events reused across flushes
+    size_t used = 0;
+    std::map<std::string, std::pair<uint64_t, double>> stats;
+
+    ~Profiler() {
+        for (auto& r : pool) {
+            cudaEventDestroy(r.a);
+            cudaEventDestroy(r.b);
+        }
+    }
+    Rec* begin(const char* name, cudaStream_t s, bool capturing) {
+        if (!on) return nullptr;
+        if (used == pool.size()) {
+            Rec r;
+            CK(cudaEventCreate(&r.a));
+            CK(cudaEventCreate(&r.b));
+            pool.push_back(r);
+        }
+        Rec* r = &pool[used++];
+        r->name = name;
+        CK(cudaEventRecordWithFlags(r->a, s, capturing ? cudaEventRecordExternal : cudaEventRecordDefault));
+        return r;
+    }
+    void end(Rec* r, cudaStream_t s, bool capturing) {
+        if (!r) return;
+        CK(cudaEventRecordWithFlags(r->b, s, capturing ? cudaEventRecordExternal : cudaEventRecordDefault));
+    }
+    // Accumulate records [first, used) after the stream has synchronised.
+    void harvest(size_t first, size_t last) {
+        for (size_t i = first; i < last; ++i) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, pool[i].a, pool[i].b) == cudaSuccess) {
+                auto& st = stats[pool[i].name];
+                st.first += 1;
+                st.second += ms;
+            }
+        }
+    }
+};
+
+}  // namespace
+}  // namespace muto
+
+using namespace muto;
+
+struct muto_handle {
+    Method method = kMlsd;
+    Params P;
+    muto_grid grid{};          // current grid (may be adopted from the initial image)
+    cudaStream_t stream = nullptr;
+    int device = 0, num_sms = 148;
+    size_t smem_optin = 0;
+    std::atomic<uint64_t> dev_bytes{0};
+    Profiler prof;
+    bool capturing = false;
+    unsigned long long launches = 0;   // launches of this handle (graph replays included)
+
+    // tracks
+    DevMem rays;
+    uint64_t n_rays = 0;
+    // initial image (host)
+    bool init_set = false;
+    bool init_missing = false;
+    std::vector<double> init_img;
+    muto_grid init_grid{};
+
+    // counters
+    DevMem ctr_mem;
+    Counters* ctr() { return ctr_mem.as<Counters>(); }
+    uint64_t n_total = 0;
+
+    // kept muons
+    uint64_t N = 0, npairs = 0;
+    DevMem kept, sd, pr2, scat, pr64, off;
+    DevMem vidx, L, T, slot, S;
+    DevMem mult, start;
+    DevMem lam, G, lam_ml, cost_hist;
+    DevMem tiles;
+    uint32_t ntiles = 0;
+    int tile_pairs = 0, tile_muons = 0, group = 32;
+    bool prepared = false;
+    int iters = 0;
+    bool stopped = false;
+    bool store_s = false;      // median / percentile mean
+    // PoCA outputs
+    DevMem img64, weight, assign;
+    // adjoint scratch
+    DevMem lam64, grad, dl, fval, loglam;
+    // graph
+    cudaGraphExec_t graph = nullptr;
+    size_t graph_prof_first = 0, graph_prof_last = 0;
+    unsigned long long graph_launches = 0;
+
+    std::string last_msg;
+    int last_err = 0;
+
+    bool fp64() const { return P.precision == 1; }
+    uint64_t V() const { return static_cast<uint64_t>(grid.nx) * grid.ny * grid.nz; }
+    bool want_cost() const { return P.compute_cost >= 0 ? P.compute_cost != 0 : (P.early_stop || P.log_results); }
+
+    void drop_graph() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
+    ~muto_handle() {
+        drop_graph();
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+void set_err(muto_handle* h, int code, const std::string& msg) {
+    if (!h) return;
+    h->last_err = code;
+    h->last_msg = msg;
+}
+
+template <class F>
+int guarded(muto_handle* h, F&& f) {
+    try {
+        f();
+        return MUTO_OK;
+    } catch (const Error& e) {
+        set_err(h, e.code, e.what());
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_err(h, MUTO_ERR_NOMEM, "host allocation failed");
+        return MUTO_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        set_err(h, MUTO_ERR_ARG, e.what());
+        return MUTO_ERR_ARG;
+    }
+}
+
+// launch helper: profiling + launch accounting
+template <class F>
+void run(muto_handle* h, const char* name, F&& f) {
+    const unsigned long long before = launches_so_far();
+    Profiler::Rec* r = h->prof.begin(name, h->stream, h->capturing);
+    f();
+    h->prof.end(r, h->stream, h->capturing);
+    if (!h->capturing) h->launches += launches_so_far() - before;
+    CK(cudaGetLastError());
+}
+
+void sync_and_harvest(muto_handle* h, size_t first) {
+    CK(cudaStreamSynchronize(h->stream));
+    h->prof.harvest(first, h->prof.used);
+    h->prof.used = first;
+}
+
+// ---------------------------------------------------------------------------
+// Setup
+// ---------------------------------------------------------------------------
+void resolve_initial_image(muto_handle* h, std::vector<double>& img) {
+    int method = h->P.initialize_method;
+    if (method == 0) {  // src/MutoMLSD.cpp:228-245
+        if (!h->init_set || h->init_missing || h->init_img.empty()) {
+            method = 1;  // file missing -> random
+        } else {
+            if (h->init_grid.nx != h->grid.nx || h->init_grid.ny != h->grid.ny || h->init_grid.nz != h->grid.nz)
+                h->grid = h->init_grid;  // adopt the image's grid
+            img = h->init_img;
+            return;
+        }
+    }
+    img.assign(h->V(), 0.0);
+    if (method == 1) {  // N(2, 0.5) * 1e-7, at least 1e-10 (src/MutoMLSD.cpp:251-261)
+        uint64_t seed = h->P.seed_set ? h->P.random_seed : std::random_device{}();
+        std::mt19937_64 gen(seed);
+        const double two_pi = 6.283185307179586;
+        for (uint64_t i = 0; i < img.size(); ++i) {
+            const double u1 = (static_cast<double>(gen() >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+            const double u2 = static_cast<double>(gen() >> 11) * (1.0 / 9007199254740992.0);
+            const double z = std::sqrt(-2.0 * std::log(u1)) * std::cos(two_pi * u2);
+            const double v = (2.0 + 0.5 * z) * 1.0e-7;
+            img[i] = 1.0e-10 <= v ? v : 1.0e-10;
+        }
+    } else {
+        std::fill(img.begin(), img.end(), h->P.initialize_value);
+    }
+}
+
+void alloc_counters(muto_handle* h) {
+    if (h->ctr_mem.empty()) h->ctr_mem.alloc(sizeof(Counters), &h->dev_bytes);
+    CK(cudaMemsetAsync(h->ctr_mem.as<void>(), 0, sizeof(Counters), h->stream));
+}
+
+void prepare_poca(muto_handle* h) {
+    const uint64_t V = h->V();
+    h->img64.alloc(V * sizeof(double), &h->dev_bytes);
+    h->weight.alloc(V * sizeof(double), &h->dev_bytes);
+    h->assign.alloc(std::max<uint64_t>(h->n_rays, 1) * 3 * sizeof(long long), &h->dev_bytes);
+    CK(cudaMemsetAsync(h->img64.as<void>(), 0, V * sizeof(double), h->stream));
+    CK(cudaMemsetAsync(h->weight.as<void>(), 0, V * sizeof(double), h->stream));
+    CK(cudaMemsetAsync(h->assign.as<void>(), 0xff, std::max<uint64_t>(h->n_rays, 1) * 3 * sizeof(long long), h->stream));
+    uint64_t nt = h->P.total_num_rays > 0 ? static_cast<uint64_t>(h->P.total_num_rays) : h->n_rays;
+    if (nt > h->n_rays) nt = h->n_rays;  // the reference would read past the end
+    h->n_total = nt;
+    PocaArgs a;
+    a.rays = h->rays.as<muto_ray>();
+    a.n = nt;
+    a.g = h->grid;
+    a.eps = h->P.eps;
+    a.mag = h->P.angle_unit_mag;
+    a.has_energy = h->P.has_energy;
+    a.straight = h->P.straight_line;
+    a.length_weighted = h->P.length_weighted;
+    a.img = h->img64.as<double>();
+    a.weight = h->weight.as<double>();
+    a.assign = h->assign.as<long long>();
+    a.ctr = h->ctr();
+    run(h, "poca", [&] { launch_poca(a, h->stream); });
+    run(h, "poca_normalize", [&] { launch_poca_normalize(h->img64.as<double>(), h->weight.as<double>(), V, h->P.eps, h->stream); });
+}
+
+template <typename Real>
+void prepare_em(muto_handle* h) {
+    using R4 = typename Vec4<Real>::type;
+    const Params& P = h->P;
+    std::vector<double> init;
+    resolve_initial_image(h, init);  // may adopt a new grid
+    const uint64_t V = h->V();
+    const muto_grid g = h->grid;
+    cudaStream_t s = h->stream;
+
+    uint64_t nt = P.total_num_rays > 0 ? static_cast<uint64_t>(P.total_num_rays) : h->n_rays;
+    if (nt > h->n_rays) nt = h->n_rays;
+    h->n_total = nt;
+
+    // --- gatherInformation: keep flags, order-preserving compaction --------
+    DevMem flags, pos, scratch;
+    flags.alloc(std::max<uint64_t>(nt, 1) * sizeof(uint32_t), &h->dev_bytes);
+    pos.alloc((nt + 1) * sizeof(uint64_t), &h->dev_bytes);
+    scratch.alloc(scan_scratch_bytes(std::max<uint64_t>(nt, V) + 1), &h->dev_bytes);
+    run(h, "keep_flags", [&] { launch_keep_flags(h->rays.as<muto_ray>(), nt, g, P.eps, flags.as<uint32_t>(), s); });
+    run(h, "scan", [&] { scan_u32_to_u64(flags.as<uint32_t>(), pos.as<uint64_t>(), nt, scratch.as<void>(), s); });
+    uint64_t N = 0;
+    CK(cudaMemcpyAsync(&N, pos.as<uint64_t>() + nt, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (N >= 65536ull * 65536ull) throw Error(MUTO_ERR_CAPACITY, "more than 2^32 kept muons");
+    h->N = N;
+    h->kept.alloc(std::max<uint64_t>(N, 1) * sizeof(uint32_t), &h->dev_bytes);
+    run(h, "compact", [&] { launch_compact(flags.as<uint32_t>(), pos.as<uint64_t>(), nt, h->kept.as<uint32_t>(), s); });
+
+    h->sd.alloc(std::max<uint64_t>(N, 1) * sizeof(R4), &h->dev_bytes);
+    h->pr2.alloc(std::max<uint64_t>(N, 1) * sizeof(Real), &h->dev_bytes);
+    h->scat.alloc(std::max<uint64_t>(N, 1) * 3 * sizeof(double), &h->dev_bytes);
+    h->pr64.alloc(std::max<uint64_t>(N, 1) * sizeof(double), &h->dev_bytes);
+    run(h, "muon_info", [&] {
+        launch_muon_info<Real>(h->rays.as<muto_ray>(), h->kept.as<uint32_t>(), N, g, P.eps, P.has_energy,
+                               h->sd.as<R4>(), h->pr2.as<Real>(), h->scat.as<double>(), h->pr64.as<double>(), s);
+    });
+
+    // --- paths: count, offsets, fill + tails --------------------------------
+    run(h, "siddon_count", [&] {
+        launch_path_count(h->rays.as<muto_ray>(), h->kept.as<uint32_t>(), h->scat.as<double>(), N, g, P.straight_line,
+                          flags.as<uint32_t>(), h->ctr(), s);
+    });
+    h->off.alloc((N + 1) * sizeof(uint64_t), &h->dev_bytes);
+    run(h, "scan", [&] { scan_u32_to_u64(flags.as<uint32_t>(), h->off.as<uint64_t>(), N, scratch.as<void>(), s); });
+    std::vector<uint64_t> off_h(N + 1);
+    CK(cudaMemcpyAsync(off_h.data(), h->off.as<uint64_t>(), (N + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const uint64_t Pn = off_h[N];
+    h->npairs = Pn;
+    h->store_s = !P.update_with_mean || P.mean_percentile != 100;
+    if (h->store_s && Pn >= 0xffffffffull)
+        throw Error(MUTO_ERR_CAPACITY, "median / percentile update needs fewer than 2^32 muon-voxel pairs");
+    flags.release();
+    pos.release();
+
+    h->vidx.alloc(std::max<uint64_t>(Pn, 1) * sizeof(uint32_t), &h->dev_bytes);
+    h->L.alloc(std::max<uint64_t>(Pn, 1) * sizeof(Real), &h->dev_bytes);
+    h->T.alloc(std::max<uint64_t>(Pn, 1) * sizeof(Real), &h->dev_bytes);
+    {
+        DevMem l64tmp;
+        double* l64 = reinterpret_cast<double*>(h->L.as<Real>());
+        if (!std::is_same<Real, double>::value) {
+            l64tmp.alloc(std::max<uint64_t>(Pn, 1) * sizeof(double), &h->dev_bytes);
+            l64 = l64tmp.as<double>();
+        }
+        run(h, "siddon_fill", [&] {
+            launch_path_fill<Real>(h->rays.as<muto_ray>(), h->kept.as<uint32_t>(), h->scat.as<double>(),
+                                   h->off.as<uint64_t>(), N, g, P.straight_line, h->vidx.as<uint32_t>(), l64,
+                                   h->L.as<Real>(), h->T.as<Real>(), s);
+        });
+        CK(cudaStreamSynchronize(s));
+    }
+
+    // --- multiplicity M_j, segment starts, slots -----------------------------
+    h->mult.alloc(V * sizeof(uint32_t), &h->dev_bytes);
+    CK(cudaMemsetAsync(h->mult.as<void>(), 0, V * sizeof(uint32_t), s));
+    run(h, "voxel_hist", [&] { launch_voxel_hist(h->vidx.as<uint32_t>(), Pn, static_cast<uint32_t>(V), h->mult.as<uint32_t>(), h->ctr(), s); });
+    if (h->store_s) {
+        h->start.alloc((V + 1) * sizeof(uint64_t), &h->dev_bytes);
+        run(h, "scan", [&] { scan_u32_to_u64(h->mult.as<uint32_t>(), h->start.as<uint64_t>(), V, scratch.as<void>(), s); });
+        DevMem cursor;
+        cursor.alloc(V * sizeof(uint32_t), &h->dev_bytes);
+        CK(cudaMemsetAsync(cursor.as<void>(), 0, V * sizeof(uint32_t), s));
+        h->slot.alloc(std::max<uint64_t>(Pn, 1) * sizeof(uint32_t), &h->dev_bytes);
+        run(h, "assign_slots", [&] {
+            launch_assign_slots(h->vidx.as<uint32_t>(), Pn, static_cast<uint32_t>(V), h->start.as<uint64_t>(),
+                                cursor.as<uint32_t>(), h->slot.as<uint32_t>(), s);
+        });
+        h->S.alloc(std::max<uint64_t>(Pn, 1) * sizeof(Real), &h->dev_bytes);
+        CK(cudaStreamSynchronize(s));
+    }
+    scratch.release();
+
+    // --- tiles of consecutive muons fitting the shared-memory stage ----------
+    uint64_t maxpath = 0;
+    for (uint64_t i = 0; i < N; ++i) maxpath = std::max<uint64_t>(maxpath, off_h[i + 1] - off_h[i]);
+    int TP = P.tile_pairs > 0 ? P.tile_pairs : (std::is_same<Real, double>::value ? 2048 : 4096);
+    while (static_cast<uint64_t>(TP) < maxpath) TP *= 2;
+    int TM = std::is_same<Real, double>::value ? 256 : 512;
+    TM = std::min<int>(TM, 65535);
+    if (em_tile_smem_bytes<Real>(TP, TM) > h->smem_optin)
+        throw Error(MUTO_ERR_CAPACITY, "longest muon path (" + std::to_string(maxpath) + " voxels) does not fit the shared-memory tile");
+    std::vector<uint32_t> tb;
+    tb.push_back(0);
+    uint64_t cs = 0;
+    for (uint64_t i = 0; i < N; ++i) {
+        if (off_h[i + 1] - off_h[cs] > static_cast<uint64_t>(TP) || i - cs >= static_cast<uint64_t>(TM)) {
+            tb.push_back(static_cast<uint32_t>(i));
+            cs = i;
+        }
+    }
+    if (N > 0) tb.push_back(static_cast<uint32_t>(N));
+    h->ntiles = static_cast<uint32_t>(tb.size() - 1);
+    h->tiles.alloc(tb.size() * sizeof(uint32_t), &h->dev_bytes);
+    CK(cudaMemcpyAsync(h->tiles.as<void>(), tb.data(), tb.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    h->tile_pairs = TP;
+    h->tile_muons = TM;
+    CK(em_tile_configure<Real>(TP, TM));
+    const double avg = N > 0 ? static_cast<double>(Pn) / static_cast<double>(N) : 0.0;
+    h->group = avg <= 32 ? 8 : (avg <= 64 ? 16 : 32);
+
+    // --- image and accumulators ---------------------------------------------
+    h->lam.alloc(V * sizeof(Real), &h->dev_bytes);
+    {
+        std::vector<Real> init_r(init.begin(), init.end());
+        CK(cudaMemcpyAsync(h->lam.as<void>(), init_r.data(), V * sizeof(Real), cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    h->G.alloc(V * sizeof(Real), &h->dev_bytes);
+    CK(cudaMemsetAsync(h->G.as<void>(), 0, V * sizeof(Real), s));
+    if (h->method == kMap) h->lam_ml.alloc(V * sizeof(double), &h->dev_bytes);
+    h->cost_hist.alloc(std::max(P.num_iteration, 1) * 4 * sizeof(double) + 4096 * sizeof(double), &h->dev_bytes);
+    CK(cudaStreamSynchronize(s));
+}
+
+// ---------------------------------------------------------------------------
+// One EM / MAP iteration (device work only; graph-capturable)
+// ---------------------------------------------------------------------------
+template <typename Real>
+void enqueue_iteration(muto_handle* h) {
+    using R4 = typename Vec4<Real>::type;
+    const Params& P = h->P;
+    cudaStream_t s = h->stream;
+    const uint32_t V = static_cast<uint32_t>(h->V());
+    const double exy = P.error_xy, ezo = P.error_dz_outer, ezi = P.error_dz_inner;  // src/MutoMLSD.cpp:168-170
+    EmArgs<Real> a;
+    a.off = h->off.as<uint64_t>();
+    a.tile_mb = h->tiles.as<uint32_t>();
+    a.ntiles = h->ntiles;
+    a.vidx = h->vidx.as<uint32_t>();
+    a.L = h->L.as<Real>();
+    a.T = h->T.as<Real>();
+    a.slot = h->store_s ? h->slot.as<uint32_t>() : nullptr;
+    a.sd = h->sd.as<R4>();
+    a.pr2 = h->pr2.as<Real>();
+    a.lam = h->lam.as<Real>();
+    a.S = h->store_s ? h->S.as<Real>() : nullptr;
+    a.G = h->G.as<Real>();
+    a.V = V;
+    a.E00 = 4.0 * exy * exy / (ezo * ezo);
+    a.E11 = 2.0 * exy * exy * (1.0 + (ezi / ezo + 1.0) * ezi / ezo);
+    a.E01 = 2.0 * exy * exy * ezi / (ezo * ezo);
+    a.mode = h->store_s ? kEmMedian : kEmMean;
+    a.compute_cost = h->want_cost() ? 1 : 0;
+    a.ctr = h->ctr();
+    const int blocks = 2 * h->num_sms;
+    run(h, "em_tile", [&] { launch_em_tile<Real>(a, h->tile_pairs, h->tile_muons, blocks, h->group, s); });
+
+    const bool map = h->method == kMap;
+    if (h->store_s) {
+        if (map)
+            run(h, "em_select", [&] {
+                launch_select<Real, double>(h->S.as<Real>(), h->start.as<uint64_t>(), h->mult.as<uint32_t>(), V,
+                                            P.update_with_mean, P.mean_percentile, h->lam_ml.as<double>(), s);
+            });
+        else
+            run(h, "em_select", [&] {
+                launch_select<Real, Real>(h->S.as<Real>(), h->start.as<uint64_t>(), h->mult.as<uint32_t>(), V,
+                                          P.update_with_mean, P.mean_percentile, h->lam.as<Real>(), s);
+            });
+    } else {
+        if (map)
+            run(h, "em_voxel", [&] {
+                launch_voxel_mean<Real, double>(h->lam.as<Real>(), h->G.as<Real>(), h->mult.as<uint32_t>(), V,
+                                                h->lam_ml.as<double>(), s);
+            });
+        else
+            run(h, "em_voxel", [&] {
+                launch_voxel_mean<Real, Real>(h->lam.as<Real>(), h->G.as<Real>(), h->mult.as<uint32_t>(), V,
+                                              h->lam.as<Real>(), s);
+            });
+    }
+    if (map) {
+        MapParams mp{P.beta, P.p, P.delta, P.eps, P.all_neighbours, P.add_object_prior, P.newton_max_iter};
+        run(h, "map_voxel", [&] {
+            launch_map_voxel<Real>(h->lam.as<Real>(), h->lam_ml.as<double>(), h->mult.as<uint32_t>(),
+                                   make_dev_grid(h->grid), mp, h->ctr(), s);
+        });
+        run(h, "map_copy", [&] { launch_copy_to<Real>(h->lam_ml.as<double>(), h->lam.as<Real>(), h->V(), s); });
+    }
+    const uint32_t cap = static_cast<uint32_t>(h->cost_hist.bytes() / sizeof(double));
+    run(h, "cost", [&] { launch_finalize_cost(h->ctr(), static_cast<double>(h->N), h->cost_hist.as<double>(), cap, s); });
+}
+
+template <typename Real>
+void iterate_impl(muto_handle* h, int n) {
+    const bool sync_each = h->P.early_stop || h->prof.on;
+    for (int it = 0; it < n && !h->stopped; ++it) {
+        const size_t pf = h->prof.used;
+        if (h->P.use_graph) {
+            if (!h->graph) {
+                // capture one iteration once; replays reuse the same buffers
+                const unsigned long long before = launches_so_far();
+                CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+                h->capturing = true;
+                h->graph_prof_first = h->prof.used;
+                try {
+                    enqueue_iteration<Real>(h);
+                } catch (...) {
+                    cudaGraph_t gtmp;
+                    cudaStreamEndCapture(h->stream, &gtmp);
+                    if (gtmp) cudaGraphDestroy(gtmp);
+                    h->capturing = false;
+                    throw;
+                }
+                h->capturing = false;
+                h->graph_prof_last = h->prof.used;
+                cudaGraph_t graph;
+                CK(cudaStreamEndCapture(h->stream, &graph));
+                const cudaError_t e = cudaGraphInstantiate(&h->graph, graph, 0);
+                cudaGraphDestroy(graph);
+                CK(e);
+                h->graph_launches = launches_so_far() - before;
+            }
+            CK(cudaGraphLaunch(h->graph, h->stream));
+            h->launches += h->graph_launches;
+        } else {
+            enqueue_iteration<Real>(h);
+        }
+        h->iters += 1;
+        if (sync_each) {
+            CK(cudaStreamSynchronize(h->stream));
+            if (h->prof.on) {
+                if (h->P.use_graph) h->prof.harvest(h->graph_prof_first, h->graph_prof_last);
+                else sync_and_harvest(h, pf);
+            }
+            if (h->P.early_stop) {
+                Counters c;
+                CK(cudaMemcpy(&c, h->ctr(), sizeof(Counters), cudaMemcpyDeviceToHost));
+                // the reference compares with an uninitialised value on iteration 0 (src/MutoMLSD.cpp:184,209);
+                // here the first possible stop is after the second iteration
+                if (h->iters > 1 && c.cost_prev < c.cost_last) h->stopped = true;
+            }
+        }
+    }
+}
+
+void check_handle(muto_handle* h) {
+    if (!h) throw Error(MUTO_ERR_ARG, "null handle");
+}
+
+template <typename Real>
+void download_image(muto_handle* h, double* out) {
+    const uint64_t V = h->V();
+    std::vector<Real> tmp(V);
+    CK(cudaMemcpyAsync(tmp.data(), h->lam.as<Real>(), V * sizeof(Real), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (uint64_t j = 0; j < V; ++j) out[j] = static_cast<double>(tmp[j]);
+}
+
+template <typename Real>
+void upload_image(muto_handle* h, const double* in) {
+    const uint64_t V = h->V();
+    std::vector<Real> tmp(in, in + V);
+    CK(cudaMemcpyAsync(h->lam.as<Real>(), tmp.data(), V * sizeof(Real), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint
+// ---------------------------------------------------------------------------
+template <typename Real>
+double nll_eval(muto_handle* h, const double* loglam_host, double* grad_host, bool dev_input = false) {
+    using R4 = typename Vec4<Real>::type;
+    const uint64_t V = h->V();
+    cudaStream_t s = h->stream;
+    const size_t pf = h->prof.used;
+    if (h->loglam.empty()) h->loglam.alloc(V * sizeof(double), &h->dev_bytes);
+    if (h->lam64.empty()) h->lam64.alloc(V * sizeof(double), &h->dev_bytes);
+    if (h->grad.empty()) h->grad.alloc(V * sizeof(double), &h->dev_bytes);
+    if (h->dl.empty()) {
+        h->dl.alloc(V * sizeof(double), &h->dev_bytes);
+        CK(cudaMemsetAsync(h->dl.as<void>(), 0, V * sizeof(double), s));
+    }
+    if (h->fval.empty()) h->fval.alloc(sizeof(double), &h->dev_bytes);
+    if (!dev_input)
+        CK(cudaMemcpyAsync(h->loglam.as<double>(), loglam_host, V * sizeof(double), cudaMemcpyHostToDevice, s));
+    // lambda in the storage precision for the muon pass and in FP64 for the prior
+    run(h, "exp_lambda", [&] { launch_exp_lambda<double>(h->loglam.as<double>(), h->mult.as<uint32_t>(), static_cast<uint32_t>(V), h->lam64.as<double>(), s); });
+    DevMem lamR;
+    Real* lam_r = reinterpret_cast<Real*>(h->lam64.as<double>());
+    if (!std::is_same<Real, double>::value) {
+        lamR.alloc(V * sizeof(Real), &h->dev_bytes);
+        lam_r = lamR.as<Real>();
+        run(h, "exp_lambda", [&] { launch_exp_lambda<Real>(h->loglam.as<double>(), h->mult.as<uint32_t>(), static_cast<uint32_t>(V), lam_r, s); });
+    }
+    Counters c0;
+    CK(cudaMemcpyAsync(&c0, h->ctr(), sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaMemsetAsync(&h->ctr()->cost_sum, 0, sizeof(double), s));
+    CK(cudaMemsetAsync(h->G.as<void>(), 0, V * sizeof(Real), s));
+    const Params& P = h->P;
+    const double exy = P.error_xy, ezo = P.error_dz_outer, ezi = P.error_dz_inner;
+    EmArgs<Real> a;
+    a.off = h->off.as<uint64_t>();
+    a.tile_mb = h->tiles.as<uint32_t>();
+    a.ntiles = h->ntiles;
+    a.vidx = h->vidx.as<uint32_t>();
+    a.L = h->L.as<Real>();
+    a.T = h->T.as<Real>();
+    a.slot = nullptr;
+    a.sd = h->sd.as<R4>();
+    a.pr2 = h->pr2.as<Real>();
+    a.lam = lam_r;
+    a.S = nullptr;
+    a.G = h->G.as<Real>();
+    a.V = static_cast<uint32_t>(V);
+    a.E00 = 4.0 * exy * exy / (ezo * ezo);
+    a.E11 = 2.0 * exy * exy * (1.0 + (ezi / ezo + 1.0) * ezi / ezo);
+    a.E01 = 2.0 * exy * exy * ezi / (ezo * ezo);
+    a.mode = grad_host ? kEmMean : kEmCostOnly;
+    a.compute_cost = 1;
+    a.ctr = h->ctr();
+    run(h, grad_host ? "nll_backward" : "nll_forward",
+        [&] { launch_em_tile<Real>(a, h->tile_pairs, h->tile_muons, 2 * h->num_sms, h->group, s); });
+    CK(cudaMemsetAsync(h->fval.as<void>(), 0, sizeof(double), s));
+    if (grad_host) {
+        run(h, "grad_finish", [&] { launch_grad_finish<Real>(h->G.as<Real>(), h->lam64.as<double>(), h->mult.as<uint32_t>(), static_cast<uint32_t>(V), h->grad.as<double>(), s); });
+    }
+    if (h->method == kMap) {
+        MapParams mp{P.beta, P.p, P.delta, P.eps, P.all_neighbours, P.add_object_prior, P.newton_max_iter};
+        DevMem gdummy;
+        double* gp = h->grad.as<double>();
+        if (!grad_host) {
+            gdummy.alloc(V * sizeof(double), &h->dev_bytes);
+            gp = gdummy.as<double>();
+        }
+        run(h, "prior", [&] { launch_prior(h->lam64.as<double>(), h->mult.as<uint32_t>(), make_dev_grid(h->grid), mp, h->dl.as<double>(), gp, h->fval.as<double>(), s); });
+        CK(cudaStreamSynchronize(s));
+    }
+    Counters c1;
+    double prior = 0.0;
+    CK(cudaMemcpyAsync(&c1, h->ctr(), sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&prior, h->fval.as<double>(), sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (grad_host) CK(cudaMemcpyAsync(grad_host, h->grad.as<double>(), V * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    // the singular counter counts covariance failures of iterations only
+    CK(cudaMemcpy(&h->ctr()->singular, &c0.singular, sizeof(unsigned long long), cudaMemcpyHostToDevice));
+    sync_and_harvest(h, pf);
+    return c1.cost_sum + prior;
+}
+
+int n_prepared_check(muto_handle* h) {
+    if (!h->prepared) throw Error(MUTO_ERR_STATE, "call muto_prepare (or muto_reconstruct) first");
+    return 0;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* muto_version(void) { return "muto-gb300 0.1 (sm_103a)"; }
+
+int muto_create(const char* method, const char* config_json, muto_handle** out) {
+    if (!method || !out) return MUTO_ERR_ARG;
+    *out = nullptr;
+    std::unique_ptr<muto_handle> h(new muto_handle());
+    const std::string m(method);
+    if (m == "poca") h->method = kPoca;
+    else if (m == "mlsd") h->method = kMlsd;
+    else if (m == "map") h->method = kMap;
+    else return MUTO_ERR_ARG;
+    const int rc = guarded(h.get(), [&] {
+        h->P = parse_params(h->method, config_json ? config_json : "");
+        h->grid = h->P.grid;
+        CK(cudaGetDevice(&h->device));
+        CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
+        int optin = 0;
+        CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+        h->smem_optin = static_cast<size_t>(optin);
+        CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        alloc_counters(h.get());
+        CK(cudaStreamSynchronize(h->stream));
+    });
+    if (rc != MUTO_OK) return rc;
+    *out = h.release();
+    return MUTO_OK;
+}
+
+int muto_destroy(muto_handle* h) {
+    if (!h) return MUTO_ERR_ARG;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    delete h;
+    return MUTO_OK;
+}
+
+int muto_get_grid(const muto_handle* h, muto_grid* out) {
+    if (!h || !out) return MUTO_ERR_ARG;
+    *out = h->grid;
+    return MUTO_OK;
+}
+
+int muto_get_status(const muto_handle* hc, muto_status* out) {
+    if (!hc || !out) return MUTO_ERR_ARG;
+    muto_handle* h = const_cast<muto_handle*>(hc);
+    std::memset(out, 0, sizeof(*out));
+    Counters c{};
+    if (!h->ctr_mem.empty()) {
+        if (cudaStreamSynchronize(h->stream) == cudaSuccess)
+            cudaMemcpy(&c, h->ctr(), sizeof(Counters), cudaMemcpyDeviceToHost);
+    }
+    out->last_error = h->last_err;
+    out->iterations_done = h->iters;
+    out->early_stopped = h->stopped ? 1 : 0;
+    out->precision = h->P.precision;
+    out->n_total = h->n_total;
+    out->n_scat_in_grid = h->method == kPoca ? c.in_grid : h->N;
+    out->n_not_parallel = c.not_parallel;
+    out->n_pairs = h->npairs;
+    out->n_singular = c.singular;
+    out->n_nonconverged = c.nonconverged;
+    out->n_bounds = c.bounds;
+    out->n_path_overflow = c.overflow;
+    out->cost = c.cost_last;
+    out->cost_prev = c.cost_prev;
+    out->device_bytes = h->dev_bytes.load();
+    std::snprintf(out->message, sizeof(out->message), "%s", h->last_msg.c_str());
+    return MUTO_OK;
+}
+
+int muto_set_initial_image(muto_handle* h, const double* img, const muto_grid* grid) {
+    if (!h) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        if (h->prepared) throw Error(MUTO_ERR_STATE, "initial image must be set before prepare");
+        h->init_set = true;
+        if (!img || !grid) {
+            h->init_missing = true;
+            h->init_img.clear();
+            return;
+        }
+        const uint64_t V = static_cast<uint64_t>(grid->nx) * grid->ny * grid->nz;
+        if (V == 0) throw Error(MUTO_ERR_ARG, "empty initial image grid");
+        h->init_missing = false;
+        h->init_grid = *grid;
+        h->init_img.assign(img, img + V);
+    });
+}
+
+int muto_load_tracks(muto_handle* h, const muto_ray* rays, uint64_t n, int on_device) {
+    if (!h) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        if (n > 0 && !rays) throw Error(MUTO_ERR_ARG, "null rays");
+        if (n >= 0xffffffffull) throw Error(MUTO_ERR_CAPACITY, "at most 2^32-1 tracks per handle");
+        h->drop_graph();
+        h->prepared = false;
+        h->n_rays = n;
+        h->rays.alloc(std::max<uint64_t>(n, 1) * sizeof(muto_ray), &h->dev_bytes);
+        if (n > 0)
+            CK(cudaMemcpyAsync(h->rays.as<void>(), rays, n * sizeof(muto_ray),
+                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    });
+}
+
+int muto_prepare(muto_handle* h) {
+    if (!h) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        if (h->rays.empty()) throw Error(MUTO_ERR_STATE, "load tracks first");
+        h->drop_graph();
+        h->iters = 0;
+        h->stopped = false;
+        h->grid = h->P.grid;
+        alloc_counters(h);
+        const size_t pf = h->prof.used;
+        if (h->method == kPoca) {
+            prepare_poca(h);
+        } else if (h->fp64()) {
+            prepare_em<double>(h);
+        } else {
+            prepare_em<float>(h);
+        }
+        sync_and_harvest(h, pf);
+        h->prepared = true;
+    });
+}
+
+int muto_iterate(muto_handle* h, int n_iter) {
+    if (!h) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        n_prepared_check(h);
+        if (h->method == kPoca) return;  // PoCA has no iterations
+        if (n_iter < 0) throw Error(MUTO_ERR_ARG, "n_iter must be >= 0");
+        if (h->fp64()) iterate_impl<double>(h, n_iter);
+        else iterate_impl<float>(h, n_iter);
+    });
+}
+
+int muto_get_image(muto_handle* h, double* out, uint64_t len) {
+    if (!h || !out) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        n_prepared_check(h);
+        if (len != h->V()) throw Error(MUTO_ERR_ARG, "image length does not match nx*ny*nz of the current grid");
+        if (h->method == kPoca) {
+            CK(cudaMemcpyAsync(out, h->img64.as<double>(), len * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+        } else if (h->fp64()) {
+            download_image<double>(h, out);
+        } else {
+            download_image<float>(h, out);
+        }
+    });
+}
+
+int muto_set_image(muto_handle* h, const double* img, uint64_t len) {
+    if (!h || !img) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        n_prepared_check(h);
+        if (h->method == kPoca) throw Error(MUTO_ERR_STATE, "PoCA has no iterate image");
+        if (len != h->V()) throw Error(MUTO_ERR_ARG, "image length does not match nx*ny*nz of the current grid");
+        if (h->fp64()) upload_image<double>(h, img);
+        else upload_image<float>(h, img);
+    });
+}
+
+int muto_reconstruct(muto_handle* h, const muto_ray* rays, uint64_t n, double* out_img, uint64_t out_len) {
+    if (!h) return MUTO_ERR_ARG;
+    int rc = muto_load_tracks(h, rays, n, 0);
+    if (rc) return rc;
+    rc = muto_prepare(h);
+    if (rc) return rc;
+    if (h->method != kPoca) {
+        rc = muto_iterate(h, h->P.num_iteration);
+        if (rc) return rc;
+    }
+    return muto_get_image(h, out_img, out_len);
+}
+
+int muto_siddon_batch(const muto_grid* g, const double* p1, const double* p2, uint64_t n, uint32_t cap, uint32_t* xyz,
+                      double* len, uint32_t* counts) {
+    if (!g || (n > 0 && (!p1 || !p2 || !counts)) || (cap > 0 && n > 0 && (!xyz || !len))) return MUTO_ERR_ARG;
+    return guarded(nullptr, [&] {
+        if (n == 0) return;
+        cudaStream_t s;
+        CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        DevMem d1, d2, dx, dl, dc;
+        d1.alloc(n * 3 * sizeof(double), nullptr);
+        d2.alloc(n * 3 * sizeof(double), nullptr);
+        dx.alloc(std::max<uint64_t>(n * cap, 1) * 3 * sizeof(uint32_t), nullptr);
+        dl.alloc(std::max<uint64_t>(n * cap, 1) * sizeof(double), nullptr);
+        dc.alloc(n * sizeof(uint32_t), nullptr);
+        CK(cudaMemcpyAsync(d1.as<void>(), p1, n * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d2.as<void>(), p2, n * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
+        launch_siddon_batch(*g, d1.as<double>(), d2.as<double>(), n, cap, dx.as<uint32_t>(), dl.as<double>(),
+                            dc.as<uint32_t>(), s);
+        CK(cudaGetLastError());
+        if (cap > 0) {
+            CK(cudaMemcpyAsync(xyz, dx.as<void>(), n * cap * 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(len, dl.as<void>(), n * cap * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
+        CK(cudaMemcpyAsync(counts, dc.as<void>(), n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        CK(cudaStreamDestroy(s));
+    });
+}
+
+int muto_export_paths(muto_handle* h, uint32_t* kept, double* info, uint64_t* off, uint32_t* idx, double* len,
+                      double* tail) {
+    if (!h) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        n_prepared_check(h);
+        if (h->method == kPoca) throw Error(MUTO_ERR_STATE, "PoCA stores no paths");
+        cudaStream_t s = h->stream;
+        const uint64_t N = h->N, Pn = h->npairs;
+        if (kept && N) CK(cudaMemcpyAsync(kept, h->kept.as<void>(), N * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        if (off) CK(cudaMemcpyAsync(off, h->off.as<void>(), (N + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        if (idx && Pn) CK(cudaMemcpyAsync(idx, h->vidx.as<void>(), Pn * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        auto fetch = [&](const DevMem& m, double* dst, uint64_t count) {
+            if (!dst || count == 0) return;
+            if (h->fp64()) {
+                CK(cudaMemcpyAsync(dst, m.as<void>(), count * sizeof(double), cudaMemcpyDeviceToHost, s));
+            } else {
+                std::vector<float> tmp(count);
+                CK(cudaMemcpyAsync(tmp.data(), m.as<void>(), count * sizeof(float), cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                for (uint64_t k = 0; k < count; ++k) dst[k] = tmp[k];
+            }
+        };
+        fetch(h->L, len, Pn);
+        fetch(h->T, tail, Pn);
+        if (info && N) {
+            std::vector<double> pr(N);
+            CK(cudaMemcpyAsync(pr.data(), h->pr64.as<void>(), N * sizeof(double), cudaMemcpyDeviceToHost, s));
+            std::vector<double> sd(4 * N);
+            if (h->fp64()) {
+                CK(cudaMemcpyAsync(sd.data(), h->sd.as<void>(), 4 * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+            } else {
+                std::vector<float> t(4 * N);
+                CK(cudaMemcpyAsync(t.data(), h->sd.as<void>(), 4 * N * sizeof(float), cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                for (uint64_t k = 0; k < 4 * N; ++k) sd[k] = t[k];
+            }
+            for (uint64_t i = 0; i < N; ++i) {  // stored as (Sx, Dx, Sy, Dy)
+                info[6 * i + 0] = sd[4 * i + 0];
+                info[6 * i + 1] = sd[4 * i + 2];
+                info[6 * i + 2] = sd[4 * i + 1];
+                info[6 * i + 3] = sd[4 * i + 3];
+                info[6 * i + 4] = pr[i];
+                info[6 * i + 5] = 0.0;
+            }
+        }
+        CK(cudaStreamSynchronize(s));
+    });
+}
+
+int muto_poca_assignment(muto_handle* h, int64_t* assign, uint64_t n) {
+    if (!h || !assign) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        n_prepared_check(h);
+        if (h->method != kPoca) throw Error(MUTO_ERR_STATE, "only PoCA bins PoCA points");
+        if (n != h->n_rays) throw Error(MUTO_ERR_ARG, "n must equal the number of loaded tracks");
+        if (n) CK(cudaMemcpy(assign, h->assign.as<void>(), n * 3 * sizeof(long long), cudaMemcpyDeviceToHost));
+    });
+}
+
+int muto_get_multiplicity(muto_handle* h, uint32_t* out, uint64_t len) {
+    if (!h || !out) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        n_prepared_check(h);
+        if (h->method == kPoca) throw Error(MUTO_ERR_STATE, "PoCA has no multiplicity");
+        if (len != h->V()) throw Error(MUTO_ERR_ARG, "length does not match nx*ny*nz");
+        CK(cudaMemcpy(out, h->mult.as<void>(), len * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    });
+}
+
+int muto_nll_forward(muto_handle* h, const double* log_lambda, double* out_value) {
+    if (!h || !log_lambda || !out_value) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        n_prepared_check(h);
+        if (h->method == kPoca) throw Error(MUTO_ERR_STATE, "PoCA has no likelihood");
+        *out_value = h->fp64() ? nll_eval<double>(h, log_lambda, nullptr) : nll_eval<float>(h, log_lambda, nullptr);
+    });
+}
+
+int muto_nll_backward(muto_handle* h, const double* log_lambda, double* out_value, double* out_grad) {
+    if (!h || !log_lambda || !out_grad) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        n_prepared_check(h);
+        if (h->method == kPoca) throw Error(MUTO_ERR_STATE, "PoCA has no likelihood");
+        const double v = h->fp64() ? nll_eval<double>(h, log_lambda, out_grad) : nll_eval<float>(h, log_lambda, out_grad);
+        if (out_value) *out_value = v;
+    });
+}
+
+int muto_gradient_solve(muto_handle* h, int n_iter, double* out_value) {
+    if (!h) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        n_prepared_check(h);
+        if (h->method == kPoca) throw Error(MUTO_ERR_STATE, "PoCA has no likelihood");
+        const uint64_t V = h->V();
+        std::vector<double> lam(V), x(V), g(V), xt(V);
+        std::vector<uint32_t> M(V);
+        if (h->fp64()) download_image<double>(h, lam.data());
+        else download_image<float>(h, lam.data());
+        CK(cudaMemcpy(M.data(), h->mult.as<void>(), V * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        const double floor_l = 1e-12;
+        for (uint64_t j = 0; j < V; ++j) x[j] = std::log(std::max(lam[j], floor_l));
+        auto F = [&](const std::vector<double>& xx, std::vector<double>* gg) {
+            if (gg) return h->fp64() ? nll_eval<double>(h, xx.data(), gg->data()) : nll_eval<float>(h, xx.data(), gg->data());
+            return h->fp64() ? nll_eval<double>(h, xx.data(), nullptr) : nll_eval<float>(h, xx.data(), nullptr);
+        };
+        double f = F(x, &g);
+        double step = 1.0;
+        for (int it = 0; it < n_iter; ++it) {
+            // step preconditioned by 1/(2 M_j): at step 1 it is the mean-mode EM move in log space
+            double slope = 0.0;
+            for (uint64_t j = 0; j < V; ++j) {
+                if (!M[j]) continue;
+                const double d = -g[j] / (2.0 * M[j]);
+                slope += g[j] * d;
+            }
+            if (slope >= 0) break;
+            double ft = f;
+            bool accepted = false;
+            for (int ls = 0; ls < 30; ++ls) {
+                for (uint64_t j = 0; j < V; ++j) xt[j] = M[j] ? x[j] - step * g[j] / (2.0 * M[j]) : x[j];
+                ft = F(xt, nullptr);
+                if (ft <= f + 1e-4 * step * slope) {
+                    accepted = true;
+                    break;
+                }
+                step *= 0.5;
+            }
+            if (!accepted) break;
+            x.swap(xt);
+            f = F(x, &g);
+            step = std::min(step * 2.0, 4.0);
+        }
+        for (uint64_t j = 0; j < V; ++j) lam[j] = M[j] ? std::exp(x[j]) : 0.0;
+        if (h->fp64()) upload_image<double>(h, lam.data());
+        else upload_image<float>(h, lam.data());
+        if (out_value) *out_value = f;
+    });
+}
+
+int muto_set_profiling(muto_handle* h, int enable) {
+    if (!h) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        if (h->prof.on != (enable != 0)) h->drop_graph();  // recapture with / without event nodes
+        h->prof.on = enable != 0;
+    });
+}
+
+int muto_kernel_stats(muto_handle* h, const char* name, uint64_t* launches, double* total_ms) {
+    if (!h || !name) return MUTO_ERR_ARG;
+    auto it = h->prof.stats.find(name);
+    if (launches) *launches = it == h->prof.stats.end() ? 0 : it->second.first;
+    if (total_ms) *total_ms = it == h->prof.stats.end() ? 0.0 : it->second.second;
+    return MUTO_OK;
+}
+
+int muto_reset_kernel_stats(muto_handle* h) {
+    if (!h) return MUTO_ERR_ARG;
+    h->prof.stats.clear();
+    return MUTO_OK;
+}
+
+int muto_launch_count(muto_handle* h, uint64_t* out) {
+    if (!h || !out) return MUTO_ERR_ARG;
+    *out = h->launches;
+    return MUTO_OK;
+}
+
+int muto_get_stream(muto_handle* h, void** out) {
+    if (!h || !out) return MUTO_ERR_ARG;
+    *out = static_cast<void*>(h->stream);
+    return MUTO_OK;
+}
+
+int muto_generate_device(const muto_grid* g, const double* lambda_dev, const muto_gen_params* p, uint64_t first,
+                         uint64_t n, muto_ray* out_dev, void* stream) {
+    if (!g || !lambda_dev || !p || (n && !out_dev)) return MUTO_ERR_ARG;
+    if (!gen::params_ok(*p)) return MUTO_ERR_ARG;
+    return guarded(nullptr, [&] {
+        launch_generate(*g, lambda_dev, *p, first, n, out_dev, static_cast<cudaStream_t>(stream));
+        CK(cudaGetLastError());
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,290 @@
+// Setup kernels of the MLSD/MAP path (run once per reconstruction):
+//   keep flags + compaction   gatherInformation, src/MutoMLSD.cpp:268-326
+//   muon info                 getScatteringAngle / getDisplacement / pr, :350-376, :320-322
+//   path count + fill         getMuonPathAndTail + generateWeightMatrix, :382-430
+//   voxel multiplicity/slots  allocateSValueMatrix + S_index, :432-437, :173-181
+// and the batched Siddon probe (MutoSiddon::getVoxelPath, src/MutoSiddon.cpp:9).
+#include "common.cuh"
+
+namespace muto {
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned blocks_for(uint64_t n, int threads = kThreads) {
+    const uint64_t b = (n + threads - 1) / threads;
+    return static_cast<unsigned>(b > 0 ? b : 1);
+}
+
+// in-grid and detector-zone test of gatherInformation (src/MutoMLSD.cpp:273-274, :298-304)
+__device__ __forceinline__ bool keep_muon(const muto_ray& r, const DevGrid& g, double eps, double zdet_min,
+                                          double zdet_max, double* ps) {
+    poca_point(r, eps, ps);
+    const double xhi = dsub(dadd(g.lo[0], dmul(g.w[0], static_cast<double>(g.n[0]))), eps);
+    const double yhi = dsub(dadd(g.lo[1], dmul(g.w[1], static_cast<double>(g.n[1]))), eps);
+    const double zhi = dsub(dadd(g.lo[2], dmul(g.w[2], static_cast<double>(g.n[2]))), eps);
+    return !(ps[0] < dadd(g.lo[0], eps) || xhi < ps[0] || ps[1] < dadd(g.lo[1], eps) || yhi < ps[1] ||
+             ps[2] < dadd(g.lo[2], eps) || zhi < ps[2] || ps[2] < dadd(zdet_min, eps) || dsub(zdet_max, eps) <= ps[2]);
+}
+
+__global__ void k_keep_flags(const muto_ray* __restrict__ rays, uint64_t n, DevGrid g, double eps,
+                             uint32_t* __restrict__ flags) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double zmin = rays[0].pout[2], zmax = rays[0].pin[2];  // detector zone from ray 0, :273-274
+    double ps[3];
+    flags[i] = keep_muon(rays[i], g, eps, zmin, zmax, ps) ? 1u : 0u;
+}
+
+__global__ void k_compact(const uint32_t* __restrict__ flags, const uint64_t* __restrict__ pos, uint64_t n,
+                          uint32_t* __restrict__ kept) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n && flags[i]) kept[pos[i]] = static_cast<uint32_t>(i);
+}
+
+template <typename Real>
+__global__ void k_muon_info(const muto_ray* __restrict__ rays, const uint32_t* __restrict__ kept, uint64_t n,
+                            DevGrid g, double eps, int has_energy, typename Vec4<Real>::type* __restrict__ sd,
+                            Real* __restrict__ pr2, double* __restrict__ scat, double* __restrict__ pr_out) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const muto_ray r = rays[kept[i]];
+    double ps[3];
+    poca_point(r, eps, ps);
+    scat[3 * i + 0] = ps[0];
+    scat[3 * i + 1] = ps[1];
+    scat[3 * i + 2] = ps[2];
+    double sx, sy, dx, dy;
+    scat_angles(r.din, r.dout, &sx, &sy);
+    displacement(r, g.lo[2], &dx, &dy);
+    typename Vec4<Real>::type v;
+    v.x = static_cast<Real>(sx);
+    v.y = static_cast<Real>(dx);
+    v.z = static_cast<Real>(sy);
+    v.w = static_cast<Real>(dy);
+    sd[i] = v;
+    const double pr = has_energy ? ddiv(3.0, r.ein) : 1.0;  // pr = p0 / p, :288, :321
+    pr2[i] = static_cast<Real>(pr * pr);
+    if (pr_out) pr_out[i] = pr;
+}
+
+struct CountSink {
+    int n = 0;
+    __device__ void operator()(uint32_t, uint32_t, uint32_t, double) { ++n; }
+};
+
+__global__ void k_path_count(const muto_ray* __restrict__ rays, const uint32_t* __restrict__ kept,
+                             const double* __restrict__ scat, uint64_t n, DevGrid g, int straight,
+                             uint32_t* __restrict__ counts, Counters* ctr) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const muto_ray& r = rays[kept[i]];
+    const double ps[3] = {scat[3 * i], scat[3 * i + 1], scat[3 * i + 2]};
+    int total = 0;
+    bool overflow = false;
+    CountSink a, b;
+    if (straight) {
+        const int c = siddon_walk(g, r.pin, r.pout, a);
+        overflow = c < 0;
+        total = overflow ? 0 : c;
+    } else {
+        const int ci = siddon_walk(g, r.pin, ps, a);
+        const int co = siddon_walk(g, ps, r.pout, b);
+        overflow = ci < 0 || co < 0;
+        // in-half, then the out-half without its first voxel (merged into the
+        // last in-voxel, or dropped when the in-half is empty), :396-402
+        total = overflow ? 0 : ci + (co > 0 ? co - 1 : 0);
+    }
+    if (overflow) atomicAdd(&ctr->overflow, 1ull);
+    counts[i] = static_cast<uint32_t>(total);
+}
+
+// Writes the merged path of one muon: voxel index (xyz2index, include/MutoMLSD.h:76,
+// in 32-bit unsigned arithmetic) and FP64 length.
+struct FillSink {
+    uint32_t* vidx;
+    double* l64;
+    uint64_t pos;
+    uint32_t nx, nxy;
+    bool pending = false;      // buffered last voxel of the in-half
+    uint32_t pj = 0;
+    double pl = 0.0;
+    int phase = 0;             // 0: in-half, 1: first out voxel, 2: rest of out-half
+    __device__ void emit(uint32_t j, double l) {
+        vidx[pos] = j;
+        l64[pos] = l;
+        ++pos;
+    }
+    __device__ void operator()(uint32_t x, uint32_t y, uint32_t z, double l) {
+        const uint32_t j = x + y * nx + z * nxy;
+        if (phase == 0) {
+            if (pending) emit(pj, pl);
+            pending = true;
+            pj = j;
+            pl = l;
+        } else if (phase == 1) {
+            if (pending) {
+                emit(pj, dadd(pl, l));  // voxelsIn.back().length += voxelsOut[0].length
+                pending = false;
+            }
+            phase = 2;
+        } else {
+            emit(j, l);
+        }
+    }
+};
+
+struct StraightSink {
+    uint32_t* vidx;
+    double* l64;
+    uint64_t pos;
+    uint32_t nx, nxy;
+    __device__ void operator()(uint32_t x, uint32_t y, uint32_t z, double l) {
+        vidx[pos] = x + y * nx + z * nxy;
+        l64[pos] = l;
+        ++pos;
+    }
+};
+
+template <typename Real>
+__global__ void k_path_fill(const muto_ray* __restrict__ rays, const uint32_t* __restrict__ kept,
+                            const double* __restrict__ scat, const uint64_t* __restrict__ off, uint64_t n, DevGrid g,
+                            int straight, uint32_t* __restrict__ vidx, double* __restrict__ l64, Real* __restrict__ L,
+                            Real* __restrict__ T) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t b = off[i], e = off[i + 1];
+    if (e == b) return;  // empty (or overflowed) path
+    const muto_ray& r = rays[kept[i]];
+    const double ps[3] = {scat[3 * i], scat[3 * i + 1], scat[3 * i + 2]};
+    const uint32_t nx = g.n[0], nxy = g.n[0] * g.n[1];
+    if (straight) {
+        StraightSink s{vidx, l64, b, nx, nxy};
+        siddon_walk(g, r.pin, r.pout, s);
+    } else {
+        FillSink s{vidx, l64, b, nx, nxy};
+        siddon_walk(g, r.pin, ps, s);
+        s.phase = 1;
+        siddon_walk(g, ps, r.pout, s);
+        if (s.pending) s.emit(s.pj, dadd(s.pl, 0.0));  // out-half empty: length += 0.0
+    }
+    // tail lengths, summed backwards in FP64 like src/MutoMLSD.cpp:407-413
+    double t = 0.0;
+    for (uint64_t k = e; k-- > b;) {
+        const double lk = l64[k];
+        if (L != reinterpret_cast<Real*>(l64)) L[k] = static_cast<Real>(lk);
+        T[k] = static_cast<Real>(t);
+        t = dadd(t, lk);
+    }
+}
+
+__global__ void k_voxel_hist(const uint32_t* __restrict__ vidx, uint64_t P, uint32_t V, uint32_t* __restrict__ mult,
+                             Counters* ctr) {
+    const uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    bool bad = false;
+    if (k < P) {
+        const uint32_t j = vidx[k];
+        if (j < V) atomicAdd(&mult[j], 1u);
+        else bad = true;
+    }
+    warp_count(&ctr->bounds, bad);
+}
+
+__global__ void k_assign_slots(const uint32_t* __restrict__ vidx, uint64_t P, uint32_t V,
+                               const uint64_t* __restrict__ start, uint32_t* __restrict__ cursor,
+                               uint32_t* __restrict__ slot) {
+    const uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k >= P) return;
+    const uint32_t j = vidx[k];
+    slot[k] = j < V ? static_cast<uint32_t>(start[j] + atomicAdd(&cursor[j], 1u)) : 0xffffffffu;
+}
+
+struct BatchSink {
+    uint32_t* xyz;
+    double* len;
+    uint64_t base;
+    uint32_t cap, k = 0;
+    __device__ void operator()(uint32_t x, uint32_t y, uint32_t z, double l) {
+        if (k < cap) {
+            xyz[(base + k) * 3 + 0] = x;
+            xyz[(base + k) * 3 + 1] = y;
+            xyz[(base + k) * 3 + 2] = z;
+            len[base + k] = l;
+        }
+        ++k;
+    }
+};
+
+__global__ void k_siddon_batch(DevGrid g, const double* __restrict__ p1, const double* __restrict__ p2, uint64_t n,
+                               uint32_t cap, uint32_t* __restrict__ xyz, double* __restrict__ len,
+                               uint32_t* __restrict__ counts) {
+    const uint64_t r = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const double a[3] = {p1[3 * r], p1[3 * r + 1], p1[3 * r + 2]};
+    const double b[3] = {p2[3 * r], p2[3 * r + 1], p2[3 * r + 2]};
+    BatchSink s{xyz, len, r * cap, cap};
+    const int c = siddon_walk(g, a, b, s);
+    counts[r] = c < 0 ? 0xffffffffu : static_cast<uint32_t>(c);
+}
+
+}  // namespace
+
+void launch_keep_flags(const muto_ray* rays, uint64_t n_total, muto_grid g, double eps, uint32_t* flags,
+                       cudaStream_t s) {
+    if (n_total == 0) return;
+    k_keep_flags<<<blocks_for(n_total), kThreads, 0, s>>>(rays, n_total, make_dev_grid(g), eps, flags); count_launches(1);
+}
+
+void launch_compact(const uint32_t* flags, const uint64_t* pos, uint64_t n, uint32_t* kept, cudaStream_t s) {
+    if (n == 0) return;
+    k_compact<<<blocks_for(n), kThreads, 0, s>>>(flags, pos, n, kept); count_launches(1);
+}
+
+template <typename Real>
+void launch_muon_info(const muto_ray* rays, const uint32_t* kept, uint64_t n, muto_grid g, double eps, int has_energy,
+                      typename Vec4<Real>::type* sd, Real* pr2, double* scat, double* pr_out, cudaStream_t s) {
+    if (n == 0) return;
+    k_muon_info<Real><<<blocks_for(n), kThreads, 0, s>>>(rays, kept, n, make_dev_grid(g), eps, has_energy, sd, pr2,
+                                                           scat, pr_out); count_launches(1);
+}
+template void launch_muon_info<float>(const muto_ray*, const uint32_t*, uint64_t, muto_grid, double, int, float4*,
+                                      float*, double*, double*, cudaStream_t);
+template void launch_muon_info<double>(const muto_ray*, const uint32_t*, uint64_t, muto_grid, double, int, double4*,
+                                       double*, double*, double*, cudaStream_t);
+
+void launch_path_count(const muto_ray* rays, const uint32_t* kept, const double* scat, uint64_t n, muto_grid g,
+                       int straight, uint32_t* counts, Counters* ctr, cudaStream_t s) {
+    if (n == 0) return;
+    k_path_count<<<blocks_for(n, 128), 128, 0, s>>>(rays, kept, scat, n, make_dev_grid(g), straight, counts, ctr); count_launches(1);
+}
+
+template <typename Real>
+void launch_path_fill(const muto_ray* rays, const uint32_t* kept, const double* scat, const uint64_t* off, uint64_t n,
+                      muto_grid g, int straight, uint32_t* vidx, double* l64, Real* L, Real* T, cudaStream_t s) {
+    if (n == 0) return;
+    k_path_fill<Real><<<blocks_for(n, 128), 128, 0, s>>>(rays, kept, scat, off, n, make_dev_grid(g), straight, vidx,
+                                                          l64, L, T); count_launches(1);
+}
+template void launch_path_fill<float>(const muto_ray*, const uint32_t*, const double*, const uint64_t*, uint64_t,
+                                      muto_grid, int, uint32_t*, double*, float*, float*, cudaStream_t);
+template void launch_path_fill<double>(const muto_ray*, const uint32_t*, const double*, const uint64_t*, uint64_t,
+                                       muto_grid, int, uint32_t*, double*, double*, double*, cudaStream_t);
+
+void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* mult, Counters* ctr, cudaStream_t s) {
+    if (P == 0) return;
+    k_voxel_hist<<<blocks_for(P), kThreads, 0, s>>>(vidx, P, V, mult, ctr); count_launches(1);
+}
+
+void launch_assign_slots(const uint32_t* vidx, uint64_t P, uint32_t V, const uint64_t* start, uint32_t* cursor,
+                         uint32_t* slot, cudaStream_t s) {
+    if (P == 0) return;
+    k_assign_slots<<<blocks_for(P), kThreads, 0, s>>>(vidx, P, V, start, cursor, slot); count_launches(1);
+}
+
+void launch_siddon_batch(muto_grid g, const double* p1, const double* p2, uint64_t n, uint32_t cap, uint32_t* xyz,
+                         double* len, uint32_t* counts, cudaStream_t s) {
+    if (n == 0) return;
+    k_siddon_batch<<<blocks_for(n, 128), 128, 0, s>>>(make_dev_grid(g), p1, p2, n, cap, xyz, len, counts); count_launches(1);
+}
+
+}  // namespace muto

@@ -1,0 +1,107 @@
+"""CPU tests: the C ABI library loads and exports every declared symbol, and
+the host-side logic (config parsing, image files, synthetic data) behaves.
+No kernel is launched here."""
+import ctypes as C
+import re
+
+import numpy as np
+import pytest
+
+import muontomography_gb300 as M
+from muontomography_gb300 import _lib
+
+
+def header_functions():
+    text = _lib.header_path().read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(muto_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_api():
+    names = header_functions()
+    for must in ("muto_create", "muto_reconstruct", "muto_siddon_batch", "muto_nll_backward", "muto_save_image"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in header_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_bindings_cover_the_header():
+    assert set(header_functions()) <= set(_lib.SIGNATURES), set(header_functions()) - set(_lib.SIGNATURES)
+
+
+@pytest.mark.parametrize("method,cfg,code", [
+    ("mlsd", "{not json", 2),
+    ("mlsd", '{"grid": {"nx": "ten"}}', 2),
+    ("mlsd", '{"precision": "half"}', 2),
+    ("mlsd", '{"grid": {"nx": 0}}', 2),
+    ("map", '{"num_iteration": -1}', 2),
+    ("mlsd", '{"update_with_mean": 3}', 2),
+    ("mlsd", '[1, 2]', 2),
+    ("slr", "{}", 1),
+])
+def test_config_errors_are_reported_before_any_device_call(lib, method, cfg, code):
+    h = C.c_void_p()
+    rc = lib.muto_create(method.encode(), cfg.encode(), C.byref(h))
+    assert rc == code
+    assert not h.value
+
+
+def test_lambda_from_x0(lib):
+    assert M.lambda_from_x0(17.57) == pytest.approx((0.0136 / 3.0) ** 2 / 17.57, rel=1e-15)
+
+
+@pytest.mark.parametrize("precision", [4, 8])
+def test_image_file_roundtrip_and_header_layout(tmp_path, precision):
+    g = M.Grid(5, 4, 3, -1.5, -2.0, -2.5, 0.5, 1.0, 1.5)
+    img = np.random.default_rng(0).uniform(0, 1e-6, g.nvox).reshape(g.shape, order="F")
+    p = tmp_path / "img.bin"
+    M.save_image(str(p), img, g, "mlsd", 123456, 50, precision)
+    raw = p.read_bytes()
+    assert len(raw) == 64 + g.nvox * precision
+    assert raw[0] == 64 and raw[1] == 1
+    assert raw[2:6] == b"mlsd" and raw[6:18] == b"\0" * 12
+    assert int.from_bytes(raw[18:22], "little") == 123456
+    assert int.from_bytes(raw[22:24], "little") == 50
+    assert int.from_bytes(raw[24:26], "little") == precision
+    assert [int.from_bytes(raw[26 + 2 * k:28 + 2 * k], "little") for k in range(3)] == [5, 4, 3]
+    assert np.frombuffer(raw[32:56], "<f4").tolist() == [-1.5, -2.0, -2.5, 0.5, 1.0, 1.5]
+    assert raw[56:64] == b"\0" * 8
+    back, hdr = M.load_image(str(p))
+    assert hdr["grid"] == g and hdr["method"] == "mlsd" and hdr["n_iter"] == 50 and hdr["precision"] == precision
+    want = img.astype(np.float32).astype(np.float64) if precision == 4 else img
+    assert np.array_equal(back, want)
+    data = np.frombuffer(raw[64:], "<f4" if precision == 4 else "<f8")
+    assert np.array_equal(data, want.reshape(-1, order="F"))  # column-major, x fastest
+
+
+def test_load_image_missing_file_is_an_io_error(tmp_path):
+    with pytest.raises(M.MutoError) as e:
+        M.load_image(str(tmp_path / "nope.bin"))
+    assert e.value.code == 6
+
+
+def test_generator_is_deterministic_per_muon():
+    g = M.Grid(8, 8, 8, -200.0, -200.0, -200.0, 50.0, 50.0, 50.0)
+    lam = M.phantom(g, [M.Block((-50, -50, -50), (50, 50, 50), M.X0_MM["iron"])])
+    a = M.generate(g, lam, 400, seed=7)
+    b = np.concatenate([M.generate(g, lam, 150, seed=7), M.generate(g, lam, 250, seed=7, first=150)])
+    assert np.array_equal(a, b)
+    c = M.generate(g, lam, 400, seed=8)
+    assert not np.array_equal(a, c)
+    # geometry: pin / pout on the grid's top / bottom faces, directions unit with d_z > 0
+    assert np.all(a[:, 4] == 200.0) and np.all(a[:, 7] == -200.0)
+    for k in (8, 11):
+        d = a[:, k:k + 3]
+        assert np.allclose(np.linalg.norm(d, axis=1), 1.0) and np.all(d[:, 2] > 0)
+    assert np.all((a[:, 0] >= 1.0) & (a[:, 0] <= 10.0))
+
+
+def test_phantom_voxel_centres():
+    g = M.Grid(4, 4, 4, 0.0, 0.0, 0.0, 10.0, 10.0, 10.0)
+    lam = M.phantom(g, [M.Block((0, 0, 0), (20, 20, 20), M.X0_MM["lead"])], M.X0_MM["air"])
+    img = lam.reshape(g.shape, order="F")
+    assert np.all(img[:2, :2, :2] == M.lambda_from_x0(M.X0_MM["lead"]))
+    assert img[2, 0, 0] == M.lambda_from_x0(M.X0_MM["air"])

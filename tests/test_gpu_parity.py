@@ -1,0 +1,237 @@
+"""GPU parity against the FP64 CPU oracle, through the C ABI.
+
+Bit-exact: Siddon voxel lists (indices and FP64 lengths), PoCA voxel of every
+ray, MLSD kept muons, merged path voxel indices and lengths.
+Tolerances: lambda after the same iteration count within 1e-10 relative L2
+(fp64 form; summation order of atomics / per-muon sums differs) and 1e-4
+(mixed form: FP32 lists and accumulation).
+"""
+import numpy as np
+import pytest
+
+import muontomography_gb300 as M
+from muontomography_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+MIXED_TOL = 1e-4
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def random_segments(n, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(lo, hi, size=(n, 3)), rng.uniform(lo, hi, size=(n, 3))
+
+
+# ---------------------------------------------------------------------------
+# Siddon
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("seed", [0, 1])
+def test_siddon_random_segments_bit_exact(gpu, oracle, seed):
+    # the reference's own Siddon probe geometry: 100^3 voxels of 2 mm at -100,
+    # segments uniform in [-500, 500]^3 (test/SiddonTest.cpp:8-17)
+    grid = M.Grid(100, 100, 100, -100.0, -100.0, -100.0, 2.0, 2.0, 2.0)
+    p1, p2 = random_segments(20000, -500.0, 500.0, seed)
+    cap = 512
+    gx, gl, gc = M.siddon_batch(grid, p1, p2, cap)
+    ox, ol, oc = oracle.siddon_batch(grid, p1, p2, cap)
+    assert np.array_equal(gc, oc)
+    assert (oc > 0).sum() > 1000
+    for r in np.nonzero(oc)[0]:
+        k = oc[r]
+        assert np.array_equal(gx[r, :k], ox[r, :k]), r
+        assert np.array_equal(gl[r, :k].view(np.uint64), ol[r, :k].view(np.uint64)), r
+
+
+def test_siddon_edge_cases_bit_exact(gpu, oracle):
+    grid = M.Grid(10, 10, 10, 0.0, 0.0, 0.0, 10.0, 10.0, 10.0)
+    segs = [
+        ((5.0, 5.0, 120.0), (5.0, 5.0, -20.0)),      # axis aligned, through centres
+        ((0.0, 0.0, 100.0), (100.0, 100.0, 0.0)),    # exact diagonal through corners
+        ((10.0, 10.0, 100.0), (10.0, 10.0, 0.0)),    # along a voxel edge
+        ((0.0, 50.0, 50.0), (100.0, 50.0, 50.0)),    # grazing a face
+        ((-5.0, 5.0, 5.0), (-5.0, 95.0, 95.0)),      # parallel to x outside: empty
+        ((50.0, 50.0, 50.0), (50.0, 50.0, 50.0)),    # degenerate point
+        ((100.0, 100.0, 100.0), (0.0, 0.0, 0.0)),    # reversed diagonal
+        ((33.3, 66.6, 99.9), (33.3000001, 66.6, 0.1)),
+        ((50.0, 50.0, 150.0), (51.0, 49.0, 40.0)),   # ends inside
+        ((-50.0, -50.0, -50.0), (150.0, 150.0, 150.0)),
+    ]
+    p1 = np.array([s[0] for s in segs])
+    p2 = np.array([s[1] for s in segs])
+    gx, gl, gc = M.siddon_batch(grid, p1, p2, 64)
+    ox, ol, oc = oracle.siddon_batch(grid, p1, p2, 64)
+    assert np.array_equal(gc, oc)
+    assert np.array_equal(gx, ox)
+    assert np.array_equal(gl.view(np.uint64), ol.view(np.uint64))
+
+
+# ---------------------------------------------------------------------------
+# PoCA
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("length_weighted,straight", [(True, False), (False, False), (True, True)])
+def test_poca_assignment_bit_exact(gpu, oracle, length_weighted, straight):
+    wl = W.small(n_muons=20000, seed=21)
+    rays = wl.tracks()
+    cfg = wl.poca_config(length_weighted=length_weighted, straight_line=straight)
+    ref_img, ref_assign, ref_cnt = oracle.poca(wl.grid, cfg, rays)
+    with M.MutoPoCA(cfg) as rec:
+        img = rec.reconstruct(rays)
+        assign = rec.poca_assignment(rays.shape[0])
+        st = rec.status()
+    assert np.array_equal(assign, ref_assign)
+    assert st["n_scat_in_grid"] == ref_cnt[2]
+    assert st["n_not_parallel"] == ref_cnt[1]
+    flat = img.reshape(-1, order="F")
+    assert rel_l2(flat, ref_img) < 1e-12
+
+
+# ---------------------------------------------------------------------------
+# MLSD
+# ---------------------------------------------------------------------------
+def _mlsd_pair(oracle, wl, rays, cfg, init, n_iter, method="mlsd"):
+    ref = oracle.Mlsd(wl.grid, cfg, rays, init, method=method)
+    ref.iterate(n_iter)
+    return ref
+
+
+@pytest.mark.parametrize("straight", [False, True])
+def test_mlsd_paths_bit_exact(gpu, oracle, straight):
+    wl = W.small(n_muons=6000, seed=31)
+    rays = wl.tracks()
+    cfg = wl.em_config(precision="fp64", straight_line=straight)
+    init = np.full(wl.grid.nvox, 1e-7)
+    ref = oracle.Mlsd(wl.grid, cfg, rays, init)
+    r = ref.export()
+    with M.MutoMLSD(cfg) as rec:
+        rec.load_tracks(rays)
+        rec.prepare()
+        g = rec.export_paths()
+    assert np.array_equal(g["kept"], r["kept"])
+    assert np.array_equal(g["off"], r["off"])
+    assert np.array_equal(g["idx"], r["idx"])
+    assert np.array_equal(g["len"].view(np.uint64), r["len"].view(np.uint64))
+    assert np.array_equal(g["tail"].view(np.uint64), r["tail"].view(np.uint64))
+    np.testing.assert_allclose(g["info"][:, :5], r["info"][:, :5], rtol=1e-13, atol=1e-15)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+@pytest.mark.parametrize("mode", ["median", "mean", "percentile"])
+def test_mlsd_lambda_matches_oracle(gpu, oracle, precision, tol, mode):
+    wl = W.small(n_muons=8000, seed=41)
+    rays = wl.tracks()
+    over = {"median": {}, "mean": {"update_with_mean": True},
+            "percentile": {"update_with_mean": True, "mean_percentile": 90}}[mode]
+    n_iter = 6
+    cfg = wl.em_config(precision=precision, num_iteration=n_iter, **over)
+    init = np.full(wl.grid.nvox, 1e-7)
+    ref = _mlsd_pair(oracle, wl, rays, cfg, init, n_iter)
+    with M.MutoMLSD(cfg) as rec:
+        img = rec.reconstruct(rays)
+        st = rec.status()
+    assert st["iterations_done"] == n_iter
+    assert rel_l2(img.reshape(-1, order="F"), ref.image()) < tol
+
+
+def test_mlsd_cost_and_early_stop(gpu, oracle):
+    wl = W.small(n_muons=5000, seed=51)
+    rays = wl.tracks()
+    cfg = wl.em_config(precision="fp64", num_iteration=8, early_stop=True)
+    init = np.full(wl.grid.nvox, 1e-7)
+    ref = _mlsd_pair(oracle, wl, rays, cfg, init, 8)
+    with M.MutoMLSD(cfg) as rec:
+        img = rec.reconstruct(rays)
+        st = rec.status()
+    rc = ref.counts()
+    assert st["iterations_done"] == rc["iterations_done"]
+    assert abs(st["cost"] - ref.costs()[-1]) <= 1e-9 * abs(ref.costs()[-1])
+    assert rel_l2(img.reshape(-1, order="F"), ref.image()) < FP64_TOL
+
+
+def test_mlsd_initial_image_grid_adoption(gpu, oracle):
+    # an initial image whose nx/ny/nz differ from the config replaces the grid
+    wl = W.small(n_muons=3000, seed=61, n=10)
+    rays = wl.tracks()
+    cfg = wl.em_config(precision="fp64", num_iteration=3, initialize_method=0)
+    cfg["grid"] = dict(cfg["grid"], nx=7, ny=7, nz=7)
+    init = np.full(wl.grid.nvox, 2e-7)
+    ref = _mlsd_pair(oracle, wl, rays, wl.em_config(precision="fp64"), init, 3)
+    with M.MutoMLSD(cfg) as rec:
+        rec.set_initial_image(init, wl.grid)
+        img = rec.reconstruct(rays)
+        assert rec.get_current_grid() == wl.grid
+    assert rel_l2(img.reshape(-1, order="F"), ref.image()) < FP64_TOL
+
+
+def test_mlsd_total_num_rays_and_no_energy(gpu, oracle):
+    wl = W.small(n_muons=5000, seed=71)
+    rays = wl.tracks()
+    cfg = wl.em_config(precision="fp64", num_iteration=4, total_num_rays=2500, has_energy=False)
+    init = np.full(wl.grid.nvox, 1e-7)
+    ref = _mlsd_pair(oracle, wl, rays, cfg, init, 4)
+    with M.MutoMLSD(cfg) as rec:
+        img = rec.reconstruct(rays)
+        st = rec.status()
+    assert st["n_scat_in_grid"] == ref.counts()["n_scat_in_grid"]
+    assert rel_l2(img.reshape(-1, order="F"), ref.image()) < FP64_TOL
+
+
+def test_graph_and_eager_agree(gpu):
+    wl = W.small(n_muons=5000, seed=81)
+    rays = wl.tracks()
+    out = []
+    for g in (True, False):
+        cfg = wl.em_config(precision="fp64", num_iteration=5, use_graph=g, update_with_mean=True)
+        with M.MutoMLSD(cfg) as rec:
+            out.append(rec.reconstruct(rays))
+    assert rel_l2(out[0], out[1]) < 1e-12
+
+
+# ---------------------------------------------------------------------------
+# MAP
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("p,all_nb,obj", [(1.0, False, False), (2.0, True, False), (1.0, True, True)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", MIXED_TOL)])
+def test_map_matches_oracle(gpu, oracle, p, all_nb, obj, precision, tol):
+    wl = W.small(n_muons=6000, seed=91)
+    rays = wl.tracks()
+    cfg = wl.em_config(precision=precision, num_iteration=4, beta=0.01, p=p, delta=0.1, all_neighbours=all_nb,
+                       add_object_prior=obj)
+    init = np.full(wl.grid.nvox, 1e-7)
+    ref = _mlsd_pair(oracle, wl, rays, cfg, init, 4, method="map")
+    with M.MutoMAP(cfg) as rec:
+        img = rec.reconstruct(rays)
+        st = rec.status()
+    assert st["n_nonconverged"] == 0
+    assert rel_l2(img.reshape(-1, order="F"), ref.image()) < tol
+
+
+# ---------------------------------------------------------------------------
+# Adjoint
+# ---------------------------------------------------------------------------
+def test_nll_and_gradient_match_oracle(gpu, oracle):
+    wl = W.small(n_muons=6000, seed=101)
+    rays = wl.tracks()
+    cfg = wl.em_config(precision="fp64", num_iteration=0)
+    init = np.full(wl.grid.nvox, 1e-7)
+    ref = oracle.Mlsd(wl.grid, cfg, rays, init)
+    rng = np.random.default_rng(0)
+    lam = wl.lam() * rng.uniform(0.5, 1.5, wl.grid.nvox) + 1e-9
+    with M.MutoMLSD(cfg) as rec:
+        rec.load_tracks(rays)
+        rec.prepare()
+        mult = rec.multiplicity()
+        lam = np.where(mult > 0, lam, 0.0)
+        x = np.log(np.where(mult > 0, lam, 1.0))
+        v, g = rec.nll_grad(x)
+        v2 = rec.nll(x)
+    rv, rg = ref.nll(lam, grad=True)
+    assert abs(v - rv) <= 1e-10 * abs(rv)
+    assert abs(v2 - rv) <= 1e-10 * abs(rv)
+    assert rel_l2(g, rg) < 1e-9
