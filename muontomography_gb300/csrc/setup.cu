@@ -104,15 +104,17 @@ __global__ void k_path_count(const muto_ray* __restrict__ rays, const uint32_t* 
 struct FillSink {
     uint32_t* vidx;
     double* l64;
-    uint64_t pos;
+    uint64_t pos, end;  // the muon's segment [pos, end) from the count pass
     uint32_t nx, nxy;
     bool pending = false;      // buffered last voxel of the in-half
     uint32_t pj = 0;
     double pl = 0.0;
     int phase = 0;             // 0: in-half, 1: first out voxel, 2: rest of out-half
     __device__ void emit(uint32_t j, double l) {
-        vidx[pos] = j;
-        l64[pos] = l;
+        if (pos < end) {  // the fill walk repeats the count walk exactly; never past the segment
+            vidx[pos] = j;
+            l64[pos] = l;
+        }
         ++pos;
     }
     __device__ void operator()(uint32_t x, uint32_t y, uint32_t z, double l) {
@@ -137,11 +139,13 @@ struct FillSink {
 struct StraightSink {
     uint32_t* vidx;
     double* l64;
-    uint64_t pos;
+    uint64_t pos, end;
     uint32_t nx, nxy;
     __device__ void operator()(uint32_t x, uint32_t y, uint32_t z, double l) {
-        vidx[pos] = x + y * nx + z * nxy;
-        l64[pos] = l;
+        if (pos < end) {
+            vidx[pos] = x + y * nx + z * nxy;
+            l64[pos] = l;
+        }
         ++pos;
     }
 };
@@ -159,10 +163,10 @@ __global__ void k_path_fill(const muto_ray* __restrict__ rays, const uint32_t* _
     const double ps[3] = {scat[3 * i], scat[3 * i + 1], scat[3 * i + 2]};
     const uint32_t nx = g.n[0], nxy = g.n[0] * g.n[1];
     if (straight) {
-        StraightSink s{vidx, l64, b, nx, nxy};
+        StraightSink s{vidx, l64, b, e, nx, nxy};
         siddon_walk(g, r.pin, r.pout, s);
     } else {
-        FillSink s{vidx, l64, b, nx, nxy};
+        FillSink s{vidx, l64, b, e, nx, nxy};
         siddon_walk(g, r.pin, ps, s);
         s.phase = 1;
         siddon_walk(g, ps, r.pout, s);
