@@ -1,0 +1,14 @@
+#!/bin/sh
+# Compile the reference's reconstruction sources in place against the
+# stand-in headers in oracle/ref_shim, into oracle/_ref/libmuto_ref.so.
+# Only possible where the reference tree is mounted; test infrastructure only.
+set -e
+HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${MUTO_REFERENCE:-/root/reference}
+[ -d "$REF/src" ] || { echo "reference sources not found at $REF" >&2; exit 2; }
+mkdir -p "$HERE/_ref"
+g++ -O2 -std=c++14 -fPIC -shared -fopenmp -ffp-contract=off -fno-fast-math -w \
+    -I "$HERE/ref_shim" -I "$REF/include" \
+    "$REF/src/MutoSiddon.cpp" "$REF/src/MutoPoCA.cpp" "$REF/src/MutoMLSD.cpp" "$REF/src/MutoMAP.cpp" \
+    "$HERE/ref_harness.cpp" -o "$HERE/_ref/libmuto_ref.so"
+echo "built $HERE/_ref/libmuto_ref.so"

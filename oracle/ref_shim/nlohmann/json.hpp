@@ -1,0 +1,46 @@
+// Stand-in for the part of nlohmann::json the reference's reconstruction
+// sources and include/MutoConfig.h use (at, value with a typed default,
+// operator[], find/end, dump, stream input, out_of_range), over this
+// project's own JSON reader.  TEST INFRASTRUCTURE ONLY.
+#pragma once
+
+#include <istream>
+#include <iterator>
+#include <string>
+
+#include "../../../muontomography_gb300/csrc/json.hpp"
+
+namespace nlohmann {
+
+class json {
+public:
+    typedef muto::json::out_of_range out_of_range;
+    typedef json value_type;
+    struct iter {
+        bool found;
+        bool operator!=(const iter& o) const { return found != o.found; }
+        bool operator==(const iter& o) const { return found == o.found; }
+    };
+    json() {}
+    json(const muto::json& v) : v_(v) {}
+    static json parse(const std::string& s) { return json(muto::json::parse(s)); }
+    json at(const std::string& k) const { return json(v_.at(k)); }
+    json operator[](const std::string& k) const { return json(v_[k]); }
+    iter find(const std::string& k) const { return iter{v_.contains(k)}; }
+    iter end() const { return iter{false}; }
+    std::string dump() const { return v_.dump(); }
+    int value(const std::string& k, int d) const { return v_.value(k, d); }
+    double value(const std::string& k, double d) const { return v_.value(k, d); }
+    bool value(const std::string& k, bool d) const { return v_.value(k, d); }
+    std::string value(const std::string& k, const char* d) const { return v_.value(k, d); }
+    friend std::istream& operator>>(std::istream& in, json& j) {
+        std::string s((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+        j.v_ = muto::json::parse(s);
+        return in;
+    }
+
+private:
+    muto::json v_;
+};
+
+}  // namespace nlohmann

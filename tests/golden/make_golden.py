@@ -1,0 +1,104 @@
+"""Generate the golden vectors in tests/golden/ from the reference itself.
+
+The reference's reconstruction sources (src/MutoSiddon.cpp, src/MutoPoCA.cpp,
+src/MutoMLSD.cpp, src/MutoMAP.cpp) are compiled in place by
+oracle/build_ref.sh and called through oracle/reference.py; the inputs
+(segments, synthetic tracks) are stored next to the outputs so the tests need
+neither the reference nor the generator.  Run where the reference tree is
+mounted:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+import muontomography_gb300 as M  # noqa: E402
+from muontomography_gb300 import workloads as W  # noqa: E402
+from oracle import reference as R  # noqa: E402
+
+
+def siddon_case():
+    # the reference's Siddon probe geometry (test/SiddonTest.cpp:8-17): 100^3 voxels
+    # of 2 mm at -100, segments uniform in [-500, 500]^3; keep the ones that hit
+    g = M.Grid(100, 100, 100, -100.0, -100.0, -100.0, 2.0, 2.0, 2.0)
+    rng = np.random.default_rng(2024)
+    p1, p2 = rng.uniform(-500, 500, (6000, 3)), rng.uniform(-500, 500, (6000, 3))
+    _, _, cnt = R.siddon(g, p1, p2, 512)
+    sel = np.nonzero(cnt)[0][:400]
+    # plus hand-made edge cases on a 10^3 grid of 10 mm scaled into this grid
+    edge = np.array([[[0.0, 0.0, 90.0], [0.0, 0.0, -110.0]],        # along a voxel edge line
+                     [[-100.0, -100.0, -100.0], [100.0, 100.0, 100.0]],  # main diagonal
+                     [[100.0, 100.0, 100.0], [-100.0, -100.0, -100.0]],
+                     [[-100.0, 0.0, 0.0], [100.0, 0.0, 0.0]],          # grazing the x axis plane
+                     [[-50.0, 150.0, 7.0], [-50.0, -150.0, 7.0]],
+                     [[13.0, 13.0, 13.0], [13.0, 13.0, 13.0]]])        # degenerate
+    p1 = np.concatenate([p1[sel], edge[:, 0]])
+    p2 = np.concatenate([p2[sel], edge[:, 1]])
+    xyz, ln, cnt = R.siddon(g, p1, p2, 512)
+    k = int(cnt.max())
+    return {"grid": np.array([g.nx, g.ny, g.nz, g.x_min, g.y_min, g.z_min, g.dx, g.dy, g.dz]), "p1": p1, "p2": p2,
+            "xyz": xyz[:, :k], "len": ln[:, :k], "count": cnt}
+
+
+def track_case():
+    wl = W.small(n_muons=2500, seed=4242, n=10)
+    rays = wl.tracks()
+    g = wl.grid
+    out = {"grid": np.array([g.nx, g.ny, g.nz, g.x_min, g.y_min, g.z_min, g.dx, g.dy, g.dz]), "rays": rays}
+    configs = {}
+    for name, cfg in {"poca_lw": wl.poca_config(length_weighted=True),
+                      "poca_dz": wl.poca_config(length_weighted=False),
+                      "poca_straight": wl.poca_config(straight_line=True)}.items():
+        img, _ = R.reconstruct("poca", cfg, rays, g.nvox)
+        out[name] = img
+        configs[name] = cfg
+    cfg = wl.em_config()
+    p = R.mlsd_paths(cfg, rays)
+    for k, v in p.items():
+        out["paths_" + k] = v
+    configs["paths"] = cfg
+    em = {"mlsd_median": ("mlsd", wl.em_config(num_iteration=6)),
+          "mlsd_mean": ("mlsd", wl.em_config(num_iteration=6, update_with_mean=True)),
+          "mlsd_pct90": ("mlsd", wl.em_config(num_iteration=6, update_with_mean=True, mean_percentile=90)),
+          "mlsd_straight": ("mlsd", wl.em_config(num_iteration=4, straight_line=True)),
+          "mlsd_noenergy": ("mlsd", wl.em_config(num_iteration=4, has_energy=False)),
+          "map_p1_6": ("map", wl.em_config(num_iteration=4, beta=0.01, p=1.0, delta=0.1)),
+          "map_p2_26": ("map", wl.em_config(num_iteration=4, beta=0.01, p=2.0, delta=0.1, all_neighbours=True)),
+          "map_p1_26_obj": ("map", wl.em_config(num_iteration=3, beta=0.005, p=1.0, delta=0.2, all_neighbours=True,
+                                                add_object_prior=True))}
+    for name, (method, cfg) in em.items():
+        img, _ = R.reconstruct(method, cfg, rays, g.nvox)
+        out[name] = img
+        configs[name] = {"method": method, **cfg}
+    # PoCA-seeded EM through an initial image (initialize_method 0), as the example configs chain them
+    seed_img = out["poca_lw"].astype(np.float32).astype(np.float64)
+    R.set_initial_image(seed_img, g)
+    cfg = wl.em_config(num_iteration=5, initialize_method=0, initial_image_file="poca.bin")
+    img, _ = R.reconstruct("mlsd", cfg, rays, g.nvox)
+    R.set_initial_image(None)
+    out["mlsd_poca_seeded"] = img
+    out["poca_seed_image"] = seed_img
+    configs["mlsd_poca_seeded"] = {"method": "mlsd", **cfg}
+    return out, configs
+
+
+def main() -> None:
+    if not R.available():
+        raise SystemExit("reference sources are not mounted here")
+    R.build()
+    np.savez_compressed(HERE / "siddon.npz", **siddon_case())
+    tracks, configs = track_case()
+    np.savez_compressed(HERE / "tracks.npz", **tracks)
+    (HERE / "configs.json").write_text(json.dumps(configs, indent=1, sort_keys=True))
+    print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
+
+
+if __name__ == "__main__":
+    main()

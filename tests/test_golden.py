@@ -1,0 +1,133 @@
+"""Golden vectors produced by the reference's own code (tests/golden/make_golden.py).
+
+CPU: the oracle reproduces every golden vector bit for bit.
+GPU: the CUDA path reproduces the voxel lists and paths bit for bit and the
+images within the stated tolerances.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import muontomography_gb300 as M
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def load():
+    s = dict(np.load(GOLD / "siddon.npz"))
+    t = dict(np.load(GOLD / "tracks.npz"))
+    cfgs = json.loads((GOLD / "configs.json").read_text())
+    return s, t, cfgs
+
+
+def grid_of(a):
+    return M.Grid(int(a[0]), int(a[1]), int(a[2]), *map(float, a[3:]))
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float64).view(np.uint64)
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-300))
+
+
+S, T, CFG = load()
+EM_CASES = [k for k in CFG if k.startswith(("mlsd_", "map_"))]
+
+
+# ----------------------------------------------------------------- oracle pin
+def test_oracle_siddon_matches_golden(oracle):
+    g = grid_of(S["grid"])
+    cap = S["xyz"].shape[1]
+    xyz, ln, cnt = oracle.siddon_batch(g, S["p1"], S["p2"], cap)
+    assert np.array_equal(cnt, S["count"])
+    assert np.array_equal(xyz, S["xyz"])
+    assert np.array_equal(bits(ln), bits(S["len"]))
+
+
+@pytest.mark.parametrize("name", ["poca_lw", "poca_dz", "poca_straight"])
+def test_oracle_poca_matches_golden(oracle, name):
+    img, _, _ = oracle.poca(grid_of(T["grid"]), CFG[name], T["rays"])
+    assert np.array_equal(bits(img), bits(T[name]))
+
+
+def test_oracle_paths_match_golden(oracle):
+    g = grid_of(T["grid"])
+    e = oracle.Mlsd(g, CFG["paths"], T["rays"], np.full(g.nvox, 1e-7)).export()
+    for k in ("kept", "off", "idx"):
+        assert np.array_equal(e[k], T["paths_" + k]), k
+    for k in ("len", "tail", "info"):
+        assert np.array_equal(bits(e[k]), bits(T["paths_" + k])), k
+
+
+@pytest.mark.parametrize("name", EM_CASES)
+def test_oracle_em_matches_golden(oracle, name):
+    cfg = dict(CFG[name])
+    method = cfg.pop("method")
+    g = grid_of(T["grid"])
+    init = T["poca_seed_image"] if cfg.get("initialize_method") == 0 else np.full(g.nvox, cfg["initialize_value"])
+    m = oracle.Mlsd(g, cfg, T["rays"], init, method=method)
+    m.iterate(cfg["num_iteration"])
+    assert np.array_equal(bits(m.image()), bits(T[name]))
+
+
+def test_reference_build_still_matches_oracle_when_mounted(oracle):
+    from oracle import reference as R
+
+    if not R.available():
+        pytest.skip("reference sources not mounted (GPU box)")
+    g = grid_of(S["grid"])
+    a = R.siddon(g, S["p1"], S["p2"], S["xyz"].shape[1])
+    assert np.array_equal(a[2], S["count"]) and np.array_equal(bits(a[1]), bits(S["len"]))
+
+
+# ------------------------------------------------------------------ GPU path
+@pytest.mark.gpu
+def test_gpu_siddon_matches_golden(gpu):
+    g = grid_of(S["grid"])
+    cap = S["xyz"].shape[1]
+    xyz, ln, cnt = M.siddon_batch(g, S["p1"], S["p2"], cap)
+    assert np.array_equal(cnt, S["count"])
+    assert np.array_equal(xyz, S["xyz"])
+    assert np.array_equal(bits(ln), bits(S["len"]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["poca_lw", "poca_dz", "poca_straight"])
+def test_gpu_poca_matches_golden(gpu, name):
+    with M.MutoPoCA(CFG[name]) as rec:
+        img = rec.reconstruct(T["rays"]).reshape(-1, order="F")
+    assert rel_l2(img, T[name]) < 1e-12
+    assert np.array_equal(img > 0, T[name] > 0)
+
+
+@pytest.mark.gpu
+def test_gpu_paths_match_golden(gpu):
+    cfg = dict(CFG["paths"], precision="fp64")
+    with M.MutoMLSD(cfg) as rec:
+        rec.load_tracks(T["rays"])
+        rec.prepare()
+        e = rec.export_paths()
+    for k in ("kept", "off", "idx"):
+        assert np.array_equal(e[k], T["paths_" + k]), k
+    for k in ("len", "tail"):
+        assert np.array_equal(bits(e[k]), bits(T["paths_" + k])), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-4)])
+@pytest.mark.parametrize("name", EM_CASES)
+def test_gpu_em_matches_golden(gpu, name, precision, tol):
+    cfg = dict(CFG[name])
+    method = cfg.pop("method")
+    cfg["precision"] = precision
+    g = grid_of(T["grid"])
+    with M.Reconstruction(method, cfg) as rec:
+        if cfg.get("initialize_method") == 0:
+            rec.set_initial_image(T["poca_seed_image"], g)
+        rec._n_iter = cfg["num_iteration"]
+        img = rec.reconstruct(T["rays"]).reshape(-1, order="F")
+    assert rel_l2(img, T[name]) < tol
