@@ -62,7 +62,7 @@ struct Counters {
     unsigned long long not_parallel;
     unsigned long long in_grid;
     unsigned long long iteration;   // device iteration index (graph replays)
-    unsigned long long pad;
+    unsigned long long timeouts;    // bounded waits that gave up (never expected)
     double cost_sum;                // cost of the current iteration
     double cost_last;               // mean cost of the last finished iteration
     double cost_prev;               // mean cost of the one before
@@ -140,6 +140,9 @@ size_t em_tile_smem_bytes(int tile_pairs, int tile_muons);
 // sets the dynamic shared-memory limit of every k_em_tile variant (call outside graph capture)
 template <typename Real>
 cudaError_t em_tile_configure(int tile_pairs, int tile_muons);
+// resident CTAs per SM (persistent grid = this x SM count)
+template <typename Real>
+int em_tile_blocks(int tile_pairs, int tile_muons, int group);
 
 template <typename Real, typename OutT>
 void launch_select(const Real* S, const uint64_t* start, const uint32_t* mult, uint32_t V, int use_mean,

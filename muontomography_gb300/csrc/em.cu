@@ -10,65 +10,121 @@
 //  k_map_voxel  MAP surrogate step (src/MutoMAP.cpp:228-247 with :207-406).
 //
 // Work layout of k_em_tile.  Kept muons are cut into tiles of consecutive
-// muons whose pairs (voxel index, L, T) fit in shared memory.  A CTA stages a
-// tile with coalesced streaming loads (each pair is read from HBM exactly once
-// per iteration), then:
-//   phase 1  GROUP lanes per muon gather lambda_j (L2-resident) and sum
-//            lambda_j * W_ij in the storage precision;
-//   phase 2  one thread per muon does the FP64 2x2 algebra: Sigma = pr^2 sum + E,
-//            det, inverse, cost, and folds everything the pairs need into three
-//            coefficients k so that, for W = [[W00,W01],[W01,W11]],
+// muons whose pairs fit in shared memory.  A CTA loops over tiles:
+//   stage    one thread issues bulk asynchronous copies (cp.async.bulk, the
+//            TMA engine) of the tile's contiguous per-pair arrays (voxel index,
+//            L, T, slot) and per-muon arrays (offsets, S/D, pr^2) into shared
+//            memory, completing on an mbarrier; every pair byte is read from
+//            HBM exactly once per iteration.  Ranges are widened to 16-byte
+//            boundaries (the arrays carry padding for that).
+//   gather   every thread fetches lambda_j for 8 pairs at once (L2-resident).
+//   sum      GROUP lanes per muon sum lambda_j * W_ij from shared memory.
+//   2x2      one thread per muon: Sigma = pr^2 sum + E, determinant and
+//            inverse in FP64, cost, and three coefficients k with
 //              pr^2 (1/2 xyS_ij - tr(Sigma^-1 W_ij)) = k0 W00 + k1 W01 + k2 W11
-//            (xyS = sum over the x and y planes of u^T W u with u = Sigma^-1 (S, D)).
-//   phase 3  one thread per pair: g_ij from the k's and s_ij = 2 l + g l^2,
-//            written to its voxel-major slot (median) or added to the voxel's
-//            sum of g (mean / gradient).
-// s_ij equals the reference's 2 l + (1/2 xyS - tr) pr^2 l^2 term by term.
+//            (xyS = sum over the x and y planes of u^T W u, u = Sigma^-1 (S, D)).
+//   scatter  one thread per pair: g_ij and s_ij = 2 l + g l^2 written to the
+//            pair's voxel-major slot (median / percentile) or g_ij added to the
+//            voxel's sum (mean / gradient).
+// Several CTAs per SM overlap one CTA's copies with another's arithmetic.
 #include "common.cuh"
 
 namespace muto {
 namespace {
 
 constexpr int kTileThreads = 256;
+constexpr int kGatherUnroll = 8;
 
+// per-tile shared-memory layout; per-pair buffers hold TP + 8 entries (the
+// tile's range widened to 16-byte boundaries at both ends)
 template <typename Real>
 struct TileLayout {
-    size_t off, sd, pr2, sig, k, idx, L, T, lam, mu, total;
+    size_t off, sd, pr2, idx, L, T, slot, lam, mu, sig, k, bar, total;
     __host__ __device__ TileLayout(int TP, int TM) {
         auto up = [](size_t x) { return (x + 15) & ~static_cast<size_t>(15); };
         size_t p = 0;
-        off = p; p = up(p + sizeof(uint32_t) * (TM + 1));
-        sd = p;  p = up(p + sizeof(typename Vec4<Real>::type) * TM);
-        pr2 = p; p = up(p + sizeof(Real) * TM);
-        sig = p; p = up(p + sizeof(Real) * 3 * TM);
-        k = p;   p = up(p + sizeof(Real) * 3 * TM);
-        idx = p; p = up(p + sizeof(uint32_t) * TP);
-        L = p;   p = up(p + sizeof(Real) * TP);
-        T = p;   p = up(p + sizeof(Real) * TP);
-        lam = p; p = up(p + sizeof(Real) * TP);
-        mu = p;  p = up(p + sizeof(uint16_t) * TP);
+        off = p;  p = up(p + sizeof(uint64_t) * (TM + 4));
+        sd = p;   p = up(p + sizeof(typename Vec4<Real>::type) * TM);
+        pr2 = p;  p = up(p + sizeof(Real) * (TM + 8));
+        idx = p;  p = up(p + sizeof(uint32_t) * (TP + 8));
+        L = p;    p = up(p + sizeof(Real) * (TP + 8));
+        T = p;    p = up(p + sizeof(Real) * (TP + 8));
+        slot = p; p = up(p + sizeof(uint32_t) * (TP + 8));
+        lam = p;  p = up(p + sizeof(Real) * TP);
+        mu = p;   p = up(p + sizeof(uint16_t) * TP);
+        sig = p;  p = up(p + sizeof(Real) * 3 * TM);
+        k = p;    p = up(p + sizeof(Real) * 3 * TM);
+        bar = p;  p = up(p + sizeof(uint64_t));
         total = p;
     }
 };
 
-template <typename Real> __device__ __forceinline__ Real ld_stream(const Real* p) { return __ldcs(p); }
-__device__ __forceinline__ uint32_t ld_stream_u32(const uint32_t* p) { return __ldcs(p); }
+// --- TMA bulk copy + mbarrier (PTX) -----------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// global -> shared bulk copy; dst, src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// The element range [b, e) of an array of `size`-byte elements widened to
+// 16-byte boundaries: returns the first element and the byte count.
+__device__ __forceinline__ void widen(uint64_t b, uint64_t e, uint32_t size, uint64_t* first, uint32_t* bytes) {
+    const uint64_t per = 16 / size;
+    const uint64_t f = b - b % per;
+    const uint64_t l = ((e + per - 1) / per) * per;
+    *first = f;
+    *bytes = static_cast<uint32_t>((l - f) * size);
+}
+
+// Bounded wait on the tile barrier; false (and a recorded timeout) if the
+// copies did not land within the limit.
+__device__ __forceinline__ bool wait_tile(uint64_t* bar, uint32_t parity, Counters* ctr) {
+    for (uint32_t spin = 0; spin < (1u << 22); ++spin)
+        if (mbar_try_wait(bar, parity)) return true;
+    if (threadIdx.x == 0) atomicAdd(&ctr->timeouts, 1ull);
+    return false;
+}
 
 template <typename Real, int GROUP>
-__global__ void __launch_bounds__(kTileThreads, 2) k_em_tile(EmArgs<Real> a, int TP, int TM) {
+__global__ void __launch_bounds__(kTileThreads, 3) k_em_tile(EmArgs<Real> a, int TP, int TM) {
     using R4 = typename Vec4<Real>::type;
-    extern __shared__ __align__(16) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     const TileLayout<Real> lay(TP, TM);
-    uint32_t* s_off = reinterpret_cast<uint32_t*>(smem + lay.off);
+    uint64_t* s_off = reinterpret_cast<uint64_t*>(smem + lay.off);
     R4* s_sd = reinterpret_cast<R4*>(smem + lay.sd);
     Real* s_pr2 = reinterpret_cast<Real*>(smem + lay.pr2);
-    Real* s_sig = reinterpret_cast<Real*>(smem + lay.sig);
-    Real* s_k = reinterpret_cast<Real*>(smem + lay.k);
     uint32_t* s_idx = reinterpret_cast<uint32_t*>(smem + lay.idx);
     Real* s_L = reinterpret_cast<Real*>(smem + lay.L);
     Real* s_T = reinterpret_cast<Real*>(smem + lay.T);
+    uint32_t* s_slot = reinterpret_cast<uint32_t*>(smem + lay.slot);
     Real* s_lam = reinterpret_cast<Real*>(smem + lay.lam);
     uint16_t* s_mu = reinterpret_cast<uint16_t*>(smem + lay.mu);
+    Real* s_sig = reinterpret_cast<Real*>(smem + lay.sig);
+    Real* s_k = reinterpret_cast<Real*>(smem + lay.k);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + lay.bar);
 
     const int tid = threadIdx.x;
     const int lane = tid & 31;
@@ -76,150 +132,147 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_em_tile(EmArgs<Real> a, int
     constexpr int kGroups = kTileThreads / GROUP;
     const unsigned gmask = GROUP == 32 ? kFull : (((1u << GROUP) - 1u) << (lane & ~(GROUP - 1)));
     const uint32_t V = a.V;
+    const bool median = a.mode == kEmMedian;
     double cost_local = 0.0;
     unsigned long long singular_local = 0;
 
-    for (uint32_t t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+    if (tid == 0) mbar_init(bar, 1);
+    __syncthreads();
+
+    uint32_t parity = 0;
+    for (uint32_t t = blockIdx.x; t < a.ntiles; t += gridDim.x, parity ^= 1u) {
         const uint32_t mb = a.tile_mb[t], me = a.tile_mb[t + 1];
         const int nm = static_cast<int>(me - mb);
-        const uint64_t pb = a.off[mb];
-        const int np = static_cast<int>(a.off[me] - pb);
-
-        // ---- stage the tile -------------------------------------------------
-        for (int m = tid; m <= nm; m += kTileThreads) s_off[m] = static_cast<uint32_t>(a.off[mb + m] - pb);
-        for (int m = tid; m < nm; m += kTileThreads) {
-            s_sd[m] = a.sd[mb + m];
-            s_pr2[m] = a.pr2[mb + m];
-        }
+        const uint64_t pb = a.off[mb], pe = a.off[me];
+        const int np = static_cast<int>(pe - pb);
+        uint64_t f_pair, f_off, f_pr2;
+        uint32_t b_idx, b_real, b_off, b_pr2;
+        widen(pb, pe, 4, &f_pair, &b_idx);
         {
-            const uint32_t* gi = a.vidx + pb;
-            const Real* gl = a.L + pb;
-            const Real* gt = a.T + pb;
-            for (int k0 = tid; k0 < np; k0 += 4 * kTileThreads) {
-                uint32_t iv[4];
-                Real lv[4], tv[4];
+            uint64_t fr;
+            widen(pb, pe, sizeof(Real), &fr, &b_real);
+            // 4-byte arrays start at f_pair; Real arrays at fr (== f_pair for float)
+            if (tid == 0) {
+                widen(mb, me + 1, 8, &f_off, &b_off);
+                widen(mb, me, sizeof(Real), &f_pr2, &b_pr2);
+                const uint32_t b_sd = static_cast<uint32_t>(nm * sizeof(R4));
+                const uint32_t total = b_idx * (median ? 2u : 1u) + 2u * b_real + b_off + b_sd + b_pr2;
+                fence_proxy_async();
+                mbar_arrive_expect_tx(bar, total);
+                if (b_idx) {  // a tile of muons with empty paths has no pair bytes
+                    bulk_load(s_idx, a.vidx + f_pair, b_idx, bar);
+                    if (median) bulk_load(s_slot, a.slot + f_pair, b_idx, bar);
+                    bulk_load(s_L, a.L + fr, b_real, bar);
+                    bulk_load(s_T, a.T + fr, b_real, bar);
+                }
+                bulk_load(s_off, a.off + f_off, b_off, bar);
+                if (b_sd) bulk_load(s_sd, a.sd + mb, b_sd, bar);
+                bulk_load(s_pr2, a.pr2 + f_pr2, b_pr2, bar);
+            }
+            // shifts from the widened range starts to the tile's first element
+            const int sh_pair = static_cast<int>(pb - f_pair);
+            const int sh_real = static_cast<int>(pb - fr);
+            const int sh_off = static_cast<int>(mb - (mb - mb % 2));
+            const int sh_pr2 = static_cast<int>(mb % (16 / sizeof(Real)));
+            const bool landed = wait_tile(bar, parity, a.ctr);
+            if (!__syncthreads_and(landed)) break;  // uniform: every thread leaves together
+
+            // ---- gather lambda for every pair of the tile (loads in flight together)
+            for (int k0 = tid; k0 < np; k0 += kGatherUnroll * kTileThreads) {
+                Real lv[kGatherUnroll];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
+                for (int u = 0; u < kGatherUnroll; ++u) {
                     const int k = k0 + u * kTileThreads;
-                    if (k < np) {
-                        iv[u] = ld_stream_u32(gi + k);
-                        lv[u] = ld_stream(gl + k);
-                        tv[u] = ld_stream(gt + k);
-                    }
+                    const uint32_t j = k < np ? s_idx[sh_pair + k] : 0xffffffffu;
+                    lv[u] = j < V ? __ldg(a.lam + j) : Real(0);
                 }
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
+                for (int u = 0; u < kGatherUnroll; ++u) {
                     const int k = k0 + u * kTileThreads;
-                    if (k < np) {
-                        s_idx[k] = iv[u];
-                        s_L[k] = lv[u];
-                        s_T[k] = tv[u];
+                    if (k < np) s_lam[k] = lv[u];
+                }
+            }
+            __syncthreads();
+
+            // ---- covariance sums, GROUP lanes per muon ------------------------
+            for (int m = group; m < nm; m += kGroups) {
+                const int b = static_cast<int>(s_off[sh_off + m] - pb), e = static_cast<int>(s_off[sh_off + m + 1] - pb);
+                Real c0 = 0, c1 = 0, c2 = 0;
+                for (int k = b + glane; k < e; k += GROUP) {
+                    s_mu[k] = static_cast<uint16_t>(m);
+                    const Real L = s_L[sh_real + k], T = s_T[sh_real + k], l = s_lam[k];
+                    const Real LT = L * T;
+                    c0 += l * L;
+                    c1 += l * (LT + L * L * Real(0.5));
+                    c2 += l * (L * L * L * Real(1.0 / 3.0) + (L + T) * LT);
+                }
+#pragma unroll
+                for (int o = GROUP / 2; o > 0; o >>= 1) {
+                    c0 += __shfl_xor_sync(gmask, c0, o, GROUP);
+                    c1 += __shfl_xor_sync(gmask, c1, o, GROUP);
+                    c2 += __shfl_xor_sync(gmask, c2, o, GROUP);
+                }
+                if (glane == 0) {
+                    s_sig[3 * m + 0] = c0;
+                    s_sig[3 * m + 1] = c1;
+                    s_sig[3 * m + 2] = c2;
+                }
+            }
+            __syncthreads();
+
+            // ---- per-muon 2x2 algebra, one thread per muon --------------------
+            for (int m = tid; m < nm; m += kTileThreads) {
+                const double p2 = static_cast<double>(s_pr2[sh_pr2 + m]);
+                const double S00 = p2 * static_cast<double>(s_sig[3 * m + 0]) + a.E00;
+                const double S01 = p2 * static_cast<double>(s_sig[3 * m + 1]) + a.E01;
+                const double S11 = p2 * static_cast<double>(s_sig[3 * m + 2]) + a.E11;
+                const double det = S00 * S11 - S01 * S01;
+                Real k0 = 0, k1 = 0, k2 = 0;
+                if (fabs(det) > 1e-12) {  // Eigen computeInverseAndDetWithCheck threshold
+                    const double r = 1.0 / det;
+                    const double i00 = S11 * r, i01 = -S01 * r, i11 = S00 * r;
+                    const R4 v = s_sd[m];
+                    // u = Sigma^-1 (S, D) per plane; in the storage precision
+                    const Real f00 = static_cast<Real>(i00), f01 = static_cast<Real>(i01), f11 = static_cast<Real>(i11);
+                    const Real ux0 = f00 * v.x + f01 * v.y, ux1 = f01 * v.x + f11 * v.y;
+                    const Real uy0 = f00 * v.z + f01 * v.w, uy1 = f01 * v.z + f11 * v.w;
+                    const Real pr2 = s_pr2[sh_pr2 + m];
+                    k0 = pr2 * (Real(0.5) * (ux0 * ux0 + uy0 * uy0) - f00);
+                    k1 = pr2 * ((ux0 * ux1 + uy0 * uy1) - Real(2) * f01);
+                    k2 = pr2 * (Real(0.5) * (ux1 * ux1 + uy1 * uy1) - f11);
+                    if (det <= 0) {
+                        ++singular_local;
+                    } else if (a.compute_cost) {
+                        const double sx = v.x, dx = v.y, sy = v.z, dy = v.w;
+                        cost_local += log(det) + ((sx * sx + sy * sy) * i00 + (dx * dx + dy * dy) * i11 +
+                                                  (sx * dx + sy * dy) * 2.0 * i01) * 0.5;
                     }
-                }
-            }
-        }
-        __syncthreads();
-
-        // ---- phase 1: covariance gather, GROUP lanes per muon ---------------
-        for (int m = group; m < nm; m += kGroups) {
-            const int b = static_cast<int>(s_off[m]), e = static_cast<int>(s_off[m + 1]);
-            Real c0 = 0, c1 = 0, c2 = 0;
-            for (int k0 = b + glane; k0 < e; k0 += 4 * GROUP) {
-                uint32_t jj[4];
-                Real ll[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int k = k0 + u * GROUP;
-                    jj[u] = k < e ? s_idx[k] : 0xffffffffu;
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) ll[u] = jj[u] < V ? __ldg(a.lam + jj[u]) : Real(0);
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int k = k0 + u * GROUP;
-                    if (k < e) {
-                        s_lam[k] = ll[u];
-                        s_mu[k] = static_cast<uint16_t>(m);
-                        const Real L = s_L[k], T = s_T[k];
-                        const Real LT = L * T;
-                        const Real w01 = LT + L * L * Real(0.5);
-                        const Real w11 = L * L * L * Real(1.0 / 3.0) + (L + T) * LT;
-                        c0 += ll[u] * L;
-                        c1 += ll[u] * w01;
-                        c2 += ll[u] * w11;
-                    }
-                }
-            }
-#pragma unroll
-            for (int o = GROUP / 2; o > 0; o >>= 1) {
-                c0 += __shfl_xor_sync(gmask, c0, o, GROUP);
-                c1 += __shfl_xor_sync(gmask, c1, o, GROUP);
-                c2 += __shfl_xor_sync(gmask, c2, o, GROUP);
-            }
-            if (glane == 0) {
-                s_sig[3 * m + 0] = c0;
-                s_sig[3 * m + 1] = c1;
-                s_sig[3 * m + 2] = c2;
-            }
-        }
-        __syncthreads();
-
-        // ---- phase 2: FP64 2x2 algebra, one thread per muon -----------------
-        for (int m = tid; m < nm; m += kTileThreads) {
-            const double p2 = static_cast<double>(s_pr2[m]);
-            const double S00 = p2 * static_cast<double>(s_sig[3 * m + 0]) + a.E00;
-            const double S01 = p2 * static_cast<double>(s_sig[3 * m + 1]) + a.E01;
-            const double S11 = p2 * static_cast<double>(s_sig[3 * m + 2]) + a.E11;
-            const double det = S00 * S11 - S01 * S01;
-            double k0 = 0.0, k1 = 0.0, k2 = 0.0;
-            if (fabs(det) > 1e-12) {  // Eigen computeInverseAndDetWithCheck threshold
-                const double r = 1.0 / det;
-                const double i00 = S11 * r, i01 = -S01 * r, i11 = S00 * r;
-                const R4 v = s_sd[m];
-                const double sx = v.x, dx = v.y, sy = v.z, dy = v.w;
-                const double ux0 = i00 * sx + i01 * dx, ux1 = i01 * sx + i11 * dx;
-                const double uy0 = i00 * sy + i01 * dy, uy1 = i01 * sy + i11 * dy;
-                const double A = ux0 * ux0 + uy0 * uy0;
-                const double B = ux0 * ux1 + uy0 * uy1;
-                const double C = ux1 * ux1 + uy1 * uy1;
-                k0 = p2 * (0.5 * A - i00);
-                k1 = p2 * (B - 2.0 * i01);
-                k2 = p2 * (0.5 * C - i11);
-                if (det <= 0) {
-                    ++singular_local;
-                } else if (a.compute_cost) {
-                    cost_local += log(det) + ((sx * sx + sy * sy) * i00 + (dx * dx + dy * dy) * i11 +
-                                              (sx * dx + sy * dy) * 2.0 * i01) * 0.5;
-                }
-            } else {
-                ++singular_local;  // inverse left at zero: s_ij = 2 l_j
-            }
-            s_k[3 * m + 0] = static_cast<Real>(k0);
-            s_k[3 * m + 1] = static_cast<Real>(k1);
-            s_k[3 * m + 2] = static_cast<Real>(k2);
-        }
-        __syncthreads();
-
-        // ---- phase 3: per-pair EM term --------------------------------------
-        if (a.mode != kEmCostOnly) {
-            for (int k = tid; k < np; k += kTileThreads) {
-                const uint32_t j = s_idx[k];
-                if (j >= V) continue;
-                const int m = s_mu[k];
-                const Real L = s_L[k], T = s_T[k], l = s_lam[k];
-                const Real LT = L * T;
-                const Real w01 = LT + L * L * Real(0.5);
-                const Real w11 = L * L * L * Real(1.0 / 3.0) + (L + T) * LT;
-                const Real g = s_k[3 * m + 0] * L + s_k[3 * m + 1] * w01 + s_k[3 * m + 2] * w11;
-                if (a.mode == kEmMedian) {
-                    const uint32_t sl = ld_stream_u32(a.slot + pb + k);
-                    a.S[sl] = Real(2) * l + g * l * l;
                 } else {
-                    atomicAdd(a.G + j, g);
+                    ++singular_local;  // inverse left at zero: s_ij = 2 l_j
+                }
+                s_k[3 * m + 0] = k0;
+                s_k[3 * m + 1] = k1;
+                s_k[3 * m + 2] = k2;
+            }
+            __syncthreads();
+
+            // ---- per-pair EM term ---------------------------------------------
+            if (a.mode != kEmCostOnly) {
+                for (int k = tid; k < np; k += kTileThreads) {
+                    const uint32_t j = s_idx[sh_pair + k];
+                    if (j >= V) continue;
+                    const int m = s_mu[k];
+                    const Real L = s_L[sh_real + k], T = s_T[sh_real + k], l = s_lam[k];
+                    const Real LT = L * T;
+                    const Real w01 = LT + L * L * Real(0.5);
+                    const Real w11 = L * L * L * Real(1.0 / 3.0) + (L + T) * LT;
+                    const Real g = s_k[3 * m + 0] * L + s_k[3 * m + 1] * w01 + s_k[3 * m + 2] * w11;
+                    if (median) a.S[s_slot[sh_pair + k]] = Real(2) * l + g * l * l;
+                    else atomicAdd(a.G + j, g);
                 }
             }
         }
-        __syncthreads();
+        __syncthreads();  // the buffers are overwritten by the next tile's copies
     }
 
     // block reduction of the cost and singular counts
@@ -385,7 +438,15 @@ __device__ double voxel_value(const Src& src, uint32_t M, int use_mean, int pct)
     return s / static_cast<double>(jm) * 0.5;
 }
 
-template <typename Real, int R, typename OutT>
+template <typename Real, int R>
+__device__ __forceinline__ double select_regs(const Real* seg, uint32_t M, int lane, int use_mean, int pct) {
+    using K = typename KeyOf<Real>::type;
+    RegKeys<Real, R> src;
+    src.load(seg, M, lane);
+    return voxel_value<Real, K>(src, M, use_mean, pct);
+}
+
+template <typename Real, typename OutT>
 __global__ void __launch_bounds__(256) k_select(const Real* __restrict__ S, const uint64_t* __restrict__ start,
                                                 const uint32_t* __restrict__ mult, uint32_t V, int use_mean, int pct,
                                                 OutT* __restrict__ out) {
@@ -398,11 +459,17 @@ __global__ void __launch_bounds__(256) k_select(const Real* __restrict__ S, cons
         double v = 0.0;
         if (M > 0) {
             const Real* seg = S + start[j];
-            if (M <= 32u * R) {
-                RegKeys<Real, R> src;
-                src.load(seg, M, lane);
-                v = voxel_value<Real, K>(src, M, use_mean, pct);
-            } else {
+            // registers per lane sized to the segment (the passes touch only those)
+            if (M <= 32u) v = select_regs<Real, 1>(seg, M, lane, use_mean, pct);
+            else if (M <= 64u) v = select_regs<Real, 2>(seg, M, lane, use_mean, pct);
+            else if (M <= 128u) v = select_regs<Real, 4>(seg, M, lane, use_mean, pct);
+            else if (M <= 192u) v = select_regs<Real, 6>(seg, M, lane, use_mean, pct);
+            else if (M <= 256u) v = select_regs<Real, 8>(seg, M, lane, use_mean, pct);
+            else if (M <= 384u) v = select_regs<Real, 12>(seg, M, lane, use_mean, pct);
+            else if (M <= 512u) v = select_regs<Real, 16>(seg, M, lane, use_mean, pct);
+            else if (M <= 768u) v = select_regs<Real, 24>(seg, M, lane, use_mean, pct);
+            else if (M <= 1024u) v = select_regs<Real, 32>(seg, M, lane, use_mean, pct);
+            else {
                 MemKeys<Real> src{seg, M, lane};
                 v = voxel_value<Real, K>(src, M, use_mean, pct);
             }
@@ -588,6 +655,20 @@ cudaError_t em_tile_configure(int tile_pairs, int tile_muons) {
     return e;
 }
 template cudaError_t em_tile_configure<float>(int, int);
+
+// resident CTAs per SM of the k_em_tile variant used for a gather group width
+template <typename Real>
+int em_tile_blocks(int tile_pairs, int tile_muons, int group) {
+    const size_t smem = em_tile_smem_bytes<Real>(tile_pairs, tile_muons);
+    int n = 0;
+    cudaError_t e;
+    if (group <= 8) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_em_tile<Real, 8>, kTileThreads, smem);
+    else if (group <= 16) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_em_tile<Real, 16>, kTileThreads, smem);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_em_tile<Real, 32>, kTileThreads, smem);
+    return (e == cudaSuccess && n > 0) ? n : 1;
+}
+template int em_tile_blocks<float>(int, int, int);
+template int em_tile_blocks<double>(int, int, int);
 template cudaError_t em_tile_configure<double>(int, int);
 
 template <typename Real>
@@ -613,7 +694,7 @@ void launch_select(const Real* S, const uint64_t* start, const uint32_t* mult, u
     if (V == 0) return;
     const uint64_t warps = V;
     const unsigned nb = blocks_for(warps * 32, 256);
-    k_select<Real, 32, OutT><<<nb, 256, 0, s>>>(S, start, mult, V, use_mean, pct, out); count_launches(1);
+    k_select<Real, OutT><<<nb, 256, 0, s>>>(S, start, mult, V, use_mean, pct, out); count_launches(1);
 }
 template void launch_select<float, float>(const float*, const uint64_t*, const uint32_t*, uint32_t, int, int, float*,
                                           cudaStream_t);

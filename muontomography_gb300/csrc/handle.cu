@@ -28,6 +28,8 @@ unsigned long long launches_so_far() { return g_launches.load(); }
 
 namespace {
 
+constexpr uint64_t kPad = 8;
+
 struct Error : std::runtime_error {
     int code;
     Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
@@ -269,7 +271,7 @@ struct muto_handle {
     DevMem lam, G, lam_ml, cost_hist;
     DevMem tiles;
     uint32_t ntiles = 0;
-    int tile_pairs = 0, tile_muons = 0, group = 32;
+    int tile_pairs = 0, tile_muons = 0, group = 32, tile_blocks = 0;
     bool prepared = false;
     int iters = 0;
     bool stopped = false;
@@ -437,7 +439,9 @@ void prepare_em(muto_handle* h) {
     run(h, "compact", [&] { launch_compact(flags.as<uint32_t>(), pos.as<uint64_t>(), nt, h->kept.as<uint32_t>(), s); });
 
     h->sd.alloc(std::max<uint64_t>(N, 1) * sizeof(R4), &h->dev_bytes);
-    h->pr2.alloc(std::max<uint64_t>(N, 1) * sizeof(Real), &h->dev_bytes);
+    // per-pair and per-muon arrays carry kPad extra entries: the tile stage copies
+    // ranges widened to 16-byte boundaries
+    h->pr2.alloc((N + kPad) * sizeof(Real), &h->dev_bytes);
     h->scat.alloc(std::max<uint64_t>(N, 1) * 3 * sizeof(double), &h->dev_bytes);
     h->pr64.alloc(std::max<uint64_t>(N, 1) * sizeof(double), &h->dev_bytes);
     run(h, "muon_info", [&] {
@@ -450,7 +454,7 @@ void prepare_em(muto_handle* h) {
         launch_path_count(h->rays.as<muto_ray>(), h->kept.as<uint32_t>(), h->scat.as<double>(), N, g, P.straight_line,
                           flags.as<uint32_t>(), h->ctr(), s);
     });
-    h->off.alloc((N + 1) * sizeof(uint64_t), &h->dev_bytes);
+    h->off.alloc((N + 1 + kPad) * sizeof(uint64_t), &h->dev_bytes);
     run(h, "scan", [&] { scan_u32_to_u64(flags.as<uint32_t>(), h->off.as<uint64_t>(), N, scratch.as<void>(), s); });
     std::vector<uint64_t> off_h(N + 1);
     CK(cudaMemcpyAsync(off_h.data(), h->off.as<uint64_t>(), (N + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
@@ -463,9 +467,9 @@ void prepare_em(muto_handle* h) {
     flags.release();
     pos.release();
 
-    h->vidx.alloc(std::max<uint64_t>(Pn, 1) * sizeof(uint32_t), &h->dev_bytes);
-    h->L.alloc(std::max<uint64_t>(Pn, 1) * sizeof(Real), &h->dev_bytes);
-    h->T.alloc(std::max<uint64_t>(Pn, 1) * sizeof(Real), &h->dev_bytes);
+    h->vidx.alloc((Pn + kPad) * sizeof(uint32_t), &h->dev_bytes);
+    h->L.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
+    h->T.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
     {
         DevMem l64tmp;
         double* l64 = reinterpret_cast<double*>(h->L.as<Real>());
@@ -491,7 +495,7 @@ void prepare_em(muto_handle* h) {
         DevMem cursor;
         cursor.alloc(V * sizeof(uint32_t), &h->dev_bytes);
         CK(cudaMemsetAsync(cursor.as<void>(), 0, V * sizeof(uint32_t), s));
-        h->slot.alloc(std::max<uint64_t>(Pn, 1) * sizeof(uint32_t), &h->dev_bytes);
+        h->slot.alloc((Pn + kPad) * sizeof(uint32_t), &h->dev_bytes);
         run(h, "assign_slots", [&] {
             launch_assign_slots(h->vidx.as<uint32_t>(), Pn, static_cast<uint32_t>(V), h->start.as<uint64_t>(),
                                 cursor.as<uint32_t>(), h->slot.as<uint32_t>(), s);
@@ -504,9 +508,9 @@ void prepare_em(muto_handle* h) {
     // --- tiles of consecutive muons fitting the shared-memory stage ----------
     uint64_t maxpath = 0;
     for (uint64_t i = 0; i < N; ++i) maxpath = std::max<uint64_t>(maxpath, off_h[i + 1] - off_h[i]);
-    int TP = P.tile_pairs > 0 ? P.tile_pairs : (std::is_same<Real, double>::value ? 2048 : 4096);
+    int TP = P.tile_pairs > 0 ? P.tile_pairs : (std::is_same<Real, double>::value ? 1024 : 2048);
     while (static_cast<uint64_t>(TP) < maxpath) TP *= 2;
-    int TM = std::is_same<Real, double>::value ? 256 : 512;
+    int TM = std::is_same<Real, double>::value ? 128 : 256;
     TM = std::min<int>(TM, 65535);
     if (em_tile_smem_bytes<Real>(TP, TM) > h->smem_optin)
         throw Error(MUTO_ERR_CAPACITY, "longest muon path (" + std::to_string(maxpath) + " voxels) does not fit the shared-memory tile");
@@ -525,9 +529,10 @@ void prepare_em(muto_handle* h) {
     CK(cudaMemcpyAsync(h->tiles.as<void>(), tb.data(), tb.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     h->tile_pairs = TP;
     h->tile_muons = TM;
-    CK(em_tile_configure<Real>(TP, TM));
     const double avg = N > 0 ? static_cast<double>(Pn) / static_cast<double>(N) : 0.0;
     h->group = avg <= 32 ? 8 : (avg <= 64 ? 16 : 32);
+    CK(em_tile_configure<Real>(TP, TM));
+    h->tile_blocks = em_tile_blocks<Real>(TP, TM, h->group) * h->num_sms;
 
     // --- image and accumulators ---------------------------------------------
     h->lam.alloc(V * sizeof(Real), &h->dev_bytes);
@@ -573,7 +578,7 @@ void enqueue_iteration(muto_handle* h) {
     a.mode = h->store_s ? kEmMedian : kEmMean;
     a.compute_cost = h->want_cost() ? 1 : 0;
     a.ctr = h->ctr();
-    const int blocks = 2 * h->num_sms;
+    const int blocks = h->tile_blocks;
     run(h, "em_tile", [&] { launch_em_tile<Real>(a, h->tile_pairs, h->tile_muons, blocks, h->group, s); });
 
     const bool map = h->method == kMap;
@@ -742,7 +747,7 @@ double nll_eval(muto_handle* h, const double* loglam_host, double* grad_host, bo
     a.compute_cost = 1;
     a.ctr = h->ctr();
     run(h, grad_host ? "nll_backward" : "nll_forward",
-        [&] { launch_em_tile<Real>(a, h->tile_pairs, h->tile_muons, 2 * h->num_sms, h->group, s); });
+        [&] { launch_em_tile<Real>(a, h->tile_pairs, h->tile_muons, h->tile_blocks, h->group, s); });
     CK(cudaMemsetAsync(h->fval.as<void>(), 0, sizeof(double), s));
     if (grad_host) {
         run(h, "grad_finish", [&] { launch_grad_finish<Real>(h->G.as<Real>(), h->lam64.as<double>(), h->mult.as<uint32_t>(), static_cast<uint32_t>(V), h->grad.as<double>(), s); });
@@ -843,7 +848,7 @@ int muto_get_status(const muto_handle* hc, muto_status* out) {
     out->n_singular = c.singular;
     out->n_nonconverged = c.nonconverged;
     out->n_bounds = c.bounds;
-    out->n_path_overflow = c.overflow;
+    out->n_path_overflow = c.overflow + c.timeouts;
     out->cost = c.cost_last;
     out->cost_prev = c.cost_prev;
     out->device_bytes = h->dev_bytes.load();
