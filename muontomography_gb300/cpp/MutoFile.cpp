@@ -1,0 +1,268 @@
+// MutoFile: raw-hit reader and image files.  See MutoFile.h.
+#include "MutoFile.h"
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+
+#include "muto_gb300.h"
+
+namespace {
+
+muto_grid to_c(const VoxelGrid& g) {
+    muto_grid c{};
+    c.nx = g.nx;
+    c.ny = g.ny;
+    c.nz = g.nz;
+    c.x_min = g.x_min;
+    c.y_min = g.y_min;
+    c.z_min = g.z_min;
+    c.dx = g.dx;
+    c.dy = g.dy;
+    c.dz = g.dz;
+    return c;
+}
+
+// Eigen-decomposition of a symmetric 3x3 matrix by cyclic Jacobi rotations;
+// returns the unit eigenvector of the largest eigenvalue.
+void principal_axis(double a[3][3], double* out) {
+    double v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int sweep = 0; sweep < 50; ++sweep) {
+        const double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+        if (off < 1e-30 * (a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2]) || off == 0.0) break;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                if (a[p][q] == 0.0) continue;
+                const double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < 3; ++k) {  // A <- A J
+                    const double akp = a[k][p], akq = a[k][q];
+                    a[k][p] = c * akp - s * akq;
+                    a[k][q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < 3; ++k) {  // A <- J^T A
+                    const double apk = a[p][k], aqk = a[q][k];
+                    a[p][k] = c * apk - s * aqk;
+                    a[q][k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < 3; ++k) {  // V <- V J
+                    const double vkp = v[k][p], vkq = v[k][q];
+                    v[k][p] = c * vkp - s * vkq;
+                    v[k][q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    int best = 0;
+    for (int k = 1; k < 3; ++k)
+        if (a[k][k] > a[best][best]) best = k;
+    for (int k = 0; k < 3; ++k) out[k] = v[k][best];
+}
+
+}  // namespace
+
+void MutoFile::fitLine(const double* x, const double* y, const double* z, int n, double* c, double* d) {
+    c[0] = c[1] = c[2] = 0.0;
+    for (int i = 0; i < n; ++i) {
+        c[0] += x[i];
+        c[1] += y[i];
+        c[2] += z[i];
+    }
+    for (int k = 0; k < 3; ++k) c[k] /= (n > 0 ? n : 1);
+    double a[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int i = 0; i < n; ++i) {
+        const double r[3] = {x[i] - c[0], y[i] - c[1], z[i] - c[2]};
+        for (int p = 0; p < 3; ++p)
+            for (int q = 0; q < 3; ++q) a[p][q] += r[p] * r[q];
+    }
+    principal_axis(a, d);
+    const double nrm = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    if (!(nrm > 0)) {
+        d[0] = d[1] = 0.0;
+        d[2] = 1.0;
+        return;
+    }
+    const double sgn = d[2] < 0 ? -1.0 : 1.0;  // the SVD leaves the sign open; d_z > 0 here
+    for (int k = 0; k < 3; ++k) d[k] = sgn * d[k] / nrm;
+}
+
+MutoMuonData MutoFile::getMuonData(std::vector<std::string> flist, std::vector<MTfloat> zlayers, int nMiddle,
+                                   int fPrecision) {
+    MutoMuonData data;
+    if (fPrecision != 4 && fPrecision != 8) {
+        std::cerr << "Floating point precision not supported. " << std::endl;
+        return data;
+    }
+    const int nz = static_cast<int>(zlayers.size());
+    if (nMiddle < 2 || nz - nMiddle < 2) {
+        std::cerr << "Error: at least two layers of detectors for both up and down area. " << std::endl;
+        return data;
+    }
+    const size_t nEach = 2 * static_cast<size_t>(nz) + 2;  // two extra values for in and out energy
+    std::vector<double> rec(nEach);
+    std::vector<double> hx(nz), hy(nz);
+    for (const std::string& name : flist) {
+        std::ifstream file(name.c_str(), std::ios::in | std::ios::binary);
+        if (file.fail()) {
+            std::cout << "Reading muon data error for : " << name << std::endl;
+            continue;
+        }
+        file.seekg(0, std::ios::end);
+        const uint64_t filesize = static_cast<uint64_t>(file.tellg());  // 64-bit: files above 4 GB are fine
+        file.seekg(0, std::ios::beg);
+        const uint64_t nRay = filesize / nEach / static_cast<uint64_t>(fPrecision);
+        std::vector<char> raw(nEach * static_cast<size_t>(fPrecision));
+        data.reserve(data.size() + nRay);
+        for (uint64_t r = 0; r < nRay; ++r) {
+            file.read(raw.data(), static_cast<std::streamsize>(raw.size()));
+            if (!file) break;
+            bool nan = false;
+            for (size_t k = 0; k < nEach; ++k) {
+                if (fPrecision == 4) {
+                    float f;
+                    std::memcpy(&f, raw.data() + 4 * k, 4);
+                    rec[k] = f;
+                } else {
+                    std::memcpy(&rec[k], raw.data() + 8 * k, 8);
+                }
+                nan = nan || std::isnan(rec[k]);
+            }
+            if (nan) continue;
+            for (int i = 0; i < nz; ++i) {
+                hx[i] = rec[1 + 2 * i];
+                hy[i] = rec[2 + 2 * i];
+            }
+            RayData ray;
+            ray.ein = rec[0];
+            ray.eout = rec[2 * nz + 1];
+            double c[3], d[3];
+            fitLine(hx.data(), hy.data(), zlayers.data(), nMiddle, c, d);  // upper layers
+            double t = (zlayers[nMiddle - 1] - c[2]) / d[2];
+            ray.din = Vector3(d[0], d[1], d[2]);
+            ray.pin = Vector3(t * d[0] + c[0], t * d[1] + c[1], zlayers[nMiddle - 1]);
+            fitLine(hx.data() + nMiddle, hy.data() + nMiddle, zlayers.data() + nMiddle, nz - nMiddle, c, d);  // lower
+            t = (zlayers[nMiddle] - c[2]) / d[2];
+            ray.dout = Vector3(d[0], d[1], d[2]);
+            ray.pout = Vector3(t * d[0] + c[0], t * d[1] + c[1], zlayers[nMiddle]);
+            data.push_back(ray);
+        }
+    }
+    return data;
+}
+
+bool MutoFile::saveImage(const Image& img, const ImageHeader& header, std::string filename) {
+    const muto_grid g = to_c(header.grid);
+    if (static_cast<uint64_t>(img.size()) != static_cast<uint64_t>(g.nx) * g.ny * g.nz) {
+        std::cout << "Writing image to file: " << filename << " failed (size does not match the grid). " << std::endl;
+        return false;
+    }
+    const int rc = muto_save_image(filename.c_str(), img.data(), &g, header.method.c_str(), header.nRay, header.nIter,
+                                   header.fPrecision);
+    if (rc == MUTO_ERR_ARG) std::cout << "Floating point precision not supported. " << std::endl;
+    else if (rc != MUTO_OK) std::cout << "Writing image to file: " << filename << " failed. " << std::endl;
+    return rc == MUTO_OK;
+}
+
+bool MutoFile::saveImagePure(const Image& img, std::string filename, MTindex fPrecision) {
+    if (fPrecision != 4 && fPrecision != 8) {
+        std::cout << "Floating point precision not supported. " << std::endl;
+        return false;
+    }
+    FILE* f = std::fopen(filename.c_str(), "wb");
+    if (!f) {
+        std::cout << "Writing image to file: " << filename << " failed. " << std::endl;
+        return false;
+    }
+    bool ok = true;
+    for (std::ptrdiff_t i = 0; i < img.size() && ok; ++i) {
+        if (fPrecision == 8) {
+            const double v = img(i);
+            ok = std::fwrite(&v, 8, 1, f) == 1;
+        } else {
+            const float v = static_cast<float>(img(i));
+            ok = std::fwrite(&v, 4, 1, f) == 1;
+        }
+    }
+    return (std::fclose(f) == 0) && ok;
+}
+
+std::pair<Image, ImageHeader> MutoFile::loadImage(std::string filename) {
+    muto_grid g{};
+    char method[17] = {0};
+    uint32_t nRay = 0, nIter = 0, prec = 0;
+    if (muto_load_image(filename.c_str(), nullptr, 0, &g, method, &nRay, &nIter, &prec) != MUTO_OK) {
+        std::cout << "Reading image file: " << filename << " failed. " << std::endl;
+        return std::pair<Image, ImageHeader>{};
+    }
+    Image img(g.nx, g.ny, g.nz);
+    if (muto_load_image(filename.c_str(), img.data(), static_cast<uint64_t>(img.size()), &g, method, &nRay, &nIter,
+                        &prec) != MUTO_OK) {
+        std::cout << "Reading image file: " << filename << " failed. " << std::endl;
+        return std::pair<Image, ImageHeader>{};
+    }
+    ImageHeader h;
+    h.method = std::string(method, strnlen(method, 16));
+    h.grid = VoxelGrid{g.nx, g.ny, g.nz, g.x_min, g.y_min, g.z_min, g.dx, g.dy, g.dz};
+    h.nRay = nRay;
+    h.nIter = nIter;
+    h.fPrecision = prec;
+    return std::pair<Image, ImageHeader>{img, h};
+}
+
+Image MutoFile::loadImagePure(std::string filename, VoxelGrid grid, MTindex fPrecision) {
+    std::ifstream file(filename.c_str(), std::ios::in | std::ios::binary);
+    if (file.fail()) {
+        std::cout << "Reading image file: " << filename << " failed. " << std::endl;
+        return Image{};
+    }
+    if (fPrecision != 4 && fPrecision != 8) {
+        std::cout << "Floating point precision not supported. " << std::endl;
+        return Image{};
+    }
+    file.seekg(0, std::ios::end);
+    const uint64_t size = static_cast<uint64_t>(file.tellg());
+    file.seekg(0, std::ios::beg);
+    const uint64_t V = static_cast<uint64_t>(grid.nx) * grid.ny * grid.nz;
+    if (V * fPrecision != size) {
+        std::cout << "Wrong size of the image file and grid: " << filename << std::endl;
+        return Image{};
+    }
+    Image img(grid.nx, grid.ny, grid.nz);
+    for (uint64_t i = 0; i < V; ++i) {
+        if (fPrecision == 8) {
+            file.read(reinterpret_cast<char*>(&img(static_cast<std::ptrdiff_t>(i))), 8);
+        } else {
+            float f;
+            file.read(reinterpret_cast<char*>(&f), 4);
+            img(static_cast<std::ptrdiff_t>(i)) = f;
+        }
+    }
+    return img;
+}
+
+// ---------------------------------------------------------------------------
+// C entry (include/muto_io.h)
+// ---------------------------------------------------------------------------
+#include "muto_io.h"
+
+extern "C" int muto_read_muon_data(const char* const* files, int n_files, const double* z_layers, int nz,
+                                   int n_middle, int precision, muto_ray* out, uint64_t cap, uint64_t* n_out) {
+    if (!n_out || (n_files > 0 && !files) || nz <= 0 || !z_layers) return MUTO_ERR_ARG;
+    if (precision != 4 && precision != 8) return MUTO_ERR_ARG;
+    if (n_middle < 2 || nz - n_middle < 2) return MUTO_ERR_ARG;
+    std::vector<std::string> fl;
+    for (int i = 0; i < n_files; ++i) fl.push_back(files[i] ? files[i] : "");
+    const std::vector<MTfloat> z(z_layers, z_layers + nz);
+    const MutoMuonData d = MutoFile::getMuonData(fl, z, n_middle, precision);
+    if (!out) {
+        *n_out = d.size();
+        return MUTO_OK;
+    }
+    const uint64_t n = d.size() < cap ? d.size() : cap;
+    if (n) std::memcpy(out, d.data(), n * sizeof(muto_ray));
+    *n_out = n;
+    return MUTO_OK;
+}

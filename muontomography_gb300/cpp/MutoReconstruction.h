@@ -1,0 +1,71 @@
+// Reconstruction classes of the reference's API, running on the GPU through
+// the C ABI (include/muto_gb300.h):
+//   MutoVReconstruction   include/MutoVReconstruction.h:11-16
+//   MutoPoCA(json)        include/MutoPoCA.h:17-50
+//   MutoMLSD(json)        include/MutoMLSD.h:27-107
+//   MutoMAP(json)         include/MutoMAP.h:16-63 (derives from MutoMLSD)
+// Constructors take the method's JSON object with the reference's keys and
+// defaults.  Errors are printed (as the reference does) and reconstruct()
+// then returns an empty image; status() has the counters and the last error.
+#pragma once
+
+#include <chrono>
+#include <string>
+
+#include "MutoConfig.h"
+#include "MutoTypes.h"
+#include "muto_gb300.h"
+
+class MutoVReconstruction {
+public:
+    MutoVReconstruction() {}
+    virtual ~MutoVReconstruction() {}
+    virtual Image reconstruct(const MutoMuonData&) = 0;
+};
+
+// Common part: one library handle per object (not copyable).
+class MutoGpuReconstruction : public MutoVReconstruction {
+public:
+    ~MutoGpuReconstruction() override;
+    MutoGpuReconstruction(const MutoGpuReconstruction&) = delete;
+    MutoGpuReconstruction& operator=(const MutoGpuReconstruction&) = delete;
+
+    VoxelGrid getCurrentGrid() const;
+    muto_status status() const;
+    bool ok() const { return fHandle != nullptr; }
+
+protected:
+    MutoGpuReconstruction(const char* method, const json& config);
+    Image fetchImage();
+    bool check(int rc, const char* what);
+    void logMessage(const std::string& msg, bool printTime = false);
+
+    muto_handle* fHandle = nullptr;
+    json fConfig;
+    bool fLogPrint = false;
+    std::chrono::steady_clock::time_point fTimeStart;
+};
+
+class MutoPoCA : public MutoGpuReconstruction {
+public:
+    MutoPoCA();
+    explicit MutoPoCA(json config);
+    Image reconstruct(const MutoMuonData& rays) override;
+};
+
+class MutoMLSD : public MutoGpuReconstruction {
+public:
+    MutoMLSD();
+    explicit MutoMLSD(json config);
+    Image reconstruct(const MutoMuonData& rays) override;
+
+protected:
+    MutoMLSD(const char* method, json config);
+    int fNIteration = 10;
+};
+
+class MutoMAP : public MutoMLSD {
+public:
+    MutoMAP();
+    explicit MutoMAP(json config);
+};

@@ -1,0 +1,118 @@
+"""The C++ host layer: raw-hit reader (MutoFile::getMuonData), the image file
+format through MutoFile, and the command-line driver (MuToTest.cpp's
+replacement) running the reconstruction classes on the GPU."""
+import ctypes as C
+import json
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import muontomography_gb300 as M
+from muontomography_gb300 import _lib, build as B
+
+Z = [1500.0, 1000.0, 500.0, -500.0, -1000.0, -1500.0]  # input/example_mlsd.json:3-4
+N_MIDDLE = 3
+
+
+@pytest.fixture(scope="module")
+def facade():
+    B.build()
+    lib = C.CDLL(str(B.facade_lib_path()))
+    lib.muto_read_muon_data.argtypes = [C.POINTER(C.c_char_p), C.c_int, C.POINTER(C.c_double), C.c_int, C.c_int,
+                                        C.c_int, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]
+    return lib
+
+
+def read(facade, files, z=Z, n_middle=N_MIDDLE, precision=4):
+    arr = (C.c_char_p * len(files))(*[str(f).encode() for f in files])
+    zz = np.asarray(z, np.float64)
+    n = C.c_uint64()
+    rc = facade.muto_read_muon_data(arr, len(files), _lib.dptr(zz), len(z), n_middle, precision, None, 0, C.byref(n))
+    assert rc == 0
+    out = np.zeros((n.value, 14), np.float64)
+    rc = facade.muto_read_muon_data(arr, len(files), _lib.dptr(zz), len(z), n_middle, precision,
+                                    out.ctypes.data_as(C.c_void_p), n.value, C.byref(n))
+    assert rc == 0
+    return out[: n.value]
+
+
+def hits_from_tracks(rays, z=Z, n_middle=N_MIDDLE):
+    """Detector records {ein, x0, y0, ..., eout} of the tracks' in/out lines."""
+    recs = []
+    for r in rays:
+        pin, pout, din, dout = r[2:5], r[5:8], r[8:11], r[11:14]
+        row = [r[0]]
+        for k, zk in enumerate(z):
+            p, d = (pin, din) if k < n_middle else (pout, dout)
+            t = (zk - p[2]) / d[2]
+            row += [p[0] + t * d[0], p[1] + t * d[1]]
+        row.append(r[1])
+        recs.append(row)
+    return np.asarray(recs)
+
+
+def test_reader_recovers_exact_lines(facade, tmp_path):
+    g = M.Grid(10, 10, 10, -500.0, -500.0, -500.0, 100.0, 100.0, 100.0)
+    rays = M.generate(g, np.full(g.nvox, 1e-7), 200, seed=3)
+    # the reader puts pin / pout on layers n_middle-1 / n_middle: move the tracks there
+    for r in rays:
+        for (p, d, zt) in ((slice(2, 5), slice(8, 11), Z[N_MIDDLE - 1]), (slice(5, 8), slice(11, 14), Z[N_MIDDLE])):
+            t = (zt - r[p][2]) / r[d][2]
+            r[p] = r[p] + t * r[d]
+    rec = hits_from_tracks(rays)
+    rec[17, 4] = np.nan  # a record with a NaN is skipped (src/MutoFile.cpp:71-76)
+    f = tmp_path / "hits.bin"
+    rec.astype(np.float64).tofile(f)
+    got = read(facade, [f, tmp_path / "missing.bin"], precision=8)
+    want = np.delete(rays, 17, axis=0)
+    assert got.shape == want.shape
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-9)
+    rec.astype(np.float32).tofile(f)
+    got32 = read(facade, [f], precision=4)
+    np.testing.assert_allclose(got32[:, 8:], want[:, 8:], atol=1e-4)
+
+
+def test_reader_rejects_bad_layouts(facade, tmp_path):
+    zz = np.asarray(Z, np.float64)
+    n = C.c_uint64()
+    arr = (C.c_char_p * 1)(b"x")
+    assert facade.muto_read_muon_data(arr, 1, _lib.dptr(zz), 6, 1, 4, None, 0, C.byref(n)) == 1
+    assert facade.muto_read_muon_data(arr, 1, _lib.dptr(zz), 6, 3, 2, None, 0, C.byref(n)) == 1
+
+
+def test_facade_library_exports_io_header(facade):
+    text = (B.INCLUDE / "muto_io.h").read_text()
+    for name in re.findall(r"\b(muto_[a-z_]+)\s*\(", re.sub(r"/\*.*?\*/", "", text, flags=re.S)):
+        assert hasattr(facade, name), name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["poca", "mlsd", "map"])
+def test_cli_end_to_end(gpu, facade, tmp_path, method):
+    from muontomography_gb300 import workloads as W
+
+    wl = W.small(n_muons=3000, seed=17, n=10)
+    rays = wl.tracks()
+    hits = hits_from_tracks(rays, z=[300.0 + 500 * k for k in (2, 1, 0)] + [-300.0 - 500 * k for k in (0, 1, 2)])
+    f = tmp_path / "hits.bin"
+    hits.astype(np.float32).tofile(f)
+    zl = [1300.0, 800.0, 300.0, -300.0, -800.0, -1300.0]
+    section = wl.poca_config() if method == "poca" else wl.em_config(num_iteration=4, precision="fp64")
+    if method == "map":
+        section.update(beta=0.01, p=1.0, delta=0.1)
+    cfg = {"data_files": [str(f)], "detector_height": zl, "detector_middle": 3,
+           "output_file": str(tmp_path / "out.bin"), method: section}
+    (tmp_path / "cfg.json").write_text(json.dumps(cfg))
+    r = subprocess.run([str(B.cli_path()), str(tmp_path / "cfg.json")], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert f"Reconstruction with <{method}> took" in r.stdout
+    img, hdr = M.load_image(str(tmp_path / "out.bin"))
+    assert hdr["method"] == method and hdr["n_ray"] == len(rays) and hdr["precision"] == 4
+    # the same tracks through the Python view of the C ABI
+    tracks = read(facade, [f], z=zl)
+    with M.Reconstruction(method, section) as rec:
+        rec._n_iter = section.get("num_iteration", 1)
+        want = rec.reconstruct(tracks)
+    assert np.array_equal(img, want.astype(np.float32).astype(np.float64))
