@@ -3,8 +3,8 @@
 // and MAP updates the reference implements:
 //   NLL(l)   = sum_i log det Sigma_i + 1/2 sum_planes v^T Sigma_i^-1 v
 //              (the per-muon cost of src/MutoMLSD.cpp:465-468)
-//   dNLL/dl_j = sum_i pr^2 (tr(Sigma_i^-1 W_ij) - 1/2 xyS_ij) = -G_j,
-//              G_j = sum_i pr^2 g_ij accumulated by k_em_tile in mean mode.
+//   dNLL/dl_j = sum_i pr^2 (tr(Sigma_i^-1 W_ij) - 1/2 xyS_ij) = -sum_i g_ij,
+//              summed per voxel by the voxel pass in gradient mode (em_voxel.cu).
 //   prior    = 2 beta sum_j sum_{m in N(j)} w_jm psi(l_j - l_m) [+ 2 beta sum_j psi(l_j)],
 //              psi(t) = (t^2 + delta^2)^(p/2), l = 1e7 lambda, stencil and edge
 //              clamping of src/MutoMAP.cpp:283-350: the penalty whose separable
@@ -26,17 +26,6 @@ __global__ void k_exp_lambda(const double* __restrict__ loglam, const uint32_t* 
                              Real* __restrict__ lam) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j < V) lam[j] = mult[j] > 0 ? static_cast<Real>(exp(loglam[j])) : Real(0);
-}
-
-// grad_j = d NLL / d log l_j = l_j * dNLL/dl_j = -l_j G_j; clears G
-template <typename Real>
-__global__ void k_grad_finish(Real* __restrict__ G, const double* __restrict__ lam64, const uint32_t* __restrict__ mult,
-                              uint32_t V, double* __restrict__ grad) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= V) return;
-    const double g = static_cast<double>(G[j]);
-    G[j] = Real(0);
-    grad[j] = mult[j] > 0 ? -lam64[j] * g : 0.0;
 }
 
 __device__ __forceinline__ void psi_and_slope(double t, double p, double d2, double* psi, double* slope) {
@@ -111,13 +100,6 @@ void launch_exp_lambda(const double* loglam, const uint32_t* mult, uint32_t V, R
 }
 template void launch_exp_lambda<float>(const double*, const uint32_t*, uint32_t, float*, cudaStream_t);
 template void launch_exp_lambda<double>(const double*, const uint32_t*, uint32_t, double*, cudaStream_t);
-
-template <typename Real>
-void launch_grad_finish(Real* G, const double* lam64, const uint32_t* mult, uint32_t V, double* grad, cudaStream_t s) {
-    k_grad_finish<Real><<<blocks_for(V, 256), 256, 0, s>>>(G, lam64, mult, V, grad); count_launches(1);
-}
-template void launch_grad_finish<float>(float*, const double*, const uint32_t*, uint32_t, double*, cudaStream_t);
-template void launch_grad_finish<double>(double*, const double*, const uint32_t*, uint32_t, double*, cudaStream_t);
 
 void launch_prior(const double* lam64, const uint32_t* mult, DevGrid g, MapParams mp, double* dl_scratch, double* grad,
                   double* value, cudaStream_t s) {

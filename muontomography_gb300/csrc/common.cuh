@@ -1,5 +1,6 @@
 // Shared device helpers and the kernel-launch interface between the handle
-// (handle.cu) and the kernel files (setup.cu, em.cu, poca.cu, scan.cu).
+// (handle.cu) and the kernel files (setup.cu, em_muon.cu, em_voxel.cu, poca.cu,
+// adjoint.cu, scan.cu, gen.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -90,8 +91,11 @@ template <typename Real>
 void launch_path_fill(const muto_ray* rays, const uint32_t* kept, const double* scat, const uint64_t* off, uint64_t n,
                       muto_grid g, int straight, uint32_t* vidx, double* l64, Real* L, Real* T, cudaStream_t s);
 void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* mult, Counters* ctr, cudaStream_t s);
-void launch_assign_slots(const uint32_t* vidx, uint64_t P, uint32_t V, const uint64_t* start, uint32_t* cursor,
-                         uint32_t* slot, cudaStream_t s);
+// voxel-major copy of the pair lists: (muon, L, T) at start[j] + rank within voxel j
+template <typename Real>
+void launch_build_voxel_major(const uint64_t* off, uint64_t n, const uint32_t* vidx, const Real* L, const Real* T,
+                              uint32_t V, const uint64_t* start, uint32_t* cursor, uint32_t* vm_mu, Real* vm_L,
+                              Real* vm_T, cudaStream_t s);
 void launch_siddon_batch(muto_grid g, const double* p1, const double* p2, uint64_t n, uint32_t cap, uint32_t* xyz,
                          double* len, uint32_t* counts, cudaStream_t s);
 
@@ -110,45 +114,56 @@ struct PocaArgs {
 void launch_poca(const PocaArgs& a, cudaStream_t s);
 void launch_poca_normalize(double* img, const double* weight, uint64_t V, double eps, cudaStream_t s);
 
-// em.cu
-enum EmMode { kEmMedian = 0, kEmMean = 1, kEmCostOnly = 2 };
-
+// em_muon.cu: the muon pass (per-muon coefficients k)
 template <typename Real>
-struct EmArgs {
-    const uint64_t* off;         // N+1 pair offsets
-    const uint32_t* tile_mb;     // ntiles+1 first muon of each tile
+struct MuonPassArgs {
+    const uint64_t* off;                      // N+1 pair offsets (+ padding)
+    const uint32_t* tile_mb;                  // ntiles+1 first muon of each tile
     uint32_t ntiles;
-    const uint32_t* vidx;        // P
-    const Real* L;               // P
-    const Real* T;               // P
-    const uint32_t* slot;        // P (median)
-    const typename Vec4<Real>::type* sd;  // N: Sx, Dx, Sy, Dy
-    const Real* pr2;             // N
-    const Real* lam;             // V: lambda gathered by the muons
-    Real* S;                     // P (median)
-    Real* G;                     // V (mean / gradient), += sum_i pr^2 g_ij
+    const uint32_t* vidx;                     // P (+ padding) voxel of each pair
+    const Real* L;                            // P (+ padding)
+    const Real* T;                            // P (+ padding)
+    const typename Vec4<Real>::type* sd;      // N: Sx, Dx, Sy, Dy
+    const Real* pr2;                          // N (+ padding)
+    const Real* lam;                          // V: lambda gathered by the muons
+    typename Vec4<Real>::type* kout;          // N: (k0, k1, k2, 0)
     uint32_t V;
     double E00, E01, E11;
-    int mode;
     int compute_cost;
     Counters* ctr;
 };
 template <typename Real>
-void launch_em_tile(const EmArgs<Real>& a, int tile_pairs, int tile_muons, int blocks, int group, cudaStream_t s);
+void launch_em_muon(const MuonPassArgs<Real>& a, int tile_pairs, int tile_muons, int blocks, int group,
+                    cudaStream_t s);
 template <typename Real>
-size_t em_tile_smem_bytes(int tile_pairs, int tile_muons);
-// sets the dynamic shared-memory limit of every k_em_tile variant (call outside graph capture)
+size_t em_muon_smem_bytes(int tile_pairs, int tile_muons);
+// sets the dynamic shared-memory limit of every k_em_muon variant (call outside graph capture)
 template <typename Real>
-cudaError_t em_tile_configure(int tile_pairs, int tile_muons);
+cudaError_t em_muon_configure(int tile_pairs, int tile_muons);
 // resident CTAs per SM (persistent grid = this x SM count)
 template <typename Real>
-int em_tile_blocks(int tile_pairs, int tile_muons, int group);
+int em_muon_blocks(int tile_pairs, int tile_muons, int group);
 
+// em_voxel.cu: the voxel pass
+enum VoxelMode { kVoxMedian = 0, kVoxPercentile = 1, kVoxMean = 2, kVoxGradient = 3 };
 template <typename Real, typename OutT>
-void launch_select(const Real* S, const uint64_t* start, const uint32_t* mult, uint32_t V, int use_mean,
-                   int percentile, OutT* out, cudaStream_t s);
+struct VoxelPassArgs {
+    const uint64_t* start;                    // V+1 segment starts of the voxel-major lists
+    const uint32_t* mult;                     // V pairs per voxel
+    const uint32_t* vm_mu;                    // P muon of each voxel-major pair
+    const Real* vm_L;                         // P
+    const Real* vm_T;                         // P
+    const typename Vec4<Real>::type* kvec;    // N per-muon coefficients
+    const Real* lam;                          // V lambda of the iteration
+    uint32_t V;
+    int mode;                                 // VoxelMode
+    int pct;                                  // mean_percentile
+    OutT* out;                                // V new value (median / percentile / mean)
+    double* grad;                             // V gradient (kVoxGradient)
+    const double* lam64;                      // V lambda in FP64 (kVoxGradient)
+};
 template <typename Real, typename OutT>
-void launch_voxel_mean(const Real* lam, Real* G, const uint32_t* mult, uint32_t V, OutT* out, cudaStream_t s);
+void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, cudaStream_t s);
 void launch_finalize_cost(Counters* ctr, double n_muons, double* hist, uint32_t hist_cap, cudaStream_t s);
 
 struct MapParams {
@@ -164,9 +179,6 @@ void launch_copy_to(const double* in, LamT* out, uint64_t n, cudaStream_t s);
 // adjoint.cu
 template <typename Real>
 void launch_exp_lambda(const double* loglam, const uint32_t* mult, uint32_t V, Real* lam, cudaStream_t s);
-template <typename Real>
-void launch_grad_finish(Real* G, const double* lam64, const uint32_t* mult, uint32_t V, double* grad,
-                        cudaStream_t s);
 // adds d prior / d log(lambda) to grad and the prior's value to *value;
 // dl_scratch: V doubles, zero on entry and on return
 void launch_prior(const double* lam64, const uint32_t* mult, DevGrid g, MapParams mp, double* dl_scratch, double* grad,

@@ -266,16 +266,16 @@ struct muto_handle {
     // kept muons
     uint64_t N = 0, npairs = 0;
     DevMem kept, sd, pr2, scat, pr64, off;
-    DevMem vidx, L, T, slot, S;
-    DevMem mult, start;
-    DevMem lam, G, lam_ml, cost_hist;
+    DevMem vidx, L, T;            // muon-major pair lists
+    DevMem vm_mu, vm_L, vm_T;     // voxel-major copy
+    DevMem mult, start, kvec;
+    DevMem lam, lam_ml, cost_hist;
     DevMem tiles;
     uint32_t ntiles = 0;
     int tile_pairs = 0, tile_muons = 0, group = 32, tile_blocks = 0;
     bool prepared = false;
     int iters = 0;
     bool stopped = false;
-    bool store_s = false;      // median / percentile mean
     // PoCA outputs
     DevMem img64, weight, assign;
     // adjoint scratch
@@ -461,9 +461,6 @@ void prepare_em(muto_handle* h) {
     CK(cudaStreamSynchronize(s));
     const uint64_t Pn = off_h[N];
     h->npairs = Pn;
-    h->store_s = !P.update_with_mean || P.mean_percentile != 100;
-    if (h->store_s && Pn >= 0xffffffffull)
-        throw Error(MUTO_ERR_CAPACITY, "median / percentile update needs fewer than 2^32 muon-voxel pairs");
     flags.release();
     pos.release();
 
@@ -485,34 +482,37 @@ void prepare_em(muto_handle* h) {
         CK(cudaStreamSynchronize(s));
     }
 
-    // --- multiplicity M_j, segment starts, slots -----------------------------
+    // --- multiplicity M_j and the voxel-major copy of the lists ---------------
     h->mult.alloc(V * sizeof(uint32_t), &h->dev_bytes);
     CK(cudaMemsetAsync(h->mult.as<void>(), 0, V * sizeof(uint32_t), s));
     run(h, "voxel_hist", [&] { launch_voxel_hist(h->vidx.as<uint32_t>(), Pn, static_cast<uint32_t>(V), h->mult.as<uint32_t>(), h->ctr(), s); });
-    if (h->store_s) {
-        h->start.alloc((V + 1) * sizeof(uint64_t), &h->dev_bytes);
-        run(h, "scan", [&] { scan_u32_to_u64(h->mult.as<uint32_t>(), h->start.as<uint64_t>(), V, scratch.as<void>(), s); });
+    h->start.alloc((V + 1) * sizeof(uint64_t), &h->dev_bytes);
+    run(h, "scan", [&] { scan_u32_to_u64(h->mult.as<uint32_t>(), h->start.as<uint64_t>(), V, scratch.as<void>(), s); });
+    {
         DevMem cursor;
         cursor.alloc(V * sizeof(uint32_t), &h->dev_bytes);
         CK(cudaMemsetAsync(cursor.as<void>(), 0, V * sizeof(uint32_t), s));
-        h->slot.alloc((Pn + kPad) * sizeof(uint32_t), &h->dev_bytes);
-        run(h, "assign_slots", [&] {
-            launch_assign_slots(h->vidx.as<uint32_t>(), Pn, static_cast<uint32_t>(V), h->start.as<uint64_t>(),
-                                cursor.as<uint32_t>(), h->slot.as<uint32_t>(), s);
+        h->vm_mu.alloc((Pn + kPad) * sizeof(uint32_t), &h->dev_bytes);
+        h->vm_L.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
+        h->vm_T.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
+        run(h, "voxel_major", [&] {
+            launch_build_voxel_major<Real>(h->off.as<uint64_t>(), N, h->vidx.as<uint32_t>(), h->L.as<Real>(),
+                                           h->T.as<Real>(), static_cast<uint32_t>(V), h->start.as<uint64_t>(),
+                                           cursor.as<uint32_t>(), h->vm_mu.as<uint32_t>(), h->vm_L.as<Real>(),
+                                           h->vm_T.as<Real>(), s);
         });
-        h->S.alloc(std::max<uint64_t>(Pn, 1) * sizeof(Real), &h->dev_bytes);
         CK(cudaStreamSynchronize(s));
     }
     scratch.release();
+    h->kvec.alloc((N + kPad) * sizeof(R4), &h->dev_bytes);
 
     // --- tiles of consecutive muons fitting the shared-memory stage ----------
     uint64_t maxpath = 0;
     for (uint64_t i = 0; i < N; ++i) maxpath = std::max<uint64_t>(maxpath, off_h[i + 1] - off_h[i]);
     int TP = P.tile_pairs > 0 ? P.tile_pairs : (std::is_same<Real, double>::value ? 1024 : 2048);
     while (static_cast<uint64_t>(TP) < maxpath) TP *= 2;
-    int TM = std::is_same<Real, double>::value ? 128 : 256;
-    TM = std::min<int>(TM, 65535);
-    if (em_tile_smem_bytes<Real>(TP, TM) > h->smem_optin)
+    const int TM = std::is_same<Real, double>::value ? 128 : 256;
+    if (em_muon_smem_bytes<Real>(TP, TM) > h->smem_optin)
         throw Error(MUTO_ERR_CAPACITY, "longest muon path (" + std::to_string(maxpath) + " voxels) does not fit the shared-memory tile");
     std::vector<uint32_t> tb;
     tb.push_back(0);
@@ -531,21 +531,69 @@ void prepare_em(muto_handle* h) {
     h->tile_muons = TM;
     const double avg = N > 0 ? static_cast<double>(Pn) / static_cast<double>(N) : 0.0;
     h->group = avg <= 32 ? 8 : (avg <= 64 ? 16 : 32);
-    CK(em_tile_configure<Real>(TP, TM));
-    h->tile_blocks = em_tile_blocks<Real>(TP, TM, h->group) * h->num_sms;
+    CK(em_muon_configure<Real>(TP, TM));
+    h->tile_blocks = em_muon_blocks<Real>(TP, TM, h->group) * h->num_sms;
 
-    // --- image and accumulators ---------------------------------------------
+    // --- image ---------------------------------------------------------------
     h->lam.alloc(V * sizeof(Real), &h->dev_bytes);
     {
         std::vector<Real> init_r(init.begin(), init.end());
         CK(cudaMemcpyAsync(h->lam.as<void>(), init_r.data(), V * sizeof(Real), cudaMemcpyHostToDevice, s));
         CK(cudaStreamSynchronize(s));
     }
-    h->G.alloc(V * sizeof(Real), &h->dev_bytes);
-    CK(cudaMemsetAsync(h->G.as<void>(), 0, V * sizeof(Real), s));
     if (h->method == kMap) h->lam_ml.alloc(V * sizeof(double), &h->dev_bytes);
     h->cost_hist.alloc(std::max(P.num_iteration, 1) * 4 * sizeof(double) + 4096 * sizeof(double), &h->dev_bytes);
     CK(cudaStreamSynchronize(s));
+}
+
+template <typename Real>
+MuonPassArgs<Real> muon_args(muto_handle* h, const Real* lam, bool cost) {
+    using R4 = typename Vec4<Real>::type;
+    const Params& P = h->P;
+    const double exy = P.error_xy, ezo = P.error_dz_outer, ezi = P.error_dz_inner;  // src/MutoMLSD.cpp:168-170
+    MuonPassArgs<Real> a;
+    a.off = h->off.as<uint64_t>();
+    a.tile_mb = h->tiles.as<uint32_t>();
+    a.ntiles = h->ntiles;
+    a.vidx = h->vidx.as<uint32_t>();
+    a.L = h->L.as<Real>();
+    a.T = h->T.as<Real>();
+    a.sd = h->sd.as<R4>();
+    a.pr2 = h->pr2.as<Real>();
+    a.lam = lam;
+    a.kout = h->kvec.as<R4>();
+    a.V = static_cast<uint32_t>(h->V());
+    a.E00 = 4.0 * exy * exy / (ezo * ezo);
+    a.E11 = 2.0 * exy * exy * (1.0 + (ezi / ezo + 1.0) * ezi / ezo);
+    a.E01 = 2.0 * exy * exy * ezi / (ezo * ezo);
+    a.compute_cost = cost ? 1 : 0;
+    a.ctr = h->ctr();
+    return a;
+}
+
+template <typename Real, typename OutT>
+VoxelPassArgs<Real, OutT> voxel_args(muto_handle* h, const Real* lam, int mode, OutT* out) {
+    using R4 = typename Vec4<Real>::type;
+    VoxelPassArgs<Real, OutT> v;
+    v.start = h->start.as<uint64_t>();
+    v.mult = h->mult.as<uint32_t>();
+    v.vm_mu = h->vm_mu.as<uint32_t>();
+    v.vm_L = h->vm_L.as<Real>();
+    v.vm_T = h->vm_T.as<Real>();
+    v.kvec = h->kvec.as<R4>();
+    v.lam = lam;
+    v.V = static_cast<uint32_t>(h->V());
+    v.mode = mode;
+    v.pct = h->P.mean_percentile;
+    v.out = out;
+    v.grad = nullptr;
+    v.lam64 = nullptr;
+    return v;
+}
+
+int voxel_mode(const Params& P) {
+    if (!P.update_with_mean) return kVoxMedian;
+    return P.mean_percentile == 100 ? kVoxMean : kVoxPercentile;
 }
 
 // ---------------------------------------------------------------------------
@@ -553,65 +601,23 @@ void prepare_em(muto_handle* h) {
 // ---------------------------------------------------------------------------
 template <typename Real>
 void enqueue_iteration(muto_handle* h) {
-    using R4 = typename Vec4<Real>::type;
     const Params& P = h->P;
     cudaStream_t s = h->stream;
-    const uint32_t V = static_cast<uint32_t>(h->V());
-    const double exy = P.error_xy, ezo = P.error_dz_outer, ezi = P.error_dz_inner;  // src/MutoMLSD.cpp:168-170
-    EmArgs<Real> a;
-    a.off = h->off.as<uint64_t>();
-    a.tile_mb = h->tiles.as<uint32_t>();
-    a.ntiles = h->ntiles;
-    a.vidx = h->vidx.as<uint32_t>();
-    a.L = h->L.as<Real>();
-    a.T = h->T.as<Real>();
-    a.slot = h->store_s ? h->slot.as<uint32_t>() : nullptr;
-    a.sd = h->sd.as<R4>();
-    a.pr2 = h->pr2.as<Real>();
-    a.lam = h->lam.as<Real>();
-    a.S = h->store_s ? h->S.as<Real>() : nullptr;
-    a.G = h->G.as<Real>();
-    a.V = V;
-    a.E00 = 4.0 * exy * exy / (ezo * ezo);
-    a.E11 = 2.0 * exy * exy * (1.0 + (ezi / ezo + 1.0) * ezi / ezo);
-    a.E01 = 2.0 * exy * exy * ezi / (ezo * ezo);
-    a.mode = h->store_s ? kEmMedian : kEmMean;
-    a.compute_cost = h->want_cost() ? 1 : 0;
-    a.ctr = h->ctr();
-    const int blocks = h->tile_blocks;
-    run(h, "em_tile", [&] { launch_em_tile<Real>(a, h->tile_pairs, h->tile_muons, blocks, h->group, s); });
-
-    const bool map = h->method == kMap;
-    if (h->store_s) {
-        if (map)
-            run(h, "em_select", [&] {
-                launch_select<Real, double>(h->S.as<Real>(), h->start.as<uint64_t>(), h->mult.as<uint32_t>(), V,
-                                            P.update_with_mean, P.mean_percentile, h->lam_ml.as<double>(), s);
-            });
-        else
-            run(h, "em_select", [&] {
-                launch_select<Real, Real>(h->S.as<Real>(), h->start.as<uint64_t>(), h->mult.as<uint32_t>(), V,
-                                          P.update_with_mean, P.mean_percentile, h->lam.as<Real>(), s);
-            });
-    } else {
-        if (map)
-            run(h, "em_voxel", [&] {
-                launch_voxel_mean<Real, double>(h->lam.as<Real>(), h->G.as<Real>(), h->mult.as<uint32_t>(), V,
-                                                h->lam_ml.as<double>(), s);
-            });
-        else
-            run(h, "em_voxel", [&] {
-                launch_voxel_mean<Real, Real>(h->lam.as<Real>(), h->G.as<Real>(), h->mult.as<uint32_t>(), V,
-                                              h->lam.as<Real>(), s);
-            });
-    }
-    if (map) {
+    const MuonPassArgs<Real> a = muon_args<Real>(h, h->lam.as<Real>(), h->want_cost());
+    run(h, "em_muon", [&] { launch_em_muon<Real>(a, h->tile_pairs, h->tile_muons, h->tile_blocks, h->group, s); });
+    const int mode = voxel_mode(P);
+    if (h->method == kMap) {  // ML step into lambda_ML, then the MAP step from the snapshot (src/MutoMAP.cpp:138-184)
+        const auto v = voxel_args<Real, double>(h, h->lam.as<Real>(), mode, h->lam_ml.as<double>());
+        run(h, "em_voxel", [&] { launch_em_voxel<Real, double>(v, s); });
         MapParams mp{P.beta, P.p, P.delta, P.eps, P.all_neighbours, P.add_object_prior, P.newton_max_iter};
         run(h, "map_voxel", [&] {
             launch_map_voxel<Real>(h->lam.as<Real>(), h->lam_ml.as<double>(), h->mult.as<uint32_t>(),
                                    make_dev_grid(h->grid), mp, h->ctr(), s);
         });
         run(h, "map_copy", [&] { launch_copy_to<Real>(h->lam_ml.as<double>(), h->lam.as<Real>(), h->V(), s); });
+    } else {  // each warp reads only its own voxel's lambda before writing it: in place
+        const auto v = voxel_args<Real, Real>(h, h->lam.as<Real>(), mode, h->lam.as<Real>());
+        run(h, "em_voxel", [&] { launch_em_voxel<Real, Real>(v, s); });
     }
     const uint32_t cap = static_cast<uint32_t>(h->cost_hist.bytes() / sizeof(double));
     run(h, "cost", [&] { launch_finalize_cost(h->ctr(), static_cast<double>(h->N), h->cost_hist.as<double>(), cap, s); });
@@ -695,8 +701,7 @@ void upload_image(muto_handle* h, const double* in) {
 // Adjoint
 // ---------------------------------------------------------------------------
 template <typename Real>
-double nll_eval(muto_handle* h, const double* loglam_host, double* grad_host, bool dev_input = false) {
-    using R4 = typename Vec4<Real>::type;
+double nll_eval(muto_handle* h, const double* loglam_host, double* grad_host) {
     const uint64_t V = h->V();
     cudaStream_t s = h->stream;
     const size_t pf = h->prof.used;
@@ -708,50 +713,31 @@ double nll_eval(muto_handle* h, const double* loglam_host, double* grad_host, bo
         CK(cudaMemsetAsync(h->dl.as<void>(), 0, V * sizeof(double), s));
     }
     if (h->fval.empty()) h->fval.alloc(sizeof(double), &h->dev_bytes);
-    if (!dev_input)
-        CK(cudaMemcpyAsync(h->loglam.as<double>(), loglam_host, V * sizeof(double), cudaMemcpyHostToDevice, s));
-    // lambda in the storage precision for the muon pass and in FP64 for the prior
+    CK(cudaMemcpyAsync(h->loglam.as<double>(), loglam_host, V * sizeof(double), cudaMemcpyHostToDevice, s));
+    // lambda in FP64 (prior, chain rule) and in the storage precision (muon pass)
     run(h, "exp_lambda", [&] { launch_exp_lambda<double>(h->loglam.as<double>(), h->mult.as<uint32_t>(), static_cast<uint32_t>(V), h->lam64.as<double>(), s); });
     DevMem lamR;
-    Real* lam_r = reinterpret_cast<Real*>(h->lam64.as<double>());
+    const Real* lam_r = reinterpret_cast<const Real*>(h->lam64.as<double>());
     if (!std::is_same<Real, double>::value) {
         lamR.alloc(V * sizeof(Real), &h->dev_bytes);
+        run(h, "exp_lambda", [&] { launch_exp_lambda<Real>(h->loglam.as<double>(), h->mult.as<uint32_t>(), static_cast<uint32_t>(V), lamR.as<Real>(), s); });
         lam_r = lamR.as<Real>();
-        run(h, "exp_lambda", [&] { launch_exp_lambda<Real>(h->loglam.as<double>(), h->mult.as<uint32_t>(), static_cast<uint32_t>(V), lam_r, s); });
     }
     Counters c0;
     CK(cudaMemcpyAsync(&c0, h->ctr(), sizeof(Counters), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     CK(cudaMemsetAsync(&h->ctr()->cost_sum, 0, sizeof(double), s));
-    CK(cudaMemsetAsync(h->G.as<void>(), 0, V * sizeof(Real), s));
-    const Params& P = h->P;
-    const double exy = P.error_xy, ezo = P.error_dz_outer, ezi = P.error_dz_inner;
-    EmArgs<Real> a;
-    a.off = h->off.as<uint64_t>();
-    a.tile_mb = h->tiles.as<uint32_t>();
-    a.ntiles = h->ntiles;
-    a.vidx = h->vidx.as<uint32_t>();
-    a.L = h->L.as<Real>();
-    a.T = h->T.as<Real>();
-    a.slot = nullptr;
-    a.sd = h->sd.as<R4>();
-    a.pr2 = h->pr2.as<Real>();
-    a.lam = lam_r;
-    a.S = nullptr;
-    a.G = h->G.as<Real>();
-    a.V = static_cast<uint32_t>(V);
-    a.E00 = 4.0 * exy * exy / (ezo * ezo);
-    a.E11 = 2.0 * exy * exy * (1.0 + (ezi / ezo + 1.0) * ezi / ezo);
-    a.E01 = 2.0 * exy * exy * ezi / (ezo * ezo);
-    a.mode = grad_host ? kEmMean : kEmCostOnly;
-    a.compute_cost = 1;
-    a.ctr = h->ctr();
+    const MuonPassArgs<Real> a = muon_args<Real>(h, lam_r, true);
     run(h, grad_host ? "nll_backward" : "nll_forward",
-        [&] { launch_em_tile<Real>(a, h->tile_pairs, h->tile_muons, h->tile_blocks, h->group, s); });
+        [&] { launch_em_muon<Real>(a, h->tile_pairs, h->tile_muons, h->tile_blocks, h->group, s); });
     CK(cudaMemsetAsync(h->fval.as<void>(), 0, sizeof(double), s));
-    if (grad_host) {
-        run(h, "grad_finish", [&] { launch_grad_finish<Real>(h->G.as<Real>(), h->lam64.as<double>(), h->mult.as<uint32_t>(), static_cast<uint32_t>(V), h->grad.as<double>(), s); });
+    if (grad_host) {  // d NLL / d log l_j = -l_j sum_i g_ij, per voxel
+        auto v = voxel_args<Real, Real>(h, lam_r, kVoxGradient, nullptr);
+        v.grad = h->grad.as<double>();
+        v.lam64 = h->lam64.as<double>();
+        run(h, "em_voxel_grad", [&] { launch_em_voxel<Real, Real>(v, s); });
     }
+    const Params& P = h->P;
     if (h->method == kMap) {
         MapParams mp{P.beta, P.p, P.delta, P.eps, P.all_neighbours, P.add_object_prior, P.newton_max_iter};
         DevMem gdummy;

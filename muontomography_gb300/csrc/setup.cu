@@ -194,13 +194,22 @@ __global__ void k_voxel_hist(const uint32_t* __restrict__ vidx, uint64_t P, uint
     warp_count(&ctr->bounds, bad);
 }
 
-__global__ void k_assign_slots(const uint32_t* __restrict__ vidx, uint64_t P, uint32_t V,
-                               const uint64_t* __restrict__ start, uint32_t* __restrict__ cursor,
-                               uint32_t* __restrict__ slot) {
-    const uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (k >= P) return;
-    const uint32_t j = vidx[k];
-    slot[k] = j < V ? static_cast<uint32_t>(start[j] + atomicAdd(&cursor[j], 1u)) : 0xffffffffu;
+// thread per muon: its pairs go to the voxel-major lists in its voxels' segments
+template <typename Real>
+__global__ void k_build_voxel_major(const uint64_t* __restrict__ off, uint64_t n, const uint32_t* __restrict__ vidx,
+                                    const Real* __restrict__ L, const Real* __restrict__ T, uint32_t V,
+                                    const uint64_t* __restrict__ start, uint32_t* __restrict__ cursor,
+                                    uint32_t* __restrict__ vm_mu, Real* __restrict__ vm_L, Real* __restrict__ vm_T) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (uint64_t p = off[i]; p < off[i + 1]; ++p) {
+        const uint32_t j = vidx[p];
+        if (j >= V) continue;  // counted by k_voxel_hist
+        const uint64_t at = start[j] + atomicAdd(&cursor[j], 1u);
+        vm_mu[at] = static_cast<uint32_t>(i);
+        vm_L[at] = L[p];
+        vm_T[at] = T[p];
+    }
 }
 
 struct BatchSink {
@@ -279,11 +288,21 @@ void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* m
     k_voxel_hist<<<blocks_for(P), kThreads, 0, s>>>(vidx, P, V, mult, ctr); count_launches(1);
 }
 
-void launch_assign_slots(const uint32_t* vidx, uint64_t P, uint32_t V, const uint64_t* start, uint32_t* cursor,
-                         uint32_t* slot, cudaStream_t s) {
-    if (P == 0) return;
-    k_assign_slots<<<blocks_for(P), kThreads, 0, s>>>(vidx, P, V, start, cursor, slot); count_launches(1);
+template <typename Real>
+void launch_build_voxel_major(const uint64_t* off, uint64_t n, const uint32_t* vidx, const Real* L, const Real* T,
+                              uint32_t V, const uint64_t* start, uint32_t* cursor, uint32_t* vm_mu, Real* vm_L,
+                              Real* vm_T, cudaStream_t s) {
+    if (n == 0) return;
+    k_build_voxel_major<Real><<<blocks_for(n), kThreads, 0, s>>>(off, n, vidx, L, T, V, start, cursor, vm_mu, vm_L,
+                                                                  vm_T);
+    count_launches(1);
 }
+template void launch_build_voxel_major<float>(const uint64_t*, uint64_t, const uint32_t*, const float*, const float*,
+                                              uint32_t, const uint64_t*, uint32_t*, uint32_t*, float*, float*,
+                                              cudaStream_t);
+template void launch_build_voxel_major<double>(const uint64_t*, uint64_t, const uint32_t*, const double*,
+                                               const double*, uint32_t, const uint64_t*, uint32_t*, uint32_t*,
+                                               double*, double*, cudaStream_t);
 
 void launch_siddon_batch(muto_grid g, const double* p1, const double* p2, uint64_t n, uint32_t cap, uint32_t* xyz,
                          double* len, uint32_t* counts, cudaStream_t s) {
