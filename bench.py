@@ -247,27 +247,26 @@ def run_ours(args) -> int:
     ms = allmax(ms_local)
     total_pairs = allsum(float(pairs))
     value = total_pairs * args.steps / (ms / 1000.0)
-    nl, tl = rec.kernel_stats("em_tile")
-    ns, ts = rec.kernel_stats("em_select")
+    nm_, tm_ = rec.kernel_stats("em_muon")
     nv_, tv = rec.kernel_stats("em_voxel")
     rec.set_profiling(False)
-    img_value = rec.image()
     rec.close()
 
-    # algorithmic bytes of one em_tile launch (mixed: 4-byte index, L, T; fp64: 8-byte L, T)
+    # algorithmic bytes per launch (mixed: 4-byte index, L, T; fp64: 8-byte L, T)
     rb = 4 if args.precision == "mixed" else 8
-    per_pair = 4 + 2 * rb + (rb if args.mode == "median" else 0)  # lists read (+ s_ij written)
-    per_muon = 4 * rb + rb + 8                                     # Sx, Dx, Sy, Dy, pr^2, offset
-    per_voxel = rb + (rb if args.mode == "mean" else 0)            # lambda read (+ sum of g)
-    tile_bytes = per_pair * pairs + per_muon * kept + per_voxel * V
+    muon_bytes = (4 + 2 * rb) * pairs + (4 * rb + rb + 8 + 4 * rb) * kept + rb * V  # lists, S/D/pr2/off, k out, lambda
+    voxel_bytes = (4 + 2 * rb) * pairs + (8 + 4 + 2 * rb) * V                       # voxel-major lists, start/M, lambda in/out
     pk = peaks()
-    tile_ms = tl / max(nl, 1)
-    achieved = tile_bytes / (tile_ms / 1000.0) / 1e9 if nl else None
+    muon_ms = tm_ / max(nm_, 1)
+    voxel_ms = tv / max(nv_, 1)
+    achieved = muon_bytes / (muon_ms / 1000.0) / 1e9 if nm_ else None
+    v_ach = voxel_bytes / (voxel_ms / 1000.0) / 1e9 if nv_ else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": (achieved / pk["hbm_gbs"]) if achieved else None, "traffic": args.ncu_traffic,
-                "kernel": "em_tile", "kernel_ms": tile_ms, "algorithmic_bytes": tile_bytes,
-                "peak_source": pk["source"], "select_ms": ts / max(ns, 1) if ns else None,
-                "voxel_ms": tv / max(nv_, 1) if nv_ else None}
+                "kernel": "k_em_muon", "kernel_ms": muon_ms, "algorithmic_bytes": muon_bytes,
+                "peak_source": pk["source"],
+                "voxel_pass": {"kernel": "k_em_voxel", "kernel_ms": voxel_ms, "algorithmic_bytes": voxel_bytes,
+                               "achieved": v_ach, "frac": (v_ach / pk["hbm_gbs"]) if v_ach else None}}
 
     # ---- e2e: full reconstruct through the C ABI from pinned host tracks ------
     e2e = None

@@ -143,6 +143,11 @@ cudaError_t em_muon_configure(int tile_pairs, int tile_muons);
 // resident CTAs per SM (persistent grid = this x SM count)
 template <typename Real>
 int em_muon_blocks(int tile_pairs, int tile_muons, int group);
+// warp-batched variant of the muon pass (no shared memory)
+template <typename Real>
+void launch_em_muon_warp(const MuonPassArgs<Real>& a, uint32_t n_muons, int blocks, int group, cudaStream_t s);
+template <typename Real>
+int em_muon_warp_blocks(int group);
 
 // em_voxel.cu: the voxel pass
 enum VoxelMode { kVoxMedian = 0, kVoxPercentile = 1, kVoxMean = 2, kVoxGradient = 3 };
@@ -161,7 +166,11 @@ struct VoxelPassArgs {
     OutT* out;                                // V new value (median / percentile / mean)
     double* grad;                             // V gradient (kVoxGradient)
     const double* lam64;                      // V lambda in FP64 (kVoxGradient)
+    typename KeyOf<Real>::type* scratch;      // P keys of segments beyond the register budget
 };
+// segments up to this many pairs are selected from registers
+template <typename Real>
+__host__ __device__ constexpr uint32_t voxel_register_cap() { return sizeof(Real) == 4 ? 1536u : 768u; }
 template <typename Real, typename OutT>
 void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, cudaStream_t s);
 void launch_finalize_cost(Counters* ctr, double n_muons, double* hist, uint32_t hist_cap, cudaStream_t s);

@@ -284,6 +284,124 @@ __global__ void __launch_bounds__(kThreads, 2) k_em_muon(MuonPassArgs<Real> a, i
     }
 }
 
+// ---------------------------------------------------------------------------
+// Warp-batched variant: no shared memory and no block barriers.  A warp takes
+// 32 consecutive muons; GROUP lanes sum one muon's lambda_j W_ij with
+// coalesced streaming loads of its pairs and L2 gathers of lambda, the sum
+// lands in the lane of that muon, and the 32 lanes then do the FP64 2x2
+// algebra of their 32 muons together (the FP64 pipe is busy for one warp
+// instruction per 32 muons, not per muon).
+// ---------------------------------------------------------------------------
+template <typename Real, int GROUP>
+__global__ void __launch_bounds__(kThreads) k_em_muon_warp(MuonPassArgs<Real> a, uint32_t n_muons) {
+    using R4 = typename Vec4<Real>::type;
+    constexpr int U = 4;                    // pair loads in flight per lane per round
+    constexpr int kPer = 32 / GROUP;        // muons summed at once per warp
+    const int lane = threadIdx.x & 31;
+    const int sub = lane / GROUP, glane = lane % GROUP;
+    const unsigned gmask = GROUP == 32 ? kFull : (((1u << GROUP) - 1u) << (lane & ~(GROUP - 1)));
+    const uint32_t V = a.V;
+    const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+    const uint64_t nbatch = (static_cast<uint64_t>(n_muons) + 31) / 32;
+    double cost_local = 0.0;
+    unsigned long long singular_local = 0;
+
+    for (uint64_t bt = warp; bt < nbatch; bt += nwarps) {
+        const uint64_t m0 = bt * 32;
+        Real my0 = 0, my1 = 0, my2 = 0;  // the sums of muon m0 + lane
+        for (int q = 0; q < 32; q += kPer) {
+            const uint64_t m = m0 + q + sub;
+            Real c0 = 0, c1 = 0, c2 = 0;
+            if (m < n_muons) {
+                const uint64_t pb = a.off[m], pe = a.off[m + 1];
+                for (uint64_t k0 = pb + glane; k0 < pe; k0 += GROUP * U) {
+                    uint32_t jj[U];
+                    Real ll[U], tt[U], lam[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        const uint64_t k = k0 + static_cast<uint64_t>(u) * GROUP;
+                        jj[u] = 0xffffffffu;
+                        if (k < pe) {
+                            jj[u] = __ldcs(a.vidx + k);
+                            ll[u] = __ldcs(a.L + k);
+                            tt[u] = __ldcs(a.T + k);
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u) lam[u] = jj[u] < V ? __ldg(a.lam + jj[u]) : Real(0);
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        if (jj[u] != 0xffffffffu) {
+                            const Real L = ll[u], T = tt[u], l = lam[u];
+                            const Real LT = L * T;
+                            c0 += l * L;
+                            c1 += l * (LT + L * L * Real(0.5));
+                            c2 += l * (L * L * L * Real(1.0 / 3.0) + (L + T) * LT);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = GROUP / 2; o > 0; o >>= 1) {
+                c0 += __shfl_xor_sync(gmask, c0, o, GROUP);
+                c1 += __shfl_xor_sync(gmask, c1, o, GROUP);
+                c2 += __shfl_xor_sync(gmask, c2, o, GROUP);
+            }
+            // lane q+s takes the sums of group s (its leader is lane s*GROUP)
+            const int src = (lane - q >= 0 && lane - q < kPer) ? (lane - q) * GROUP : 0;
+            const Real v0 = __shfl_sync(kFull, c0, src), v1 = __shfl_sync(kFull, c1, src),
+                       v2 = __shfl_sync(kFull, c2, src);
+            if (lane - q >= 0 && lane - q < kPer) {
+                my0 = v0;
+                my1 = v1;
+                my2 = v2;
+            }
+        }
+        // ---- FP64 2x2 algebra of the warp's 32 muons, one per lane ----------
+        const uint64_t m = m0 + lane;
+        if (m < n_muons) {
+            const Real pr2 = a.pr2[m];
+            const double p2 = static_cast<double>(pr2);
+            const double S00 = p2 * static_cast<double>(my0) + a.E00;
+            const double S01 = p2 * static_cast<double>(my1) + a.E01;
+            const double S11 = p2 * static_cast<double>(my2) + a.E11;
+            const double det = S00 * S11 - S01 * S01;
+            R4 kv;
+            kv.x = kv.y = kv.z = kv.w = Real(0);
+            if (fabs(det) > 1e-12) {  // Eigen computeInverseAndDetWithCheck threshold
+                const double r = 1.0 / det;
+                const double i00 = S11 * r, i01 = -S01 * r, i11 = S00 * r;
+                const R4 v = a.sd[m];
+                const Real f00 = static_cast<Real>(i00), f01 = static_cast<Real>(i01), f11 = static_cast<Real>(i11);
+                const Real ux0 = f00 * v.x + f01 * v.y, ux1 = f01 * v.x + f11 * v.y;
+                const Real uy0 = f00 * v.z + f01 * v.w, uy1 = f01 * v.z + f11 * v.w;
+                kv.x = pr2 * (Real(0.5) * (ux0 * ux0 + uy0 * uy0) - f00);
+                kv.y = pr2 * ((ux0 * ux1 + uy0 * uy1) - Real(2) * f01);
+                kv.z = pr2 * (Real(0.5) * (ux1 * ux1 + uy1 * uy1) - f11);
+                if (det <= 0) {
+                    ++singular_local;
+                } else if (a.compute_cost) {
+                    const double sx = v.x, dx = v.y, sy = v.z, dy = v.w;
+                    cost_local += log(det) + ((sx * sx + sy * sy) * i00 + (dx * dx + dy * dy) * i11 +
+                                              (sx * dx + sy * dy) * 2.0 * i01) * 0.5;
+                }
+            } else {
+                ++singular_local;
+            }
+            a.kout[m] = kv;
+        }
+    }
+    const double c = warp_sum(cost_local);
+    unsigned long long ns = singular_local;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ns += __shfl_xor_sync(kFull, ns, o);
+    if (lane == 0) {
+        if (a.compute_cost && c != 0.0) atomicAdd(&a.ctr->cost_sum, c);
+        if (ns) atomicAdd(&a.ctr->singular, ns);
+    }
+}
+
 template <typename Real, int G>
 cudaError_t set_smem(size_t smem) {
     return cudaFuncSetAttribute(k_em_muon<Real, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -335,5 +453,31 @@ void launch_em_muon(const MuonPassArgs<Real>& a, int tile_pairs, int tile_muons,
 }
 template void launch_em_muon<float>(const MuonPassArgs<float>&, int, int, int, int, cudaStream_t);
 template void launch_em_muon<double>(const MuonPassArgs<double>&, int, int, int, int, cudaStream_t);
+
+template <typename Real>
+int em_muon_warp_blocks(int group) {
+    int n = 0;
+    cudaError_t e;
+    if (group <= 8) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_em_muon_warp<Real, 8>, kThreads, 0);
+    else if (group <= 16) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_em_muon_warp<Real, 16>, kThreads, 0);
+    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_em_muon_warp<Real, 32>, kThreads, 0);
+    return (e == cudaSuccess && n > 0) ? n : 1;
+}
+template int em_muon_warp_blocks<float>(int);
+template int em_muon_warp_blocks<double>(int);
+
+template <typename Real>
+void launch_em_muon_warp(const MuonPassArgs<Real>& a, uint32_t n_muons, int blocks, int group, cudaStream_t s) {
+    if (n_muons == 0) return;
+    const uint64_t batches = (static_cast<uint64_t>(n_muons) + 31) / 32;
+    const uint64_t need = (batches + kThreads / 32 - 1) / (kThreads / 32);
+    const unsigned nb = static_cast<unsigned>(need < static_cast<uint64_t>(blocks) ? need : blocks);
+    if (group <= 8) k_em_muon_warp<Real, 8><<<nb, kThreads, 0, s>>>(a, n_muons);
+    else if (group <= 16) k_em_muon_warp<Real, 16><<<nb, kThreads, 0, s>>>(a, n_muons);
+    else k_em_muon_warp<Real, 32><<<nb, kThreads, 0, s>>>(a, n_muons);
+    count_launches(1);
+}
+template void launch_em_muon_warp<float>(const MuonPassArgs<float>&, uint32_t, int, int, cudaStream_t);
+template void launch_em_muon_warp<double>(const MuonPassArgs<double>&, uint32_t, int, int, cudaStream_t);
 
 }  // namespace muto

@@ -92,9 +92,10 @@ __device__ K kth_radix(const Src& src, uint32_t k) {
     return prefix;
 }
 
-// keys staged in shared memory (the window candidates)
+// keys in memory (the window candidates in shared memory, or a long
+// segment's keys in the global scratch array)
 template <typename K>
-struct SmemKeys {
+struct PtrKeys {
     const K* p;
     uint32_t n;
     int lane;
@@ -102,6 +103,15 @@ struct SmemKeys {
     __device__ __forceinline__ void each(F f) const {
         for (uint32_t i = lane; i < n; i += 32) f(p[i]);
     }
+    template <class F>
+    __device__ __forceinline__ void each_all(F f) const {
+        for (uint32_t i0 = 0; i0 < n; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            f(i < n ? p[i] : K(0), i < n);
+        }
+    }
+    __device__ __forceinline__ K sample() const { return p[(static_cast<uint64_t>(lane) * n) / 32u]; }
+    __device__ __forceinline__ uint32_t size() const { return n; }
 };
 
 // The voxel's s_ij as order-preserving keys, element r*32+lane in key[r].
@@ -117,41 +127,23 @@ struct VoxKeys {
         for (int r = 0; r < R; ++r)
             if (static_cast<uint32_t>(r * 32 + lane) < M) f(key[r]);
     }
-};
-
-// Same keys recomputed from global memory for segments longer than the register budget.
-template <typename Real>
-struct StreamKeys {
-    using K = typename KeyOf<Real>::type;
-    using R4 = typename Vec4<Real>::type;
-    const uint32_t* mu;
-    const Real* L;
-    const Real* T;
-    const R4* kv;
-    Real lam;
-    uint32_t M;
-    int lane;
     template <class F>
-    __device__ __forceinline__ void each(F f) const {
-        for (uint32_t i = lane; i < M; i += 32) {
-            const R4 k = ldg4(kv + mu[i]);
-            const Real l = L[i], t = T[i];
-            const Real lt = l * t;
-            const Real g = k.x * l + k.y * (lt + l * l * Real(0.5)) + k.z * (l * l * l * Real(1.0 / 3.0) + (l + t) * lt);
-            f(to_key(Real(2) * lam + g * lam * lam));
-        }
+    __device__ __forceinline__ void each_all(F f) const {
+#pragma unroll
+        for (int r = 0; r < R; ++r) f(key[r], static_cast<uint32_t>(r * 32 + lane) < M);
     }
+    __device__ __forceinline__ K sample() const { return key[0]; }  // element `lane`: positions follow slot order
+    __device__ __forceinline__ uint32_t size() const { return M; }
 };
 
-// k-th smallest with a sampled window (registers), exact.
-template <typename Real, int R>
-__device__ typename KeyOf<Real>::type kth_window(const VoxKeys<Real, R>& v, uint32_t k,
-                                                 typename KeyOf<Real>::type* cand) {
-    using K = typename KeyOf<Real>::type;
-    const int lane = v.lane;
-    // 32 samples: element `lane` of the segment (key[0]); positions follow the
-    // slot order, which is unrelated to the values
-    K s = v.key[0];
+// k-th smallest with a sampled window, exact: sort 32 samples, take the
+// samples 6 ranks either side of the target as the window, count the keys
+// below it and compact the keys inside it into shared memory, then search the
+// window; a window that misses the target falls back to the full search.
+template <typename K, class Src>
+__device__ K kth_window(const Src& v, uint32_t k, K* cand, int lane) {
+    const uint32_t M = v.size();
+    K s = v.sample();
 #pragma unroll
     for (int size = 2; size <= 32; size <<= 1) {
 #pragma unroll
@@ -162,7 +154,7 @@ __device__ typename KeyOf<Real>::type kth_window(const VoxKeys<Real, R>& v, uint
             s = (lower == up) ? (o < s ? o : s) : (o > s ? o : s);
         }
     }
-    const int pos = static_cast<int>((static_cast<uint64_t>(k) * 32u) / v.M);
+    const int pos = static_cast<int>((static_cast<uint64_t>(k) * 32u) / M);
     const int ql = pos - 6, qh = pos + 6;
     const K slo = __shfl_sync(kFull, s, ql < 0 ? 0 : ql);
     const K shi = __shfl_sync(kFull, s, qh > 31 ? 31 : qh);
@@ -170,10 +162,8 @@ __device__ typename KeyOf<Real>::type kth_window(const VoxKeys<Real, R>& v, uint
     const K hi = qh > 31 ? ~K(0) : shi;
     uint32_t c_lo = 0, c_in = 0;
     const unsigned below_me = (1u << lane) - 1u;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        const bool valid = static_cast<uint32_t>(r * 32 + lane) < v.M;
-        const K x = v.key[r];
+    // lanes walk the keys in lock step (each() visits r*32+lane / i = lane + 32 t)
+    auto visit = [&](K x, bool valid) {
         const bool lt = valid && x < lo;
         const bool in = valid && !lt && x <= hi;
         c_lo += __popc(__ballot_sync(kFull, lt));
@@ -183,11 +173,12 @@ __device__ typename KeyOf<Real>::type kth_window(const VoxKeys<Real, R>& v, uint
             if (at < kCap) cand[at] = x;
         }
         c_in += __popc(m);
-    }
+    };
+    v.each_all(visit);
     __syncwarp();
     K res;
     if (c_lo <= k && k < c_lo + c_in && c_in <= kCap) {
-        SmemKeys<K> src{cand, c_in, lane};
+        PtrKeys<K> src{cand, c_in, lane};
         res = kth_radix<K>(src, k - c_lo);
     } else {
         res = kth_radix<K>(v, k);
@@ -199,13 +190,13 @@ __device__ typename KeyOf<Real>::type kth_window(const VoxKeys<Real, R>& v, uint
 template <typename Real, int R>
 __device__ __forceinline__ typename KeyOf<Real>::type kth_any(const VoxKeys<Real, R>& v, uint32_t k,
                                                               typename KeyOf<Real>::type* cand) {
-    if (R >= 4) return kth_window<Real, R>(v, k, cand);
-    return kth_radix<typename KeyOf<Real>::type>(v, k);
+    using K = typename KeyOf<Real>::type;
+    if (R >= 4) return kth_window<K>(v, k, cand, v.lane);
+    return kth_radix<K>(v, k);
 }
-template <typename Real>
-__device__ __forceinline__ typename KeyOf<Real>::type kth_any(const StreamKeys<Real>& v, uint32_t k,
-                                                              typename KeyOf<Real>::type*) {
-    return kth_radix<typename KeyOf<Real>::type>(v, k);
+template <typename K>
+__device__ __forceinline__ K kth_any(const PtrKeys<K>& v, uint32_t k, K* cand) {
+    return kth_window<K>(v, k, cand, v.lane);
 }
 
 // the voxel's new value from its keys (median or percentile mean)
@@ -306,23 +297,30 @@ __device__ __forceinline__ void voxel_regs(const VoxelPassArgs<Real, OutT>& a, u
     if (lane == 0) a.out[j] = static_cast<OutT>(out);
 }
 
+// segments longer than the register budget: the keys go once to the scratch
+// array (same offsets as the voxel-major lists) and the selection reads them there
 template <typename Real, typename OutT>
 __device__ void voxel_stream(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uint64_t base, uint32_t M, int lane,
                              typename KeyOf<Real>::type* cand) {
+    using K = typename KeyOf<Real>::type;
     const Real lam = a.lam[j];
-    StreamKeys<Real> src{a.vm_mu + base, a.vm_L + base, a.vm_T + base, a.kvec, lam, M, lane};
+    const bool keys = a.mode == kVoxMedian || a.mode == kVoxPercentile;
+    K* kp = a.scratch + base;
+    double gs = 0.0;
+    for (uint32_t i = lane; i < M; i += 32) {
+        const auto k = ldg4(a.kvec + __ldcs(a.vm_mu + base + i));
+        const Real l = __ldcs(a.vm_L + base + i), t = __ldcs(a.vm_T + base + i);
+        const Real lt = l * t;
+        const Real g = k.x * l + k.y * (lt + l * l * Real(0.5)) + k.z * (l * l * l * Real(1.0 / 3.0) + (l + t) * lt);
+        if (keys) kp[i] = to_key(Real(2) * lam + g * lam * lam);
+        else gs += static_cast<double>(g);
+    }
     double out;
-    if (a.mode == kVoxMedian || a.mode == kVoxPercentile) {
+    if (keys) {
+        __syncwarp();  // the lanes' key stores are visible to the whole warp
+        PtrKeys<K> src{kp, M, lane};
         out = order_update<Real>(src, M, a.mode, a.pct, cand);
     } else {
-        double gs = 0.0;
-        for (uint32_t i = lane; i < M; i += 32) {
-            const auto k = ldg4(a.kvec + a.vm_mu[base + i]);
-            const Real l = a.vm_L[base + i], t = a.vm_T[base + i];
-            const Real lt = l * t;
-            gs += static_cast<double>(k.x * l + k.y * (lt + l * l * Real(0.5)) +
-                                      k.z * (l * l * l * Real(1.0 / 3.0) + (l + t) * lt));
-        }
         gs = warp_sum(gs);
         if (a.mode == kVoxGradient) {
             if (lane == 0) a.grad[j] = -a.lam64[j] * gs;
@@ -362,7 +360,7 @@ __global__ void __launch_bounds__(kVoxThreads) k_em_voxel(VoxelPassArgs<Real, Ou
     else if (M <= 512u) voxel_regs<Real, 16>(a, j, base, M, lane, cand);
     else if (M <= 768u) voxel_regs<Real, 24>(a, j, base, M, lane, cand);
     else {
-        if constexpr (sizeof(Real) == 4) {  // 64-bit keys stay at 24 registers per lane
+        if constexpr (voxel_register_cap<Real>() > 768u) {  // 64-bit keys stay at 24 registers per lane
             if (M <= 1024u) {
                 voxel_regs<Real, 32>(a, j, base, M, lane, cand);
                 return;

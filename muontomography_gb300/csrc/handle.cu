@@ -103,6 +103,7 @@ struct Params {
     int compute_cost = -1;
     int newton_max_iter = 200;
     int tile_pairs = 0;
+    int muon_pass = 0;  // 0 autotune, 1 tile (TMA), 2 warp-batched
 };
 
 Params parse_params(Method m, const std::string& text) {
@@ -175,6 +176,11 @@ Params parse_params(Method m, const std::string& text) {
         if (cfg.contains("compute_cost")) P.compute_cost = cfg.value("compute_cost", false) ? 1 : 0;
         P.newton_max_iter = cfg.value("newton_max_iter", 200);
         P.tile_pairs = cfg.value("tile_pairs", 0);
+        const std::string mp = cfg.value("muon_pass", "auto");
+        if (mp == "auto") P.muon_pass = 0;
+        else if (mp == "tile") P.muon_pass = 1;
+        else if (mp == "warp") P.muon_pass = 2;
+        else throw Error(MUTO_ERR_CONFIG, "muon_pass must be \"auto\", \"tile\" or \"warp\"");
         if (P.newton_max_iter < 1) throw Error(MUTO_ERR_CONFIG, "newton_max_iter must be >= 1");
     } catch (const json::type_error& e) {
         throw Error(MUTO_ERR_CONFIG, std::string("config value of the wrong type: ") + e.what());
@@ -268,11 +274,13 @@ struct muto_handle {
     DevMem kept, sd, pr2, scat, pr64, off;
     DevMem vidx, L, T;            // muon-major pair lists
     DevMem vm_mu, vm_L, vm_T;     // voxel-major copy
-    DevMem mult, start, kvec;
+    DevMem mult, start, kvec, keys;   // keys: scratch for voxels beyond the register budget
     DevMem lam, lam_ml, cost_hist;
     DevMem tiles;
     uint32_t ntiles = 0;
     int tile_pairs = 0, tile_muons = 0, group = 32, tile_blocks = 0;
+    int muon_kind = 1, muon_group = 32, warp_blocks = 0;  // chosen muon-pass variant
+    float tune_ms[4] = {0, 0, 0, 0};
     bool prepared = false;
     int iters = 0;
     bool stopped = false;
@@ -505,6 +513,13 @@ void prepare_em(muto_handle* h) {
     }
     scratch.release();
     h->kvec.alloc((N + kPad) * sizeof(R4), &h->dev_bytes);
+    {  // voxels with more pairs than the register budget select from a scratch key array
+        std::vector<uint32_t> m_h(V);
+        CK(cudaMemcpy(m_h.data(), h->mult.as<void>(), V * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        const uint32_t mmax = V ? *std::max_element(m_h.begin(), m_h.end()) : 0u;
+        if (mmax > voxel_register_cap<Real>())
+            h->keys.alloc(std::max<uint64_t>(Pn, 1) * sizeof(typename KeyOf<Real>::type), &h->dev_bytes);
+    }
 
     // --- tiles of consecutive muons fitting the shared-memory stage ----------
     uint64_t maxpath = 0;
@@ -547,6 +562,14 @@ void prepare_em(muto_handle* h) {
 }
 
 template <typename Real>
+void launch_muon_pass(muto_handle* h, const MuonPassArgs<Real>& a, cudaStream_t s) {
+    if (h->muon_kind == 2)
+        launch_em_muon_warp<Real>(a, static_cast<uint32_t>(h->N), h->warp_blocks, h->muon_group, s);
+    else
+        launch_em_muon<Real>(a, h->tile_pairs, h->tile_muons, h->tile_blocks, h->group, s);
+}
+
+template <typename Real>
 MuonPassArgs<Real> muon_args(muto_handle* h, const Real* lam, bool cost) {
     using R4 = typename Vec4<Real>::type;
     const Params& P = h->P;
@@ -571,6 +594,62 @@ MuonPassArgs<Real> muon_args(muto_handle* h, const Real* lam, bool cost) {
     return a;
 }
 
+// In-project autotuner: time the candidate muon-pass variants on this scan's
+// own lists (one warm-up and three timed launches each) and keep the fastest.
+template <typename Real>
+void autotune_muon_pass(muto_handle* h) {
+    if (h->N == 0) return;
+    struct Cand {
+        int kind, group;
+    };
+    std::vector<Cand> cands;
+    if (h->P.muon_pass != 2) cands.push_back({1, h->group});
+    if (h->P.muon_pass != 1)
+        for (int g : {8, 16, 32}) cands.push_back({2, g});
+    auto apply = [&](const Cand& c) {
+        h->muon_kind = c.kind;
+        h->muon_group = c.group;
+        if (c.kind == 2) h->warp_blocks = em_muon_warp_blocks<Real>(c.group) * h->num_sms;
+    };
+    if (cands.size() == 1) {
+        apply(cands[0]);
+        return;
+    }
+    cudaStream_t s = h->stream;
+    Counters saved;
+    CK(cudaMemcpyAsync(&saved, h->ctr(), sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const MuonPassArgs<Real> a = muon_args<Real>(h, h->lam.as<Real>(), false);
+    float best = 1e30f;
+    Cand pick = cands[0];
+    for (size_t i = 0; i < cands.size(); ++i) {
+        apply(cands[i]);
+        launch_muon_pass<Real>(h, a, s);
+        CK(cudaEventRecord(e0, s));
+        for (int r = 0; r < 3; ++r) launch_muon_pass<Real>(h, a, s);
+        CK(cudaEventRecord(e1, s));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaGetLastError());
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= 3.f;
+        if (i < 4) h->tune_ms[i] = ms;
+        if (ms < best) {
+            best = ms;
+            pick = cands[i];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    h->launches += 4 * cands.size();
+    apply(pick);
+    CK(cudaMemcpyAsync(h->ctr(), &saved, sizeof(Counters), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+}
+
 template <typename Real, typename OutT>
 VoxelPassArgs<Real, OutT> voxel_args(muto_handle* h, const Real* lam, int mode, OutT* out) {
     using R4 = typename Vec4<Real>::type;
@@ -588,6 +667,7 @@ VoxelPassArgs<Real, OutT> voxel_args(muto_handle* h, const Real* lam, int mode, 
     v.out = out;
     v.grad = nullptr;
     v.lam64 = nullptr;
+    v.scratch = h->keys.empty() ? nullptr : h->keys.as<typename KeyOf<Real>::type>();
     return v;
 }
 
@@ -604,7 +684,7 @@ void enqueue_iteration(muto_handle* h) {
     const Params& P = h->P;
     cudaStream_t s = h->stream;
     const MuonPassArgs<Real> a = muon_args<Real>(h, h->lam.as<Real>(), h->want_cost());
-    run(h, "em_muon", [&] { launch_em_muon<Real>(a, h->tile_pairs, h->tile_muons, h->tile_blocks, h->group, s); });
+    run(h, "em_muon", [&] { launch_muon_pass<Real>(h, a, s); });
     const int mode = voxel_mode(P);
     if (h->method == kMap) {  // ML step into lambda_ML, then the MAP step from the snapshot (src/MutoMAP.cpp:138-184)
         const auto v = voxel_args<Real, double>(h, h->lam.as<Real>(), mode, h->lam_ml.as<double>());
@@ -729,7 +809,7 @@ double nll_eval(muto_handle* h, const double* loglam_host, double* grad_host) {
     CK(cudaMemsetAsync(&h->ctr()->cost_sum, 0, sizeof(double), s));
     const MuonPassArgs<Real> a = muon_args<Real>(h, lam_r, true);
     run(h, grad_host ? "nll_backward" : "nll_forward",
-        [&] { launch_em_muon<Real>(a, h->tile_pairs, h->tile_muons, h->tile_blocks, h->group, s); });
+        [&] { launch_muon_pass<Real>(h, a, s); });
     CK(cudaMemsetAsync(h->fval.as<void>(), 0, sizeof(double), s));
     if (grad_host) {  // d NLL / d log l_j = -l_j sum_i g_ij, per voxel
         auto v = voxel_args<Real, Real>(h, lam_r, kVoxGradient, nullptr);
@@ -838,6 +918,10 @@ int muto_get_status(const muto_handle* hc, muto_status* out) {
     out->cost = c.cost_last;
     out->cost_prev = c.cost_prev;
     out->device_bytes = h->dev_bytes.load();
+    out->muon_pass = h->method == kPoca ? 0 : h->muon_kind;
+    out->muon_group = h->muon_kind == 2 ? h->muon_group : h->group;
+    out->tile_pairs = h->tile_pairs;
+    out->tile_muons = h->tile_muons;
     std::snprintf(out->message, sizeof(out->message), "%s", h->last_msg.c_str());
     return MUTO_OK;
 }
@@ -890,8 +974,10 @@ int muto_prepare(muto_handle* h) {
             prepare_poca(h);
         } else if (h->fp64()) {
             prepare_em<double>(h);
+            autotune_muon_pass<double>(h);
         } else {
             prepare_em<float>(h);
+            autotune_muon_pass<float>(h);
         }
         sync_and_harvest(h, pf);
         h->prepared = true;

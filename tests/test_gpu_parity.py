@@ -235,3 +235,48 @@ def test_nll_and_gradient_match_oracle(gpu, oracle):
     assert abs(v - rv) <= 1e-10 * abs(rv)
     assert abs(v2 - rv) <= 1e-10 * abs(rv)
     assert rel_l2(g, rg) < 1e-9
+
+
+# ---------------------------------------------------------------------------
+# Long voxel segments and the muon-pass variants
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_TOL)])
+@pytest.mark.parametrize("mode", ["median", "percentile", "mean"])
+def test_long_segments_match_oracle(gpu, oracle, precision, tol, mode):
+    # 4^3 voxels and 30k muons: thousands of pairs per voxel, beyond the register budget
+    wl = W.small(n_muons=30000, seed=111, n=4)
+    rays = wl.tracks()
+    over = {"median": {}, "mean": {"update_with_mean": True},
+            "percentile": {"update_with_mean": True, "mean_percentile": 80}}[mode]
+    cfg = wl.em_config(precision=precision, num_iteration=3, **over)
+    ref = oracle.Mlsd(wl.grid, cfg, rays, np.full(wl.grid.nvox, 1e-7))
+    ref.iterate(3)
+    with M.MutoMLSD(cfg) as rec:
+        rec.load_tracks(rays)
+        rec.prepare()
+        assert rec.multiplicity().max() > 1600
+        rec.iterate(3)
+        img = rec.image()
+    assert rel_l2(img.reshape(-1, order="F"), ref.image()) < tol
+
+
+@pytest.mark.parametrize("variant", ["tile", "warp"])
+def test_muon_pass_variants_agree(gpu, oracle, variant):
+    wl = W.small(n_muons=8000, seed=121)
+    rays = wl.tracks()
+    cfg = wl.em_config(precision="fp64", num_iteration=4, muon_pass=variant)
+    ref = _mlsd_pair(oracle, wl, rays, cfg, np.full(wl.grid.nvox, 1e-7), 4)
+    with M.MutoMLSD(cfg) as rec:
+        img = rec.reconstruct(rays)
+        st = rec.status()
+    assert st["muon_pass"] == {"tile": 1, "warp": 2}[variant]
+    assert rel_l2(img.reshape(-1, order="F"), ref.image()) < FP64_TOL
+
+
+def test_autotuner_reports_its_choice(gpu):
+    wl = W.small(n_muons=8000, seed=131)
+    with M.MutoMLSD(wl.em_config()) as rec:
+        rec.load_tracks(wl.tracks())
+        rec.prepare()
+        st = rec.status()
+    assert st["muon_pass"] in (1, 2) and st["muon_group"] in (8, 16, 32)
