@@ -113,7 +113,7 @@ def workload(args, rank: int):
 
 
 def em_config(wl, args, precision: str, n_iter: int) -> dict:
-    over = {"precision": precision, "num_iteration": n_iter}
+    over = {"precision": precision, "num_iteration": n_iter, "muon_pass": args.muon_pass}
     if args.mode == "mean":
         over.update(update_with_mean=True, mean_percentile=100)
     return wl.em_config(**over)
@@ -351,7 +351,8 @@ def run_ours(args) -> int:
                        "precision": args.precision, "per_muon_2x2": "f64", "graph": True,
                        "parallelism": f"replicas x{world} (one scan per GPU)",
                        "l2": "inputs larger than L2: pair lists and s_ij far exceed 126 MB, no flush",
-                       "setup_s": t_setup, "generate_s": t_gen},
+                                  "setup_s": t_setup, "generate_s": t_gen, "muon_pass": {1: "tma_tiles", 2: "warp_batched"}.get(st["muon_pass"]),
+            "muon_group": st["muon_group"], "tile_pairs": st["tile_pairs"]},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
@@ -379,6 +380,7 @@ def main() -> int:
     ap.add_argument("--e2e-iters", type=int, default=10)
     ap.add_argument("--ttl-iters", type=int, default=50)
     ap.add_argument("--cpu-sample", type=int, default=150_000)
+    ap.add_argument("--muon-pass", choices=["auto", "tile", "warp"], default="auto")
     ap.add_argument("--ncu-traffic", type=float, default=None,
                     help="dram bytes per em_tile launch from an ncu capture (profiles/)")
     args = ap.parse_args()
