@@ -19,6 +19,9 @@ constexpr unsigned kFull = 0xffffffffu;
 template <typename Real> struct Vec4;
 template <> struct Vec4<float> { using type = float4; };
 template <> struct Vec4<double> { using type = double4; };
+template <typename Real> struct Vec2;
+template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<double> { using type = double2; };
 
 // Order-preserving integer keys for the per-voxel selection.
 __device__ __forceinline__ uint32_t to_key(float f) {
@@ -94,8 +97,8 @@ void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* m
 // voxel-major copy of the pair lists: (muon, L, T) at start[j] + rank within voxel j
 template <typename Real>
 void launch_build_voxel_major(const uint64_t* off, uint64_t n, const uint32_t* vidx, const Real* L, const Real* T,
-                              uint32_t V, const uint64_t* start, uint32_t* cursor, uint32_t* vm_mu, Real* vm_L,
-                              Real* vm_T, cudaStream_t s);
+                              uint32_t V, const uint64_t* start, uint32_t* cursor, uint32_t* vm_mu,
+                              typename Vec2<Real>::type* vm_LT, cudaStream_t s);
 void launch_siddon_batch(muto_grid g, const double* p1, const double* p2, uint64_t n, uint32_t cap, uint32_t* xyz,
                          double* len, uint32_t* counts, cudaStream_t s);
 
@@ -156,8 +159,7 @@ struct VoxelPassArgs {
     const uint64_t* start;                    // V+1 segment starts of the voxel-major lists
     const uint32_t* mult;                     // V pairs per voxel
     const uint32_t* vm_mu;                    // P muon of each voxel-major pair
-    const Real* vm_L;                         // P
-    const Real* vm_T;                         // P
+    const typename Vec2<Real>::type* vm_LT;   // P (L, T) of each voxel-major pair
     const typename Vec4<Real>::type* kvec;    // N per-muon coefficients
     const Real* lam;                          // V lambda of the iteration
     uint32_t V;
@@ -171,8 +173,11 @@ struct VoxelPassArgs {
 // segments up to this many pairs are selected from registers
 template <typename Real>
 __host__ __device__ constexpr uint32_t voxel_register_cap() { return sizeof(Real) == 4 ? 1536u : 768u; }
+// voxels in three classes by segment length (lists[c], counts[c]): M <= 256,
+// M <= 768, longer; voxels without pairs go with the first class
 template <typename Real, typename OutT>
-void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, cudaStream_t s);
+void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const uint32_t* const* lists, const uint32_t* counts,
+                     cudaStream_t s);
 void launch_finalize_cost(Counters* ctr, double n_muons, double* hist, uint32_t hist_cap, cudaStream_t s);
 
 struct MapParams {

@@ -9,16 +9,19 @@
 //     s_ij = 2 l_j + (k0 W00 + k1 W01 + k2 W11) l_j^2,
 // the reference's 2 l + (1/2 xyS - tr(Sigma^-1 W)) pr^2 l^2.  No s_ij array is
 // written; nothing is accumulated with atomics.
-//   median       exact order statistics of the s_ij (nth_element semantics):
-//                a 32-element sample of the segment is sorted in the warp, the
-//                window around the target rank is counted and its members
-//                compacted in shared memory, and the k-th key is found there by
-//                a bitwise radix search; a window that misses falls back to
-//                the radix search over all keys.
+//   median       exact order statistics of the s_ij (nth_element semantics).
+//                Two rounds of sampling narrow the search: 32 samples of the
+//                segment are sorted in the warp, the keys within 6 sample ranks
+//                of the target are counted and compacted into shared memory,
+//                the same is done once more on the compacted keys, and the
+//                survivors (<= 64) are sorted by a warp bitonic sort.  A window
+//                that misses the target falls back to a bitwise radix search.
 //   percentile   mean of the lowest floor(pct/100 M) values: the order
 //                statistic t plus the sum of the values below it.
 //   mean         l + l^2 (sum_i g_ij) / (2 M)  ==  (sum_i s_ij) / M / 2.
 //   gradient     d NLL / d log l_j = -l_j sum_i g_ij (the adjoint).
+// Voxels are grouped by segment length into classes, each its own kernel
+// instantiation, so short segments run with few registers and many warps.
 #include "common.cuh"
 
 namespace muto {
@@ -26,7 +29,10 @@ namespace {
 
 constexpr int kVoxThreads = 256;
 constexpr int kWarps = kVoxThreads / 32;
-constexpr int kCap = 640;  // window candidates kept per warp
+
+template <typename K> struct CandCap;
+template <> struct CandCap<uint32_t> { static constexpr int c1 = 640, c2 = 128; };
+template <> struct CandCap<unsigned long long> { static constexpr int c1 = 448, c2 = 128; };
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 __device__ __forceinline__ double4 ldg4(const double4* p) {
@@ -92,8 +98,8 @@ __device__ K kth_radix(const Src& src, uint32_t k) {
     return prefix;
 }
 
-// keys in memory (the window candidates in shared memory, or a long
-// segment's keys in the global scratch array)
+// keys in memory (window candidates in shared memory, or a long segment's
+// keys in the global scratch array)
 template <typename K>
 struct PtrKeys {
     const K* p;
@@ -110,7 +116,7 @@ struct PtrKeys {
             f(i < n ? p[i] : K(0), i < n);
         }
     }
-    __device__ __forceinline__ K sample() const { return p[(static_cast<uint64_t>(lane) * n) / 32u]; }
+    __device__ __forceinline__ K sample() const { return p[(lane * n) >> 5]; }
     __device__ __forceinline__ uint32_t size() const { return n; }
 };
 
@@ -136,14 +142,9 @@ struct VoxKeys {
     __device__ __forceinline__ uint32_t size() const { return M; }
 };
 
-// k-th smallest with a sampled window, exact: sort 32 samples, take the
-// samples 6 ranks either side of the target as the window, count the keys
-// below it and compact the keys inside it into shared memory, then search the
-// window; a window that misses the target falls back to the full search.
-template <typename K, class Src>
-__device__ K kth_window(const Src& v, uint32_t k, K* cand, int lane) {
-    const uint32_t M = v.size();
-    K s = v.sample();
+// ascending warp bitonic sort of one key per lane
+template <typename K>
+__device__ __forceinline__ K sort32(K s, int lane) {
 #pragma unroll
     for (int size = 2; size <= 32; size <<= 1) {
 #pragma unroll
@@ -154,58 +155,119 @@ __device__ K kth_window(const Src& v, uint32_t k, K* cand, int lane) {
             s = (lower == up) ? (o < s ? o : s) : (o > s ? o : s);
         }
     }
-    const int pos = static_cast<int>((static_cast<uint64_t>(k) * 32u) / M);
+    return s;
+}
+
+// k-th smallest of n <= 64 keys in shared memory: warp bitonic sort of 64
+// (element e = 2 lane + t held in register t of its lane), then a shuffle
+template <typename K>
+__device__ K kth_sort64(const K* c, uint32_t n, uint32_t k, int lane) {
+    K a = static_cast<uint32_t>(2 * lane) < n ? c[2 * lane] : ~K(0);
+    K b = static_cast<uint32_t>(2 * lane + 1) < n ? c[2 * lane + 1] : ~K(0);
+#pragma unroll
+    for (int size = 2; size <= 64; size <<= 1) {
+        const bool up = ((2 * lane) & size) == 0 || size == 64;
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride == 1) {
+                const K lo = a < b ? a : b, hi = a < b ? b : a;
+                a = up ? lo : hi;
+                b = up ? hi : lo;
+            } else {
+                const int ls = stride >> 1;
+                const K pa = __shfl_xor_sync(kFull, a, ls), pb = __shfl_xor_sync(kFull, b, ls);
+                const bool keep_min = ((lane & ls) == 0) == up;
+                a = keep_min ? (pa < a ? pa : a) : (pa > a ? pa : a);
+                b = keep_min ? (pb < b ? pb : b) : (pb > b ? pb : b);
+            }
+        }
+    }
+    const K va = __shfl_sync(kFull, a, static_cast<int>(k >> 1)), vb = __shfl_sync(kFull, b, static_cast<int>(k >> 1));
+    return (k & 1u) ? vb : va;
+}
+
+// One sampling round: window of the keys within 6 sample ranks of rank k.
+// Counts the keys below it into *below and compacts the keys inside it into
+// out (up to cap).  Returns the number inside.
+template <typename K, class Src>
+__device__ uint32_t window_round(const Src& v, uint32_t k, K* out, int cap, uint32_t* below, int lane) {
+    const uint32_t M = v.size();
+    const K s = sort32(v.sample(), lane);
+    const int pos = static_cast<int>((static_cast<float>(k) * 32.0f) / static_cast<float>(M));
     const int ql = pos - 6, qh = pos + 6;
-    const K slo = __shfl_sync(kFull, s, ql < 0 ? 0 : ql);
-    const K shi = __shfl_sync(kFull, s, qh > 31 ? 31 : qh);
-    const K lo = ql < 0 ? K(0) : slo;
-    const K hi = qh > 31 ? ~K(0) : shi;
+    const K slo = __shfl_sync(kFull, s, ql < 0 ? 0 : (ql > 31 ? 31 : ql));
+    const K shi = __shfl_sync(kFull, s, qh > 31 ? 31 : (qh < 0 ? 0 : qh));
+    const K lo = ql <= 0 ? K(0) : slo;
+    const K hi = qh >= 31 ? ~K(0) : shi;
     uint32_t c_lo = 0, c_in = 0;
     const unsigned below_me = (1u << lane) - 1u;
-    // lanes walk the keys in lock step (each() visits r*32+lane / i = lane + 32 t)
-    auto visit = [&](K x, bool valid) {
+    v.each_all([&](K x, bool valid) {
         const bool lt = valid && x < lo;
         const bool in = valid && !lt && x <= hi;
         c_lo += __popc(__ballot_sync(kFull, lt));
         const unsigned m = __ballot_sync(kFull, in);
         if (in) {
             const uint32_t at = c_in + __popc(m & below_me);
-            if (at < kCap) cand[at] = x;
+            if (at < static_cast<uint32_t>(cap)) out[at] = x;
         }
         c_in += __popc(m);
-    };
-    v.each_all(visit);
+    });
     __syncwarp();
+    *below = c_lo;
+    return c_in;
+}
+
+// k-th smallest key of a source, exact (see the file comment)
+template <typename K, class Src>
+__device__ K kth_select(const Src& v, uint32_t k, K* cand, K* cand2, int lane) {
+    constexpr int C1 = CandCap<K>::c1, C2 = CandCap<K>::c2;
+    const uint32_t M = v.size();
+    if (M <= 64) {  // short segment: stage it and sort it
+        uint32_t t = 0;
+        v.each_all([&](K x, bool valid) {
+            if (valid) cand[t * 32 + lane] = x;
+            ++t;
+        });
+        __syncwarp();
+        const K r = kth_sort64<K>(cand, M, k, lane);
+        __syncwarp();
+        return r;
+    }
+    uint32_t b1;
+    const uint32_t n1 = window_round<K>(v, k, cand, C1, &b1, lane);
     K res;
-    if (c_lo <= k && k < c_lo + c_in && c_in <= kCap) {
-        PtrKeys<K> src{cand, c_in, lane};
-        res = kth_radix<K>(src, k - c_lo);
+    if (b1 <= k && k < b1 + n1 && n1 <= static_cast<uint32_t>(C1)) {
+        const uint32_t k1 = k - b1;
+        if (n1 <= 64) {
+            res = kth_sort64<K>(cand, n1, k1, lane);
+        } else {
+            const PtrKeys<K> c1{cand, n1, lane};
+            uint32_t b2;
+            const uint32_t n2 = window_round<K>(c1, k1, cand2, C2, &b2, lane);
+            if (b2 <= k1 && k1 < b2 + n2 && n2 <= 64) {
+                res = kth_sort64<K>(cand2, n2, k1 - b2, lane);
+            } else if (b2 <= k1 && k1 < b2 + n2 && n2 <= static_cast<uint32_t>(C2)) {
+                const PtrKeys<K> c2{cand2, n2, lane};
+                res = kth_radix<K>(c2, k1 - b2);
+            } else {
+                res = kth_radix<K>(c1, k1);
+            }
+        }
     } else {
         res = kth_radix<K>(v, k);
     }
-    __syncwarp();  // cand is reused by the next selection
+    __syncwarp();  // the candidate buffers are reused by the next selection
     return res;
-}
-
-template <typename Real, int R>
-__device__ __forceinline__ typename KeyOf<Real>::type kth_any(const VoxKeys<Real, R>& v, uint32_t k,
-                                                              typename KeyOf<Real>::type* cand) {
-    using K = typename KeyOf<Real>::type;
-    if (R >= 4) return kth_window<K>(v, k, cand, v.lane);
-    return kth_radix<K>(v, k);
-}
-template <typename K>
-__device__ __forceinline__ K kth_any(const PtrKeys<K>& v, uint32_t k, K* cand) {
-    return kth_window<K>(v, k, cand, v.lane);
 }
 
 // the voxel's new value from its keys (median or percentile mean)
 template <typename Real, class Src>
-__device__ double order_update(const Src& src, uint32_t M, int mode, int pct, typename KeyOf<Real>::type* cand) {
+__device__ Real order_update(const Src& src, uint32_t M, int mode, int pct, typename KeyOf<Real>::type* cand,
+                             typename KeyOf<Real>::type* cand2, int lane) {
     using K = typename KeyOf<Real>::type;
     if (mode == kVoxMedian) {  // src/MutoMLSD.cpp:506-516
-        const K k1 = kth_any(src, M / 2, cand);
-        const double v1 = static_cast<double>(from_key(k1));
+        const K k1 = kth_select<K>(src, M / 2, cand, cand2, lane);
+        const Real v1 = from_key(k1);
         if (M % 2 == 0) {  // s_(M/2-1) is v1 itself or the largest key below it
             uint32_t c = 0;
             K mb = K(0);
@@ -217,53 +279,61 @@ __device__ double order_update(const Src& src, uint32_t M, int mode, int pct, ty
             });
             c = __reduce_add_sync(kFull, c);
             mb = warp_max_k(mb);
-            const double v0 = c < M / 2 ? v1 : static_cast<double>(from_key(mb));
-            return (v1 + v0) * 0.25;
+            const Real v0 = c < M / 2 ? v1 : from_key(mb);
+            return (v1 + v0) * Real(0.25);
         }
-        return v1 * 0.5;
+        return v1 * Real(0.5);
     }
     // mean of the lowest floor(pct/100 M) values, at least 1 (src/MutoMLSD.cpp:500-504)
     uint32_t jm = u32_cast_x86(pct / 100.0 * M);
     if (jm < 1) jm = 1;
     if (jm > M) jm = M;
-    const K kt = kth_any(src, jm - 1, cand);
-    const double t = static_cast<double>(from_key(kt));
-    double s = 0.0;
+    const K kt = kth_select<K>(src, jm - 1, cand, cand2, lane);
+    const Real t = from_key(kt);
+    Real s = 0;
     uint32_t c = 0;
     src.each([&](K x) {
         if (x < kt) {
-            s += static_cast<double>(from_key(x));
+            s += from_key(x);
             ++c;
         }
     });
-    s = warp_sum(s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(kFull, s, o);
     c = __reduce_add_sync(kFull, c);
-    s += static_cast<double>(jm - c) * t;
-    return s / static_cast<double>(jm) * 0.5;
+    s += static_cast<Real>(jm - c) * t;
+    return s / static_cast<Real>(jm) * Real(0.5);
+}
+
+template <typename Real>
+__device__ __forceinline__ Real pair_g(const typename Vec4<Real>::type& k, Real l, Real t) {
+    const Real lt = l * t;
+    return k.x * l + k.y * (lt + l * l * Real(0.5)) + k.z * (l * l * l * Real(1.0 / 3.0) + (l + t) * lt);
 }
 
 template <typename Real, int R, typename OutT>
 __device__ __forceinline__ void voxel_regs(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uint64_t base, uint32_t M,
-                                           int lane, typename KeyOf<Real>::type* cand) {
+                                           int lane, typename KeyOf<Real>::type* cand,
+                                           typename KeyOf<Real>::type* cand2) {
     using R4 = typename Vec4<Real>::type;
+    using R2 = typename Vec2<Real>::type;
     const Real lam = a.lam[j];
     const bool keys = a.mode == kVoxMedian || a.mode == kVoxPercentile;
     VoxKeys<Real, R> v;
     v.M = M;
     v.lane = lane;
-    double gs = 0.0;
+    Real gs = 0;
     constexpr int C = R < 8 ? R : 8;  // loads in flight per lane per chunk
 #pragma unroll
     for (int r0 = 0; r0 < R; r0 += C) {
         uint32_t mu[C];
-        Real L[C], T[C];
+        R2 lt[C];
 #pragma unroll
         for (int u = 0; u < C; ++u) {
             const uint32_t e = static_cast<uint32_t>((r0 + u) * 32 + lane);
             if (r0 + u < R && e < M) {
                 mu[u] = __ldcs(a.vm_mu + base + e);
-                L[u] = __ldcs(a.vm_L + base + e);
-                T[u] = __ldcs(a.vm_T + base + e);
+                lt[u] = __ldcs(a.vm_LT + base + e);
             }
         }
 #pragma unroll
@@ -272,27 +342,23 @@ __device__ __forceinline__ void voxel_regs(const VoxelPassArgs<Real, OutT>& a, u
             const uint32_t e = static_cast<uint32_t>((r0 + u) * 32 + lane);
             v.key[r0 + u] = 0;
             if (e < M) {
-                const R4 k = ldg4(a.kvec + mu[u]);
-                const Real l = L[u], t = T[u];
-                const Real lt = l * t;
-                const Real g =
-                    k.x * l + k.y * (lt + l * l * Real(0.5)) + k.z * (l * l * l * Real(1.0 / 3.0) + (l + t) * lt);
+                const Real g = pair_g<Real>(ldg4(a.kvec + mu[u]), lt[u].x, lt[u].y);
                 if (keys) v.key[r0 + u] = to_key(Real(2) * lam + g * lam * lam);
-                else gs += static_cast<double>(g);
+                else gs += g;
             }
         }
     }
-    double out;
+    Real out;
     if (keys) {
-        out = order_update<Real>(v, M, a.mode, a.pct, cand);
+        out = order_update<Real>(v, M, a.mode, a.pct, cand, cand2, lane);
     } else {
-        gs = warp_sum(gs);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) gs += __shfl_xor_sync(kFull, gs, o);
         if (a.mode == kVoxGradient) {
-            if (lane == 0) a.grad[j] = -a.lam64[j] * gs;
+            if (lane == 0) a.grad[j] = -a.lam64[j] * static_cast<double>(gs);
             return;
         }
-        const double l = static_cast<double>(lam);
-        out = l + l * l * gs / (2.0 * static_cast<double>(M));
+        out = lam + lam * lam * gs / (Real(2) * static_cast<Real>(M));
     }
     if (lane == 0) a.out[j] = static_cast<OutT>(out);
 }
@@ -301,46 +367,48 @@ __device__ __forceinline__ void voxel_regs(const VoxelPassArgs<Real, OutT>& a, u
 // array (same offsets as the voxel-major lists) and the selection reads them there
 template <typename Real, typename OutT>
 __device__ void voxel_stream(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uint64_t base, uint32_t M, int lane,
-                             typename KeyOf<Real>::type* cand) {
+                             typename KeyOf<Real>::type* cand, typename KeyOf<Real>::type* cand2) {
     using K = typename KeyOf<Real>::type;
     const Real lam = a.lam[j];
     const bool keys = a.mode == kVoxMedian || a.mode == kVoxPercentile;
     K* kp = a.scratch + base;
-    double gs = 0.0;
+    Real gs = 0;
     for (uint32_t i = lane; i < M; i += 32) {
-        const auto k = ldg4(a.kvec + __ldcs(a.vm_mu + base + i));
-        const Real l = __ldcs(a.vm_L + base + i), t = __ldcs(a.vm_T + base + i);
-        const Real lt = l * t;
-        const Real g = k.x * l + k.y * (lt + l * l * Real(0.5)) + k.z * (l * l * l * Real(1.0 / 3.0) + (l + t) * lt);
+        const auto lt = __ldcs(a.vm_LT + base + i);
+        const Real g = pair_g<Real>(ldg4(a.kvec + __ldcs(a.vm_mu + base + i)), lt.x, lt.y);
         if (keys) kp[i] = to_key(Real(2) * lam + g * lam * lam);
-        else gs += static_cast<double>(g);
+        else gs += g;
     }
-    double out;
+    Real out;
     if (keys) {
         __syncwarp();  // the lanes' key stores are visible to the whole warp
-        PtrKeys<K> src{kp, M, lane};
-        out = order_update<Real>(src, M, a.mode, a.pct, cand);
+        const PtrKeys<K> src{kp, M, lane};
+        out = order_update<Real>(src, M, a.mode, a.pct, cand, cand2, lane);
     } else {
-        gs = warp_sum(gs);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) gs += __shfl_xor_sync(kFull, gs, o);
         if (a.mode == kVoxGradient) {
-            if (lane == 0) a.grad[j] = -a.lam64[j] * gs;
+            if (lane == 0) a.grad[j] = -a.lam64[j] * static_cast<double>(gs);
             return;
         }
-        const double l = static_cast<double>(lam);
-        out = l + l * l * gs / (2.0 * static_cast<double>(M));
+        out = lam + lam * lam * gs / (Real(2) * static_cast<Real>(M));
     }
     if (lane == 0) a.out[j] = static_cast<OutT>(out);
 }
 
-template <typename Real, typename OutT>
-__global__ void __launch_bounds__(kVoxThreads) k_em_voxel(VoxelPassArgs<Real, OutT> a) {
+// one warp per voxel of class CLS (0: M <= 256, 1: M <= 768, 2: longer)
+template <typename Real, typename OutT, int CLS>
+__global__ void __launch_bounds__(kVoxThreads) k_em_voxel(VoxelPassArgs<Real, OutT> a, const uint32_t* __restrict__ list,
+                                                          uint32_t n) {
     using K = typename KeyOf<Real>::type;
-    __shared__ K cand_all[kWarps][kCap];
+    __shared__ K cand_all[kWarps][CandCap<K>::c1];
+    __shared__ K cand2_all[kWarps][CandCap<K>::c2];
     const int lane = threadIdx.x & 31;
     K* cand = cand_all[threadIdx.x >> 5];
-    const uint64_t j64 = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (j64 >= a.V) return;  // whole warps leave together
-    const uint32_t j = static_cast<uint32_t>(j64);
+    K* cand2 = cand2_all[threadIdx.x >> 5];
+    const uint64_t w = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (w >= n) return;  // whole warps leave together
+    const uint32_t j = list[w];
     const uint32_t M = a.mult[j];
     if (M == 0) {  // no muon crossed the voxel, src/MutoMLSD.cpp:494-496
         if (lane == 0) {
@@ -350,27 +418,28 @@ __global__ void __launch_bounds__(kVoxThreads) k_em_voxel(VoxelPassArgs<Real, Ou
         return;
     }
     const uint64_t base = a.start[j];
-    // registers per lane sized to the segment; the loops touch only those
-    if (M <= 32u) voxel_regs<Real, 1>(a, j, base, M, lane, cand);
-    else if (M <= 64u) voxel_regs<Real, 2>(a, j, base, M, lane, cand);
-    else if (M <= 128u) voxel_regs<Real, 4>(a, j, base, M, lane, cand);
-    else if (M <= 192u) voxel_regs<Real, 6>(a, j, base, M, lane, cand);
-    else if (M <= 256u) voxel_regs<Real, 8>(a, j, base, M, lane, cand);
-    else if (M <= 384u) voxel_regs<Real, 12>(a, j, base, M, lane, cand);
-    else if (M <= 512u) voxel_regs<Real, 16>(a, j, base, M, lane, cand);
-    else if (M <= 768u) voxel_regs<Real, 24>(a, j, base, M, lane, cand);
-    else {
+    if constexpr (CLS == 0) {
+        if (M <= 32u) voxel_regs<Real, 1>(a, j, base, M, lane, cand, cand2);
+        else if (M <= 64u) voxel_regs<Real, 2>(a, j, base, M, lane, cand, cand2);
+        else if (M <= 128u) voxel_regs<Real, 4>(a, j, base, M, lane, cand, cand2);
+        else if (M <= 192u) voxel_regs<Real, 6>(a, j, base, M, lane, cand, cand2);
+        else voxel_regs<Real, 8>(a, j, base, M, lane, cand, cand2);
+    } else if constexpr (CLS == 1) {
+        if (M <= 384u) voxel_regs<Real, 12>(a, j, base, M, lane, cand, cand2);
+        else if (M <= 512u) voxel_regs<Real, 16>(a, j, base, M, lane, cand, cand2);
+        else voxel_regs<Real, 24>(a, j, base, M, lane, cand, cand2);
+    } else {
         if constexpr (voxel_register_cap<Real>() > 768u) {  // 64-bit keys stay at 24 registers per lane
             if (M <= 1024u) {
-                voxel_regs<Real, 32>(a, j, base, M, lane, cand);
+                voxel_regs<Real, 32>(a, j, base, M, lane, cand, cand2);
                 return;
             }
             if (M <= 1536u) {
-                voxel_regs<Real, 48>(a, j, base, M, lane, cand);
+                voxel_regs<Real, 48>(a, j, base, M, lane, cand, cand2);
                 return;
             }
         }
-        voxel_stream<Real, OutT>(a, j, base, M, lane, cand);
+        voxel_stream<Real, OutT>(a, j, base, M, lane, cand, cand2);
     }
 }
 
@@ -524,15 +593,23 @@ inline unsigned blocks_for(uint64_t n, int threads) {
 }  // namespace
 
 template <typename Real, typename OutT>
-void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, cudaStream_t s) {
-    if (a.V == 0) return;
-    const uint64_t threads = static_cast<uint64_t>(a.V) * 32u;
-    k_em_voxel<Real, OutT><<<blocks_for(threads, kVoxThreads), kVoxThreads, 0, s>>>(a);
-    count_launches(1);
+void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const uint32_t* const* lists, const uint32_t* counts,
+                     cudaStream_t s) {
+    for (int c = 0; c < 3; ++c) {
+        if (counts[c] == 0) continue;
+        const unsigned nb = blocks_for(static_cast<uint64_t>(counts[c]) * 32u, kVoxThreads);
+        if (c == 0) k_em_voxel<Real, OutT, 0><<<nb, kVoxThreads, 0, s>>>(a, lists[c], counts[c]);
+        else if (c == 1) k_em_voxel<Real, OutT, 1><<<nb, kVoxThreads, 0, s>>>(a, lists[c], counts[c]);
+        else k_em_voxel<Real, OutT, 2><<<nb, kVoxThreads, 0, s>>>(a, lists[c], counts[c]);
+        count_launches(1);
+    }
 }
-template void launch_em_voxel<float, float>(const VoxelPassArgs<float, float>&, cudaStream_t);
-template void launch_em_voxel<float, double>(const VoxelPassArgs<float, double>&, cudaStream_t);
-template void launch_em_voxel<double, double>(const VoxelPassArgs<double, double>&, cudaStream_t);
+template void launch_em_voxel<float, float>(const VoxelPassArgs<float, float>&, const uint32_t* const*,
+                                            const uint32_t*, cudaStream_t);
+template void launch_em_voxel<float, double>(const VoxelPassArgs<float, double>&, const uint32_t* const*,
+                                             const uint32_t*, cudaStream_t);
+template void launch_em_voxel<double, double>(const VoxelPassArgs<double, double>&, const uint32_t* const*,
+                                              const uint32_t*, cudaStream_t);
 
 void launch_finalize_cost(Counters* ctr, double n_muons, double* hist, uint32_t cap, cudaStream_t s) {
     k_finalize_cost<<<1, 1, 0, s>>>(ctr, n_muons, hist, cap);

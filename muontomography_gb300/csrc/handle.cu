@@ -273,7 +273,10 @@ struct muto_handle {
     uint64_t N = 0, npairs = 0;
     DevMem kept, sd, pr2, scat, pr64, off;
     DevMem vidx, L, T;            // muon-major pair lists
-    DevMem vm_mu, vm_L, vm_T;     // voxel-major copy
+    DevMem vm_mu, vm_LT;          // voxel-major copy (muon, (L, T))
+    DevMem vclass;                // voxel ids by segment-length class
+    uint32_t vclass_n[3] = {0, 0, 0};
+    uint64_t vclass_off[3] = {0, 0, 0};
     DevMem mult, start, kvec, keys;   // keys: scratch for voxels beyond the register budget
     DevMem lam, lam_ml, cost_hist;
     DevMem tiles;
@@ -501,13 +504,12 @@ void prepare_em(muto_handle* h) {
         cursor.alloc(V * sizeof(uint32_t), &h->dev_bytes);
         CK(cudaMemsetAsync(cursor.as<void>(), 0, V * sizeof(uint32_t), s));
         h->vm_mu.alloc((Pn + kPad) * sizeof(uint32_t), &h->dev_bytes);
-        h->vm_L.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
-        h->vm_T.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
+        h->vm_LT.alloc((Pn + kPad) * sizeof(typename Vec2<Real>::type), &h->dev_bytes);
         run(h, "voxel_major", [&] {
             launch_build_voxel_major<Real>(h->off.as<uint64_t>(), N, h->vidx.as<uint32_t>(), h->L.as<Real>(),
                                            h->T.as<Real>(), static_cast<uint32_t>(V), h->start.as<uint64_t>(),
-                                           cursor.as<uint32_t>(), h->vm_mu.as<uint32_t>(), h->vm_L.as<Real>(),
-                                           h->vm_T.as<Real>(), s);
+                                           cursor.as<uint32_t>(), h->vm_mu.as<uint32_t>(),
+                                           h->vm_LT.as<typename Vec2<Real>::type>(), s);
         });
         CK(cudaStreamSynchronize(s));
     }
@@ -519,6 +521,19 @@ void prepare_em(muto_handle* h) {
         const uint32_t mmax = V ? *std::max_element(m_h.begin(), m_h.end()) : 0u;
         if (mmax > voxel_register_cap<Real>())
             h->keys.alloc(std::max<uint64_t>(Pn, 1) * sizeof(typename KeyOf<Real>::type), &h->dev_bytes);
+        // voxel classes by segment length, one voxel-pass kernel each
+        std::vector<uint32_t> cls[3];
+        for (uint64_t j = 0; j < V; ++j) cls[m_h[j] <= 256u ? 0 : (m_h[j] <= 768u ? 1 : 2)].push_back(static_cast<uint32_t>(j));
+        h->vclass.alloc(std::max<uint64_t>(V, 1) * sizeof(uint32_t), &h->dev_bytes);
+        uint64_t at = 0;
+        for (int c = 0; c < 3; ++c) {
+            h->vclass_off[c] = at;
+            h->vclass_n[c] = static_cast<uint32_t>(cls[c].size());
+            if (!cls[c].empty())
+                CK(cudaMemcpy(h->vclass.as<uint32_t>() + at, cls[c].data(), cls[c].size() * sizeof(uint32_t),
+                              cudaMemcpyHostToDevice));
+            at += cls[c].size();
+        }
     }
 
     // --- tiles of consecutive muons fitting the shared-memory stage ----------
@@ -657,8 +672,7 @@ VoxelPassArgs<Real, OutT> voxel_args(muto_handle* h, const Real* lam, int mode, 
     v.start = h->start.as<uint64_t>();
     v.mult = h->mult.as<uint32_t>();
     v.vm_mu = h->vm_mu.as<uint32_t>();
-    v.vm_L = h->vm_L.as<Real>();
-    v.vm_T = h->vm_T.as<Real>();
+    v.vm_LT = h->vm_LT.as<typename Vec2<Real>::type>();
     v.kvec = h->kvec.as<R4>();
     v.lam = lam;
     v.V = static_cast<uint32_t>(h->V());
@@ -669,6 +683,13 @@ VoxelPassArgs<Real, OutT> voxel_args(muto_handle* h, const Real* lam, int mode, 
     v.lam64 = nullptr;
     v.scratch = h->keys.empty() ? nullptr : h->keys.as<typename KeyOf<Real>::type>();
     return v;
+}
+
+template <typename Real, typename OutT>
+void launch_voxel_pass(muto_handle* h, const VoxelPassArgs<Real, OutT>& v, cudaStream_t s) {
+    const uint32_t* lists[3];
+    for (int c = 0; c < 3; ++c) lists[c] = h->vclass.as<uint32_t>() + h->vclass_off[c];
+    launch_em_voxel<Real, OutT>(v, lists, h->vclass_n, s);
 }
 
 int voxel_mode(const Params& P) {
@@ -688,7 +709,7 @@ void enqueue_iteration(muto_handle* h) {
     const int mode = voxel_mode(P);
     if (h->method == kMap) {  // ML step into lambda_ML, then the MAP step from the snapshot (src/MutoMAP.cpp:138-184)
         const auto v = voxel_args<Real, double>(h, h->lam.as<Real>(), mode, h->lam_ml.as<double>());
-        run(h, "em_voxel", [&] { launch_em_voxel<Real, double>(v, s); });
+        run(h, "em_voxel", [&] { launch_voxel_pass<Real, double>(h, v, s); });
         MapParams mp{P.beta, P.p, P.delta, P.eps, P.all_neighbours, P.add_object_prior, P.newton_max_iter};
         run(h, "map_voxel", [&] {
             launch_map_voxel<Real>(h->lam.as<Real>(), h->lam_ml.as<double>(), h->mult.as<uint32_t>(),
@@ -697,7 +718,7 @@ void enqueue_iteration(muto_handle* h) {
         run(h, "map_copy", [&] { launch_copy_to<Real>(h->lam_ml.as<double>(), h->lam.as<Real>(), h->V(), s); });
     } else {  // each warp reads only its own voxel's lambda before writing it: in place
         const auto v = voxel_args<Real, Real>(h, h->lam.as<Real>(), mode, h->lam.as<Real>());
-        run(h, "em_voxel", [&] { launch_em_voxel<Real, Real>(v, s); });
+        run(h, "em_voxel", [&] { launch_voxel_pass<Real, Real>(h, v, s); });
     }
     const uint32_t cap = static_cast<uint32_t>(h->cost_hist.bytes() / sizeof(double));
     run(h, "cost", [&] { launch_finalize_cost(h->ctr(), static_cast<double>(h->N), h->cost_hist.as<double>(), cap, s); });
@@ -815,7 +836,7 @@ double nll_eval(muto_handle* h, const double* loglam_host, double* grad_host) {
         auto v = voxel_args<Real, Real>(h, lam_r, kVoxGradient, nullptr);
         v.grad = h->grad.as<double>();
         v.lam64 = h->lam64.as<double>();
-        run(h, "em_voxel_grad", [&] { launch_em_voxel<Real, Real>(v, s); });
+        run(h, "em_voxel_grad", [&] { launch_voxel_pass<Real, Real>(h, v, s); });
     }
     const Params& P = h->P;
     if (h->method == kMap) {

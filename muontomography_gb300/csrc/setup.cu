@@ -199,7 +199,7 @@ template <typename Real>
 __global__ void k_build_voxel_major(const uint64_t* __restrict__ off, uint64_t n, const uint32_t* __restrict__ vidx,
                                     const Real* __restrict__ L, const Real* __restrict__ T, uint32_t V,
                                     const uint64_t* __restrict__ start, uint32_t* __restrict__ cursor,
-                                    uint32_t* __restrict__ vm_mu, Real* __restrict__ vm_L, Real* __restrict__ vm_T) {
+                                    uint32_t* __restrict__ vm_mu, typename Vec2<Real>::type* __restrict__ vm_LT) {
     const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     for (uint64_t p = off[i]; p < off[i + 1]; ++p) {
@@ -207,8 +207,10 @@ __global__ void k_build_voxel_major(const uint64_t* __restrict__ off, uint64_t n
         if (j >= V) continue;  // counted by k_voxel_hist
         const uint64_t at = start[j] + atomicAdd(&cursor[j], 1u);
         vm_mu[at] = static_cast<uint32_t>(i);
-        vm_L[at] = L[p];
-        vm_T[at] = T[p];
+        typename Vec2<Real>::type lt;
+        lt.x = L[p];
+        lt.y = T[p];
+        vm_LT[at] = lt;
     }
 }
 
@@ -290,19 +292,17 @@ void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* m
 
 template <typename Real>
 void launch_build_voxel_major(const uint64_t* off, uint64_t n, const uint32_t* vidx, const Real* L, const Real* T,
-                              uint32_t V, const uint64_t* start, uint32_t* cursor, uint32_t* vm_mu, Real* vm_L,
-                              Real* vm_T, cudaStream_t s) {
+                              uint32_t V, const uint64_t* start, uint32_t* cursor, uint32_t* vm_mu,
+                              typename Vec2<Real>::type* vm_LT, cudaStream_t s) {
     if (n == 0) return;
-    k_build_voxel_major<Real><<<blocks_for(n), kThreads, 0, s>>>(off, n, vidx, L, T, V, start, cursor, vm_mu, vm_L,
-                                                                  vm_T);
+    k_build_voxel_major<Real><<<blocks_for(n), kThreads, 0, s>>>(off, n, vidx, L, T, V, start, cursor, vm_mu, vm_LT);
     count_launches(1);
 }
 template void launch_build_voxel_major<float>(const uint64_t*, uint64_t, const uint32_t*, const float*, const float*,
-                                              uint32_t, const uint64_t*, uint32_t*, uint32_t*, float*, float*,
-                                              cudaStream_t);
+                                              uint32_t, const uint64_t*, uint32_t*, uint32_t*, float2*, cudaStream_t);
 template void launch_build_voxel_major<double>(const uint64_t*, uint64_t, const uint32_t*, const double*,
                                                const double*, uint32_t, const uint64_t*, uint32_t*, uint32_t*,
-                                               double*, double*, cudaStream_t);
+                                               double2*, cudaStream_t);
 
 void launch_siddon_batch(muto_grid g, const double* p1, const double* p2, uint64_t n, uint32_t cap, uint32_t* xyz,
                          double* len, uint32_t* counts, cudaStream_t s) {
