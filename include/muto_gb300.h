@@ -170,6 +170,21 @@ int muto_nll_backward(muto_handle* h, const double* log_lambda, double* out_valu
 int muto_gradient_solve(muto_handle* h, int n_iter, double* out_value);
 
 /* ---------------------------------------------------------------------------
+ * Batches: many independent scans (each its own grid and tracks) in one
+ * handle.  Their muons and voxels are concatenated, so every pass of an EM
+ * iteration is one launch over all scans.  Not in the reference, which runs
+ * one scan per process.  Method "mlsd" only; initialize_method 1 or 2; no
+ * early_stop.  muto_prepare / muto_iterate / muto_get_status apply to the
+ * whole batch; images are read per scan.
+ * ------------------------------------------------------------------------- */
+int muto_batch_create(const char* method, const char* config_json, uint32_t n_scans, const muto_grid* grids,
+                      muto_handle** out);
+int muto_batch_load_tracks(muto_handle* h, uint32_t scan, const muto_ray* rays, uint64_t n, int on_device);
+int muto_batch_get_image(muto_handle* h, uint32_t scan, double* out_img, uint64_t out_len);
+/* kept muons and muon-voxel pairs of one scan, after prepare */
+int muto_batch_scan_info(muto_handle* h, uint32_t scan, uint64_t* kept, uint64_t* pairs);
+
+/* ---------------------------------------------------------------------------
  * Multiplicity per voxel (number of pairs M_j), after prepare.
  * ------------------------------------------------------------------------- */
 int muto_get_multiplicity(muto_handle* h, uint32_t* out, uint64_t len);

@@ -25,7 +25,7 @@ from ._lib import MutoError, check
 
 __all__ = [
     "Grid", "Block", "X0_MM", "RAY_FIELDS", "MutoError", "Reconstruction", "MutoPoCA", "MutoMLSD", "MutoMAP",
-    "phantom", "generate", "lambda_from_x0", "save_image", "load_image", "siddon_batch", "library",
+    "phantom", "generate", "lambda_from_x0", "save_image", "load_image", "siddon_batch", "library", "Batch",
 ]
 
 RAY_FIELDS = ("ein", "eout", "pin", "pout", "din", "dout")
@@ -301,6 +301,52 @@ class MutoMAP(Reconstruction):
     def __init__(self, config: dict | None = None):
         super().__init__("map", config)
         self._n_iter = int((config or {}).get("num_iteration", 10))
+
+
+class Batch(Reconstruction):
+    """Many independent MLSD scans (own grids and tracks) reconstructed together:
+    every pass of an EM iteration is one launch over all scans (muto_batch_*)."""
+
+    def __init__(self, config: dict, grids: Sequence[Grid]):
+        self._lib = library()
+        self.method = "mlsd"
+        arr = (_lib.muto_grid * len(grids))(*[g.c() for g in grids])
+        h = C.c_void_p()
+        check(self._lib.muto_batch_create(b"mlsd", _json.dumps(config).encode(), len(grids), arr, C.byref(h)),
+              "muto_batch_create")
+        self._h = h
+        self.grids = list(grids)
+        self._n_iter = int(config.get("num_iteration", 10))
+
+    def load_scan(self, scan: int, rays: np.ndarray | None = None, on_device_ptr: int | None = None,
+                  n: int | None = None) -> None:
+        if on_device_ptr is not None:
+            self._check(self._lib.muto_batch_load_tracks(self._h, scan, C.c_void_p(on_device_ptr), int(n), 1),
+                        "muto_batch_load_tracks")
+            return
+        rays = np.ascontiguousarray(rays, dtype=np.float64)
+        self._keep_rays = getattr(self, "_keep_rays", {})
+        self._keep_rays[scan] = rays
+        self._check(self._lib.muto_batch_load_tracks(self._h, scan, rays.ctypes.data_as(C.c_void_p), rays.shape[0], 0),
+                    "muto_batch_load_tracks")
+
+    def scan_image(self, scan: int) -> np.ndarray:
+        g = self.grids[scan]
+        out = np.empty(g.nvox, dtype=np.float64)
+        self._check(self._lib.muto_batch_get_image(self._h, scan, _lib.dptr(out), out.size), "muto_batch_get_image")
+        return _as_image(out, g)
+
+    def scan_info(self, scan: int) -> tuple[int, int]:
+        k, p = C.c_uint64(), C.c_uint64()
+        self._check(self._lib.muto_batch_scan_info(self._h, scan, C.byref(k), C.byref(p)), "muto_batch_scan_info")
+        return int(k.value), int(p.value)
+
+    def reconstruct_all(self, scans: Sequence[np.ndarray]) -> list[np.ndarray]:
+        for k, r in enumerate(scans):
+            self.load_scan(k, r)
+        self.prepare()
+        self.iterate(self._n_iter)
+        return [self.scan_image(k) for k in range(len(scans))]
 
 
 def siddon_batch(grid: Grid, p1: np.ndarray, p2: np.ndarray, cap: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:

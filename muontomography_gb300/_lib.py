@@ -88,6 +88,10 @@ SIGNATURES = {
     "muto_generate_device": (C.c_int, [C.POINTER(muto_grid), _P, C.POINTER(muto_gen_params), C.c_uint64, C.c_uint64,
                                        _P, _P]),
     "muto_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "muto_batch_create": (C.c_int, [C.c_char_p, C.c_char_p, C.c_uint32, C.POINTER(muto_grid), C.POINTER(_P)]),
+    "muto_batch_load_tracks": (C.c_int, [_P, C.c_uint32, _P, C.c_uint64, C.c_int]),
+    "muto_batch_get_image": (C.c_int, [_P, C.c_uint32, _D, C.c_uint64]),
+    "muto_batch_scan_info": (C.c_int, [_P, C.c_uint32, _U64, _U64]),
     "muto_version": (C.c_char_p, []),
 }
 

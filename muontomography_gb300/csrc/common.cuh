@@ -93,6 +93,8 @@ void launch_path_count(const muto_ray* rays, const uint32_t* kept, const double*
 template <typename Real>
 void launch_path_fill(const muto_ray* rays, const uint32_t* kept, const double* scat, const uint64_t* off, uint64_t n,
                       muto_grid g, int straight, uint32_t* vidx, double* l64, Real* L, Real* T, cudaStream_t s);
+// scan-local voxel indices j < V_scan become voff + j; others become 0xffffffff
+void launch_offset_voxels(uint32_t* vidx, uint64_t n, uint32_t v_scan, uint32_t voff, cudaStream_t s);
 void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* mult, Counters* ctr, cudaStream_t s);
 // voxel-major copy of the pair lists: (muon, L, T) at start[j] + rank within voxel j
 template <typename Real>

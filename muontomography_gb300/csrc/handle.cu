@@ -255,9 +255,17 @@ struct muto_handle {
     bool capturing = false;
     unsigned long long launches = 0;   // launches of this handle (graph replays included)
 
-    // tracks
+    // tracks (scan 0; a batch handle keeps scans 1.. in batch_rays)
     DevMem rays;
     uint64_t n_rays = 0;
+    bool batch = false;
+    struct ScanMeta {
+        muto_grid grid{};
+        uint64_t n_rays = 0, n_total = 0, N = 0, noff = 0, V = 0, voff = 0;
+    };
+    std::vector<ScanMeta> scans;                       // per scan (one entry when not a batch)
+    std::vector<std::unique_ptr<DevMem>> batch_rays;   // tracks of scans 1..
+    uint64_t vtot = 0;                                 // voxels of all scans
     // initial image (host)
     bool init_set = false;
     bool init_missing = false;
@@ -300,7 +308,10 @@ struct muto_handle {
     int last_err = 0;
 
     bool fp64() const { return P.precision == 1; }
-    uint64_t V() const { return static_cast<uint64_t>(grid.nx) * grid.ny * grid.nz; }
+    uint64_t V() const { return batch ? vtot : static_cast<uint64_t>(grid.nx) * grid.ny * grid.nz; }
+    const muto_ray* scan_rays(size_t s) const {
+        return s == 0 ? rays.as<muto_ray>() : batch_rays[s - 1]->as<muto_ray>();
+    }
     bool want_cost() const { return P.compute_cost >= 0 ? P.compute_cost != 0 : (P.early_stop || P.log_results); }
 
     void drop_graph() {
@@ -358,7 +369,7 @@ void sync_and_harvest(muto_handle* h, size_t first) {
 // ---------------------------------------------------------------------------
 // Setup
 // ---------------------------------------------------------------------------
-void resolve_initial_image(muto_handle* h, std::vector<double>& img) {
+void resolve_initial_image(muto_handle* h, std::vector<double>& img, uint64_t seed_offset = 0) {
     int method = h->P.initialize_method;
     if (method == 0) {  // src/MutoMLSD.cpp:228-245
         if (!h->init_set || h->init_missing || h->init_img.empty()) {
@@ -370,9 +381,9 @@ void resolve_initial_image(muto_handle* h, std::vector<double>& img) {
             return;
         }
     }
-    img.assign(h->V(), 0.0);
+    img.assign(static_cast<uint64_t>(h->grid.nx) * h->grid.ny * h->grid.nz, 0.0);
     if (method == 1) {  // N(2, 0.5) * 1e-7, at least 1e-10 (src/MutoMLSD.cpp:251-261)
-        uint64_t seed = h->P.seed_set ? h->P.random_seed : std::random_device{}();
+        uint64_t seed = (h->P.seed_set ? h->P.random_seed : std::random_device{}()) + seed_offset;
         std::mt19937_64 gen(seed);
         const double two_pi = 6.283185307179586;
         for (uint64_t i = 0; i < img.size(); ++i) {
@@ -424,56 +435,103 @@ template <typename Real>
 void prepare_em(muto_handle* h) {
     using R4 = typename Vec4<Real>::type;
     const Params& P = h->P;
-    std::vector<double> init;
-    resolve_initial_image(h, init);  // may adopt a new grid
-    const uint64_t V = h->V();
-    const muto_grid g = h->grid;
     cudaStream_t s = h->stream;
+    std::vector<double> init;
+    if (!h->batch) {
+        resolve_initial_image(h, init);  // may adopt a new grid
+        h->scans.resize(1);
+        h->scans[0].grid = h->grid;
+        h->scans[0].n_rays = h->n_rays;
+    }
+    const size_t S = h->scans.size();
+    uint64_t V = 0;  // voxels of all scans: scan s owns [voff, voff + V_s)
+    for (auto& sc : h->scans) {
+        sc.V = static_cast<uint64_t>(sc.grid.nx) * sc.grid.ny * sc.grid.nz;
+        sc.voff = V;
+        V += sc.V;
+    }
+    if (V >= 0xffffffffull) throw Error(MUTO_ERR_CAPACITY, "more than 2^32-1 voxels in the batch");
+    h->vtot = V;
+    if (h->batch) {  // one initial image per scan (initialize_method 1 or 2)
+        init.clear();
+        for (size_t k = 0; k < S; ++k) {
+            std::vector<double> one;
+            h->grid = h->scans[k].grid;
+            resolve_initial_image(h, one, k);
+            init.insert(init.end(), one.begin(), one.end());
+        }
+        h->grid = h->scans[0].grid;
+    }
+    uint64_t nt_max = 0;
+    for (auto& sc : h->scans) {
+        uint64_t nt = P.total_num_rays > 0 ? static_cast<uint64_t>(P.total_num_rays) : sc.n_rays;
+        sc.n_total = nt > sc.n_rays ? sc.n_rays : nt;  // the reference would read past the end
+        nt_max = std::max(nt_max, sc.n_total);
+    }
+    h->n_total = 0;
+    for (auto& sc : h->scans) h->n_total += sc.n_total;
 
-    uint64_t nt = P.total_num_rays > 0 ? static_cast<uint64_t>(P.total_num_rays) : h->n_rays;
-    if (nt > h->n_rays) nt = h->n_rays;
-    h->n_total = nt;
-
-    // --- gatherInformation: keep flags, order-preserving compaction --------
-    DevMem flags, pos, scratch;
-    flags.alloc(std::max<uint64_t>(nt, 1) * sizeof(uint32_t), &h->dev_bytes);
-    pos.alloc((nt + 1) * sizeof(uint64_t), &h->dev_bytes);
-    scratch.alloc(scan_scratch_bytes(std::max<uint64_t>(nt, V) + 1), &h->dev_bytes);
-    run(h, "keep_flags", [&] { launch_keep_flags(h->rays.as<muto_ray>(), nt, g, P.eps, flags.as<uint32_t>(), s); });
-    run(h, "scan", [&] { scan_u32_to_u64(flags.as<uint32_t>(), pos.as<uint64_t>(), nt, scratch.as<void>(), s); });
+    // --- gatherInformation per scan: keep flags, order-preserving compaction ---
+    // (the flags are computed again in the second loop; the flag buffer is shared)
+    DevMem flags, scratch;
+    std::vector<std::unique_ptr<DevMem>> pos(S);
+    flags.alloc(std::max<uint64_t>(nt_max, 1) * sizeof(uint32_t), &h->dev_bytes);
     uint64_t N = 0;
-    CK(cudaMemcpyAsync(&N, pos.as<uint64_t>() + nt, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (N >= 65536ull * 65536ull) throw Error(MUTO_ERR_CAPACITY, "more than 2^32 kept muons");
+    for (size_t k = 0; k < S; ++k) {
+        auto& sc = h->scans[k];
+        pos[k].reset(new DevMem());
+        pos[k]->alloc((sc.n_total + 1) * sizeof(uint64_t), &h->dev_bytes);
+        if (scratch.bytes() < scan_scratch_bytes(sc.n_total + 1))
+            scratch.alloc(scan_scratch_bytes(std::max<uint64_t>(sc.n_total, V) + 1), &h->dev_bytes);
+        run(h, "keep_flags", [&] { launch_keep_flags(h->scan_rays(k), sc.n_total, sc.grid, P.eps, flags.as<uint32_t>(), s); });
+        run(h, "scan", [&] { scan_u32_to_u64(flags.as<uint32_t>(), pos[k]->as<uint64_t>(), sc.n_total, scratch.as<void>(), s); });
+        uint64_t n = 0;
+        CK(cudaMemcpyAsync(&n, pos[k]->as<uint64_t>() + sc.n_total, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        sc.N = n;
+        sc.noff = N;
+        N += n;
+    }
+    if (N >= 0xffffffffull) throw Error(MUTO_ERR_CAPACITY, "more than 2^32-1 kept muons");
     h->N = N;
     h->kept.alloc(std::max<uint64_t>(N, 1) * sizeof(uint32_t), &h->dev_bytes);
-    run(h, "compact", [&] { launch_compact(flags.as<uint32_t>(), pos.as<uint64_t>(), nt, h->kept.as<uint32_t>(), s); });
-
     h->sd.alloc(std::max<uint64_t>(N, 1) * sizeof(R4), &h->dev_bytes);
     // per-pair and per-muon arrays carry kPad extra entries: the tile stage copies
     // ranges widened to 16-byte boundaries
     h->pr2.alloc((N + kPad) * sizeof(Real), &h->dev_bytes);
     h->scat.alloc(std::max<uint64_t>(N, 1) * 3 * sizeof(double), &h->dev_bytes);
     h->pr64.alloc(std::max<uint64_t>(N, 1) * sizeof(double), &h->dev_bytes);
-    run(h, "muon_info", [&] {
-        launch_muon_info<Real>(h->rays.as<muto_ray>(), h->kept.as<uint32_t>(), N, g, P.eps, P.has_energy,
-                               h->sd.as<R4>(), h->pr2.as<Real>(), h->scat.as<double>(), h->pr64.as<double>(), s);
-    });
-
-    // --- paths: count, offsets, fill + tails --------------------------------
-    run(h, "siddon_count", [&] {
-        launch_path_count(h->rays.as<muto_ray>(), h->kept.as<uint32_t>(), h->scat.as<double>(), N, g, P.straight_line,
-                          flags.as<uint32_t>(), h->ctr(), s);
-    });
+    DevMem counts;
+    counts.alloc(std::max<uint64_t>(N, 1) * sizeof(uint32_t), &h->dev_bytes);
+    for (size_t k = 0; k < S; ++k) {
+        const auto& sc = h->scans[k];
+        const muto_ray* r = h->scan_rays(k);
+        uint32_t* kept = h->kept.as<uint32_t>() + sc.noff;
+        double* scat = h->scat.as<double>() + 3 * sc.noff;
+        run(h, "keep_flags", [&] { launch_keep_flags(r, sc.n_total, sc.grid, P.eps, flags.as<uint32_t>(), s); });
+        run(h, "compact", [&] { launch_compact(flags.as<uint32_t>(), pos[k]->as<uint64_t>(), sc.n_total, kept, s); });
+        run(h, "muon_info", [&] {
+            launch_muon_info<Real>(r, kept, sc.N, sc.grid, P.eps, P.has_energy, h->sd.as<R4>() + sc.noff,
+                                   h->pr2.as<Real>() + sc.noff, scat, h->pr64.as<double>() + sc.noff, s);
+        });
+        // --- path lengths (count walk) ---
+        run(h, "siddon_count", [&] {
+            launch_path_count(r, kept, scat, sc.N, sc.grid, P.straight_line, counts.as<uint32_t>() + sc.noff,
+                              h->ctr(), s);
+        });
+    }
+    flags.release();
+    pos.clear();
+    if (scratch.bytes() < scan_scratch_bytes(std::max<uint64_t>(N, V) + 1))
+        scratch.alloc(scan_scratch_bytes(std::max<uint64_t>(N, V) + 1), &h->dev_bytes);
     h->off.alloc((N + 1 + kPad) * sizeof(uint64_t), &h->dev_bytes);
-    run(h, "scan", [&] { scan_u32_to_u64(flags.as<uint32_t>(), h->off.as<uint64_t>(), N, scratch.as<void>(), s); });
+    run(h, "scan", [&] { scan_u32_to_u64(counts.as<uint32_t>(), h->off.as<uint64_t>(), N, scratch.as<void>(), s); });
+    counts.release();
     std::vector<uint64_t> off_h(N + 1);
     CK(cudaMemcpyAsync(off_h.data(), h->off.as<uint64_t>(), (N + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     const uint64_t Pn = off_h[N];
     h->npairs = Pn;
-    flags.release();
-    pos.release();
 
     h->vidx.alloc((Pn + kPad) * sizeof(uint32_t), &h->dev_bytes);
     h->L.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
@@ -485,11 +543,23 @@ void prepare_em(muto_handle* h) {
             l64tmp.alloc(std::max<uint64_t>(Pn, 1) * sizeof(double), &h->dev_bytes);
             l64 = l64tmp.as<double>();
         }
-        run(h, "siddon_fill", [&] {
-            launch_path_fill<Real>(h->rays.as<muto_ray>(), h->kept.as<uint32_t>(), h->scat.as<double>(),
-                                   h->off.as<uint64_t>(), N, g, P.straight_line, h->vidx.as<uint32_t>(), l64,
-                                   h->L.as<Real>(), h->T.as<Real>(), s);
-        });
+        for (size_t k = 0; k < S; ++k) {
+            const auto& sc = h->scans[k];
+            run(h, "siddon_fill", [&] {
+                launch_path_fill<Real>(h->scan_rays(k), h->kept.as<uint32_t>() + sc.noff,
+                                       h->scat.as<double>() + 3 * sc.noff, h->off.as<uint64_t>() + sc.noff, sc.N,
+                                       sc.grid, P.straight_line, h->vidx.as<uint32_t>(), l64, h->L.as<Real>(),
+                                       h->T.as<Real>(), s);
+            });
+            // scan-local voxel indices into the batch's voxel space
+            if (h->batch) {
+                const uint64_t pb = off_h[sc.noff], pe = off_h[sc.noff + sc.N];
+                run(h, "voxel_offset", [&] {
+                    launch_offset_voxels(h->vidx.as<uint32_t>() + pb, pe - pb, static_cast<uint32_t>(sc.V),
+                                         static_cast<uint32_t>(sc.voff), s);
+                });
+            }
+        }
         CK(cudaStreamSynchronize(s));
     }
 
@@ -985,10 +1055,12 @@ int muto_prepare(muto_handle* h) {
     if (!h) return MUTO_ERR_ARG;
     return guarded(h, [&] {
         if (h->rays.empty()) throw Error(MUTO_ERR_STATE, "load tracks first");
+        for (const auto& r : h->batch_rays)
+            if (!r || r->empty()) throw Error(MUTO_ERR_STATE, "load the tracks of every scan first");
         h->drop_graph();
         h->iters = 0;
         h->stopped = false;
-        h->grid = h->P.grid;
+        if (!h->batch) h->grid = h->P.grid;
         alloc_counters(h);
         const size_t pf = h->prof.used;
         if (h->method == kPoca) {
@@ -1020,6 +1092,7 @@ int muto_get_image(muto_handle* h, double* out, uint64_t len) {
     if (!h || !out) return MUTO_ERR_ARG;
     return guarded(h, [&] {
         n_prepared_check(h);
+        if (h->batch) throw Error(MUTO_ERR_STATE, "a batch handle returns images per scan (muto_batch_get_image)");
         if (len != h->V()) throw Error(MUTO_ERR_ARG, "image length does not match nx*ny*nz of the current grid");
         if (h->method == kPoca) {
             CK(cudaMemcpyAsync(out, h->img64.as<double>(), len * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1250,6 +1323,95 @@ int muto_launch_count(muto_handle* h, uint64_t* out) {
     if (!h || !out) return MUTO_ERR_ARG;
     *out = h->launches;
     return MUTO_OK;
+}
+
+int muto_batch_create(const char* method, const char* config_json, uint32_t n_scans, const muto_grid* grids,
+                      muto_handle** out) {
+    if (!method || !out || !grids || n_scans == 0) return MUTO_ERR_ARG;
+    *out = nullptr;
+    if (std::string(method) != "mlsd") return MUTO_ERR_ARG;  // MAP stencils need one grid
+    muto_handle* h = nullptr;
+    int rc = muto_create(method, config_json, &h);
+    if (rc != MUTO_OK) return rc;
+    rc = guarded(h, [&] {
+        if (h->P.initialize_method == 0)
+            throw Error(MUTO_ERR_CONFIG, "a batch starts from initialize_method 1 or 2 (no per-scan image files)");
+        if (h->P.early_stop) throw Error(MUTO_ERR_CONFIG, "early_stop applies to one scan, not to a batch");
+        h->batch = true;
+        h->scans.resize(n_scans);
+        for (uint32_t k = 0; k < n_scans; ++k) {
+            const muto_grid& g = grids[k];
+            if (g.nx == 0 || g.ny == 0 || g.nz == 0 || !(g.dx > 0 && g.dy > 0 && g.dz > 0))
+                throw Error(MUTO_ERR_ARG, "scan " + std::to_string(k) + ": invalid grid");
+            h->scans[k].grid = g;
+        }
+        h->grid = grids[0];
+        h->batch_rays.resize(n_scans - 1);
+    });
+    if (rc != MUTO_OK) {
+        muto_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return MUTO_OK;
+}
+
+int muto_batch_load_tracks(muto_handle* h, uint32_t scan, const muto_ray* rays, uint64_t n, int on_device) {
+    if (!h) return MUTO_ERR_ARG;
+    if (!h->batch) return scan == 0 ? muto_load_tracks(h, rays, n, on_device) : MUTO_ERR_ARG;
+    if (scan >= h->scans.size()) return MUTO_ERR_ARG;
+    if (scan == 0) {
+        const int rc = muto_load_tracks(h, rays, n, on_device);
+        if (rc == MUTO_OK) h->scans[0].n_rays = n;
+        return rc;
+    }
+    return guarded(h, [&] {
+        if (n > 0 && !rays) throw Error(MUTO_ERR_ARG, "null rays");
+        if (n >= 0xffffffffull) throw Error(MUTO_ERR_CAPACITY, "at most 2^32-1 tracks per scan");
+        h->drop_graph();
+        h->prepared = false;
+        auto& slot = h->batch_rays[scan - 1];
+        slot.reset(new DevMem());
+        slot->alloc(std::max<uint64_t>(n, 1) * sizeof(muto_ray), &h->dev_bytes);
+        if (n > 0)
+            CK(cudaMemcpyAsync(slot->as<void>(), rays, n * sizeof(muto_ray),
+                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        h->scans[scan].n_rays = n;
+    });
+}
+
+int muto_batch_get_image(muto_handle* h, uint32_t scan, double* out, uint64_t len) {
+    if (!h || !out) return MUTO_ERR_ARG;
+    if (!h->batch) return scan == 0 ? muto_get_image(h, out, len) : MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        n_prepared_check(h);
+        if (scan >= h->scans.size()) throw Error(MUTO_ERR_ARG, "no such scan");
+        const auto& sc = h->scans[scan];
+        if (len != sc.V) throw Error(MUTO_ERR_ARG, "image length does not match the scan's grid");
+        const size_t es = h->fp64() ? sizeof(double) : sizeof(float);
+        std::vector<unsigned char> tmp(len * es);
+        CK(cudaMemcpyAsync(tmp.data(), static_cast<const unsigned char*>(h->lam.as<void>()) + sc.voff * es, len * es,
+                           cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        for (uint64_t j = 0; j < len; ++j)
+            out[j] = h->fp64() ? reinterpret_cast<const double*>(tmp.data())[j]
+                               : static_cast<double>(reinterpret_cast<const float*>(tmp.data())[j]);
+    });
+}
+
+int muto_batch_scan_info(muto_handle* h, uint32_t scan, uint64_t* kept, uint64_t* pairs) {
+    if (!h) return MUTO_ERR_ARG;
+    return guarded(h, [&] {
+        n_prepared_check(h);
+        if (scan >= h->scans.size()) throw Error(MUTO_ERR_ARG, "no such scan");
+        const auto& sc = h->scans[scan];
+        std::vector<uint64_t> o(2);
+        CK(cudaMemcpy(&o[0], h->off.as<uint64_t>() + sc.noff, sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&o[1], h->off.as<uint64_t>() + sc.noff + sc.N, sizeof(uint64_t), cudaMemcpyDeviceToHost));
+        if (kept) *kept = sc.N;
+        if (pairs) *pairs = o[1] - o[0];
+    });
 }
 
 int muto_get_stream(muto_handle* h, void** out) {

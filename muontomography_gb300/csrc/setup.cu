@@ -182,6 +182,14 @@ __global__ void k_path_fill(const muto_ray* __restrict__ rays, const uint32_t* _
     }
 }
 
+__global__ void k_offset_voxels(uint32_t* __restrict__ vidx, uint64_t n, uint32_t v_scan, uint32_t voff) {
+    const uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k < n) {
+        const uint32_t j = vidx[k];
+        vidx[k] = j < v_scan ? voff + j : 0xffffffffu;
+    }
+}
+
 __global__ void k_voxel_hist(const uint32_t* __restrict__ vidx, uint64_t P, uint32_t V, uint32_t* __restrict__ mult,
                              Counters* ctr) {
     const uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -284,6 +292,12 @@ template void launch_path_fill<float>(const muto_ray*, const uint32_t*, const do
                                       muto_grid, int, uint32_t*, double*, float*, float*, cudaStream_t);
 template void launch_path_fill<double>(const muto_ray*, const uint32_t*, const double*, const uint64_t*, uint64_t,
                                        muto_grid, int, uint32_t*, double*, double*, double*, cudaStream_t);
+
+void launch_offset_voxels(uint32_t* vidx, uint64_t n, uint32_t v_scan, uint32_t voff, cudaStream_t s) {
+    if (n == 0) return;
+    k_offset_voxels<<<blocks_for(n), kThreads, 0, s>>>(vidx, n, v_scan, voff);
+    count_launches(1);
+}
 
 void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* mult, Counters* ctr, cudaStream_t s) {
     if (P == 0) return;

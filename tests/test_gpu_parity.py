@@ -280,3 +280,35 @@ def test_autotuner_reports_its_choice(gpu):
         rec.prepare()
         st = rec.status()
     assert st["muon_pass"] in (1, 2) and st["muon_group"] in (8, 16, 32)
+
+
+# ---------------------------------------------------------------------------
+# Batches of independent scans
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("precision,mode", [("fp64", "median"), ("mixed", "mean"), ("mixed", "median")])
+def test_batch_equals_separate_scans(gpu, precision, mode):
+    wls = [W.small(n_muons=4000, seed=200 + k, n=n) for k, n in enumerate((6, 9, 12))]
+    over = {"median": {}, "mean": {"update_with_mean": True}}[mode]
+    cfg = wls[0].em_config(precision=precision, num_iteration=4, **over)
+    cfg.pop("grid")
+    tracks = [wl.tracks() for wl in wls]
+    with M.Batch(cfg, [wl.grid for wl in wls]) as b:
+        imgs = b.reconstruct_all(tracks)
+        st = b.status()
+        info = [b.scan_info(k) for k in range(3)]
+    assert st["iterations_done"] == 4
+    for wl, trk, img, (kept, pairs) in zip(wls, tracks, imgs, info):
+        with M.MutoMLSD(dict(cfg, grid=wl.grid.json())) as rec:
+            one = rec.reconstruct(trk)
+            s1 = rec.status()
+        assert kept == s1["n_scat_in_grid"] and pairs == s1["n_pairs"]
+        tol = 1e-12 if precision == "fp64" else 1e-6
+        assert rel_l2(img, one) < tol
+
+
+def test_batch_rejects_what_it_cannot_do(gpu):
+    g = [W.small(n=6).grid]
+    with pytest.raises(M.MutoError):
+        M.Batch({"initialize_method": 0}, g)
+    with pytest.raises(M.MutoError):
+        M.Batch({"initialize_method": 2, "early_stop": True}, g)
