@@ -135,6 +135,32 @@ int muto_set_image(muto_handle* h, const double* img, uint64_t len);
 int muto_siddon_batch(const muto_grid* g, const double* p1, const double* p2, uint64_t n, uint32_t cap,
                       uint32_t* xyz, double* len, uint32_t* counts);
 
+/* The same batched Siddon walk without any allocation.  No counterpart in
+ * the reference.
+ *
+ * For callers that cannot let a library allocate device memory: a process
+ * whose device memory is all reserved up front by its own pool allocator
+ * has none left to give, and a loop that keeps other streams of the device
+ * busy (data acquisition, online monitoring) cannot take the device-wide
+ * synchronisation that cudaFree performs.  Inputs, outputs and errors are
+ * those of muto_siddon_batch; slots past min(counts[r], cap) come back 0.
+ * The work runs on `stream` (a cudaStream_t; NULL is the legacy default
+ * stream) and the call returns when it is done.
+ *
+ * Instead of allocating, the call stages rays and voxel lists, a chunk of
+ * rays at a time, through one fixed device array of
+ * MUTO_NOALLOC_SCRATCH_BYTES compiled into the library.  n is unbounded;
+ * cap above MUTO_NOALLOC_MAX_CAP returns MUTO_ERR_CAPACITY before the
+ * device is touched.  The first call on a device looks up the array's
+ * address on that device (the current one); make that first call before
+ * any stream capture begins.  All calls on one device share the array:
+ * calls that overlap in time (several host threads, or several streams)
+ * race on it, so the caller must serialise them. */
+#define MUTO_NOALLOC_SCRATCH_BYTES (16u << 20)
+#define MUTO_NOALLOC_MAX_CAP 65536u
+int muto_siddon_batch_noalloc(const muto_grid* g, const double* p1, const double* p2, uint64_t n, uint32_t cap,
+                              uint32_t* xyz, double* len, uint32_t* counts, void* stream);
+
 /* MLSD/MAP after prepare: the kept muons and their merged paths
  * (src/MutoMLSD.cpp:268-326, :382-430).  Any pointer may be NULL.
  * kept: n_scat_in_grid ray indices; info: 6 doubles per kept muon

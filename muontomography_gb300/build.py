@@ -31,7 +31,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas"
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-Wno-unused-function"]
 
 CUDA_UNITS = ["scan.cu", "setup.cu", "em_muon.cu", "em_voxel.cu", "poca.cu", "adjoint.cu", "gen.cu",
-              "handle.cu"]
+              "handle.cu", "noalloc.cu"]
 HOST_UNITS = ["host.cpp"]
 FACADE_UNITS = ["MutoFile.cpp", "MutoReconstruction.cpp"]
 
