@@ -103,7 +103,8 @@ def dist_env():
 def workload(args, rank: int):
     from muontomography_gb300 import workloads as W
 
-    fn = {"config1": W.config1, "config2": W.config2, "config3": W.config3, "config5": W.config5}[args.workload]
+    fn = {"config1": W.config1, "config2": W.config2, "config2_coarse": W.config2_coarse, "config3": W.config3,
+          "config5": W.config5}[args.workload]
     kw = {}
     if args.n_muons:
         kw["n_muons"] = args.n_muons
@@ -372,7 +373,7 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3", "config5"])
+    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config2_coarse", "config3", "config5"])
     ap.add_argument("--n-muons", type=int, default=0)
     ap.add_argument("--mode", choices=["median", "mean"], default="median")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")

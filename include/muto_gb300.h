@@ -161,6 +161,18 @@ int muto_siddon_batch(const muto_grid* g, const double* p1, const double* p2, ui
 int muto_siddon_batch_noalloc(const muto_grid* g, const double* p1, const double* p2, uint64_t n, uint32_t cap,
                               uint32_t* xyz, double* len, uint32_t* counts, void* stream);
 
+/* The voxel update of the EM step (src/MutoMLSD.cpp:493-517) on synthetic
+ * segments, through the same kernels as an iteration: segment j holds
+ * values[seg_off[j] .. seg_off[j+1]) and its pairs get s_i = 2 + x_i
+ * (lambda = 1, L = 1, T = 0, per-muon coefficients (x_i, 0, 0)), computed
+ * in float (precision 0) or double (1).  out[j] is the updated lambda of
+ * segment j: the halved median of the s_i (even counts: the mean of the two
+ * middle values), or with update_with_mean the halved mean of the lowest
+ * mean_percentile % (100: all).  Not in the reference: a probe that lets
+ * tests check the exact order statistics on chosen inputs. */
+int muto_select_probe(int precision, const double* values, uint64_t n, const uint64_t* seg_off, uint32_t n_segs,
+                      int update_with_mean, int mean_percentile, double* out);
+
 /* MLSD/MAP after prepare: the kept muons and their merged paths
  * (src/MutoMLSD.cpp:268-326, :382-430).  Any pointer may be NULL.
  * kept: n_scat_in_grid ray indices; info: 6 doubles per kept muon

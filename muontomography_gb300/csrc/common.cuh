@@ -40,6 +40,18 @@ __device__ __forceinline__ double from_key(unsigned long long k) {
     const unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
     return __longlong_as_double(static_cast<long long>(u));
 }
+// one bulk prefetch of [p, p + bytes) into L2, widened to 16-byte bounds
+// (callers keep the widened range inside their arrays' padding)
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes) {
+    const uintptr_t a0 = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(15);
+    const uintptr_t a1 = (reinterpret_cast<uintptr_t>(p) + bytes + 15) & ~uintptr_t(15);
+    if (a1 > a0)
+        asm volatile(
+            "{\n\t.reg .u64 ga;\n\tcvta.to.global.u64 ga, %0;\n\tcp.async.bulk.prefetch.L2.global [ga], %1;\n\t}"
+            ::"l"(static_cast<unsigned long long>(a0)), "r"(static_cast<uint32_t>(a1 - a0))
+            : "memory");
+}
+
 template <typename Real> struct KeyOf;
 template <> struct KeyOf<float> { using type = uint32_t; static constexpr int bits = 32; };
 template <> struct KeyOf<double> { using type = unsigned long long; static constexpr int bits = 64; };
@@ -175,11 +187,20 @@ struct VoxelPassArgs {
 // segments up to this many pairs are selected from registers
 template <typename Real>
 __host__ __device__ constexpr uint32_t voxel_register_cap() { return sizeof(Real) == 4 ? 1536u : 768u; }
+// one voxel of a class list: its index, pair count and first voxel-major pair
+struct alignas(16) VoxDesc {
+    uint32_t j, M;
+    unsigned long long start;
+};
 // voxels in three classes by segment length (lists[c], counts[c]): M <= 256,
-// M <= 768, longer; voxels without pairs go with the first class
+// M <= 768, longer; voxels without pairs go with the first class.
+// resident_blocks[c]: blocks of class c resident on the whole GPU at once.
 template <typename Real, typename OutT>
-void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const uint32_t* const* lists, const uint32_t* counts,
-                     cudaStream_t s);
+void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists, const uint32_t* counts,
+                     const int* resident_blocks, cudaStream_t s);
+// resident blocks per SM of the three class kernels
+template <typename Real, typename OutT>
+void em_voxel_occupancy(int blocks_per_sm[3]);
 void launch_finalize_cost(Counters* ctr, double n_muons, double* hist, uint32_t hist_cap, cudaStream_t s);
 
 struct MapParams {

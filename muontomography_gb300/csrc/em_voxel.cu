@@ -22,6 +22,8 @@
 //   gradient     d NLL / d log l_j = -l_j sum_i g_ij (the adjoint).
 // Voxels are grouped by segment length into classes, each its own kernel
 // instantiation, so short segments run with few registers and many warps.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace muto {
@@ -30,10 +32,15 @@ namespace {
 constexpr int kVoxThreads = 256;
 constexpr int kWarps = kVoxThreads / 32;
 
-template <typename K> struct CandCap;
-template <> struct CandCap<uint32_t> { static constexpr int c1 = 640, c2 = 128; };
-template <> struct CandCap<unsigned long long> { static constexpr int c1 = 448, c2 = 128; };
-
+// shared-memory candidate buffers per warp: the first window of a short
+// segment holds about 3/8 of it (at most 256 keys below M = 256)
+template <typename K, int CLS> struct CandCap;
+template <> struct CandCap<uint32_t, 0> { static constexpr int c1 = 256, c2 = 128; };
+template <> struct CandCap<uint32_t, 1> { static constexpr int c1 = 640, c2 = 256; };
+template <> struct CandCap<uint32_t, 2> { static constexpr int c1 = 640, c2 = 256; };
+template <> struct CandCap<unsigned long long, 0> { static constexpr int c1 = 256, c2 = 128; };
+template <> struct CandCap<unsigned long long, 1> { static constexpr int c1 = 448, c2 = 192; };
+template <> struct CandCap<unsigned long long, 2> { static constexpr int c1 = 448, c2 = 192; };
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 __device__ __forceinline__ double4 ldg4(const double4* p) {
     const double2* q = reinterpret_cast<const double2*>(p);
@@ -142,6 +149,14 @@ struct VoxKeys {
     __device__ __forceinline__ uint32_t size() const { return M; }
 };
 
+// order statistic k of a segment and, when the final candidates hold it,
+// order statistic k-1 (the lower median of an even segment)
+template <typename K>
+struct Sel {
+    K kth, prev;
+    bool have_prev;
+};
+
 // ascending warp bitonic sort of one key per lane
 template <typename K>
 __device__ __forceinline__ K sort32(K s, int lane) {
@@ -158,10 +173,21 @@ __device__ __forceinline__ K sort32(K s, int lane) {
     return s;
 }
 
-// k-th smallest of n <= 64 keys in shared memory: warp bitonic sort of 64
-// (element e = 2 lane + t held in register t of its lane), then a shuffle
+// order statistics k and k-1 of n <= 32 keys in shared memory
 template <typename K>
-__device__ K kth_sort64(const K* c, uint32_t n, uint32_t k, int lane) {
+__device__ Sel<K> sel32(const K* c, uint32_t n, uint32_t k, int lane) {
+    const K s = sort32(static_cast<uint32_t>(lane) < n ? c[lane] : ~K(0), lane);
+    Sel<K> r;
+    r.kth = __shfl_sync(kFull, s, static_cast<int>(k));
+    r.prev = __shfl_sync(kFull, s, static_cast<int>(k ? k - 1 : 0));
+    r.have_prev = k >= 1;
+    return r;
+}
+
+// order statistics k and k-1 of n <= 64 keys in shared memory: warp bitonic
+// sort of 64 (element e = 2 lane + t held in register t of its lane)
+template <typename K>
+__device__ Sel<K> sel64(const K* c, uint32_t n, uint32_t k, int lane) {
     K a = static_cast<uint32_t>(2 * lane) < n ? c[2 * lane] : ~K(0);
     K b = static_cast<uint32_t>(2 * lane + 1) < n ? c[2 * lane + 1] : ~K(0);
 #pragma unroll
@@ -182,8 +208,14 @@ __device__ K kth_sort64(const K* c, uint32_t n, uint32_t k, int lane) {
             }
         }
     }
+    const uint32_t kp = k ? k - 1 : 0;
     const K va = __shfl_sync(kFull, a, static_cast<int>(k >> 1)), vb = __shfl_sync(kFull, b, static_cast<int>(k >> 1));
-    return (k & 1u) ? vb : va;
+    const K pa = __shfl_sync(kFull, a, static_cast<int>(kp >> 1)), pb = __shfl_sync(kFull, b, static_cast<int>(kp >> 1));
+    Sel<K> r;
+    r.kth = (k & 1u) ? vb : va;
+    r.prev = (kp & 1u) ? pb : pa;
+    r.have_prev = k >= 1;
+    return r;
 }
 
 // One sampling round: window of the keys within 6 sample ranks of rank k.
@@ -204,7 +236,7 @@ __device__ uint32_t window_round(const Src& v, uint32_t k, K* out, int cap, uint
     v.each_all([&](K x, bool valid) {
         const bool lt = valid && x < lo;
         const bool in = valid && !lt && x <= hi;
-        c_lo += __popc(__ballot_sync(kFull, lt));
+        c_lo += lt ? 1u : 0u;
         const unsigned m = __ballot_sync(kFull, in);
         if (in) {
             const uint32_t at = c_in + __popc(m & below_me);
@@ -213,73 +245,112 @@ __device__ uint32_t window_round(const Src& v, uint32_t k, K* out, int cap, uint
         c_in += __popc(m);
     });
     __syncwarp();
-    *below = c_lo;
+    *below = __reduce_add_sync(kFull, c_lo);
     return c_in;
 }
 
-// k-th smallest key of a source, exact (see the file comment)
+// Order statistics kk and kk-1 of the n window candidates in cand, exact:
+// further sampling rounds between the two buffers until at most 64 remain,
+// which are sorted.  A window that misses the target, overflows or stops
+// shrinking falls back to a bitwise radix search.  Shared by every segment
+// length, so kept out of line.
+template <typename K>
+__device__ __noinline__ Sel<K> select_candidates(K* cand, int cap1, K* cand2, int cap2, uint32_t n, uint32_t kk,
+                                                 int lane) {
+    Sel<K> r;
+    r.have_prev = false;
+    K* cur = cand;
+    K* oth = cand2;
+    int oth_cap = cap2, cur_cap = cap1;
+#pragma unroll 1
+    for (int round = 0; n > 64 && round < 6; ++round) {
+        const PtrKeys<K> c{cur, n, lane};
+        uint32_t b2;
+        const uint32_t n2 = window_round<K>(c, kk, oth, oth_cap, &b2, lane);
+        if (!(b2 <= kk && kk < b2 + n2 && n2 <= static_cast<uint32_t>(oth_cap)) || n2 >= n) {
+            r.kth = kth_radix<K>(c, kk);
+            __syncwarp();
+            return r;
+        }
+        kk -= b2;
+        n = n2;
+        K* t = cur;
+        cur = oth;
+        oth = t;
+        const int tc = cur_cap;
+        cur_cap = oth_cap;
+        oth_cap = tc;
+    }
+    if (n > 64) {
+        const PtrKeys<K> c{cur, n, lane};
+        r.kth = kth_radix<K>(c, kk);
+    } else {
+        r = n <= 32 ? sel32<K>(cur, n, kk, lane) : sel64<K>(cur, n, kk, lane);
+    }
+    __syncwarp();  // the candidate buffers are reused by the next selection
+    return r;
+}
+
+// Order statistic k (and usually k-1) of a key source, exact.  Short
+// segments are staged and sorted; longer ones go through a first sampling
+// round (32 samples sorted in the warp, the keys within 6 sample ranks of
+// the target kept) and then select_candidates.
 template <typename K, class Src>
-__device__ K kth_select(const Src& v, uint32_t k, K* cand, K* cand2, int lane) {
-    constexpr int C1 = CandCap<K>::c1, C2 = CandCap<K>::c2;
+__device__ Sel<K> kth_select(const Src& v, uint32_t k, K* cand, int cap1, K* cand2, int cap2, int lane) {
     const uint32_t M = v.size();
-    if (M <= 64) {  // short segment: stage it and sort it
+    if (M <= 64) {
         uint32_t t = 0;
         v.each_all([&](K x, bool valid) {
             if (valid) cand[t * 32 + lane] = x;
             ++t;
         });
         __syncwarp();
-        const K r = kth_sort64<K>(cand, M, k, lane);
+        return select_candidates<K>(cand, cap1, cand2, cap2, M, k, lane);
+    }
+    uint32_t b;
+    const uint32_t n = window_round<K>(v, k, cand, cap1, &b, lane);
+    if (!(b <= k && k < b + n && n <= static_cast<uint32_t>(cap1))) {
+        Sel<K> r;
+        r.have_prev = false;
+        r.kth = kth_radix<K>(v, k);
         __syncwarp();
         return r;
     }
-    uint32_t b1;
-    const uint32_t n1 = window_round<K>(v, k, cand, C1, &b1, lane);
-    K res;
-    if (b1 <= k && k < b1 + n1 && n1 <= static_cast<uint32_t>(C1)) {
-        const uint32_t k1 = k - b1;
-        if (n1 <= 64) {
-            res = kth_sort64<K>(cand, n1, k1, lane);
-        } else {
-            const PtrKeys<K> c1{cand, n1, lane};
-            uint32_t b2;
-            const uint32_t n2 = window_round<K>(c1, k1, cand2, C2, &b2, lane);
-            if (b2 <= k1 && k1 < b2 + n2 && n2 <= 64) {
-                res = kth_sort64<K>(cand2, n2, k1 - b2, lane);
-            } else if (b2 <= k1 && k1 < b2 + n2 && n2 <= static_cast<uint32_t>(C2)) {
-                const PtrKeys<K> c2{cand2, n2, lane};
-                res = kth_radix<K>(c2, k1 - b2);
-            } else {
-                res = kth_radix<K>(c1, k1);
-            }
-        }
-    } else {
-        res = kth_radix<K>(v, k);
-    }
-    __syncwarp();  // the candidate buffers are reused by the next selection
-    return res;
+    return select_candidates<K>(cand, cap1, cand2, cap2, n, k - b, lane);
 }
+
+struct CandBufs {
+    void* c1;
+    void* c2;
+    int cap1, cap2;
+};
 
 // the voxel's new value from its keys (median or percentile mean)
 template <typename Real, class Src>
-__device__ Real order_update(const Src& src, uint32_t M, int mode, int pct, typename KeyOf<Real>::type* cand,
-                             typename KeyOf<Real>::type* cand2, int lane) {
+__device__ Real order_update(const Src& src, uint32_t M, int mode, int pct, const CandBufs& cb, int lane) {
     using K = typename KeyOf<Real>::type;
+    K* cand = static_cast<K*>(cb.c1);
+    K* cand2 = static_cast<K*>(cb.c2);
     if (mode == kVoxMedian) {  // src/MutoMLSD.cpp:506-516
-        const K k1 = kth_select<K>(src, M / 2, cand, cand2, lane);
-        const Real v1 = from_key(k1);
-        if (M % 2 == 0) {  // s_(M/2-1) is v1 itself or the largest key below it
-            uint32_t c = 0;
-            K mb = K(0);
-            src.each([&](K x) {
-                if (x < k1) {
-                    ++c;
-                    mb = x > mb ? x : mb;
-                }
-            });
-            c = __reduce_add_sync(kFull, c);
-            mb = warp_max_k(mb);
-            const Real v0 = c < M / 2 ? v1 : from_key(mb);
+        const Sel<K> s = kth_select<K>(src, M / 2, cand, cb.cap1, cand2, cb.cap2, lane);
+        const Real v1 = from_key(s.kth);
+        if (M % 2 == 0) {  // s_(M/2-1): from the sorted candidates, else v1 itself or the largest key below it
+            Real v0;
+            if (s.have_prev) {
+                v0 = from_key(s.prev);
+            } else {
+                uint32_t c = 0;
+                K mb = K(0);
+                src.each([&](K x) {
+                    if (x < s.kth) {
+                        ++c;
+                        mb = x > mb ? x : mb;
+                    }
+                });
+                c = __reduce_add_sync(kFull, c);
+                mb = warp_max_k(mb);
+                v0 = c < M / 2 ? v1 : from_key(mb);
+            }
             return (v1 + v0) * Real(0.25);
         }
         return v1 * Real(0.5);
@@ -288,7 +359,7 @@ __device__ Real order_update(const Src& src, uint32_t M, int mode, int pct, type
     uint32_t jm = u32_cast_x86(pct / 100.0 * M);
     if (jm < 1) jm = 1;
     if (jm > M) jm = M;
-    const K kt = kth_select<K>(src, jm - 1, cand, cand2, lane);
+    const K kt = kth_select<K>(src, jm - 1, cand, cb.cap1, cand2, cb.cap2, lane).kth;
     const Real t = from_key(kt);
     Real s = 0;
     uint32_t c = 0;
@@ -311,11 +382,10 @@ __device__ __forceinline__ Real pair_g(const typename Vec4<Real>::type& k, Real 
     return k.x * l + k.y * (lt + l * l * Real(0.5)) + k.z * (l * l * l * Real(1.0 / 3.0) + (l + t) * lt);
 }
 
+// the voxel's pairs held in registers, R per lane
 template <typename Real, int R, typename OutT>
 __device__ __forceinline__ void voxel_regs(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uint64_t base, uint32_t M,
-                                           int lane, typename KeyOf<Real>::type* cand,
-                                           typename KeyOf<Real>::type* cand2) {
-    using R4 = typename Vec4<Real>::type;
+                                           int lane, const CandBufs& cb) {
     using R2 = typename Vec2<Real>::type;
     const Real lam = a.lam[j];
     const bool keys = a.mode == kVoxMedian || a.mode == kVoxPercentile;
@@ -350,7 +420,7 @@ __device__ __forceinline__ void voxel_regs(const VoxelPassArgs<Real, OutT>& a, u
     }
     Real out;
     if (keys) {
-        out = order_update<Real>(v, M, a.mode, a.pct, cand, cand2, lane);
+        out = order_update<Real>(v, M, a.mode, a.pct, cb, lane);
     } else {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) gs += __shfl_xor_sync(kFull, gs, o);
@@ -367,7 +437,7 @@ __device__ __forceinline__ void voxel_regs(const VoxelPassArgs<Real, OutT>& a, u
 // array (same offsets as the voxel-major lists) and the selection reads them there
 template <typename Real, typename OutT>
 __device__ void voxel_stream(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uint64_t base, uint32_t M, int lane,
-                             typename KeyOf<Real>::type* cand, typename KeyOf<Real>::type* cand2) {
+                             const CandBufs& cb) {
     using K = typename KeyOf<Real>::type;
     const Real lam = a.lam[j];
     const bool keys = a.mode == kVoxMedian || a.mode == kVoxPercentile;
@@ -383,7 +453,7 @@ __device__ void voxel_stream(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uin
     if (keys) {
         __syncwarp();  // the lanes' key stores are visible to the whole warp
         const PtrKeys<K> src{kp, M, lane};
-        out = order_update<Real>(src, M, a.mode, a.pct, cand, cand2, lane);
+        out = order_update<Real>(src, M, a.mode, a.pct, cb, lane);
     } else {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) gs += __shfl_xor_sync(kFull, gs, o);
@@ -396,20 +466,10 @@ __device__ void voxel_stream(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uin
     if (lane == 0) a.out[j] = static_cast<OutT>(out);
 }
 
-// one warp per voxel of class CLS (0: M <= 256, 1: M <= 768, 2: longer)
 template <typename Real, typename OutT, int CLS>
-__global__ void __launch_bounds__(kVoxThreads) k_em_voxel(VoxelPassArgs<Real, OutT> a, const uint32_t* __restrict__ list,
-                                                          uint32_t n) {
-    using K = typename KeyOf<Real>::type;
-    __shared__ K cand_all[kWarps][CandCap<K>::c1];
-    __shared__ K cand2_all[kWarps][CandCap<K>::c2];
-    const int lane = threadIdx.x & 31;
-    K* cand = cand_all[threadIdx.x >> 5];
-    K* cand2 = cand2_all[threadIdx.x >> 5];
-    const uint64_t w = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (w >= n) return;  // whole warps leave together
-    const uint32_t j = list[w];
-    const uint32_t M = a.mult[j];
+__device__ __forceinline__ void voxel_one(const VoxelPassArgs<Real, OutT>& a, const VoxDesc& d, int lane,
+                                          const CandBufs& cb) {
+    const uint32_t j = d.j, M = d.M;
     if (M == 0) {  // no muon crossed the voxel, src/MutoMLSD.cpp:494-496
         if (lane == 0) {
             if (a.mode == kVoxGradient) a.grad[j] = 0.0;
@@ -417,30 +477,57 @@ __global__ void __launch_bounds__(kVoxThreads) k_em_voxel(VoxelPassArgs<Real, Ou
         }
         return;
     }
-    const uint64_t base = a.start[j];
+    const uint64_t base = d.start;
     if constexpr (CLS == 0) {
-        if (M <= 32u) voxel_regs<Real, 1>(a, j, base, M, lane, cand, cand2);
-        else if (M <= 64u) voxel_regs<Real, 2>(a, j, base, M, lane, cand, cand2);
-        else if (M <= 128u) voxel_regs<Real, 4>(a, j, base, M, lane, cand, cand2);
-        else if (M <= 192u) voxel_regs<Real, 6>(a, j, base, M, lane, cand, cand2);
-        else voxel_regs<Real, 8>(a, j, base, M, lane, cand, cand2);
+        if (M <= 32u) voxel_regs<Real, 1>(a, j, base, M, lane, cb);
+        else if (M <= 64u) voxel_regs<Real, 2>(a, j, base, M, lane, cb);
+        else if (M <= 128u) voxel_regs<Real, 4>(a, j, base, M, lane, cb);
+        else if (M <= 192u) voxel_regs<Real, 6>(a, j, base, M, lane, cb);
+        else voxel_regs<Real, 8>(a, j, base, M, lane, cb);
     } else if constexpr (CLS == 1) {
-        if (M <= 384u) voxel_regs<Real, 12>(a, j, base, M, lane, cand, cand2);
-        else if (M <= 512u) voxel_regs<Real, 16>(a, j, base, M, lane, cand, cand2);
-        else voxel_regs<Real, 24>(a, j, base, M, lane, cand, cand2);
+        if (M <= 384u) voxel_regs<Real, 12>(a, j, base, M, lane, cb);
+        else if (M <= 512u) voxel_regs<Real, 16>(a, j, base, M, lane, cb);
+        else voxel_regs<Real, 24>(a, j, base, M, lane, cb);
     } else {
         if constexpr (voxel_register_cap<Real>() > 768u) {  // 64-bit keys stay at 24 registers per lane
             if (M <= 1024u) {
-                voxel_regs<Real, 32>(a, j, base, M, lane, cand, cand2);
+                voxel_regs<Real, 32>(a, j, base, M, lane, cb);
                 return;
             }
             if (M <= 1536u) {
-                voxel_regs<Real, 48>(a, j, base, M, lane, cand, cand2);
+                voxel_regs<Real, 48>(a, j, base, M, lane, cb);
                 return;
             }
         }
-        voxel_stream<Real, OutT>(a, j, base, M, lane, cand, cand2);
+        voxel_stream<Real, OutT>(a, j, base, M, lane, cb);
     }
+}
+
+// Voxels of class CLS (0: M <= 256, 1: M <= 768, 2: longer), one warp per
+// voxel.  Each warp also prefetches into L2 the pair lists of the voxel
+// `ahead` places further down the class list, which a warp of the next wave
+// of resident blocks will read.
+template <typename Real, typename OutT, int CLS>
+__global__ void __launch_bounds__(kVoxThreads)
+    k_em_voxel(VoxelPassArgs<Real, OutT> a, const VoxDesc* __restrict__ desc, uint32_t n, uint32_t ahead) {
+    using K = typename KeyOf<Real>::type;
+    using R2 = typename Vec2<Real>::type;
+    constexpr int C1 = CandCap<K, CLS>::c1, C2 = CandCap<K, CLS>::c2;
+    __shared__ K cand_all[kWarps][C1];
+    __shared__ K cand2_all[kWarps][C2];
+    const int lane = threadIdx.x & 31;
+    const CandBufs cb{cand_all[threadIdx.x >> 5], cand2_all[threadIdx.x >> 5], C1, C2};
+    const uint64_t w = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (w >= n) return;  // whole warps leave together
+    const VoxDesc d = desc[w];
+    if (lane == 0 && w + ahead < n) {
+        const VoxDesc f = desc[w + ahead];
+        if (f.M > 0) {
+            prefetch_l2(a.vm_mu + f.start, size_t(f.M) * sizeof(uint32_t));
+            prefetch_l2(a.vm_LT + f.start, size_t(f.M) * sizeof(R2));
+        }
+    }
+    voxel_one<Real, OutT, CLS>(a, d, lane, cb);
 }
 
 __global__ void k_finalize_cost(Counters* ctr, double n_muons, double* hist, uint32_t cap) {
@@ -592,24 +679,43 @@ inline unsigned blocks_for(uint64_t n, int threads) {
 
 }  // namespace
 
+template <typename Real, typename OutT, int CLS>
+int voxel_blocks_per_sm() {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_em_voxel<Real, OutT, CLS>, kVoxThreads, 0) != cudaSuccess)
+        nb = 0;
+    return nb > 0 ? nb : 1;
+}
+
 template <typename Real, typename OutT>
-void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const uint32_t* const* lists, const uint32_t* counts,
-                     cudaStream_t s) {
+void em_voxel_occupancy(int blocks_per_sm[3]) {
+    blocks_per_sm[0] = voxel_blocks_per_sm<Real, OutT, 0>();
+    blocks_per_sm[1] = voxel_blocks_per_sm<Real, OutT, 1>();
+    blocks_per_sm[2] = voxel_blocks_per_sm<Real, OutT, 2>();
+}
+template void em_voxel_occupancy<float, float>(int*);
+template void em_voxel_occupancy<float, double>(int*);
+template void em_voxel_occupancy<double, double>(int*);
+
+template <typename Real, typename OutT>
+void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists, const uint32_t* counts,
+                     const int* resident_blocks, cudaStream_t s) {
     for (int c = 0; c < 3; ++c) {
         if (counts[c] == 0) continue;
         const unsigned nb = blocks_for(static_cast<uint64_t>(counts[c]) * 32u, kVoxThreads);
-        if (c == 0) k_em_voxel<Real, OutT, 0><<<nb, kVoxThreads, 0, s>>>(a, lists[c], counts[c]);
-        else if (c == 1) k_em_voxel<Real, OutT, 1><<<nb, kVoxThreads, 0, s>>>(a, lists[c], counts[c]);
-        else k_em_voxel<Real, OutT, 2><<<nb, kVoxThreads, 0, s>>>(a, lists[c], counts[c]);
+        const uint32_t ahead = static_cast<uint32_t>(resident_blocks[c]) * kWarps;  // warps of one wave
+        if (c == 0) k_em_voxel<Real, OutT, 0><<<nb, kVoxThreads, 0, s>>>(a, lists[c], counts[c], ahead);
+        else if (c == 1) k_em_voxel<Real, OutT, 1><<<nb, kVoxThreads, 0, s>>>(a, lists[c], counts[c], ahead);
+        else k_em_voxel<Real, OutT, 2><<<nb, kVoxThreads, 0, s>>>(a, lists[c], counts[c], ahead);
         count_launches(1);
     }
 }
-template void launch_em_voxel<float, float>(const VoxelPassArgs<float, float>&, const uint32_t* const*,
-                                            const uint32_t*, cudaStream_t);
-template void launch_em_voxel<float, double>(const VoxelPassArgs<float, double>&, const uint32_t* const*,
-                                             const uint32_t*, cudaStream_t);
-template void launch_em_voxel<double, double>(const VoxelPassArgs<double, double>&, const uint32_t* const*,
-                                              const uint32_t*, cudaStream_t);
+template void launch_em_voxel<float, float>(const VoxelPassArgs<float, float>&, const VoxDesc* const*,
+                                            const uint32_t*, const int*, cudaStream_t);
+template void launch_em_voxel<float, double>(const VoxelPassArgs<float, double>&, const VoxDesc* const*,
+                                             const uint32_t*, const int*, cudaStream_t);
+template void launch_em_voxel<double, double>(const VoxelPassArgs<double, double>&, const VoxDesc* const*,
+                                              const uint32_t*, const int*, cudaStream_t);
 
 void launch_finalize_cost(Counters* ctr, double n_muons, double* hist, uint32_t cap, cudaStream_t s) {
     k_finalize_cost<<<1, 1, 0, s>>>(ctr, n_muons, hist, cap);

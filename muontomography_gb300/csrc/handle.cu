@@ -282,8 +282,9 @@ struct muto_handle {
     DevMem kept, sd, pr2, scat, pr64, off;
     DevMem vidx, L, T;            // muon-major pair lists
     DevMem vm_mu, vm_LT;          // voxel-major copy (muon, (L, T))
-    DevMem vclass;                // voxel ids by segment-length class
+    DevMem vclass;                // VoxDesc of every voxel, by segment-length class
     uint32_t vclass_n[3] = {0, 0, 0};
+    int vox_blocks_real[3] = {1, 1, 1}, vox_blocks_f64[3] = {1, 1, 1};  // grid caps of the class kernels
     uint64_t vclass_off[3] = {0, 0, 0};
     DevMem mult, start, kvec, keys;   // keys: scratch for voxels beyond the register budget
     DevMem lam, lam_ml, cost_hist;
@@ -591,18 +592,32 @@ void prepare_em(muto_handle* h) {
         const uint32_t mmax = V ? *std::max_element(m_h.begin(), m_h.end()) : 0u;
         if (mmax > voxel_register_cap<Real>())
             h->keys.alloc(std::max<uint64_t>(Pn, 1) * sizeof(typename KeyOf<Real>::type), &h->dev_bytes);
-        // voxel classes by segment length, one voxel-pass kernel each
-        std::vector<uint32_t> cls[3];
-        for (uint64_t j = 0; j < V; ++j) cls[m_h[j] <= 256u ? 0 : (m_h[j] <= 768u ? 1 : 2)].push_back(static_cast<uint32_t>(j));
-        h->vclass.alloc(std::max<uint64_t>(V, 1) * sizeof(uint32_t), &h->dev_bytes);
+        // voxel classes by segment length, one voxel-pass kernel each; a
+        // descriptor carries the voxel, its pair count and its first pair
+        // (the exclusive sum of the counts, as the device scan has it)
+        std::vector<VoxDesc> cls[3];
+        uint64_t first = 0;
+        for (uint64_t j = 0; j < V; ++j) {
+            const uint32_t m = m_h[j];
+            cls[m <= 256u ? 0 : (m <= 768u ? 1 : 2)].push_back(VoxDesc{static_cast<uint32_t>(j), m, first});
+            first += m;
+        }
+        if (first != Pn) throw Error(MUTO_ERR_STATE, "voxel multiplicities do not add up to the pair count");
+        h->vclass.alloc(std::max<uint64_t>(V, 1) * sizeof(VoxDesc), &h->dev_bytes);
         uint64_t at = 0;
         for (int c = 0; c < 3; ++c) {
             h->vclass_off[c] = at;
             h->vclass_n[c] = static_cast<uint32_t>(cls[c].size());
             if (!cls[c].empty())
-                CK(cudaMemcpy(h->vclass.as<uint32_t>() + at, cls[c].data(), cls[c].size() * sizeof(uint32_t),
+                CK(cudaMemcpy(h->vclass.as<VoxDesc>() + at, cls[c].data(), cls[c].size() * sizeof(VoxDesc),
                               cudaMemcpyHostToDevice));
             at += cls[c].size();
+        }
+        em_voxel_occupancy<Real, Real>(h->vox_blocks_real);
+        em_voxel_occupancy<Real, double>(h->vox_blocks_f64);
+        for (int c = 0; c < 3; ++c) {
+            h->vox_blocks_real[c] *= h->num_sms;
+            h->vox_blocks_f64[c] *= h->num_sms;
         }
     }
 
@@ -757,9 +772,10 @@ VoxelPassArgs<Real, OutT> voxel_args(muto_handle* h, const Real* lam, int mode, 
 
 template <typename Real, typename OutT>
 void launch_voxel_pass(muto_handle* h, const VoxelPassArgs<Real, OutT>& v, cudaStream_t s) {
-    const uint32_t* lists[3];
-    for (int c = 0; c < 3; ++c) lists[c] = h->vclass.as<uint32_t>() + h->vclass_off[c];
-    launch_em_voxel<Real, OutT>(v, lists, h->vclass_n, s);
+    const VoxDesc* lists[3];
+    for (int c = 0; c < 3; ++c) lists[c] = h->vclass.as<VoxDesc>() + h->vclass_off[c];
+    launch_em_voxel<Real, OutT>(v, lists, h->vclass_n,
+                                std::is_same<OutT, Real>::value ? h->vox_blocks_real : h->vox_blocks_f64, s);
 }
 
 int voxel_mode(const Params& P) {
@@ -942,6 +958,91 @@ int n_prepared_check(muto_handle* h) {
 // ===========================================================================
 // C ABI
 // ===========================================================================
+namespace {
+
+// the voxel pass on synthetic segments: pair i has L = 1, T = 0 and its own
+// muon with k = (x_i, 0, 0), every voxel lambda = 1, so s_i = 2 + x_i
+template <typename Real>
+void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off, uint32_t n_segs, int mode, int pct,
+                      double* out) {
+    using R2 = typename Vec2<Real>::type;
+    using R4 = typename Vec4<Real>::type;
+    cudaStream_t s;
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    std::vector<uint32_t> mu(n);
+    std::vector<R2> lt(n);
+    std::vector<R4> kv(n);
+    for (uint64_t i = 0; i < n; ++i) {
+        mu[i] = static_cast<uint32_t>(i);
+        lt[i].x = Real(1);
+        lt[i].y = Real(0);
+        kv[i].x = static_cast<Real>(values[i]);
+        kv[i].y = kv[i].z = kv[i].w = Real(0);
+    }
+    std::vector<VoxDesc> cls[3];
+    uint32_t mmax = 0;
+    for (uint32_t j = 0; j < n_segs; ++j) {
+        const uint64_t m64 = seg_off[j + 1] - seg_off[j];
+        if (seg_off[j + 1] < seg_off[j] || seg_off[j + 1] > n || m64 > 0xffffffffull)
+            throw Error(MUTO_ERR_ARG, "segment offsets must be non-decreasing and within the values");
+        const uint32_t m = static_cast<uint32_t>(m64);
+        mmax = std::max(mmax, m);
+        cls[m <= 256u ? 0 : (m <= 768u ? 1 : 2)].push_back(VoxDesc{j, m, seg_off[j]});
+    }
+    std::vector<Real> lam(n_segs, Real(1));
+    DevMem d_mu, d_lt, d_kv, d_lam, d_out, d_desc, d_keys;
+    const uint64_t np = n + kPad;
+    d_mu.alloc(np * sizeof(uint32_t), nullptr);
+    d_lt.alloc(np * sizeof(R2), nullptr);
+    d_kv.alloc(np * sizeof(R4), nullptr);
+    d_lam.alloc(std::max<uint64_t>(n_segs, 1) * sizeof(Real), nullptr);
+    d_out.alloc(std::max<uint64_t>(n_segs, 1) * sizeof(Real), nullptr);
+    d_desc.alloc(std::max<uint64_t>(n_segs, 1) * sizeof(VoxDesc), nullptr);
+    if (mmax > voxel_register_cap<Real>()) d_keys.alloc(np * sizeof(typename KeyOf<Real>::type), nullptr);
+    if (n) {
+        CK(cudaMemcpyAsync(d_mu.as<void>(), mu.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_lt.as<void>(), lt.data(), n * sizeof(R2), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_kv.as<void>(), kv.data(), n * sizeof(R4), cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaMemcpyAsync(d_lam.as<void>(), lam.data(), n_segs * sizeof(Real), cudaMemcpyHostToDevice, s));
+    const VoxDesc* lists[3];
+    uint32_t counts[3];
+    uint64_t at = 0;
+    for (int c = 0; c < 3; ++c) {
+        lists[c] = d_desc.as<VoxDesc>() + at;
+        counts[c] = static_cast<uint32_t>(cls[c].size());
+        if (counts[c])
+            CK(cudaMemcpyAsync(d_desc.as<VoxDesc>() + at, cls[c].data(), counts[c] * sizeof(VoxDesc),
+                               cudaMemcpyHostToDevice, s));
+        at += counts[c];
+    }
+    int dev = 0, sms = 1;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int resident[3];
+    em_voxel_occupancy<Real, Real>(resident);
+    for (int c = 0; c < 3; ++c) resident[c] *= sms;
+    VoxelPassArgs<Real, Real> v{};
+    v.vm_mu = d_mu.as<uint32_t>();
+    v.vm_LT = d_lt.as<R2>();
+    v.kvec = d_kv.as<R4>();
+    v.lam = d_lam.as<Real>();
+    v.V = n_segs;
+    v.mode = mode;
+    v.pct = pct;
+    v.out = d_out.as<Real>();
+    v.scratch = d_keys.empty() ? nullptr : d_keys.as<typename KeyOf<Real>::type>();
+    launch_em_voxel<Real, Real>(v, lists, counts, resident, s);
+    CK(cudaGetLastError());
+    std::vector<Real> o(n_segs);
+    CK(cudaMemcpyAsync(o.data(), d_out.as<void>(), n_segs * sizeof(Real), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaStreamDestroy(s));
+    for (uint32_t j = 0; j < n_segs; ++j) out[j] = static_cast<double>(o[j]);
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* muto_version(void) { return "muto-gb300 0.1 (sm_103a)"; }
@@ -1127,6 +1228,19 @@ int muto_reconstruct(muto_handle* h, const muto_ray* rays, uint64_t n, double* o
         if (rc) return rc;
     }
     return muto_get_image(h, out_img, out_len);
+}
+
+int muto_select_probe(int precision, const double* values, uint64_t n, const uint64_t* seg_off, uint32_t n_segs,
+                      int update_with_mean, int mean_percentile, double* out) {
+    if ((n > 0 && !values) || !seg_off || (n_segs > 0 && !out) || (precision != 0 && precision != 1) ||
+        mean_percentile < 0 || mean_percentile > 100 || n > 0xffffffffull)
+        return MUTO_ERR_ARG;
+    const int mode = !update_with_mean ? kVoxMedian : (mean_percentile == 100 ? kVoxMean : kVoxPercentile);
+    return guarded(nullptr, [&] {
+        if (n_segs == 0) return;
+        if (precision == 1) select_probe_run<double>(values, n, seg_off, n_segs, mode, mean_percentile, out);
+        else select_probe_run<float>(values, n, seg_off, n_segs, mode, mean_percentile, out);
+    });
 }
 
 int muto_siddon_batch(const muto_grid* g, const double* p1, const double* p2, uint64_t n, uint32_t cap, uint32_t* xyz,

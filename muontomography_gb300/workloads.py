@@ -75,6 +75,14 @@ def config2(n_muons: int = 10_000_000, seed: int = 2) -> Workload:
     return Workload("config2_100cube_10M", g, blocks, n_muons, seed, True, 50)
 
 
+def config2_coarse(n_muons: int = 2_500_000, seed: int = 2) -> Workload:
+    """config2's scene on 50^3 voxels of 40 mm with a quarter of the muons: the same
+    pairs per voxel (about 550) in a quarter of the memory, for profiler captures."""
+    full = config2(seed=seed)
+    g = Grid(50, 50, 50, -1000.0, -1000.0, -1000.0, 40.0, 40.0, 40.0)
+    return Workload("config2_coarse_50cube_2.5M", g, full.blocks, n_muons, seed, True, 50)
+
+
 def config3(n_muons: int = 20_000_000, seed: int = 3) -> Workload:
     """128x128x64 voxels of 15 mm, MAP with the 26-neighbour prior."""
     g = Grid(128, 128, 64, -960.0, -960.0, -480.0, 15.0, 15.0, 15.0)
