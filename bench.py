@@ -113,8 +113,16 @@ def workload(args, rank: int):
     return wl
 
 
+# set-up kernels and host phases reported by the library's profiler
+SETUP_KERNELS = ["keep_flags", "scan", "compact", "muon_info", "siddon_count", "siddon_fill", "voxel_offset",
+                 "voxel_hist", "voxel_major", "voxel_classes"]
+SETUP_PHASES = ["gather", "info_count", "offsets", "fill", "voxel_major", "classes", "tiles", "image", "autotune"]
+
+
 def em_config(wl, args, precision: str, n_iter: int) -> dict:
     over = {"precision": precision, "num_iteration": n_iter, "muon_pass": args.muon_pass}
+    if getattr(args, "voxel_stream_above", None) is not None:
+        over["voxel_stream_above"] = args.voxel_stream_above
     if args.mode == "mean":
         over.update(update_with_mean=True, mean_percentile=100)
     return wl.em_config(**over)
@@ -217,17 +225,25 @@ def run_ours(args) -> int:
     cfg = em_config(wl, args, args.precision, args.warmup + args.steps)
     rec = M.Reconstruction("mlsd", cfg)
     rec.load_tracks(None, on_device_ptr=d_rays.data_ptr(), n=n)
+    rec.set_profiling(True)
     t0 = time.perf_counter()
     rec.prepare()
     t_setup = time.perf_counter() - t0
+    setup_ms = {}
+    for name in SETUP_KERNELS + ["host:" + p for p in SETUP_PHASES]:
+        cnt, tot = rec.kernel_stats(name)
+        if cnt:
+            setup_ms[name] = round(tot, 3)
     st = rec.status()
     pairs, kept, V = st["n_pairs"], st["n_scat_in_grid"], wl.grid.nvox
     sp = C.c_void_p()
     lib.muto_get_stream(rec._h, C.byref(sp))
     stream = torch.cuda.ExternalStream(sp.value)
-    rec.set_profiling(True)
     for _ in range(args.warmup):
         rec.iterate(1)
+    cnt, tot = rec.kernel_stats("host:graph_capture")
+    if cnt:
+        setup_ms["host:graph_capture"] = round(tot, 3)
     rec.reset_kernel_stats()
     l0 = rec.launch_count()
     clocks = ClockSampler(torch.cuda.current_device())
@@ -294,10 +310,24 @@ def run_ours(args) -> int:
             if k > 0:
                 times.append(a.elapsed_time(b))
             r2.close()
+        # the set-up of one more reconstruct, untimed, by phase (modules loaded)
+        r2 = M.Reconstruction("mlsd", ecfg)
+        r2.set_profiling(True)
+        t0 = time.perf_counter()
+        r2.load_tracks(host.numpy())
+        setup_warm = {"load_tracks_h2d": round((time.perf_counter() - t0) * 1e3, 3)}
+        t0 = time.perf_counter()
+        r2.prepare()
+        setup_warm["prepare"] = round((time.perf_counter() - t0) * 1e3, 3)
+        for name in SETUP_KERNELS + ["host:" + p for p in SETUP_PHASES]:
+            cnt, tot = r2.kernel_stats(name)
+            if cnt:
+                setup_warm[name] = round(tot, 3)
+        r2.close()
         e_ms = allmax(statistics.mean(times))
         e2e = {"value": total_pairs * args.e2e_iters / (e_ms / 1000.0), "unit": UNIT,
                "h2d_bytes_per_step": int(n * 14 * 8), "d2h_bytes_per_step": int(V * rb),
-               "ms_per_step": e_ms, "em_iterations_per_step": args.e2e_iters,
+               "ms_per_step": e_ms, "em_iterations_per_step": args.e2e_iters, "setup_ms": setup_warm,
                "what": "muto_reconstruct: H2D of pinned tracks, setup (gather, Siddon lists), "
                        f"{args.e2e_iters} EM iterations, D2H of the image"}
     else:
@@ -352,7 +382,7 @@ def run_ours(args) -> int:
                        "precision": args.precision, "per_muon_2x2": "f64", "graph": True,
                        "parallelism": f"replicas x{world} (one scan per GPU)",
                        "l2": "inputs larger than L2: pair lists and s_ij far exceed 126 MB, no flush",
-                                  "setup_s": t_setup, "generate_s": t_gen, "muon_pass": {1: "tma_tiles", 2: "warp_batched"}.get(st["muon_pass"]),
+                                  "setup_s": t_setup, "setup_ms": setup_ms, "generate_s": t_gen, "muon_pass": {1: "tma_tiles", 2: "warp_batched"}.get(st["muon_pass"]),
             "muon_group": st["muon_group"], "tile_pairs": st["tile_pairs"]},
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -382,6 +412,8 @@ def main() -> int:
     ap.add_argument("--ttl-iters", type=int, default=50)
     ap.add_argument("--cpu-sample", type=int, default=150_000)
     ap.add_argument("--muon-pass", choices=["auto", "tile", "warp"], default="auto")
+    ap.add_argument("--voxel-stream-above", type=int, default=None,
+                    help="segments longer than this are selected without holding their keys (-1: never)")
     ap.add_argument("--ncu-traffic", type=float, default=None,
                     help="dram bytes per em_tile launch from an ncu capture (profiles/)")
     args = ap.parse_args()

@@ -187,20 +187,55 @@ struct VoxelPassArgs {
 // segments up to this many pairs are selected from registers
 template <typename Real>
 __host__ __device__ constexpr uint32_t voxel_register_cap() { return sizeof(Real) == 4 ? 1536u : 768u; }
+// Voxel classes by segment length, one voxel-pass kernel each: class c holds
+// the voxels with vox_class_lo(c) < M <= vox_class_hi(c) and keeps
+// vox_class_rows(c) keys per lane in registers; the last class (rows 0)
+// selects from the scratch array.  Voxels without pairs go with class 0.
+constexpr int kVoxClasses = 11;
+__host__ __device__ constexpr uint32_t vox_class_hi(int c) {
+    return c == 0 ? 32u : c == 1 ? 64u : c == 2 ? 128u : c == 3 ? 192u : c == 4 ? 256u : c == 5 ? 384u
+         : c == 6 ? 512u : c == 7 ? 768u : c == 8 ? 1024u : c == 9 ? 1536u : 0xffffffffu;
+}
+__host__ __device__ constexpr int vox_class_rows(int c) { return c < kVoxClasses - 1 ? int(vox_class_hi(c) / 32u) : 0; }
+template <typename Real>
+__host__ __device__ constexpr int vox_class_of(uint32_t M) {
+    int c = 0;
+    while (c < kVoxClasses - 1 && M > vox_class_hi(c)) ++c;
+    if (M > voxel_register_cap<Real>()) c = kVoxClasses - 1;
+    return c;
+}
 // one voxel of a class list: its index, pair count and first voxel-major pair
 struct alignas(16) VoxDesc {
     uint32_t j, M;
     unsigned long long start;
 };
-// voxels in three classes by segment length (lists[c], counts[c]): M <= 256,
-// M <= 768, longer; voxels without pairs go with the first class.
-// resident_blocks[c]: blocks of class c resident on the whole GPU at once.
+// lists[c], counts[c]: the descriptors of class c; resident_blocks[c] and
+// [kVoxClasses + c]: blocks of class c's register and streamed kernels
+// resident on the whole GPU at once; bit c of `streamed`: class c (M > 256
+// only) is selected without holding its keys in registers, which needs the
+// scratch array for its fallback.
 template <typename Real, typename OutT>
 void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists, const uint32_t* counts,
-                     const int* resident_blocks, cudaStream_t s);
-// resident blocks per SM of the three class kernels
+                     const int* resident_blocks, uint32_t streamed, cudaStream_t s);
+// descriptors of all voxels partitioned by class (voxel order within a
+// class): counts needs kVoxClasses * voxel_class_blocks(V) entries, first one
+// more (exclusive scan; class c starts at first[c * blocks]); scan_scratch
+// as for scan_u32_to_u64 of that length
+uint32_t voxel_class_blocks(uint64_t V);
+template <typename Real>
+void launch_voxel_classes(const uint32_t* mult, const uint64_t* start, uint32_t V, uint32_t* counts, uint64_t* first,
+                          void* scan_scratch, VoxDesc* out, cudaStream_t s);
+// classes that hold segments of more than `pairs` pairs: the streamed mask
+__host__ __device__ constexpr uint32_t vox_streamed_mask(uint32_t pairs) {
+    uint32_t m = 0;
+    for (int c = 5; c < kVoxClasses; ++c)
+        if (vox_class_hi(c - 1) >= pairs) m |= 1u << c;
+    return m;
+}
+// resident blocks per SM of the class kernels (also sets their shared-memory
+// limit: call before any launch, outside stream capture)
 template <typename Real, typename OutT>
-void em_voxel_occupancy(int blocks_per_sm[3]);
+void em_voxel_occupancy(int blocks_per_sm[2 * kVoxClasses]);
 void launch_finalize_cost(Counters* ctr, double n_muons, double* hist, uint32_t hist_cap, cudaStream_t s);
 
 struct MapParams {

@@ -23,6 +23,7 @@
 // Voxels are grouped by segment length into classes, each its own kernel
 // instantiation, so short segments run with few registers and many warps.
 #include <algorithm>
+#include <utility>
 
 #include "common.cuh"
 
@@ -32,15 +33,30 @@ namespace {
 constexpr int kVoxThreads = 256;
 constexpr int kWarps = kVoxThreads / 32;
 
-// shared-memory candidate buffers per warp: the first window of a short
-// segment holds about 3/8 of it (at most 256 keys below M = 256)
-template <typename K, int CLS> struct CandCap;
-template <> struct CandCap<uint32_t, 0> { static constexpr int c1 = 256, c2 = 128; };
-template <> struct CandCap<uint32_t, 1> { static constexpr int c1 = 640, c2 = 256; };
-template <> struct CandCap<uint32_t, 2> { static constexpr int c1 = 640, c2 = 256; };
-template <> struct CandCap<unsigned long long, 0> { static constexpr int c1 = 256, c2 = 128; };
-template <> struct CandCap<unsigned long long, 1> { static constexpr int c1 = 448, c2 = 192; };
-template <> struct CandCap<unsigned long long, 2> { static constexpr int c1 = 448, c2 = 192; };
+// Rows of 32 keys in each of a warp's two candidate buffers.  Segments held
+// in registers get enough for any first window (at most R rows per lane).
+// Streamed segments get about 0.6 R + 4, at most 28 (a first window keeps
+// about 3/8 of the keys); the scratch-array class keeps 48 (32-bit keys) or
+// 24 rows.  A first window that does not fit falls back to the scratch array.
+template <typename K, int C, bool STREAMED>
+__host__ __device__ constexpr int cand_rows() {
+    return STREAMED ? (vox_class_rows(C) == 0 || (vox_class_rows(C) * 5) / 8 + 4 > 28 ? 28
+                                                                               : (vox_class_rows(C) * 5) / 8 + 4)
+         : vox_class_rows(C) == 0 ? (sizeof(K) == 4 ? 48 : 24)
+         : (vox_class_rows(C) < 8 ? 8 : vox_class_rows(C));
+}
+// resident blocks per SM each class kernel is compiled for (its register cap)
+__host__ __device__ constexpr int vox_min_blocks(int C, bool streamed) {
+    return streamed ? 4 : C <= 4 ? 5 : C <= 6 ? 4 : C == 7 ? 3 : C <= 9 ? 2 : 5;
+}
+// classes whose segments are long enough (M > 256) to be selected by the
+// streamed path
+__host__ __device__ constexpr bool streamable(int C) { return C >= 5; }
+template <typename K, int C, bool STREAMED>
+__host__ __device__ constexpr size_t voxel_smem_bytes() {
+    return size_t(2) * kWarps * cand_rows<K, C, STREAMED>() * 32 * sizeof(K);
+}
+
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 __device__ __forceinline__ double4 ldg4(const double4* p) {
     const double2* q = reinterpret_cast<const double2*>(p);
@@ -52,6 +68,11 @@ __device__ __forceinline__ double4 ldg4(const double4* p) {
     r.w = b.y;
     return r;
 }
+
+// Keys are order-preserving images of finite values, so the all-ones key
+// (a NaN pattern) never occurs: it marks empty slots.
+template <typename K>
+__device__ __forceinline__ constexpr K empty_key() { return ~K(0); }
 
 template <typename K>
 __device__ __forceinline__ K warp_min_k(K v) {
@@ -105,48 +126,63 @@ __device__ K kth_radix(const Src& src, uint32_t k) {
     return prefix;
 }
 
-// keys in memory (window candidates in shared memory, or a long segment's
-// keys in the global scratch array)
-template <typename K>
-struct PtrKeys {
-    const K* p;
-    uint32_t n;
-    int lane;
-    template <class F>
-    __device__ __forceinline__ void each(F f) const {
-        for (uint32_t i = lane; i < n; i += 32) f(p[i]);
-    }
-    template <class F>
-    __device__ __forceinline__ void each_all(F f) const {
-        for (uint32_t i0 = 0; i0 < n; i0 += 32) {
-            const uint32_t i = i0 + lane;
-            f(i < n ? p[i] : K(0), i < n);
-        }
-    }
-    __device__ __forceinline__ K sample() const { return p[(lane * n) >> 5]; }
-    __device__ __forceinline__ uint32_t size() const { return n; }
-};
+// Key sources.  Each gives rows() rows of one key per lane (get(r), the
+// empty key where a lane has none), one sample per lane, and each() over
+// its own keys only.
 
-// The voxel's s_ij as order-preserving keys, element r*32+lane in key[r].
+// The voxel's s_ij in registers: element r*32+lane in key[r], empty past M.
 template <typename Real, int R>
 struct VoxKeys {
     using K = typename KeyOf<Real>::type;
     K key[R];
     uint32_t M;
     int lane;
+    static constexpr bool kBounded = true;  // a lane never has more than R keys
+    __device__ __forceinline__ uint32_t rows() const { return R; }
+    __device__ __forceinline__ K get(int r) const { return key[r]; }
+    __device__ __forceinline__ K sample() const { return key[0]; }  // element `lane`: slot order is random
     template <class F>
     __device__ __forceinline__ void each(F f) const {
 #pragma unroll
         for (int r = 0; r < R; ++r)
             if (static_cast<uint32_t>(r * 32 + lane) < M) f(key[r]);
     }
-    template <class F>
-    __device__ __forceinline__ void each_all(F f) const {
-#pragma unroll
-        for (int r = 0; r < R; ++r) f(key[r], static_cast<uint32_t>(r * 32 + lane) < M);
+};
+
+// A long segment's keys in the global scratch array, contiguous.
+template <typename K>
+struct PtrKeys {
+    const K* p;
+    uint32_t n;
+    int lane;
+    static constexpr bool kBounded = false;
+    __device__ __forceinline__ uint32_t rows() const { return (n + 31) >> 5; }
+    __device__ __forceinline__ K get(uint32_t r) const {
+        const uint32_t i = r * 32 + lane;
+        return i < n ? p[i] : empty_key<K>();
     }
-    __device__ __forceinline__ K sample() const { return key[0]; }  // element `lane`: positions follow slot order
-    __device__ __forceinline__ uint32_t size() const { return M; }
+    __device__ __forceinline__ K sample() const { return p[(lane * n) >> 5]; }
+    template <class F>
+    __device__ __forceinline__ void each(F f) const {
+        for (uint32_t i = lane; i < n; i += 32) f(p[i]);
+    }
+};
+
+// Window candidates in shared memory, ragged: lane l holds t keys, at rows
+// 0 .. t-1 of column l; rows is the largest t of the warp.
+template <typename K>
+struct Ragged {
+    K* buf;
+    uint32_t t, nrows;
+    int lane;
+    static constexpr bool kBounded = false;
+    __device__ __forceinline__ uint32_t rows() const { return nrows; }
+    __device__ __forceinline__ K get(uint32_t r) const { return r < t ? buf[r * 32 + lane] : empty_key<K>(); }
+    __device__ __forceinline__ K sample() const { return t > 0 ? buf[lane] : empty_key<K>(); }
+    template <class F>
+    __device__ __forceinline__ void each(F f) const {
+        for (uint32_t r = 0; r < t; ++r) f(buf[r * 32 + lane]);
+    }
 };
 
 // order statistic k of a segment and, when the final candidates hold it,
@@ -173,10 +209,10 @@ __device__ __forceinline__ K sort32(K s, int lane) {
     return s;
 }
 
-// order statistics k and k-1 of n <= 32 keys in shared memory
+// order statistics k and k-1 of n <= 32 contiguous keys in shared memory
 template <typename K>
 __device__ Sel<K> sel32(const K* c, uint32_t n, uint32_t k, int lane) {
-    const K s = sort32(static_cast<uint32_t>(lane) < n ? c[lane] : ~K(0), lane);
+    const K s = sort32(static_cast<uint32_t>(lane) < n ? c[lane] : empty_key<K>(), lane);
     Sel<K> r;
     r.kth = __shfl_sync(kFull, s, static_cast<int>(k));
     r.prev = __shfl_sync(kFull, s, static_cast<int>(k ? k - 1 : 0));
@@ -184,12 +220,12 @@ __device__ Sel<K> sel32(const K* c, uint32_t n, uint32_t k, int lane) {
     return r;
 }
 
-// order statistics k and k-1 of n <= 64 keys in shared memory: warp bitonic
-// sort of 64 (element e = 2 lane + t held in register t of its lane)
+// order statistics k and k-1 of n <= 64 contiguous keys in shared memory:
+// warp bitonic sort of 64 (element e = 2 lane + t in register t of its lane)
 template <typename K>
 __device__ Sel<K> sel64(const K* c, uint32_t n, uint32_t k, int lane) {
-    K a = static_cast<uint32_t>(2 * lane) < n ? c[2 * lane] : ~K(0);
-    K b = static_cast<uint32_t>(2 * lane + 1) < n ? c[2 * lane + 1] : ~K(0);
+    K a = static_cast<uint32_t>(2 * lane) < n ? c[2 * lane] : empty_key<K>();
+    K b = static_cast<uint32_t>(2 * lane + 1) < n ? c[2 * lane + 1] : empty_key<K>();
 #pragma unroll
     for (int size = 2; size <= 64; size <<= 1) {
         const bool up = ((2 * lane) & size) == 0 || size == 64;
@@ -218,121 +254,133 @@ __device__ Sel<K> sel64(const K* c, uint32_t n, uint32_t k, int lane) {
     return r;
 }
 
-// One sampling round: window of the keys within 6 sample ranks of rank k.
-// Counts the keys below it into *below and compacts the keys inside it into
-// out (up to cap).  Returns the number inside.
+// One sampling round over n keys: the (up to 32) samples are sorted in the
+// warp and the keys within 6 sample ranks of rank k are kept, each lane
+// appending its own to its column of `out` (no cross-lane compaction).
+// Returns false when the window misses rank k, overflows `out_rows` or
+// keeps everything; otherwise `out` holds the candidates and the counts.
 template <typename K, class Src>
-__device__ uint32_t window_round(const Src& v, uint32_t k, K* out, int cap, uint32_t* below, int lane) {
-    const uint32_t M = v.size();
-    const K s = sort32(v.sample(), lane);
-    const int pos = static_cast<int>((static_cast<float>(k) * 32.0f) / static_cast<float>(M));
+__device__ __forceinline__ bool sample_round(const Src& v, uint32_t n, uint32_t k, K* out, uint32_t out_rows,
+                                             int lane, Ragged<K>& res, uint32_t& below) {
+    const K smp = v.sample();
+    const uint32_t ns = __popc(__ballot_sync(kFull, smp != empty_key<K>()));
+    const K s = sort32(smp, lane);  // empty samples sort last
+    const int pos = static_cast<int>((static_cast<float>(k) * static_cast<float>(ns)) / static_cast<float>(n));
     const int ql = pos - 6, qh = pos + 6;
     const K slo = __shfl_sync(kFull, s, ql < 0 ? 0 : (ql > 31 ? 31 : ql));
     const K shi = __shfl_sync(kFull, s, qh > 31 ? 31 : (qh < 0 ? 0 : qh));
     const K lo = ql <= 0 ? K(0) : slo;
-    const K hi = qh >= 31 ? ~K(0) : shi;
-    uint32_t c_lo = 0, c_in = 0;
-    const unsigned below_me = (1u << lane) - 1u;
-    v.each_all([&](K x, bool valid) {
-        const bool lt = valid && x < lo;
-        const bool in = valid && !lt && x <= hi;
+    const K hi = qh >= static_cast<int>(ns) - 1 ? empty_key<K>() - 1 : shi;
+    uint32_t c_lo = 0, t = 0;
+    const uint32_t nr = v.rows();
+#pragma unroll
+    for (uint32_t r = 0; r < nr; ++r) {
+        const K x = v.get(r);
+        const bool lt = x < lo;
         c_lo += lt ? 1u : 0u;
-        const unsigned m = __ballot_sync(kFull, in);
-        if (in) {
-            const uint32_t at = c_in + __popc(m & below_me);
-            if (at < static_cast<uint32_t>(cap)) out[at] = x;
+        if (!lt && x <= hi) {
+            if (Src::kBounded || t < out_rows) out[t * 32 + lane] = x;
+            ++t;
         }
-        c_in += __popc(m);
-    });
-    __syncwarp();
-    *below = __reduce_add_sync(kFull, c_lo);
-    return c_in;
+    }
+    below = __reduce_add_sync(kFull, c_lo);
+    const uint32_t n_in = __reduce_add_sync(kFull, t);
+    const uint32_t rows = __reduce_max_sync(kFull, t);
+    res.buf = out;
+    res.t = t;
+    res.nrows = rows;
+    res.lane = lane;
+    return rows <= out_rows && below <= k && k < below + n_in && n_in < n;
 }
 
-// Order statistics kk and kk-1 of the n window candidates in cand, exact:
-// further sampling rounds between the two buffers until at most 64 remain,
-// which are sorted.  A window that misses the target, overflows or stops
-// shrinking falls back to a bitwise radix search.  Shared by every segment
-// length, so kept out of line.
+// Order statistics kk and kk-1 of the candidates in `cur`, exact: more
+// sampling rounds between the two buffers until at most 64 remain, which
+// are gathered and sorted.  A round that fails falls back to a bitwise radix
+// search of the candidates.  Shared by every segment length, so out of line.
 template <typename K>
-__device__ __noinline__ Sel<K> select_candidates(K* cand, int cap1, K* cand2, int cap2, uint32_t n, uint32_t kk,
-                                                 int lane) {
+__device__ __noinline__ Sel<K> select_candidates(K* cur_buf, K* oth_buf, uint32_t cap_rows, uint32_t t,
+                                                 uint32_t nrows, uint32_t n, uint32_t kk, int lane) {
+    Ragged<K> cur{cur_buf, t, nrows, lane};
+    K* oth = oth_buf;
     Sel<K> r;
     r.have_prev = false;
-    K* cur = cand;
-    K* oth = cand2;
-    int oth_cap = cap2, cur_cap = cap1;
 #pragma unroll 1
-    for (int round = 0; n > 64 && round < 6; ++round) {
-        const PtrKeys<K> c{cur, n, lane};
+    for (int round = 0; n > 64 && round < 8; ++round) {
+        Ragged<K> nxt;
         uint32_t b2;
-        const uint32_t n2 = window_round<K>(c, kk, oth, oth_cap, &b2, lane);
-        if (!(b2 <= kk && kk < b2 + n2 && n2 <= static_cast<uint32_t>(oth_cap)) || n2 >= n) {
-            r.kth = kth_radix<K>(c, kk);
+        if (!sample_round<K>(cur, n, kk, oth, cap_rows, lane, nxt, b2)) {
+            r.kth = kth_radix<K>(cur, kk);
             __syncwarp();
             return r;
         }
         kk -= b2;
-        n = n2;
-        K* t = cur;
-        cur = oth;
-        oth = t;
-        const int tc = cur_cap;
-        cur_cap = oth_cap;
-        oth_cap = tc;
+        n = __reduce_add_sync(kFull, nxt.t);
+        oth = cur.buf;
+        cur = nxt;
     }
     if (n > 64) {
-        const PtrKeys<K> c{cur, n, lane};
-        r.kth = kth_radix<K>(c, kk);
-    } else {
-        r = n <= 32 ? sel32<K>(cur, n, kk, lane) : sel64<K>(cur, n, kk, lane);
+        r.kth = kth_radix<K>(cur, kk);
+        __syncwarp();
+        return r;
     }
+    // gather the ragged candidates into oth[0 .. n)
+    uint32_t incl = cur.t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const uint32_t first = incl - cur.t;
+    for (uint32_t q = 0; q < cur.t; ++q) oth[first + q] = cur.buf[q * 32 + lane];
+    __syncwarp();
+    r = n <= 32 ? sel32<K>(oth, n, kk, lane) : sel64<K>(oth, n, kk, lane);
     __syncwarp();  // the candidate buffers are reused by the next selection
     return r;
 }
 
-// Order statistic k (and usually k-1) of a key source, exact.  Short
-// segments are staged and sorted; longer ones go through a first sampling
-// round (32 samples sorted in the warp, the keys within 6 sample ranks of
-// the target kept) and then select_candidates.
+// Order statistic k (and usually k-1) of a key source of M keys, exact.
+// Short segments are staged and sorted; longer ones go through a first
+// sampling round into buffer a, then select_candidates.
 template <typename K, class Src>
-__device__ Sel<K> kth_select(const Src& v, uint32_t k, K* cand, int cap1, K* cand2, int cap2, int lane) {
-    const uint32_t M = v.size();
+__device__ Sel<K> kth_select(const Src& v, uint32_t M, uint32_t k, K* a, K* b, uint32_t cap_rows, int lane) {
     if (M <= 64) {
-        uint32_t t = 0;
-        v.each_all([&](K x, bool valid) {
-            if (valid) cand[t * 32 + lane] = x;
-            ++t;
-        });
+        const uint32_t nr = v.rows();
+#pragma unroll
+        for (uint32_t r = 0; r < nr; ++r) {
+            const uint32_t i = r * 32 + lane;
+            if (i < M) a[i] = v.get(r);
+        }
         __syncwarp();
-        return select_candidates<K>(cand, cap1, cand2, cap2, M, k, lane);
+        const Sel<K> r = M <= 32 ? sel32<K>(a, M, k, lane) : sel64<K>(a, M, k, lane);
+        __syncwarp();
+        return r;
     }
-    uint32_t b;
-    const uint32_t n = window_round<K>(v, k, cand, cap1, &b, lane);
-    if (!(b <= k && k < b + n && n <= static_cast<uint32_t>(cap1))) {
+    Ragged<K> cur;
+    uint32_t b1;
+    if (!sample_round<K>(v, M, k, a, cap_rows, lane, cur, b1)) {
         Sel<K> r;
         r.have_prev = false;
         r.kth = kth_radix<K>(v, k);
         __syncwarp();
         return r;
     }
-    return select_candidates<K>(cand, cap1, cand2, cap2, n, k - b, lane);
+    return select_candidates<K>(a, b, cap_rows, cur.t, cur.nrows, __reduce_add_sync(kFull, cur.t), k - b1, lane);
 }
 
 struct CandBufs {
-    void* c1;
-    void* c2;
-    int cap1, cap2;
+    void* a;
+    void* b;
+    uint32_t rows;
 };
 
 // the voxel's new value from its keys (median or percentile mean)
 template <typename Real, class Src>
 __device__ Real order_update(const Src& src, uint32_t M, int mode, int pct, const CandBufs& cb, int lane) {
     using K = typename KeyOf<Real>::type;
-    K* cand = static_cast<K*>(cb.c1);
-    K* cand2 = static_cast<K*>(cb.c2);
+    K* ba = static_cast<K*>(cb.a);
+    K* bb = static_cast<K*>(cb.b);
     if (mode == kVoxMedian) {  // src/MutoMLSD.cpp:506-516
-        const Sel<K> s = kth_select<K>(src, M / 2, cand, cb.cap1, cand2, cb.cap2, lane);
+        const Sel<K> s = kth_select<K>(src, M, M / 2, ba, bb, cb.rows, lane);
         const Real v1 = from_key(s.kth);
         if (M % 2 == 0) {  // s_(M/2-1): from the sorted candidates, else v1 itself or the largest key below it
             Real v0;
@@ -359,7 +407,7 @@ __device__ Real order_update(const Src& src, uint32_t M, int mode, int pct, cons
     uint32_t jm = u32_cast_x86(pct / 100.0 * M);
     if (jm < 1) jm = 1;
     if (jm > M) jm = M;
-    const K kt = kth_select<K>(src, jm - 1, cand, cb.cap1, cand2, cb.cap2, lane).kth;
+    const K kt = kth_select<K>(src, M, jm - 1, ba, bb, cb.rows, lane).kth;
     const Real t = from_key(kt);
     Real s = 0;
     uint32_t c = 0;
@@ -386,6 +434,7 @@ __device__ __forceinline__ Real pair_g(const typename Vec4<Real>::type& k, Real 
 template <typename Real, int R, typename OutT>
 __device__ __forceinline__ void voxel_regs(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uint64_t base, uint32_t M,
                                            int lane, const CandBufs& cb) {
+    using K = typename KeyOf<Real>::type;
     using R2 = typename Vec2<Real>::type;
     const Real lam = a.lam[j];
     const bool keys = a.mode == kVoxMedian || a.mode == kVoxPercentile;
@@ -410,7 +459,7 @@ __device__ __forceinline__ void voxel_regs(const VoxelPassArgs<Real, OutT>& a, u
         for (int u = 0; u < C; ++u) {
             if (r0 + u >= R) break;
             const uint32_t e = static_cast<uint32_t>((r0 + u) * 32 + lane);
-            v.key[r0 + u] = 0;
+            v.key[r0 + u] = empty_key<K>();
             if (e < M) {
                 const Real g = pair_g<Real>(ldg4(a.kvec + mu[u]), lt[u].x, lt[u].y);
                 if (keys) v.key[r0 + u] = to_key(Real(2) * lam + g * lam * lam);
@@ -466,68 +515,198 @@ __device__ void voxel_stream(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uin
     if (lane == 0) a.out[j] = static_cast<OutT>(out);
 }
 
-template <typename Real, typename OutT, int CLS>
-__device__ __forceinline__ void voxel_one(const VoxelPassArgs<Real, OutT>& a, const VoxDesc& d, int lane,
-                                          const CandBufs& cb) {
-    const uint32_t j = d.j, M = d.M;
-    if (M == 0) {  // no muon crossed the voxel, src/MutoMLSD.cpp:494-496
-        if (lane == 0) {
-            if (a.mode == kVoxGradient) a.grad[j] = 0.0;
-            else a.out[j] = OutT(0);
-        }
-        return;
-    }
-    const uint64_t base = d.start;
-    if constexpr (CLS == 0) {
-        if (M <= 32u) voxel_regs<Real, 1>(a, j, base, M, lane, cb);
-        else if (M <= 64u) voxel_regs<Real, 2>(a, j, base, M, lane, cb);
-        else if (M <= 128u) voxel_regs<Real, 4>(a, j, base, M, lane, cb);
-        else if (M <= 192u) voxel_regs<Real, 6>(a, j, base, M, lane, cb);
-        else voxel_regs<Real, 8>(a, j, base, M, lane, cb);
-    } else if constexpr (CLS == 1) {
-        if (M <= 384u) voxel_regs<Real, 12>(a, j, base, M, lane, cb);
-        else if (M <= 512u) voxel_regs<Real, 16>(a, j, base, M, lane, cb);
-        else voxel_regs<Real, 24>(a, j, base, M, lane, cb);
-    } else {
-        if constexpr (voxel_register_cap<Real>() > 768u) {  // 64-bit keys stay at 24 registers per lane
-            if (M <= 1024u) {
-                voxel_regs<Real, 32>(a, j, base, M, lane, cb);
-                return;
-            }
-            if (M <= 1536u) {
-                voxel_regs<Real, 48>(a, j, base, M, lane, cb);
-                return;
+// The keys of a voxel's pairs recomputed from the lists, C rows of 32 at a
+// time; f(key, element) is called for each element below M.
+template <typename Real, int C, typename OutT, class F>
+__device__ __forceinline__ void for_each_key(const VoxelPassArgs<Real, OutT>& a, uint64_t base, uint32_t M, Real lam,
+                                             int lane, F f) {
+    using R2 = typename Vec2<Real>::type;
+    for (uint32_t r0 = 0; r0 * 32 < M; r0 += C) {
+        uint32_t mu[C];
+        R2 lt[C];
+#pragma unroll
+        for (int u = 0; u < C; ++u) {
+            const uint32_t e = (r0 + u) * 32 + lane;
+            if (e < M) {
+                mu[u] = __ldcs(a.vm_mu + base + e);
+                lt[u] = __ldcs(a.vm_LT + base + e);
             }
         }
-        voxel_stream<Real, OutT>(a, j, base, M, lane, cb);
+#pragma unroll
+        for (int u = 0; u < C; ++u) {
+            const uint32_t e = (r0 + u) * 32 + lane;
+            if (e < M) {
+                const Real g = pair_g<Real>(ldg4(a.kvec + mu[u]), lt[u].x, lt[u].y);
+                f(to_key(Real(2) * lam + g * lam * lam), e);
+            }
+        }
     }
 }
 
-// Voxels of class CLS (0: M <= 256, 1: M <= 768, 2: longer), one warp per
-// voxel.  Each warp also prefetches into L2 the pair lists of the voxel
-// `ahead` places further down the class list, which a warp of the next wave
-// of resident blocks will read.
-template <typename Real, typename OutT, int CLS>
-__global__ void __launch_bounds__(kVoxThreads)
+// Segments selected without holding their keys: the first 32 keys are
+// sorted as samples, then one pass over the lists recomputes every key,
+// counts those below the window and appends those inside it to the warp's
+// ragged candidate buffer.  Rounds on the candidates follow
+// (select_candidates).  A window that misses, overflows the buffer or keeps
+// everything sends the segment to the scratch array (keys written once,
+// selected there).  Registers then hold only the loads in flight, whatever
+// the segment length.
+template <typename Real, typename OutT>
+__device__ void voxel_streamed(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uint64_t base, uint32_t M, int lane,
+                               const CandBufs& cb) {
+    using K = typename KeyOf<Real>::type;
+    using R2 = typename Vec2<Real>::type;
+    constexpr int C = 8;
+    const Real lam = a.lam[j];
+    if (a.mode == kVoxMean || a.mode == kVoxGradient) {
+        Real gs = 0;
+        for (uint32_t i = lane; i < M; i += 32) {
+            const R2 lt = __ldcs(a.vm_LT + base + i);
+            gs += pair_g<Real>(ldg4(a.kvec + __ldcs(a.vm_mu + base + i)), lt.x, lt.y);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) gs += __shfl_xor_sync(kFull, gs, o);
+        if (a.mode == kVoxGradient) {
+            if (lane == 0) a.grad[j] = -a.lam64[j] * static_cast<double>(gs);
+        } else if (lane == 0) {
+            a.out[j] = static_cast<OutT>(lam + lam * lam * gs / (Real(2) * static_cast<Real>(M)));
+        }
+        return;
+    }
+    // rank of the wanted order statistic (src/MutoMLSD.cpp:500-516)
+    uint32_t k, jm = 0;
+    if (a.mode == kVoxMedian) {
+        k = M / 2;
+    } else {
+        jm = u32_cast_x86(a.pct / 100.0 * M);
+        if (jm < 1) jm = 1;
+        if (jm > M) jm = M;
+        k = jm - 1;
+    }
+    K* ba = static_cast<K*>(cb.a);
+    K* bb = static_cast<K*>(cb.b);
+    Sel<K> sel;
+    bool done = false;
+    {
+        // samples: the segment's first 32 keys (M > 64: all present)
+        const R2 lt0 = __ldcs(a.vm_LT + base + lane);
+        const Real g0 = pair_g<Real>(ldg4(a.kvec + __ldcs(a.vm_mu + base + lane)), lt0.x, lt0.y);
+        const K s = sort32(to_key(Real(2) * lam + g0 * lam * lam), lane);
+        const int pos = static_cast<int>((static_cast<float>(k) * 32.0f) / static_cast<float>(M));
+        const int ql = pos - 6, qh = pos + 6;
+        const K slo = __shfl_sync(kFull, s, ql < 0 ? 0 : (ql > 31 ? 31 : ql));
+        const K shi = __shfl_sync(kFull, s, qh > 31 ? 31 : (qh < 0 ? 0 : qh));
+        const K lo = ql <= 0 ? K(0) : slo;
+        const K hi = qh >= 31 ? empty_key<K>() - 1 : shi;
+        uint32_t c_lo = 0, t = 0;
+        const uint32_t cap = cb.rows;
+        for_each_key<Real, C>(a, base, M, lam, lane, [&](K x, uint32_t) {
+            if (x < lo) {
+                ++c_lo;
+            } else if (x <= hi) {
+                if (t < cap) ba[t * 32 + lane] = x;
+                ++t;
+            }
+        });
+        const uint32_t below = __reduce_add_sync(kFull, c_lo);
+        const uint32_t n_in = __reduce_add_sync(kFull, t);
+        const uint32_t rows = __reduce_max_sync(kFull, t);
+        __syncwarp();
+        if (rows <= cap && below <= k && k < below + n_in && n_in < M) {
+            sel = select_candidates<K>(ba, bb, cap, t, rows, n_in, k - below, lane);
+            done = true;
+        }
+    }
+    if (!done) {  // the scratch array, at the segment's own offsets
+        K* kp = a.scratch + base;
+        for_each_key<Real, C>(a, base, M, lam, lane, [&](K x, uint32_t e) { kp[e] = x; });
+        __syncwarp();
+        const PtrKeys<K> src{kp, M, lane};
+        sel = kth_select<K>(src, M, k, ba, bb, cb.rows, lane);
+    }
+    Real out;
+    if (a.mode == kVoxMedian) {
+        const Real v1 = from_key(sel.kth);
+        if (M % 2 == 0) {
+            Real v0;
+            if (sel.have_prev) {
+                v0 = from_key(sel.prev);
+            } else {  // v1 itself or the largest key below it
+                uint32_t c = 0;
+                K mb = K(0);
+                for_each_key<Real, C>(a, base, M, lam, lane, [&](K x, uint32_t) {
+                    if (x < sel.kth) {
+                        ++c;
+                        mb = x > mb ? x : mb;
+                    }
+                });
+                c = __reduce_add_sync(kFull, c);
+                mb = warp_max_k(mb);
+                v0 = c < M / 2 ? v1 : from_key(mb);
+            }
+            out = (v1 + v0) * Real(0.25);
+        } else {
+            out = v1 * Real(0.5);
+        }
+    } else {  // mean of the lowest jm values
+        const Real tk = from_key(sel.kth);
+        Real sum = 0;
+        uint32_t c = 0;
+        for_each_key<Real, C>(a, base, M, lam, lane, [&](K x, uint32_t) {
+            if (x < sel.kth) {
+                sum += from_key(x);
+                ++c;
+            }
+        });
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+        c = __reduce_add_sync(kFull, c);
+        sum += static_cast<Real>(jm - c) * tk;
+        out = sum / static_cast<Real>(jm) * Real(0.5);
+    }
+    if (lane == 0) a.out[j] = static_cast<OutT>(out);
+}
+
+// Voxels of class C, one warp per voxel: registers hold vox_class_rows(C)
+// keys per lane (the last class selects from the scratch array).  Each warp
+// also prefetches into L2 the pair lists of the voxel `ahead` places further
+// down the class list, which a warp of the next wave of resident blocks will
+// read.  Dynamic shared memory: two candidate buffers per warp.
+template <typename Real, typename OutT, int C, bool STREAMED>
+__global__ void __launch_bounds__(kVoxThreads, vox_min_blocks(C, STREAMED))
     k_em_voxel(VoxelPassArgs<Real, OutT> a, const VoxDesc* __restrict__ desc, uint32_t n, uint32_t ahead) {
     using K = typename KeyOf<Real>::type;
     using R2 = typename Vec2<Real>::type;
-    constexpr int C1 = CandCap<K, CLS>::c1, C2 = CandCap<K, CLS>::c2;
-    __shared__ K cand_all[kWarps][C1];
-    __shared__ K cand2_all[kWarps][C2];
-    const int lane = threadIdx.x & 31;
-    const CandBufs cb{cand_all[threadIdx.x >> 5], cand2_all[threadIdx.x >> 5], C1, C2};
-    const uint64_t w = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (w >= n) return;  // whole warps leave together
-    const VoxDesc d = desc[w];
-    if (lane == 0 && w + ahead < n) {
-        const VoxDesc f = desc[w + ahead];
-        if (f.M > 0) {
-            prefetch_l2(a.vm_mu + f.start, size_t(f.M) * sizeof(uint32_t));
-            prefetch_l2(a.vm_LT + f.start, size_t(f.M) * sizeof(R2));
+    constexpr int R = vox_class_rows(C);
+    constexpr int RB = cand_rows<K, C, STREAMED>();
+    if constexpr (R * 32 > static_cast<int>(voxel_register_cap<Real>()) || (STREAMED && !streamable(C))) {
+        return;  // no voxel of this precision is put in the class
+    } else {
+        extern __shared__ __align__(16) unsigned char vox_smem[];
+        const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+        K* bufs = reinterpret_cast<K*>(vox_smem);
+        const CandBufs cb{bufs + (2 * wib) * RB * 32, bufs + (2 * wib + 1) * RB * 32, static_cast<uint32_t>(RB)};
+        const uint64_t w = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+        if (w >= n) return;  // whole warps leave together
+        const VoxDesc d = desc[w];
+        if (lane == 0 && w + ahead < n) {
+            const VoxDesc f = desc[w + ahead];
+            if (f.M > 0) {
+                prefetch_l2(a.vm_mu + f.start, size_t(f.M) * sizeof(uint32_t));
+                prefetch_l2(a.vm_LT + f.start, size_t(f.M) * sizeof(R2));
+            }
         }
+        if (d.M == 0) {  // no muon crossed the voxel, src/MutoMLSD.cpp:494-496
+            if (lane == 0) {
+                if (a.mode == kVoxGradient) a.grad[d.j] = 0.0;
+                else a.out[d.j] = OutT(0);
+            }
+            return;
+        }
+        if constexpr (STREAMED) voxel_streamed<Real, OutT>(a, d.j, d.start, d.M, lane, cb);
+        else if constexpr (R > 0) voxel_regs<Real, R>(a, d.j, d.start, d.M, lane, cb);
+        else voxel_stream<Real, OutT>(a, d.j, d.start, d.M, lane, cb);
     }
-    voxel_one<Real, OutT, CLS>(a, d, lane, cb);
 }
 
 __global__ void k_finalize_cost(Counters* ctr, double n_muons, double* hist, uint32_t cap) {
@@ -679,19 +858,50 @@ inline unsigned blocks_for(uint64_t n, int threads) {
 
 }  // namespace
 
-template <typename Real, typename OutT, int CLS>
+template <typename Real, typename OutT, int C, bool STREAMED>
 int voxel_blocks_per_sm() {
+    using K = typename KeyOf<Real>::type;
+    constexpr size_t smem = voxel_smem_bytes<K, C, STREAMED>();
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_em_voxel<Real, OutT, CLS>, kVoxThreads, 0) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_em_voxel<Real, OutT, C, STREAMED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem)) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_em_voxel<Real, OutT, C, STREAMED>, kVoxThreads, smem) !=
+            cudaSuccess)
         nb = 0;
     return nb > 0 ? nb : 1;
 }
 
+template <typename Real, typename OutT, int... C>
+void occupancy_all(int* regs, int* streamed, std::integer_sequence<int, C...>) {
+    ((regs[C] = voxel_blocks_per_sm<Real, OutT, C, false>()), ...);
+    ((streamed[C] = streamable(C) ? voxel_blocks_per_sm<Real, OutT, C, true>() : 0), ...);
+}
+
+template <typename Real, typename OutT, int... C>
+void launch_all(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists, const uint32_t* counts,
+                const int* resident_blocks, uint32_t streamed, cudaStream_t s, std::integer_sequence<int, C...>) {
+    using K = typename KeyOf<Real>::type;
+    auto one = [&](auto cc) {
+        constexpr int c = decltype(cc)::value;
+        if (counts[c] == 0) return;
+        const bool st = streamable(c) && ((streamed >> c) & 1u);
+        const unsigned nb = blocks_for(static_cast<uint64_t>(counts[c]) * 32u, kVoxThreads);
+        const uint32_t ahead = static_cast<uint32_t>(resident_blocks[st ? kVoxClasses + c : c]) * kWarps;
+        if (st)
+            k_em_voxel<Real, OutT, c, true>
+                <<<nb, kVoxThreads, voxel_smem_bytes<K, c, true>(), s>>>(a, lists[c], counts[c], ahead);
+        else
+            k_em_voxel<Real, OutT, c, false>
+                <<<nb, kVoxThreads, voxel_smem_bytes<K, c, false>(), s>>>(a, lists[c], counts[c], ahead);
+        count_launches(1);
+    };
+    (one(std::integral_constant<int, C>{}), ...);
+}
+
 template <typename Real, typename OutT>
-void em_voxel_occupancy(int blocks_per_sm[3]) {
-    blocks_per_sm[0] = voxel_blocks_per_sm<Real, OutT, 0>();
-    blocks_per_sm[1] = voxel_blocks_per_sm<Real, OutT, 1>();
-    blocks_per_sm[2] = voxel_blocks_per_sm<Real, OutT, 2>();
+void em_voxel_occupancy(int blocks_per_sm[2 * kVoxClasses]) {
+    occupancy_all<Real, OutT>(blocks_per_sm, blocks_per_sm + kVoxClasses,
+                              std::make_integer_sequence<int, kVoxClasses>{});
 }
 template void em_voxel_occupancy<float, float>(int*);
 template void em_voxel_occupancy<float, double>(int*);
@@ -699,23 +909,16 @@ template void em_voxel_occupancy<double, double>(int*);
 
 template <typename Real, typename OutT>
 void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists, const uint32_t* counts,
-                     const int* resident_blocks, cudaStream_t s) {
-    for (int c = 0; c < 3; ++c) {
-        if (counts[c] == 0) continue;
-        const unsigned nb = blocks_for(static_cast<uint64_t>(counts[c]) * 32u, kVoxThreads);
-        const uint32_t ahead = static_cast<uint32_t>(resident_blocks[c]) * kWarps;  // warps of one wave
-        if (c == 0) k_em_voxel<Real, OutT, 0><<<nb, kVoxThreads, 0, s>>>(a, lists[c], counts[c], ahead);
-        else if (c == 1) k_em_voxel<Real, OutT, 1><<<nb, kVoxThreads, 0, s>>>(a, lists[c], counts[c], ahead);
-        else k_em_voxel<Real, OutT, 2><<<nb, kVoxThreads, 0, s>>>(a, lists[c], counts[c], ahead);
-        count_launches(1);
-    }
+                     const int* resident_blocks, uint32_t streamed, cudaStream_t s) {
+    launch_all<Real, OutT>(a, lists, counts, resident_blocks, streamed, s,
+                           std::make_integer_sequence<int, kVoxClasses>{});
 }
 template void launch_em_voxel<float, float>(const VoxelPassArgs<float, float>&, const VoxDesc* const*,
-                                            const uint32_t*, const int*, cudaStream_t);
+                                            const uint32_t*, const int*, uint32_t, cudaStream_t);
 template void launch_em_voxel<float, double>(const VoxelPassArgs<float, double>&, const VoxDesc* const*,
-                                             const uint32_t*, const int*, cudaStream_t);
+                                             const uint32_t*, const int*, uint32_t, cudaStream_t);
 template void launch_em_voxel<double, double>(const VoxelPassArgs<double, double>&, const VoxDesc* const*,
-                                              const uint32_t*, const int*, cudaStream_t);
+                                              const uint32_t*, const int*, uint32_t, cudaStream_t);
 
 void launch_finalize_cost(Counters* ctr, double n_muons, double* hist, uint32_t cap, cudaStream_t s) {
     k_finalize_cost<<<1, 1, 0, s>>>(ctr, n_muons, hist, cap);

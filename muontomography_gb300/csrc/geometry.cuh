@@ -48,6 +48,12 @@ __device__ __forceinline__ double dot3(const double* a, const double* b) {
     return dadd(dadd(dmul(a[0], b[0]), dmul(a[1], b[1])), dmul(a[2], b[2]));
 }
 
+// Order of doubles through their bit patterns: for two values whose sign
+// bits are clear (non-negative, and not -0.0) the signed 64-bit integers
+// order exactly as the doubles do, so the walk's comparisons can run on the
+// integer pipe; it falls back to FP64 compares when a sign bit is set.
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+
 // Upper bound on the steps of one walk: every step crosses one plane of the
 // grid, and a segment crosses each of the n+1 planes of an axis at most once.
 __device__ __forceinline__ int siddon_step_bound(const DevGrid& g) {
@@ -110,15 +116,29 @@ __device__ __forceinline__ int siddon_walk(const DevGrid& g, const double* p1, c
     int count = 0;
     const int bound = siddon_step_bound(g);
     int steps = 0;
-    while (alpha < amax) {  // :108-138
+    // integer compares need finite values (then every later crossing is finite too)
+    const bool fast = isfinite(alpha) && isfinite(amax) && isfinite(an[0]) && isfinite(an[1]) && isfinite(an[2]);
+    const long long amax_b = fast ? dbits(amax) : -1, eps_b = dbits(eps);
+    for (;;) {  // :108-138
+        const long long alpha_b = fast ? dbits(alpha) : -1;
+        if (!((alpha_b | amax_b) >= 0 ? alpha_b < amax_b : alpha < amax)) break;
         if (++steps > bound) return -1;
         const uint32_t vx = idx[0], vy = idx[1], vz = idx[2];
         // min of the three next crossings, reference tie-break order
-        if (an[0] < an[1] && an[0] < an[2]) {
+        const long long b0 = fast ? dbits(an[0]) : -1, b1 = dbits(an[1]), b2 = dbits(an[2]);
+        bool t0, t1;
+        if ((b0 | b1 | b2) >= 0) {
+            t0 = b0 < b1 && b0 < b2;
+            t1 = b1 < b2;
+        } else {
+            t0 = an[0] < an[1] && an[0] < an[2];
+            t1 = an[1] < an[2];
+        }
+        if (t0) {
             idx[0] += static_cast<uint32_t>(dir[0]);
             alpha = an[0];
             an[0] = dadd(an[0], da[0]);
-        } else if (an[1] < an[2]) {
+        } else if (t1) {
             idx[1] += static_cast<uint32_t>(dir[1]);
             alpha = an[1];
             an[1] = dadd(an[1], da[1]);
@@ -127,8 +147,10 @@ __device__ __forceinline__ int siddon_walk(const DevGrid& g, const double* p1, c
             alpha = an[2];
             an[2] = dadd(an[2], da[2]);
         }
-        const double dalpha = dsub(smin(alpha, amax), alpha_last);
-        if (eps < dalpha) {
+        const long long ab = dbits(alpha);
+        const double upto = (ab | amax_b) >= 0 ? (amax_b < ab ? amax : alpha) : smin(alpha, amax);
+        const double dalpha = dsub(upto, alpha_last);
+        if (fast ? eps_b < dbits(dalpha) : eps < dalpha) {  // eps is positive
             sink(vx, vy, vz, dmul(dalpha, seg));
             ++count;
             alpha_last = alpha;

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -104,6 +105,7 @@ struct Params {
     int newton_max_iter = 200;
     int tile_pairs = 0;
     int muon_pass = 0;  // 0 autotune, 1 tile (TMA), 2 warp-batched
+    long long voxel_stream_above = 512;  // segments longer than this are selected without registers
 };
 
 Params parse_params(Method m, const std::string& text) {
@@ -181,6 +183,7 @@ Params parse_params(Method m, const std::string& text) {
         else if (mp == "tile") P.muon_pass = 1;
         else if (mp == "warp") P.muon_pass = 2;
         else throw Error(MUTO_ERR_CONFIG, "muon_pass must be \"auto\", \"tile\" or \"warp\"");
+        P.voxel_stream_above = cfg.value("voxel_stream_above", static_cast<int64_t>(512));
         if (P.newton_max_iter < 1) throw Error(MUTO_ERR_CONFIG, "newton_max_iter must be >= 1");
     } catch (const json::type_error& e) {
         throw Error(MUTO_ERR_CONFIG, std::string("config value of the wrong type: ") + e.what());
@@ -283,9 +286,10 @@ struct muto_handle {
     DevMem vidx, L, T;            // muon-major pair lists
     DevMem vm_mu, vm_LT;          // voxel-major copy (muon, (L, T))
     DevMem vclass;                // VoxDesc of every voxel, by segment-length class
-    uint32_t vclass_n[3] = {0, 0, 0};
-    int vox_blocks_real[3] = {1, 1, 1}, vox_blocks_f64[3] = {1, 1, 1};  // grid caps of the class kernels
-    uint64_t vclass_off[3] = {0, 0, 0};
+    uint32_t vclass_n[kVoxClasses] = {};
+    int vox_blocks_real[2 * kVoxClasses] = {}, vox_blocks_f64[2 * kVoxClasses] = {};  // resident blocks per class kernel
+    uint32_t vox_streamed = 0;  // classes selected by the streamed path
+    uint64_t vclass_off[kVoxClasses] = {};
     DevMem mult, start, kvec, keys;   // keys: scratch for voxels beyond the register budget
     DevMem lam, lam_ml, cost_hist;
     DevMem tiles;
@@ -360,6 +364,23 @@ void run(muto_handle* h, const char* name, F&& f) {
     if (!h->capturing) h->launches += launches_so_far() - before;
     CK(cudaGetLastError());
 }
+
+// wall time of a host-side set-up phase (including the device waits inside
+// it), kept with the kernel statistics under "host:<phase>" when profiling
+struct HostPhase {
+    muto_handle* h;
+    const char* name;
+    std::chrono::steady_clock::time_point t0;
+    HostPhase(muto_handle* hh, const char* n) : h(hh), name(n), t0(std::chrono::steady_clock::now()) {}
+    ~HostPhase() {
+        if (!h->prof.on) return;
+        const double ms =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        auto& st = h->prof.stats[std::string("host:") + name];
+        st.first += 1;
+        st.second += ms;
+    }
+};
 
 void sync_and_harvest(muto_handle* h, size_t first) {
     CK(cudaStreamSynchronize(h->stream));
@@ -476,6 +497,7 @@ void prepare_em(muto_handle* h) {
     // (the flags are computed again in the second loop; the flag buffer is shared)
     DevMem flags, scratch;
     std::vector<std::unique_ptr<DevMem>> pos(S);
+    std::unique_ptr<HostPhase> ph(new HostPhase(h, "gather"));
     flags.alloc(std::max<uint64_t>(nt_max, 1) * sizeof(uint32_t), &h->dev_bytes);
     uint64_t N = 0;
     for (size_t k = 0; k < S; ++k) {
@@ -504,6 +526,7 @@ void prepare_em(muto_handle* h) {
     h->pr64.alloc(std::max<uint64_t>(N, 1) * sizeof(double), &h->dev_bytes);
     DevMem counts;
     counts.alloc(std::max<uint64_t>(N, 1) * sizeof(uint32_t), &h->dev_bytes);
+    ph.reset(new HostPhase(h, "info_count"));
     for (size_t k = 0; k < S; ++k) {
         const auto& sc = h->scans[k];
         const muto_ray* r = h->scan_rays(k);
@@ -525,15 +548,26 @@ void prepare_em(muto_handle* h) {
     pos.clear();
     if (scratch.bytes() < scan_scratch_bytes(std::max<uint64_t>(N, V) + 1))
         scratch.alloc(scan_scratch_bytes(std::max<uint64_t>(N, V) + 1), &h->dev_bytes);
+    ph.reset(new HostPhase(h, "offsets"));
     h->off.alloc((N + 1 + kPad) * sizeof(uint64_t), &h->dev_bytes);
     run(h, "scan", [&] { scan_u32_to_u64(counts.as<uint32_t>(), h->off.as<uint64_t>(), N, scratch.as<void>(), s); });
     counts.release();
-    std::vector<uint64_t> off_h(N + 1);
-    CK(cudaMemcpyAsync(off_h.data(), h->off.as<uint64_t>(), (N + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    // pair offsets on the host: each scan's first pair and the total, and
+    // every muon's for the tile schedule
+    std::vector<uint64_t> scan_off(S + 1), off_h;
+    for (size_t k = 0; k < S; ++k)
+        CK(cudaMemcpyAsync(&scan_off[k], h->off.as<uint64_t>() + h->scans[k].noff, sizeof(uint64_t),
+                           cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&scan_off[S], h->off.as<uint64_t>() + N, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    if (P.muon_pass == 1) {
+        off_h.resize(N + 1);
+        CK(cudaMemcpyAsync(off_h.data(), h->off.as<uint64_t>(), (N + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    }
     CK(cudaStreamSynchronize(s));
-    const uint64_t Pn = off_h[N];
+    const uint64_t Pn = scan_off[S];
     h->npairs = Pn;
 
+    ph.reset(new HostPhase(h, "fill"));
     h->vidx.alloc((Pn + kPad) * sizeof(uint32_t), &h->dev_bytes);
     h->L.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
     h->T.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
@@ -554,7 +588,7 @@ void prepare_em(muto_handle* h) {
             });
             // scan-local voxel indices into the batch's voxel space
             if (h->batch) {
-                const uint64_t pb = off_h[sc.noff], pe = off_h[sc.noff + sc.N];
+                const uint64_t pb = scan_off[k], pe = scan_off[k + 1];
                 run(h, "voxel_offset", [&] {
                     launch_offset_voxels(h->vidx.as<uint32_t>() + pb, pe - pb, static_cast<uint32_t>(sc.V),
                                          static_cast<uint32_t>(sc.voff), s);
@@ -565,6 +599,7 @@ void prepare_em(muto_handle* h) {
     }
 
     // --- multiplicity M_j and the voxel-major copy of the lists ---------------
+    ph.reset(new HostPhase(h, "voxel_major"));
     h->mult.alloc(V * sizeof(uint32_t), &h->dev_bytes);
     CK(cudaMemsetAsync(h->mult.as<void>(), 0, V * sizeof(uint32_t), s));
     run(h, "voxel_hist", [&] { launch_voxel_hist(h->vidx.as<uint32_t>(), Pn, static_cast<uint32_t>(V), h->mult.as<uint32_t>(), h->ctr(), s); });
@@ -586,70 +621,86 @@ void prepare_em(muto_handle* h) {
     }
     scratch.release();
     h->kvec.alloc((N + kPad) * sizeof(R4), &h->dev_bytes);
-    {  // voxels with more pairs than the register budget select from a scratch key array
-        std::vector<uint32_t> m_h(V);
-        CK(cudaMemcpy(m_h.data(), h->mult.as<void>(), V * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-        const uint32_t mmax = V ? *std::max_element(m_h.begin(), m_h.end()) : 0u;
-        if (mmax > voxel_register_cap<Real>())
-            h->keys.alloc(std::max<uint64_t>(Pn, 1) * sizeof(typename KeyOf<Real>::type), &h->dev_bytes);
-        // voxel classes by segment length, one voxel-pass kernel each; a
-        // descriptor carries the voxel, its pair count and its first pair
-        // (the exclusive sum of the counts, as the device scan has it)
-        std::vector<VoxDesc> cls[3];
-        uint64_t first = 0;
-        for (uint64_t j = 0; j < V; ++j) {
-            const uint32_t m = m_h[j];
-            cls[m <= 256u ? 0 : (m <= 768u ? 1 : 2)].push_back(VoxDesc{static_cast<uint32_t>(j), m, first});
-            first += m;
-        }
-        if (first != Pn) throw Error(MUTO_ERR_STATE, "voxel multiplicities do not add up to the pair count");
+    ph.reset(new HostPhase(h, "classes"));
+    {
+        // voxel classes by segment length, one voxel-pass kernel each, built on
+        // the device; a descriptor carries the voxel, its pair count and its
+        // first voxel-major pair
+        const uint32_t nb = voxel_class_blocks(V);
+        const uint64_t nc = static_cast<uint64_t>(nb) * kVoxClasses;
+        DevMem ccount, cfirst, cscr;
+        ccount.alloc(nc * sizeof(uint32_t), &h->dev_bytes);
+        cfirst.alloc((nc + 1) * sizeof(uint64_t), &h->dev_bytes);
+        cscr.alloc(scan_scratch_bytes(nc + 1), &h->dev_bytes);
         h->vclass.alloc(std::max<uint64_t>(V, 1) * sizeof(VoxDesc), &h->dev_bytes);
-        uint64_t at = 0;
-        for (int c = 0; c < 3; ++c) {
-            h->vclass_off[c] = at;
-            h->vclass_n[c] = static_cast<uint32_t>(cls[c].size());
-            if (!cls[c].empty())
-                CK(cudaMemcpy(h->vclass.as<VoxDesc>() + at, cls[c].data(), cls[c].size() * sizeof(VoxDesc),
-                              cudaMemcpyHostToDevice));
-            at += cls[c].size();
+        run(h, "voxel_classes", [&] {
+            launch_voxel_classes<Real>(h->mult.as<uint32_t>(), h->start.as<uint64_t>(), static_cast<uint32_t>(V),
+                                       ccount.as<uint32_t>(), cfirst.as<uint64_t>(), cscr.as<void>(),
+                                       h->vclass.as<VoxDesc>(), s);
+        });
+        uint64_t bnd[kVoxClasses + 1];
+        for (int c = 0; c <= kVoxClasses; ++c)
+            CK(cudaMemcpyAsync(&bnd[c], cfirst.as<uint64_t>() + static_cast<uint64_t>(c) * nb, sizeof(uint64_t),
+                               cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (bnd[kVoxClasses] != V) throw Error(MUTO_ERR_STATE, "voxel classes do not cover the voxels");
+        for (int c = 0; c < kVoxClasses; ++c) {
+            h->vclass_off[c] = bnd[c];
+            h->vclass_n[c] = static_cast<uint32_t>(bnd[c + 1] - bnd[c]);
         }
+        // segments beyond the register budget, and the fall-back of streamed
+        // ones, select from a scratch key array
+        h->vox_streamed = P.voxel_stream_above < 0 ? 0u
+                          : vox_streamed_mask(static_cast<uint32_t>(std::min<long long>(P.voxel_stream_above, 0xffffffffLL)));
+        bool need_keys = h->vclass_n[kVoxClasses - 1] > 0;
+        for (int c = 0; c < kVoxClasses; ++c)
+            if (((h->vox_streamed >> c) & 1u) && h->vclass_n[c] > 0) need_keys = true;
+        if (need_keys) h->keys.alloc(std::max<uint64_t>(Pn, 1) * sizeof(typename KeyOf<Real>::type), &h->dev_bytes);
         em_voxel_occupancy<Real, Real>(h->vox_blocks_real);
         em_voxel_occupancy<Real, double>(h->vox_blocks_f64);
-        for (int c = 0; c < 3; ++c) {
+        for (int c = 0; c < 2 * kVoxClasses; ++c) {
             h->vox_blocks_real[c] *= h->num_sms;
             h->vox_blocks_f64[c] *= h->num_sms;
         }
     }
 
     // --- tiles of consecutive muons fitting the shared-memory stage ----------
-    uint64_t maxpath = 0;
-    for (uint64_t i = 0; i < N; ++i) maxpath = std::max<uint64_t>(maxpath, off_h[i + 1] - off_h[i]);
-    int TP = P.tile_pairs > 0 ? P.tile_pairs : (std::is_same<Real, double>::value ? 1024 : 2048);
-    while (static_cast<uint64_t>(TP) < maxpath) TP *= 2;
-    const int TM = std::is_same<Real, double>::value ? 128 : 256;
-    if (em_muon_smem_bytes<Real>(TP, TM) > h->smem_optin)
-        throw Error(MUTO_ERR_CAPACITY, "longest muon path (" + std::to_string(maxpath) + " voxels) does not fit the shared-memory tile");
-    std::vector<uint32_t> tb;
-    tb.push_back(0);
-    uint64_t cs = 0;
-    for (uint64_t i = 0; i < N; ++i) {
-        if (off_h[i + 1] - off_h[cs] > static_cast<uint64_t>(TP) || i - cs >= static_cast<uint64_t>(TM)) {
-            tb.push_back(static_cast<uint32_t>(i));
-            cs = i;
-        }
-    }
-    if (N > 0) tb.push_back(static_cast<uint32_t>(N));
-    h->ntiles = static_cast<uint32_t>(tb.size() - 1);
-    h->tiles.alloc(tb.size() * sizeof(uint32_t), &h->dev_bytes);
-    CK(cudaMemcpyAsync(h->tiles.as<void>(), tb.data(), tb.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    h->tile_pairs = TP;
-    h->tile_muons = TM;
+    // (only for the TMA tile pass)
+    ph.reset(new HostPhase(h, "tiles"));
     const double avg = N > 0 ? static_cast<double>(Pn) / static_cast<double>(N) : 0.0;
     h->group = avg <= 32 ? 8 : (avg <= 64 ? 16 : 32);
-    CK(em_muon_configure<Real>(TP, TM));
-    h->tile_blocks = em_muon_blocks<Real>(TP, TM, h->group) * h->num_sms;
+    h->ntiles = 0;
+    h->tile_pairs = 0;
+    h->tile_muons = 0;
+    if (P.muon_pass == 1) {
+        uint64_t maxpath = 0;
+        for (uint64_t i = 0; i < N; ++i) maxpath = std::max<uint64_t>(maxpath, off_h[i + 1] - off_h[i]);
+        int TP = P.tile_pairs > 0 ? P.tile_pairs : (std::is_same<Real, double>::value ? 1024 : 2048);
+        while (static_cast<uint64_t>(TP) < maxpath) TP *= 2;
+        const int TM = std::is_same<Real, double>::value ? 128 : 256;
+        if (em_muon_smem_bytes<Real>(TP, TM) > h->smem_optin)
+            throw Error(MUTO_ERR_CAPACITY, "longest muon path (" + std::to_string(maxpath) + " voxels) does not fit the shared-memory tile");
+        std::vector<uint32_t> tb;
+        tb.push_back(0);
+        uint64_t cs = 0;
+        for (uint64_t i = 0; i < N; ++i) {
+            if (off_h[i + 1] - off_h[cs] > static_cast<uint64_t>(TP) || i - cs >= static_cast<uint64_t>(TM)) {
+                tb.push_back(static_cast<uint32_t>(i));
+                cs = i;
+            }
+        }
+        if (N > 0) tb.push_back(static_cast<uint32_t>(N));
+        h->ntiles = static_cast<uint32_t>(tb.size() - 1);
+        h->tiles.alloc(tb.size() * sizeof(uint32_t), &h->dev_bytes);
+        CK(cudaMemcpyAsync(h->tiles.as<void>(), tb.data(), tb.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        h->tile_pairs = TP;
+        h->tile_muons = TM;
+        CK(em_muon_configure<Real>(TP, TM));
+        h->tile_blocks = em_muon_blocks<Real>(TP, TM, h->group) * h->num_sms;
+    }
 
     // --- image ---------------------------------------------------------------
+    ph.reset(new HostPhase(h, "image"));
     h->lam.alloc(V * sizeof(Real), &h->dev_bytes);
     {
         std::vector<Real> init_r(init.begin(), init.end());
@@ -695,17 +746,23 @@ MuonPassArgs<Real> muon_args(muto_handle* h, const Real* lam, bool cost) {
 }
 
 // In-project autotuner: time the candidate muon-pass variants on this scan's
-// own lists (one warm-up and three timed launches each) and keep the fastest.
+// own lists (one warm-up and two timed launches each) and keep the fastest.
 template <typename Real>
 void autotune_muon_pass(muto_handle* h) {
     if (h->N == 0) return;
+    HostPhase ph(h, "autotune");
     struct Cand {
         int kind, group;
     };
     std::vector<Cand> cands;
-    if (h->P.muon_pass != 2) cands.push_back({1, h->group});
-    if (h->P.muon_pass != 1)
-        for (int g : {8, 16, 32}) cands.push_back({2, g});
+    // "auto": the warp-batched pass at the group size the mean path length
+    // suggests and its neighbour (the TMA tile pass, slower on every workload
+    // measured, runs only when asked for)
+    if (h->P.muon_pass == 1) cands.push_back({1, h->group});
+    if (h->P.muon_pass != 1) {
+        cands.push_back({2, h->group});
+        cands.push_back({2, h->group == 32 ? 16 : h->group * 2});
+    }
     auto apply = [&](const Cand& c) {
         h->muon_kind = c.kind;
         h->muon_group = c.group;
@@ -729,13 +786,13 @@ void autotune_muon_pass(muto_handle* h) {
         apply(cands[i]);
         launch_muon_pass<Real>(h, a, s);
         CK(cudaEventRecord(e0, s));
-        for (int r = 0; r < 3; ++r) launch_muon_pass<Real>(h, a, s);
+        for (int r = 0; r < 2; ++r) launch_muon_pass<Real>(h, a, s);
         CK(cudaEventRecord(e1, s));
         CK(cudaEventSynchronize(e1));
         CK(cudaGetLastError());
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, e0, e1));
-        ms /= 3.f;
+        ms /= 2.f;
         if (i < 4) h->tune_ms[i] = ms;
         if (ms < best) {
             best = ms;
@@ -744,7 +801,7 @@ void autotune_muon_pass(muto_handle* h) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    h->launches += 4 * cands.size();
+    h->launches += 3 * cands.size();
     apply(pick);
     CK(cudaMemcpyAsync(h->ctr(), &saved, sizeof(Counters), cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
@@ -772,10 +829,11 @@ VoxelPassArgs<Real, OutT> voxel_args(muto_handle* h, const Real* lam, int mode, 
 
 template <typename Real, typename OutT>
 void launch_voxel_pass(muto_handle* h, const VoxelPassArgs<Real, OutT>& v, cudaStream_t s) {
-    const VoxDesc* lists[3];
-    for (int c = 0; c < 3; ++c) lists[c] = h->vclass.as<VoxDesc>() + h->vclass_off[c];
+    const VoxDesc* lists[kVoxClasses];
+    for (int c = 0; c < kVoxClasses; ++c) lists[c] = h->vclass.as<VoxDesc>() + h->vclass_off[c];
     launch_em_voxel<Real, OutT>(v, lists, h->vclass_n,
-                                std::is_same<OutT, Real>::value ? h->vox_blocks_real : h->vox_blocks_f64, s);
+                                std::is_same<OutT, Real>::value ? h->vox_blocks_real : h->vox_blocks_f64,
+                                h->vox_streamed, s);
 }
 
 int voxel_mode(const Params& P) {
@@ -818,6 +876,7 @@ void iterate_impl(muto_handle* h, int n) {
         if (h->P.use_graph) {
             if (!h->graph) {
                 // capture one iteration once; replays reuse the same buffers
+                HostPhase ph(h, "graph_capture");
                 const unsigned long long before = launches_so_far();
                 CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
                 h->capturing = true;
@@ -964,7 +1023,7 @@ namespace {
 // muon with k = (x_i, 0, 0), every voxel lambda = 1, so s_i = 2 + x_i
 template <typename Real>
 void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off, uint32_t n_segs, int mode, int pct,
-                      double* out) {
+                      uint32_t streamed, double* out) {
     using R2 = typename Vec2<Real>::type;
     using R4 = typename Vec4<Real>::type;
     cudaStream_t s;
@@ -979,7 +1038,7 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
         kv[i].x = static_cast<Real>(values[i]);
         kv[i].y = kv[i].z = kv[i].w = Real(0);
     }
-    std::vector<VoxDesc> cls[3];
+    std::vector<VoxDesc> cls[kVoxClasses];
     uint32_t mmax = 0;
     for (uint32_t j = 0; j < n_segs; ++j) {
         const uint64_t m64 = seg_off[j + 1] - seg_off[j];
@@ -987,7 +1046,7 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
             throw Error(MUTO_ERR_ARG, "segment offsets must be non-decreasing and within the values");
         const uint32_t m = static_cast<uint32_t>(m64);
         mmax = std::max(mmax, m);
-        cls[m <= 256u ? 0 : (m <= 768u ? 1 : 2)].push_back(VoxDesc{j, m, seg_off[j]});
+        cls[vox_class_of<Real>(m)].push_back(VoxDesc{j, m, seg_off[j]});
     }
     std::vector<Real> lam(n_segs, Real(1));
     DevMem d_mu, d_lt, d_kv, d_lam, d_out, d_desc, d_keys;
@@ -998,17 +1057,18 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
     d_lam.alloc(std::max<uint64_t>(n_segs, 1) * sizeof(Real), nullptr);
     d_out.alloc(std::max<uint64_t>(n_segs, 1) * sizeof(Real), nullptr);
     d_desc.alloc(std::max<uint64_t>(n_segs, 1) * sizeof(VoxDesc), nullptr);
-    if (mmax > voxel_register_cap<Real>()) d_keys.alloc(np * sizeof(typename KeyOf<Real>::type), nullptr);
+    if (mmax > voxel_register_cap<Real>() || (streamed && mmax > 256u))
+        d_keys.alloc(np * sizeof(typename KeyOf<Real>::type), nullptr);
     if (n) {
         CK(cudaMemcpyAsync(d_mu.as<void>(), mu.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(d_lt.as<void>(), lt.data(), n * sizeof(R2), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(d_kv.as<void>(), kv.data(), n * sizeof(R4), cudaMemcpyHostToDevice, s));
     }
     CK(cudaMemcpyAsync(d_lam.as<void>(), lam.data(), n_segs * sizeof(Real), cudaMemcpyHostToDevice, s));
-    const VoxDesc* lists[3];
-    uint32_t counts[3];
+    const VoxDesc* lists[kVoxClasses];
+    uint32_t counts[kVoxClasses];
     uint64_t at = 0;
-    for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < kVoxClasses; ++c) {
         lists[c] = d_desc.as<VoxDesc>() + at;
         counts[c] = static_cast<uint32_t>(cls[c].size());
         if (counts[c])
@@ -1019,9 +1079,9 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
     int dev = 0, sms = 1;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    int resident[3];
+    int resident[2 * kVoxClasses];
     em_voxel_occupancy<Real, Real>(resident);
-    for (int c = 0; c < 3; ++c) resident[c] *= sms;
+    for (int c = 0; c < 2 * kVoxClasses; ++c) resident[c] *= sms;
     VoxelPassArgs<Real, Real> v{};
     v.vm_mu = d_mu.as<uint32_t>();
     v.vm_LT = d_lt.as<R2>();
@@ -1032,7 +1092,7 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
     v.pct = pct;
     v.out = d_out.as<Real>();
     v.scratch = d_keys.empty() ? nullptr : d_keys.as<typename KeyOf<Real>::type>();
-    launch_em_voxel<Real, Real>(v, lists, counts, resident, s);
+    launch_em_voxel<Real, Real>(v, lists, counts, resident, streamed, s);
     CK(cudaGetLastError());
     std::vector<Real> o(n_segs);
     CK(cudaMemcpyAsync(o.data(), d_out.as<void>(), n_segs * sizeof(Real), cudaMemcpyDeviceToHost, s));
@@ -1231,15 +1291,17 @@ int muto_reconstruct(muto_handle* h, const muto_ray* rays, uint64_t n, double* o
 }
 
 int muto_select_probe(int precision, const double* values, uint64_t n, const uint64_t* seg_off, uint32_t n_segs,
-                      int update_with_mean, int mean_percentile, double* out) {
+                      int update_with_mean, int mean_percentile, long long stream_above, double* out) {
     if ((n > 0 && !values) || !seg_off || (n_segs > 0 && !out) || (precision != 0 && precision != 1) ||
         mean_percentile < 0 || mean_percentile > 100 || n > 0xffffffffull)
         return MUTO_ERR_ARG;
     const int mode = !update_with_mean ? kVoxMedian : (mean_percentile == 100 ? kVoxMean : kVoxPercentile);
     return guarded(nullptr, [&] {
         if (n_segs == 0) return;
-        if (precision == 1) select_probe_run<double>(values, n, seg_off, n_segs, mode, mean_percentile, out);
-        else select_probe_run<float>(values, n, seg_off, n_segs, mode, mean_percentile, out);
+        const uint32_t streamed =
+            stream_above < 0 ? 0u : vox_streamed_mask(static_cast<uint32_t>(std::min<long long>(stream_above, 0xffffffffLL)));
+        if (precision == 1) select_probe_run<double>(values, n, seg_off, n_segs, mode, mean_percentile, streamed, out);
+        else select_probe_run<float>(values, n, seg_off, n_segs, mode, mean_percentile, streamed, out);
     });
 }
 

@@ -202,15 +202,18 @@ __global__ void k_voxel_hist(const uint32_t* __restrict__ vidx, uint64_t P, uint
     warp_count(&ctr->bounds, bad);
 }
 
-// thread per muon: its pairs go to the voxel-major lists in its voxels' segments
+// warp per muon: its pairs, read coalesced, go to the voxel-major lists in
+// their voxels' segments (a slot per pair from the voxel's cursor)
 template <typename Real>
 __global__ void k_build_voxel_major(const uint64_t* __restrict__ off, uint64_t n, const uint32_t* __restrict__ vidx,
                                     const Real* __restrict__ L, const Real* __restrict__ T, uint32_t V,
                                     const uint64_t* __restrict__ start, uint32_t* __restrict__ cursor,
                                     uint32_t* __restrict__ vm_mu, typename Vec2<Real>::type* __restrict__ vm_LT) {
-    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const uint64_t i = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (i >= n) return;
-    for (uint64_t p = off[i]; p < off[i + 1]; ++p) {
+    const uint64_t pe = off[i + 1];
+    for (uint64_t p = off[i] + lane; p < pe; p += 32) {
         const uint32_t j = vidx[p];
         if (j >= V) continue;  // counted by k_voxel_hist
         const uint64_t at = start[j] + atomicAdd(&cursor[j], 1u);
@@ -248,6 +251,51 @@ __global__ void k_siddon_batch(DevGrid g, const double* __restrict__ p1, const d
     BatchSink s{xyz, len, r * cap, cap};
     const int c = siddon_walk(g, a, b, s);
     counts[r] = c < 0 ? 0xffffffffu : static_cast<uint32_t>(c);
+}
+
+// Voxel classes on the device: a stable partition of the voxels by segment
+// length class (one counting pass of a radix sort with kVoxClasses buckets).
+// Per block of 256 voxels: the class counts (class-major, so one exclusive
+// scan gives every block's first slot in every class), then the scatter of
+// each voxel's descriptor to its slot, in voxel order within a class.
+template <typename Real>
+__global__ void k_class_count(const uint32_t* __restrict__ mult, uint32_t V, uint32_t nblocks,
+                              uint32_t* __restrict__ counts) {
+    __shared__ uint32_t c_s[kVoxClasses];
+    if (threadIdx.x < kVoxClasses) c_s[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cls = j < V ? vox_class_of<Real>(mult[j]) : -1;
+    const int lane = threadIdx.x & 31;
+    for (int c = 0; c < kVoxClasses; ++c) {
+        const uint32_t n = __popc(__ballot_sync(kFull, cls == c));
+        if (lane == 0 && n) atomicAdd(&c_s[c], n);
+    }
+    __syncthreads();
+    if (threadIdx.x < kVoxClasses) counts[threadIdx.x * nblocks + blockIdx.x] = c_s[threadIdx.x];
+}
+
+template <typename Real>
+__global__ void k_class_scatter(const uint32_t* __restrict__ mult, const uint64_t* __restrict__ start, uint32_t V,
+                                uint32_t nblocks, const uint64_t* __restrict__ first, VoxDesc* __restrict__ out) {
+    constexpr int W = kThreads / 32;
+    __shared__ uint32_t wc[W][kVoxClasses];
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cls = j < V ? vox_class_of<Real>(mult[j]) : -1;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t my_rank = 0;
+    for (int c = 0; c < kVoxClasses; ++c) {
+        const unsigned m = __ballot_sync(kFull, cls == c);
+        if (cls == c) my_rank = __popc(m & ((1u << lane) - 1u));
+        if (lane == 0) wc[w][c] = __popc(m);
+    }
+    __syncthreads();
+    if (cls >= 0) {
+        uint32_t before = 0;
+        for (int q = 0; q < w; ++q) before += wc[q][cls];
+        const uint64_t at = first[static_cast<uint64_t>(cls) * nblocks + blockIdx.x] + before + my_rank;
+        out[at] = VoxDesc{j, mult[j], start[j]};
+    }
 }
 
 }  // namespace
@@ -309,7 +357,8 @@ void launch_build_voxel_major(const uint64_t* off, uint64_t n, const uint32_t* v
                               uint32_t V, const uint64_t* start, uint32_t* cursor, uint32_t* vm_mu,
                               typename Vec2<Real>::type* vm_LT, cudaStream_t s) {
     if (n == 0) return;
-    k_build_voxel_major<Real><<<blocks_for(n), kThreads, 0, s>>>(off, n, vidx, L, T, V, start, cursor, vm_mu, vm_LT);
+    k_build_voxel_major<Real><<<blocks_for(n * 32), kThreads, 0, s>>>(off, n, vidx, L, T, V, start, cursor, vm_mu,
+                                                                      vm_LT);
     count_launches(1);
 }
 template void launch_build_voxel_major<float>(const uint64_t*, uint64_t, const uint32_t*, const float*, const float*,
@@ -323,5 +372,27 @@ void launch_siddon_batch(muto_grid g, const double* p1, const double* p2, uint64
     if (n == 0) return;
     k_siddon_batch<<<blocks_for(n, 128), 128, 0, s>>>(make_dev_grid(g), p1, p2, n, cap, xyz, len, counts); count_launches(1);
 }
+
+}  // namespace muto
+
+namespace muto {
+
+uint32_t voxel_class_blocks(uint64_t V) { return blocks_for(V); }
+
+template <typename Real>
+void launch_voxel_classes(const uint32_t* mult, const uint64_t* start, uint32_t V, uint32_t* counts, uint64_t* first,
+                          void* scan_scratch, VoxDesc* out, cudaStream_t s) {
+    if (V == 0) return;
+    const uint32_t nb = blocks_for(V);
+    k_class_count<Real><<<nb, kThreads, 0, s>>>(mult, V, nb, counts);
+    count_launches(1);
+    scan_u32_to_u64(counts, first, static_cast<uint64_t>(nb) * kVoxClasses, scan_scratch, s);
+    k_class_scatter<Real><<<nb, kThreads, 0, s>>>(mult, start, V, nb, first, out);
+    count_launches(1);
+}
+template void launch_voxel_classes<float>(const uint32_t*, const uint64_t*, uint32_t, uint32_t*, uint64_t*, void*,
+                                          VoxDesc*, cudaStream_t);
+template void launch_voxel_classes<double>(const uint32_t*, const uint64_t*, uint32_t, uint32_t*, uint64_t*, void*,
+                                           VoxDesc*, cudaStream_t);
 
 }  // namespace muto

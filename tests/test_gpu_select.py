@@ -5,7 +5,8 @@ The probe runs the voxel-pass kernels of an EM iteration on chosen segments
 purpose: staged sorts of short segments, the sampling rounds, the window
 misses that fall back to the radix search (sorted inputs put the samples at
 one end), duplicates that stop the windows shrinking, the three segment-length
-classes and the scratch-array path of the longest segments.
+classes and the scratch-array path of the longest segments, with long
+segments held in registers or streamed ("voxel_stream_above").
 
 The median update is compared bit for bit with numpy on the same float32 (or
 float64) s_i: halved middle value, or a quarter of the sum of the two middle
@@ -56,14 +57,14 @@ def _segments(seed, dtype):
     return segs
 
 
-def _probe(segs, precision, update_with_mean=0, pct=100):
+def _probe(segs, precision, update_with_mean=0, pct=100, stream_above=-1):
     lib = _lib.load()
     vals = np.ascontiguousarray(np.concatenate(segs).astype(np.float64))
     off = np.zeros(len(segs) + 1, np.uint64)
     off[1:] = np.cumsum([len(s) for s in segs])
     out = np.full(len(segs), np.nan)
     rc = lib.muto_select_probe(precision, _lib.dptr(vals), vals.size, off.ctypes.data_as(C.POINTER(C.c_uint64)),
-                               len(segs), update_with_mean, pct, _lib.dptr(out))
+                               len(segs), update_with_mean, pct, stream_above, _lib.dptr(out))
     assert rc == _lib.MUTO_OK
     return out
 
@@ -80,9 +81,10 @@ def _median_update(x, dtype):
 
 @pytest.mark.parametrize("precision,dtype", [(0, np.float32), (1, np.float64)])
 @pytest.mark.parametrize("seed", [0, 1])
-def test_median_update_bit_exact(gpu, precision, dtype, seed):
+@pytest.mark.parametrize("stream_above", [-1, 256, 512])
+def test_median_update_bit_exact(gpu, precision, dtype, seed, stream_above):
     segs = _segments(seed, dtype)
-    got = _probe(segs, precision)
+    got = _probe(segs, precision, stream_above=stream_above)
     want = np.array([_median_update(s, dtype) for s in segs])
     bad = np.nonzero(got.view(np.uint64) != want.view(np.uint64))[0]
     assert bad.size == 0, [(len(segs[i]), KINDS[i % len(KINDS)] if i < len(LENGTHS) * len(KINDS) else "empty",
@@ -91,9 +93,10 @@ def test_median_update_bit_exact(gpu, precision, dtype, seed):
 
 @pytest.mark.parametrize("precision,dtype,tol", [(0, np.float32, 1e-5), (1, np.float64, 1e-12)])
 @pytest.mark.parametrize("pct", [1, 37, 50, 90, 100])
-def test_percentile_and_mean_update(gpu, precision, dtype, tol, pct):
+@pytest.mark.parametrize("stream_above", [-1, 256])
+def test_percentile_and_mean_update(gpu, precision, dtype, tol, pct, stream_above):
     segs = _segments(7, dtype)
-    got = _probe(segs, precision, update_with_mean=1, pct=pct)
+    got = _probe(segs, precision, update_with_mean=1, pct=pct, stream_above=stream_above)
     for i, x in enumerate(segs):
         if x.size == 0:
             assert got[i] == 0.0
