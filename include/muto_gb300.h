@@ -69,9 +69,9 @@ typedef struct muto_status {
     double cost;                /* mean cost of the last iteration (when computed) */
     double cost_prev;           /* mean cost of the iteration before */
     uint64_t device_bytes;      /* device memory held by the handle */
-    int32_t muon_pass;          /* muon-pass variant chosen by the autotuner: 1 TMA tiles, 2 warp-batched */
+    int32_t muon_pass;          /* muon-pass variant in use: 1 TMA tiles, 2 warp-batched */
     int32_t muon_group;         /* lanes per muon in its covariance sums */
-    int32_t tile_pairs;         /* pairs per tile (TMA variant) */
+    int32_t tile_pairs;         /* pairs per tile (TMA variant; 0 when it is not used) */
     int32_t tile_muons;         /* muons per tile (TMA variant) */
     char message[256];          /* text of the last error */
 } muto_status;
@@ -90,8 +90,11 @@ typedef struct muto_handle muto_handle;
  * ("mixed" default, or "fp64"), "use_graph" (true), "random_seed",
  * "compute_cost" (computed when early_stop/log_results is set, or when true),
  * "newton_max_iter" (MAP cubic cap, 200), "tile_pairs" (pairs per TMA tile),
- * "muon_pass" ("auto": the variant is chosen by timing on the scan's data
- * at prepare; "tile" or "warp" force one). */
+ * "muon_pass" ("auto": the warp-batched variant, its group size chosen by
+ * timing on the scan's data at prepare; "tile" or "warp" force one),
+ * "voxel_stream_above" (-1: every segment up to 1536 pairs (768 in fp64)
+ * is selected from registers; n >= 256: segments longer than n are
+ * selected without holding their keys). */
 int muto_create(const char* method, const char* config_json, muto_handle** out);
 int muto_destroy(muto_handle* h);
 

@@ -105,7 +105,7 @@ struct Params {
     int newton_max_iter = 200;
     int tile_pairs = 0;
     int muon_pass = 0;  // 0 autotune, 1 tile (TMA), 2 warp-batched
-    long long voxel_stream_above = 512;  // segments longer than this are selected without registers
+    long long voxel_stream_above = -1;  // segments longer than this are selected without registers (-1: none)
 };
 
 Params parse_params(Method m, const std::string& text) {
@@ -183,7 +183,7 @@ Params parse_params(Method m, const std::string& text) {
         else if (mp == "tile") P.muon_pass = 1;
         else if (mp == "warp") P.muon_pass = 2;
         else throw Error(MUTO_ERR_CONFIG, "muon_pass must be \"auto\", \"tile\" or \"warp\"");
-        P.voxel_stream_above = cfg.value("voxel_stream_above", static_cast<int64_t>(512));
+        P.voxel_stream_above = cfg.value("voxel_stream_above", static_cast<int64_t>(-1));
         if (P.newton_max_iter < 1) throw Error(MUTO_ERR_CONFIG, "newton_max_iter must be >= 1");
     } catch (const json::type_error& e) {
         throw Error(MUTO_ERR_CONFIG, std::string("config value of the wrong type: ") + e.what());
