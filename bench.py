@@ -63,6 +63,13 @@ class ClockSampler:
                                          stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        # the timed region starts once sampling has begun (first line, at most 3 s)
+        t0 = time.time()
+        while time.time() - t0 < 3.0 and self.proc.poll() is None:
+            if Path(self.f.name).stat().st_size > 0:
+                break
+            time.sleep(0.02)
 
     def stop(self) -> dict:
         if not self.proc:
@@ -112,6 +119,11 @@ def workload(args, rank: int):
     wl.seed = wl.seed + 1000 * rank  # every rank reconstructs its own scan (weak scaling)
     return wl
 
+
+# DRAM bytes per pair per launch, measured by ncu (--set full) on the 50^3-voxel
+# 2.5 M-muon case of the default scene (median EM, mixed form): muon pass
+# 868.4 MB and voxel pass (all classes) 964.4 MB for 68 700 086 pairs
+TRAFFIC_PER_PAIR = {"muon": 868.4e6 / 68700086, "voxel": 964.4e6 / 68700086}
 
 # set-up kernels and host phases reported by the library's profiler
 SETUP_KERNELS = ["keep_flags", "scan", "compact", "muon_info", "siddon_count", "siddon_fill", "voxel_offset",
@@ -272,18 +284,26 @@ def run_ours(args) -> int:
     # algorithmic bytes per launch (mixed: 4-byte index, L, T; fp64: 8-byte L, T)
     rb = 4 if args.precision == "mixed" else 8
     muon_bytes = (4 + 2 * rb) * pairs + (4 * rb + rb + 8 + 4 * rb) * kept + rb * V  # lists, S/D/pr2/off, k out, lambda
-    voxel_bytes = (4 + 2 * rb) * pairs + (8 + 4 + 2 * rb) * V                       # voxel-major lists, start/M, lambda in/out
+    voxel_bytes = (4 + 2 * rb) * pairs + (16 + 2 * rb) * V                          # voxel-major lists, descriptor, lambda in/out
     pk = peaks()
     muon_ms = tm_ / max(nm_, 1)
-    voxel_ms = tv / max(nv_, 1)
+    voxel_ms = tv / max(nv_, 1)  # the voxel pass: all class launches of one iteration
     achieved = muon_bytes / (muon_ms / 1000.0) / 1e9 if nm_ else None
     v_ach = voxel_bytes / (voxel_ms / 1000.0) / 1e9 if nv_ else None
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": (achieved / pk["hbm_gbs"]) if achieved else None, "traffic": args.ncu_traffic,
-                "kernel": "k_em_muon", "kernel_ms": muon_ms, "algorithmic_bytes": muon_bytes,
-                "peak_source": pk["source"],
-                "voxel_pass": {"kernel": "k_em_voxel", "kernel_ms": voxel_ms, "algorithmic_bytes": voxel_bytes,
-                               "achieved": v_ach, "frac": (v_ach / pk["hbm_gbs"]) if v_ach else None}}
+    # DRAM traffic (read + write) per launch: ncu's bytes per pair on the 50^3-voxel
+    # case of the same scene, scaled by this run's pairs
+    measured = args.precision == "mixed" and args.mode == "median" and args.workload in ("config2", "config2_coarse")
+    t_voxel = (args.ncu_traffic if args.ncu_traffic is not None
+               else (TRAFFIC_PER_PAIR["voxel"] * pairs if measured else None))
+    t_muon = TRAFFIC_PER_PAIR["muon"] * pairs if measured else None
+    # the voxel pass takes about three quarters of an iteration: it is the dominant kernel
+    roofline = {"bound": "hbm", "achieved": v_ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": (v_ach / pk["hbm_gbs"]) if v_ach else None, "traffic": t_voxel,
+                "kernel": "k_em_voxel (one launch per segment-length class)", "kernel_ms": voxel_ms,
+                "algorithmic_bytes": voxel_bytes, "peak_source": pk["source"],
+                "muon_pass": {"kernel": "k_em_muon", "kernel_ms": muon_ms, "algorithmic_bytes": muon_bytes,
+                              "achieved": achieved, "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
+                              "traffic": t_muon}}
 
     # ---- e2e: full reconstruct through the C ABI from pinned host tracks ------
     e2e = None
@@ -400,7 +420,7 @@ def run_ours(args) -> int:
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config2_coarse", "config3", "config5"])
@@ -415,7 +435,7 @@ def main() -> int:
     ap.add_argument("--voxel-stream-above", type=int, default=None,
                     help="segments longer than this are selected without holding their keys (-1: never)")
     ap.add_argument("--ncu-traffic", type=float, default=None,
-                    help="dram bytes per em_tile launch from an ncu capture (profiles/)")
+                    help="DRAM bytes per voxel-pass iteration from an ncu capture of this workload")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
