@@ -172,10 +172,15 @@ int muto_siddon_batch_noalloc(const muto_grid* g, const double* p1, const double
  * segment j: the halved median of the s_i (even counts: the mean of the two
  * middle values), or with update_with_mean the halved mean of the lowest
  * mean_percentile % (100: all).  stream_above is the "voxel_stream_above"
- * key of the configuration (-1: never).  Not in the reference: a probe that
- * lets tests check the exact order statistics on chosen inputs. */
+ * key of the configuration (-1: never).  With repeat > 1, values holds
+ * repeat * n values and the pass runs repeat times, pass r on values
+ * [r*n, (r+1)*n), each starting from the selection windows the previous
+ * pass left (as iterations do); out is the last pass's.  Not in the
+ * reference: a probe that lets tests check the exact order statistics on
+ * chosen inputs. */
 int muto_select_probe(int precision, const double* values, uint64_t n, const uint64_t* seg_off, uint32_t n_segs,
-                      int update_with_mean, int mean_percentile, long long stream_above, double* out);
+                      int update_with_mean, int mean_percentile, long long stream_above, uint32_t repeat,
+                      double* out);
 
 /* MLSD/MAP after prepare: the kept muons and their merged paths
  * (src/MutoMLSD.cpp:268-326, :382-430).  Any pointer may be NULL.

@@ -71,7 +71,8 @@ SIGNATURES = {
     "muto_siddon_batch": (C.c_int, [C.POINTER(muto_grid), _D, _D, C.c_uint64, C.c_uint32, _U32, _D, _U32]),
     "muto_siddon_batch_noalloc": (C.c_int, [C.POINTER(muto_grid), _D, _D, C.c_uint64, C.c_uint32, _U32, _D, _U32,
                                              _P]),
-    "muto_select_probe": (C.c_int, [C.c_int, _D, C.c_uint64, _U64, C.c_uint32, C.c_int, C.c_int, C.c_longlong, _D]),
+    "muto_select_probe": (C.c_int, [C.c_int, _D, C.c_uint64, _U64, C.c_uint32, C.c_int, C.c_int, C.c_longlong,
+                                     C.c_uint32, _D]),
     "muto_export_paths": (C.c_int, [_P, _U32, _D, _U64, _U32, _D, _D]),
     "muto_poca_assignment": (C.c_int, [_P, _I64, C.c_uint64]),
     "muto_nll_forward": (C.c_int, [_P, _D, _D]),

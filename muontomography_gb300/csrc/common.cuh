@@ -183,6 +183,7 @@ struct VoxelPassArgs {
     double* grad;                             // V gradient (kVoxGradient)
     const double* lam64;                      // V lambda in FP64 (kVoxGradient)
     typename KeyOf<Real>::type* scratch;      // P keys of segments beyond the register budget
+    Real* win;                                // 2V selection window per voxel (center, half), or NULL
 };
 // segments up to this many pairs are selected from registers
 template <typename Real>

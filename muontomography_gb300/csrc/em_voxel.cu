@@ -191,6 +191,8 @@ template <typename K>
 struct Sel {
     K kth, prev;
     bool have_prev;
+    K wlo, whi;     // smallest and largest key of the final sorted candidates
+    uint32_t nfin;  // their number (0: the selection ended in a radix search)
 };
 
 // ascending warp bitonic sort of one key per lane
@@ -217,6 +219,9 @@ __device__ Sel<K> sel32(const K* c, uint32_t n, uint32_t k, int lane) {
     r.kth = __shfl_sync(kFull, s, static_cast<int>(k));
     r.prev = __shfl_sync(kFull, s, static_cast<int>(k ? k - 1 : 0));
     r.have_prev = k >= 1;
+    r.wlo = __shfl_sync(kFull, s, 0);
+    r.whi = __shfl_sync(kFull, s, static_cast<int>(n - 1));
+    r.nfin = n;
     return r;
 }
 
@@ -247,30 +252,25 @@ __device__ Sel<K> sel64(const K* c, uint32_t n, uint32_t k, int lane) {
     const uint32_t kp = k ? k - 1 : 0;
     const K va = __shfl_sync(kFull, a, static_cast<int>(k >> 1)), vb = __shfl_sync(kFull, b, static_cast<int>(k >> 1));
     const K pa = __shfl_sync(kFull, a, static_cast<int>(kp >> 1)), pb = __shfl_sync(kFull, b, static_cast<int>(kp >> 1));
+    const uint32_t kl = n - 1;
+    const K la = __shfl_sync(kFull, a, static_cast<int>(kl >> 1)), lb = __shfl_sync(kFull, b, static_cast<int>(kl >> 1));
     Sel<K> r;
     r.kth = (k & 1u) ? vb : va;
     r.prev = (kp & 1u) ? pb : pa;
     r.have_prev = k >= 1;
+    r.wlo = __shfl_sync(kFull, a, 0);
+    r.whi = (kl & 1u) ? lb : la;
+    r.nfin = n;
     return r;
 }
 
-// One sampling round over n keys: the (up to 32) samples are sorted in the
-// warp and the keys within 6 sample ranks of rank k are kept, each lane
-// appending its own to its column of `out` (no cross-lane compaction).
-// Returns false when the window misses rank k, overflows `out_rows` or
-// keeps everything; otherwise `out` holds the candidates and the counts.
+// One pass over n keys with the window [lo, hi]: counts the keys below it
+// and appends those inside to the lane's own column of `out` (no cross-lane
+// compaction).  Returns false when the window misses rank k, overflows
+// `out_rows` or keeps everything; otherwise `res` holds the candidates.
 template <typename K, class Src>
-__device__ __forceinline__ bool sample_round(const Src& v, uint32_t n, uint32_t k, K* out, uint32_t out_rows,
-                                             int lane, Ragged<K>& res, uint32_t& below) {
-    const K smp = v.sample();
-    const uint32_t ns = __popc(__ballot_sync(kFull, smp != empty_key<K>()));
-    const K s = sort32(smp, lane);  // empty samples sort last
-    const int pos = static_cast<int>((static_cast<float>(k) * static_cast<float>(ns)) / static_cast<float>(n));
-    const int ql = pos - 6, qh = pos + 6;
-    const K slo = __shfl_sync(kFull, s, ql < 0 ? 0 : (ql > 31 ? 31 : ql));
-    const K shi = __shfl_sync(kFull, s, qh > 31 ? 31 : (qh < 0 ? 0 : qh));
-    const K lo = ql <= 0 ? K(0) : slo;
-    const K hi = qh >= static_cast<int>(ns) - 1 ? empty_key<K>() - 1 : shi;
+__device__ __forceinline__ bool window_pass(const Src& v, uint32_t n, uint32_t k, K lo, K hi, K* out,
+                                            uint32_t out_rows, int lane, Ragged<K>& res, uint32_t& below) {
     uint32_t c_lo = 0, t = 0;
     const uint32_t nr = v.rows();
 #pragma unroll
@@ -293,6 +293,23 @@ __device__ __forceinline__ bool sample_round(const Src& v, uint32_t n, uint32_t 
     return rows <= out_rows && below <= k && k < below + n_in && n_in < n;
 }
 
+// One sampling round: the (up to 32) samples are sorted in the warp and the
+// window is the keys within 6 sample ranks of rank k (window_pass).
+template <typename K, class Src>
+__device__ __forceinline__ bool sample_round(const Src& v, uint32_t n, uint32_t k, K* out, uint32_t out_rows,
+                                             int lane, Ragged<K>& res, uint32_t& below) {
+    const K smp = v.sample();
+    const uint32_t ns = __popc(__ballot_sync(kFull, smp != empty_key<K>()));
+    const K s = sort32(smp, lane);  // empty samples sort last
+    const int pos = static_cast<int>((static_cast<float>(k) * static_cast<float>(ns)) / static_cast<float>(n));
+    const int ql = pos - 6, qh = pos + 6;
+    const K slo = __shfl_sync(kFull, s, ql < 0 ? 0 : (ql > 31 ? 31 : ql));
+    const K shi = __shfl_sync(kFull, s, qh > 31 ? 31 : (qh < 0 ? 0 : qh));
+    const K lo = ql <= 0 ? K(0) : slo;
+    const K hi = qh >= static_cast<int>(ns) - 1 ? empty_key<K>() - 1 : shi;
+    return window_pass<K>(v, n, k, lo, hi, out, out_rows, lane, res, below);
+}
+
 // Order statistics kk and kk-1 of the candidates in `cur`, exact: more
 // sampling rounds between the two buffers until at most 64 remain, which
 // are gathered and sorted.  A round that fails falls back to a bitwise radix
@@ -304,6 +321,7 @@ __device__ __noinline__ Sel<K> select_candidates(K* cur_buf, K* oth_buf, uint32_
     K* oth = oth_buf;
     Sel<K> r;
     r.have_prev = false;
+    r.nfin = 0;
 #pragma unroll 1
     for (int round = 0; n > 64 && round < 8; ++round) {
         Ragged<K> nxt;
@@ -360,11 +378,32 @@ __device__ Sel<K> kth_select(const Src& v, uint32_t M, uint32_t k, K* a, K* b, u
     if (!sample_round<K>(v, M, k, a, cap_rows, lane, cur, b1)) {
         Sel<K> r;
         r.have_prev = false;
+        r.nfin = 0;
         r.kth = kth_radix<K>(v, k);
         __syncwarp();
         return r;
     }
     return select_candidates<K>(a, b, cap_rows, cur.t, cur.nrows, __reduce_add_sync(kFull, cur.t), k - b1, lane);
+}
+
+// kth_select starting from a predicted window [lo, hi] (the previous
+// iteration's): one pass keeps the keys inside it and, if it holds rank k,
+// the candidate rounds follow; otherwise the sampled path.  *hit tells which.
+template <typename K, class Src>
+__device__ Sel<K> kth_select_from(const Src& v, uint32_t M, uint32_t k, K lo, K hi, K* a, K* b, uint32_t cap_rows,
+                                  int lane, bool* hit) {
+    *hit = false;
+    if (M > 64) {
+        Ragged<K> cur;
+        uint32_t b1;
+        if (window_pass<K>(v, M, k, lo, hi, a, cap_rows, lane, cur, b1)) {
+            *hit = true;
+            return select_candidates<K>(a, b, cap_rows, cur.t, cur.nrows, __reduce_add_sync(kFull, cur.t), k - b1,
+                                        lane);
+        }
+        __syncwarp();
+    }
+    return kth_select<K>(v, M, k, a, b, cap_rows, lane);
 }
 
 struct CandBufs {
@@ -373,47 +412,92 @@ struct CandBufs {
     uint32_t rows;
 };
 
-// the voxel's new value from its keys (median or percentile mean)
-template <typename Real, class Src>
-__device__ Real order_update(const Src& src, uint32_t M, int mode, int pct, const CandBufs& cb, int lane) {
+// A voxel's selection window from the previous iteration, in the units of
+// its keys: the order statistic found then (center) and a half-width.
+template <typename Real>
+struct Pred {
+    Real center, half;
+};
+
+// Next window: centred on the order statistic just found, wide enough for
+// about 40 keys at the density of the final sorted candidates, and for
+// twice the drift since the last prediction (twice the old width after a
+// miss).  0: no prediction (sampling next time).
+template <typename Real, typename K>
+__device__ __forceinline__ Pred<Real> next_window(const Sel<K>& sel, bool used, bool hit, const Pred<Real>& old) {
+    const Real c = from_key(sel.kth);
+    Real h = 0;
+    if (sel.nfin >= 2) h = (from_key(sel.whi) - from_key(sel.wlo)) * Real(20) / static_cast<Real>(sel.nfin);
+    if (used) {
+        const Real drift = c > old.center ? c - old.center : old.center - c;
+        h = h > Real(2) * drift ? h : Real(2) * drift;
+        if (!hit) h = h > Real(2) * old.half ? h : Real(2) * old.half;
+    }
+    if (!(h > Real(0)) || !isfinite(h) || !isfinite(c)) h = 0;
+    return Pred<Real>{c, h};
+}
+
+// The voxel's new value from its keys (median or percentile mean); val(key)
+// is the s_ij a key stands for.  With `win`, the selection starts from the
+// voxel's predicted window and the window for the next iteration is stored.
+template <typename Real, class Src, class Val>
+__device__ Real order_update(const Src& src, uint32_t M, int mode, int pct, const CandBufs& cb, int lane, Val val,
+                             Pred<Real>* win) {
     using K = typename KeyOf<Real>::type;
     K* ba = static_cast<K*>(cb.a);
     K* bb = static_cast<K*>(cb.b);
+    uint32_t k, jm = 0;
     if (mode == kVoxMedian) {  // src/MutoMLSD.cpp:506-516
-        const Sel<K> s = kth_select<K>(src, M, M / 2, ba, bb, cb.rows, lane);
-        const Real v1 = from_key(s.kth);
+        k = M / 2;
+    } else {  // mean of the lowest floor(pct/100 M) values, at least 1 (src/MutoMLSD.cpp:500-504)
+        jm = u32_cast_x86(pct / 100.0 * M);
+        if (jm < 1) jm = 1;
+        if (jm > M) jm = M;
+        k = jm - 1;
+    }
+    Sel<K> sel;
+    bool used = false, hit = false;
+    Pred<Real> old{0, 0};
+    if (win && M > 64) {
+        old = *win;
+        used = old.half > Real(0);
+    }
+    if (used) {
+        sel = kth_select_from<K>(src, M, k, to_key(old.center - old.half), to_key(old.center + old.half), ba, bb,
+                                 cb.rows, lane, &hit);
+    } else {
+        sel = kth_select<K>(src, M, k, ba, bb, cb.rows, lane);
+    }
+    if (win && M > 64 && lane == 0) *win = next_window<Real, K>(sel, used, hit, old);
+    if (mode == kVoxMedian) {
+        const Real v1 = val(sel.kth);
         if (M % 2 == 0) {  // s_(M/2-1): from the sorted candidates, else v1 itself or the largest key below it
             Real v0;
-            if (s.have_prev) {
-                v0 = from_key(s.prev);
+            if (sel.have_prev) {
+                v0 = val(sel.prev);
             } else {
                 uint32_t c = 0;
                 K mb = K(0);
                 src.each([&](K x) {
-                    if (x < s.kth) {
+                    if (x < sel.kth) {
                         ++c;
                         mb = x > mb ? x : mb;
                     }
                 });
                 c = __reduce_add_sync(kFull, c);
                 mb = warp_max_k(mb);
-                v0 = c < M / 2 ? v1 : from_key(mb);
+                v0 = c < M / 2 ? v1 : val(mb);
             }
             return (v1 + v0) * Real(0.25);
         }
         return v1 * Real(0.5);
     }
-    // mean of the lowest floor(pct/100 M) values, at least 1 (src/MutoMLSD.cpp:500-504)
-    uint32_t jm = u32_cast_x86(pct / 100.0 * M);
-    if (jm < 1) jm = 1;
-    if (jm > M) jm = M;
-    const K kt = kth_select<K>(src, M, jm - 1, ba, bb, cb.rows, lane).kth;
-    const Real t = from_key(kt);
+    const Real t = val(sel.kth);
     Real s = 0;
     uint32_t c = 0;
     src.each([&](K x) {
-        if (x < kt) {
-            s += from_key(x);
+        if (x < sel.kth) {
+            s += val(x);
             ++c;
         }
     });
@@ -462,14 +546,19 @@ __device__ __forceinline__ void voxel_regs(const VoxelPassArgs<Real, OutT>& a, u
             v.key[r0 + u] = empty_key<K>();
             if (e < M) {
                 const Real g = pair_g<Real>(ldg4(a.kvec + mu[u]), lt[u].x, lt[u].y);
-                if (keys) v.key[r0 + u] = to_key(Real(2) * lam + g * lam * lam);
+                if (keys) v.key[r0 + u] = to_key(g);  // s_ij = 2 l + g l^2 is non-decreasing in g
                 else gs += g;
             }
         }
     }
     Real out;
     if (keys) {
-        out = order_update<Real>(v, M, a.mode, a.pct, cb, lane);
+        auto val = [lam](K x) {
+            const Real g = from_key(x);
+            return Real(2) * lam + g * lam * lam;
+        };
+        out = order_update<Real>(v, M, a.mode, a.pct, cb, lane, val,
+                                 a.win ? reinterpret_cast<Pred<Real>*>(a.win) + j : nullptr);
     } else {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) gs += __shfl_xor_sync(kFull, gs, o);
@@ -502,7 +591,8 @@ __device__ void voxel_stream(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uin
     if (keys) {
         __syncwarp();  // the lanes' key stores are visible to the whole warp
         const PtrKeys<K> src{kp, M, lane};
-        out = order_update<Real>(src, M, a.mode, a.pct, cb, lane);
+        out = order_update<Real>(src, M, a.mode, a.pct, cb, lane, [](K x) { return from_key(x); },
+                                 static_cast<Pred<Real>*>(nullptr));
     } else {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) gs += __shfl_xor_sync(kFull, gs, o);

@@ -291,6 +291,7 @@ struct muto_handle {
     uint32_t vox_streamed = 0;  // classes selected by the streamed path
     uint64_t vclass_off[kVoxClasses] = {};
     DevMem mult, start, kvec, keys;   // keys: scratch for voxels beyond the register budget
+    DevMem win;                       // per voxel: the last selection window (center, half-width)
     DevMem lam, lam_ml, cost_hist;
     DevMem tiles;
     uint32_t ntiles = 0;
@@ -702,6 +703,8 @@ void prepare_em(muto_handle* h) {
     // --- image ---------------------------------------------------------------
     ph.reset(new HostPhase(h, "image"));
     h->lam.alloc(V * sizeof(Real), &h->dev_bytes);
+    h->win.alloc(2 * V * sizeof(Real), &h->dev_bytes);
+    CK(cudaMemsetAsync(h->win.as<void>(), 0, 2 * V * sizeof(Real), s));  // half-width 0: no prediction yet
     {
         std::vector<Real> init_r(init.begin(), init.end());
         CK(cudaMemcpyAsync(h->lam.as<void>(), init_r.data(), V * sizeof(Real), cudaMemcpyHostToDevice, s));
@@ -810,7 +813,7 @@ void autotune_muon_pass(muto_handle* h) {
 template <typename Real, typename OutT>
 VoxelPassArgs<Real, OutT> voxel_args(muto_handle* h, const Real* lam, int mode, OutT* out) {
     using R4 = typename Vec4<Real>::type;
-    VoxelPassArgs<Real, OutT> v;
+    VoxelPassArgs<Real, OutT> v{};
     v.start = h->start.as<uint64_t>();
     v.mult = h->mult.as<uint32_t>();
     v.vm_mu = h->vm_mu.as<uint32_t>();
@@ -824,6 +827,7 @@ VoxelPassArgs<Real, OutT> voxel_args(muto_handle* h, const Real* lam, int mode, 
     v.grad = nullptr;
     v.lam64 = nullptr;
     v.scratch = h->keys.empty() ? nullptr : h->keys.as<typename KeyOf<Real>::type>();
+    v.win = (mode == kVoxMedian || mode == kVoxPercentile) && !h->win.empty() ? h->win.as<Real>() : nullptr;
     return v;
 }
 
@@ -1023,7 +1027,7 @@ namespace {
 // muon with k = (x_i, 0, 0), every voxel lambda = 1, so s_i = 2 + x_i
 template <typename Real>
 void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off, uint32_t n_segs, int mode, int pct,
-                      uint32_t streamed, double* out) {
+                      uint32_t streamed, uint32_t repeat, double* out) {
     using R2 = typename Vec2<Real>::type;
     using R4 = typename Vec4<Real>::type;
     cudaStream_t s;
@@ -1035,7 +1039,6 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
         mu[i] = static_cast<uint32_t>(i);
         lt[i].x = Real(1);
         lt[i].y = Real(0);
-        kv[i].x = static_cast<Real>(values[i]);
         kv[i].y = kv[i].z = kv[i].w = Real(0);
     }
     std::vector<VoxDesc> cls[kVoxClasses];
@@ -1049,7 +1052,7 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
         cls[vox_class_of<Real>(m)].push_back(VoxDesc{j, m, seg_off[j]});
     }
     std::vector<Real> lam(n_segs, Real(1));
-    DevMem d_mu, d_lt, d_kv, d_lam, d_out, d_desc, d_keys;
+    DevMem d_mu, d_lt, d_kv, d_lam, d_out, d_desc, d_keys, d_win;
     const uint64_t np = n + kPad;
     d_mu.alloc(np * sizeof(uint32_t), nullptr);
     d_lt.alloc(np * sizeof(R2), nullptr);
@@ -1059,10 +1062,11 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
     d_desc.alloc(std::max<uint64_t>(n_segs, 1) * sizeof(VoxDesc), nullptr);
     if (mmax > voxel_register_cap<Real>() || (streamed && mmax > 256u))
         d_keys.alloc(np * sizeof(typename KeyOf<Real>::type), nullptr);
+    d_win.alloc(std::max<uint64_t>(n_segs, 1) * 2 * sizeof(Real), nullptr);
+    CK(cudaMemsetAsync(d_win.as<void>(), 0, std::max<uint64_t>(n_segs, 1) * 2 * sizeof(Real), s));
     if (n) {
         CK(cudaMemcpyAsync(d_mu.as<void>(), mu.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(d_lt.as<void>(), lt.data(), n * sizeof(R2), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(d_kv.as<void>(), kv.data(), n * sizeof(R4), cudaMemcpyHostToDevice, s));
     }
     CK(cudaMemcpyAsync(d_lam.as<void>(), lam.data(), n_segs * sizeof(Real), cudaMemcpyHostToDevice, s));
     const VoxDesc* lists[kVoxClasses];
@@ -1092,8 +1096,14 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
     v.pct = pct;
     v.out = d_out.as<Real>();
     v.scratch = d_keys.empty() ? nullptr : d_keys.as<typename KeyOf<Real>::type>();
-    launch_em_voxel<Real, Real>(v, lists, counts, resident, streamed, s);
-    CK(cudaGetLastError());
+    v.win = mode == kVoxMedian || mode == kVoxPercentile ? d_win.as<Real>() : nullptr;
+    for (uint32_t rep = 0; rep < repeat; ++rep) {  // each pass its own values; windows carry over
+        for (uint64_t i = 0; i < n; ++i) kv[i].x = static_cast<Real>(values[rep * n + i]);
+        if (n) CK(cudaMemcpyAsync(d_kv.as<void>(), kv.data(), n * sizeof(R4), cudaMemcpyHostToDevice, s));
+        launch_em_voxel<Real, Real>(v, lists, counts, resident, streamed, s);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(s));  // kv is rewritten by the next pass
+    }
     std::vector<Real> o(n_segs);
     CK(cudaMemcpyAsync(o.data(), d_out.as<void>(), n_segs * sizeof(Real), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -1291,17 +1301,20 @@ int muto_reconstruct(muto_handle* h, const muto_ray* rays, uint64_t n, double* o
 }
 
 int muto_select_probe(int precision, const double* values, uint64_t n, const uint64_t* seg_off, uint32_t n_segs,
-                      int update_with_mean, int mean_percentile, long long stream_above, double* out) {
+                      int update_with_mean, int mean_percentile, long long stream_above, uint32_t repeat,
+                      double* out) {
     if ((n > 0 && !values) || !seg_off || (n_segs > 0 && !out) || (precision != 0 && precision != 1) ||
-        mean_percentile < 0 || mean_percentile > 100 || n > 0xffffffffull)
+        mean_percentile < 0 || mean_percentile > 100 || n > 0xffffffffull || repeat < 1)
         return MUTO_ERR_ARG;
     const int mode = !update_with_mean ? kVoxMedian : (mean_percentile == 100 ? kVoxMean : kVoxPercentile);
     return guarded(nullptr, [&] {
         if (n_segs == 0) return;
         const uint32_t streamed =
             stream_above < 0 ? 0u : vox_streamed_mask(static_cast<uint32_t>(std::min<long long>(stream_above, 0xffffffffLL)));
-        if (precision == 1) select_probe_run<double>(values, n, seg_off, n_segs, mode, mean_percentile, streamed, out);
-        else select_probe_run<float>(values, n, seg_off, n_segs, mode, mean_percentile, streamed, out);
+        if (precision == 1)
+            select_probe_run<double>(values, n, seg_off, n_segs, mode, mean_percentile, streamed, repeat, out);
+        else
+            select_probe_run<float>(values, n, seg_off, n_segs, mode, mean_percentile, streamed, repeat, out);
     });
 }
 

@@ -4,9 +4,11 @@ The probe runs the voxel-pass kernels of an EM iteration on chosen segments
 (s_i = 2 + x_i, lambda = 1), so every path of the selection is reached on
 purpose: staged sorts of short segments, the sampling rounds, the window
 misses that fall back to the radix search (sorted inputs put the samples at
-one end), duplicates that stop the windows shrinking, the three segment-length
-classes and the scratch-array path of the longest segments, with long
-segments held in registers or streamed ("voxel_stream_above").
+one end), duplicates that stop the windows shrinking, every segment-length
+class and the scratch-array path of the longest segments, with long
+segments held in registers or streamed ("voxel_stream_above"), and passes
+that start from the selection windows an earlier pass left, whether those
+still hold the target or not.
 
 The median update is compared bit for bit with numpy on the same float32 (or
 float64) s_i: halved middle value, or a quarter of the sum of the two middle
@@ -57,14 +59,18 @@ def _segments(seed, dtype):
     return segs
 
 
-def _probe(segs, precision, update_with_mean=0, pct=100, stream_above=-1):
+def _probe(segs, precision, update_with_mean=0, pct=100, stream_above=-1, earlier=()):
+    """The probe's last pass on segs; `earlier` passes (same lengths) run first
+    and leave the selection windows the last pass starts from."""
     lib = _lib.load()
-    vals = np.ascontiguousarray(np.concatenate(segs).astype(np.float64))
+    passes = list(earlier) + [segs]
+    vals = np.ascontiguousarray(np.concatenate([np.concatenate(p) for p in passes]).astype(np.float64))
+    n = vals.size // len(passes)
     off = np.zeros(len(segs) + 1, np.uint64)
     off[1:] = np.cumsum([len(s) for s in segs])
     out = np.full(len(segs), np.nan)
-    rc = lib.muto_select_probe(precision, _lib.dptr(vals), vals.size, off.ctypes.data_as(C.POINTER(C.c_uint64)),
-                               len(segs), update_with_mean, pct, stream_above, _lib.dptr(out))
+    rc = lib.muto_select_probe(precision, _lib.dptr(vals), n, off.ctypes.data_as(C.POINTER(C.c_uint64)),
+                               len(segs), update_with_mean, pct, stream_above, len(passes), _lib.dptr(out))
     assert rc == _lib.MUTO_OK
     return out
 
@@ -107,4 +113,36 @@ def test_percentile_and_mean_update(gpu, precision, dtype, tol, pct, stream_abov
         else:
             jm = min(max(int(pct / 100.0 * s.size), 1), s.size)
             want = s[:jm].mean() * 0.5
+        assert abs(got[i] - want) <= tol * max(1.0, abs(want)) * 8, (i, s.size, got[i], want)
+
+
+@pytest.mark.parametrize("precision,dtype", [(0, np.float32), (1, np.float64)])
+@pytest.mark.parametrize("before", ["same", "drift", "other"])
+def test_median_from_carried_windows_bit_exact(gpu, precision, dtype, before):
+    # iterations start from the window the previous one left: exact whether
+    # it still holds the median (same values, a small drift) or not (other values)
+    segs = _segments(3, dtype)
+    if before == "same":
+        earlier = [segs, segs]
+    elif before == "drift":
+        earlier = [[(s * dtype(1.02) - dtype(0.01)).astype(dtype) for s in segs],
+                   [(s * dtype(1.01) + dtype(0.003)).astype(dtype) for s in segs]]
+    else:
+        earlier = [_segments(4, dtype), _segments(5, dtype)]
+    got = _probe(segs, precision, earlier=earlier)
+    want = np.array([_median_update(s, dtype) for s in segs])
+    bad = np.nonzero(got.view(np.uint64) != want.view(np.uint64))[0]
+    assert bad.size == 0, [(len(segs[i]), got[i], want[i]) for i in bad[:10]]
+
+
+@pytest.mark.parametrize("precision,dtype,tol", [(0, np.float32, 1e-5), (1, np.float64, 1e-12)])
+def test_percentile_from_carried_windows(gpu, precision, dtype, tol):
+    segs = _segments(8, dtype)
+    got = _probe(segs, precision, update_with_mean=1, pct=37, earlier=[_segments(9, dtype), segs])
+    for i, x in enumerate(segs):
+        if x.size == 0:
+            continue
+        s = np.sort((dtype(2) + x.astype(dtype)).astype(np.float64))
+        jm = min(max(int(0.37 * s.size), 1), s.size)
+        want = s[:jm].mean() * 0.5
         assert abs(got[i] - want) <= tol * max(1.0, abs(want)) * 8, (i, s.size, got[i], want)
