@@ -264,13 +264,20 @@ __device__ Sel<K> sel64(const K* c, uint32_t n, uint32_t k, int lane) {
     return r;
 }
 
+// Outcome of a window pass.
+enum WinStatus { kWinCand = 0, kWinEqual = 1, kWinFail = 2 };
+
 // One pass over n keys with the window [lo, hi]: counts the keys below it
 // and appends those inside to the lane's own column of `out` (no cross-lane
-// compaction).  Returns false when the window misses rank k, overflows
-// `out_rows` or keeps everything; otherwise `res` holds the candidates.
+// compaction).  kWinCand: `res` holds the candidates and rank k is among
+// them.  kWinEqual: the window is one key value and holds rank k, so that
+// value is the answer, written to *direct (runs of equal keys need no more
+// rounds).  kWinFail: the window misses rank k, overflows `out_rows` or
+// keeps everything.
 template <typename K, class Src>
-__device__ __forceinline__ bool window_pass(const Src& v, uint32_t n, uint32_t k, K lo, K hi, K* out,
-                                            uint32_t out_rows, int lane, Ragged<K>& res, uint32_t& below) {
+__device__ __forceinline__ int window_pass(const Src& v, uint32_t n, uint32_t k, K lo, K hi, K* out,
+                                           uint32_t out_rows, int lane, Ragged<K>& res, uint32_t& below,
+                                           Sel<K>* direct) {
     uint32_t c_lo = 0, t = 0;
     const uint32_t nr = v.rows();
 #pragma unroll
@@ -290,14 +297,24 @@ __device__ __forceinline__ bool window_pass(const Src& v, uint32_t n, uint32_t k
     res.t = t;
     res.nrows = rows;
     res.lane = lane;
-    return rows <= out_rows && below <= k && k < below + n_in && n_in < n;
+    const bool hit = below <= k && k < below + n_in;
+    if (hit && lo == hi) {
+        direct->kth = lo;
+        direct->prev = lo;
+        direct->have_prev = k > below;
+        direct->wlo = lo;
+        direct->whi = lo;
+        direct->nfin = n_in;
+        return kWinEqual;
+    }
+    return hit && rows <= out_rows && n_in < n ? kWinCand : kWinFail;
 }
 
 // One sampling round: the (up to 32) samples are sorted in the warp and the
 // window is the keys within 6 sample ranks of rank k (window_pass).
 template <typename K, class Src>
-__device__ __forceinline__ bool sample_round(const Src& v, uint32_t n, uint32_t k, K* out, uint32_t out_rows,
-                                             int lane, Ragged<K>& res, uint32_t& below) {
+__device__ __forceinline__ int sample_round(const Src& v, uint32_t n, uint32_t k, K* out, uint32_t out_rows,
+                                            int lane, Ragged<K>& res, uint32_t& below, Sel<K>* direct) {
     const K smp = v.sample();
     const uint32_t ns = __popc(__ballot_sync(kFull, smp != empty_key<K>()));
     const K s = sort32(smp, lane);  // empty samples sort last
@@ -307,7 +324,7 @@ __device__ __forceinline__ bool sample_round(const Src& v, uint32_t n, uint32_t 
     const K shi = __shfl_sync(kFull, s, qh > 31 ? 31 : (qh < 0 ? 0 : qh));
     const K lo = ql <= 0 ? K(0) : slo;
     const K hi = qh >= static_cast<int>(ns) - 1 ? empty_key<K>() - 1 : shi;
-    return window_pass<K>(v, n, k, lo, hi, out, out_rows, lane, res, below);
+    return window_pass<K>(v, n, k, lo, hi, out, out_rows, lane, res, below, direct);
 }
 
 // Order statistics kk and kk-1 of the candidates in `cur`, exact: more
@@ -326,7 +343,12 @@ __device__ __noinline__ Sel<K> select_candidates(K* cur_buf, K* oth_buf, uint32_
     for (int round = 0; n > 64 && round < 8; ++round) {
         Ragged<K> nxt;
         uint32_t b2;
-        if (!sample_round<K>(cur, n, kk, oth, cap_rows, lane, nxt, b2)) {
+        const int st = sample_round<K>(cur, n, kk, oth, cap_rows, lane, nxt, b2, &r);
+        if (st == kWinEqual) {
+            __syncwarp();
+            return r;
+        }
+        if (st == kWinFail) {
             r.kth = kth_radix<K>(cur, kk);
             __syncwarp();
             return r;
@@ -375,8 +397,13 @@ __device__ Sel<K> kth_select(const Src& v, uint32_t M, uint32_t k, K* a, K* b, u
     }
     Ragged<K> cur;
     uint32_t b1;
-    if (!sample_round<K>(v, M, k, a, cap_rows, lane, cur, b1)) {
-        Sel<K> r;
+    Sel<K> r;
+    const int st = sample_round<K>(v, M, k, a, cap_rows, lane, cur, b1, &r);
+    if (st == kWinEqual) {
+        __syncwarp();
+        return r;
+    }
+    if (st == kWinFail) {
         r.have_prev = false;
         r.nfin = 0;
         r.kth = kth_radix<K>(v, k);
@@ -396,7 +423,14 @@ __device__ Sel<K> kth_select_from(const Src& v, uint32_t M, uint32_t k, K lo, K 
     if (M > 64) {
         Ragged<K> cur;
         uint32_t b1;
-        if (window_pass<K>(v, M, k, lo, hi, a, cap_rows, lane, cur, b1)) {
+        Sel<K> r;
+        const int st = window_pass<K>(v, M, k, lo, hi, a, cap_rows, lane, cur, b1, &r);
+        if (st == kWinEqual) {
+            *hit = true;
+            __syncwarp();
+            return r;
+        }
+        if (st == kWinCand) {
             *hit = true;
             return select_candidates<K>(a, b, cap_rows, cur.t, cur.nrows, __reduce_add_sync(kFull, cur.t), k - b1,
                                         lane);
