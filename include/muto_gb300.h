@@ -91,7 +91,8 @@ typedef struct muto_handle muto_handle;
  * "compute_cost" (computed when early_stop/log_results is set, or when true),
  * "newton_max_iter" (MAP cubic cap, 200), "tile_pairs" (pairs per TMA tile),
  * "muon_pass" ("auto": the warp-batched variant, its group size chosen by
- * timing on the scan's data at prepare; "tile" or "warp" force one),
+ * timing on the scan's data at prepare and reused for later scans of the
+ * same shape in the process; "tile" or "warp" force one),
  * "voxel_stream_above" (-1: every segment up to 1536 pairs (768 in fp64)
  * is selected from registers; n >= 256: segments longer than n are
  * selected without holding their keys). */

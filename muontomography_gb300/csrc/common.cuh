@@ -109,10 +109,12 @@ void launch_path_fill(const muto_ray* rays, const uint32_t* kept, const double* 
 void launch_offset_voxels(uint32_t* vidx, uint64_t n, uint32_t v_scan, uint32_t voff, cudaStream_t s);
 void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* mult, Counters* ctr, cudaStream_t s);
 // voxel-major copy of the pair lists: (muon, L, T) at start[j] + rank within voxel j
+// (rec: P staging records, free after the call's work is done)
 template <typename Real>
 void launch_build_voxel_major(const uint64_t* off, uint64_t n, const uint32_t* vidx, const Real* L, const Real* T,
-                              uint32_t V, const uint64_t* start, uint32_t* cursor, uint32_t* vm_mu,
-                              typename Vec2<Real>::type* vm_LT, cudaStream_t s);
+                              uint32_t V, const uint64_t* start, uint32_t* cursor, uint64_t P,
+                              typename Vec4<Real>::type* rec, uint32_t* vm_mu, typename Vec2<Real>::type* vm_LT,
+                              cudaStream_t s);
 void launch_siddon_batch(muto_grid g, const double* p1, const double* p2, uint64_t n, uint32_t cap, uint32_t* xyz,
                          double* len, uint32_t* counts, cudaStream_t s);
 

@@ -10,10 +10,12 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <random>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/muto_gb300.h"
@@ -612,10 +614,12 @@ void prepare_em(muto_handle* h) {
         CK(cudaMemsetAsync(cursor.as<void>(), 0, V * sizeof(uint32_t), s));
         h->vm_mu.alloc((Pn + kPad) * sizeof(uint32_t), &h->dev_bytes);
         h->vm_LT.alloc((Pn + kPad) * sizeof(typename Vec2<Real>::type), &h->dev_bytes);
+        DevMem staging;
+        staging.alloc(std::max<uint64_t>(Pn, 1) * sizeof(R4), &h->dev_bytes);
         run(h, "voxel_major", [&] {
             launch_build_voxel_major<Real>(h->off.as<uint64_t>(), N, h->vidx.as<uint32_t>(), h->L.as<Real>(),
                                            h->T.as<Real>(), static_cast<uint32_t>(V), h->start.as<uint64_t>(),
-                                           cursor.as<uint32_t>(), h->vm_mu.as<uint32_t>(),
+                                           cursor.as<uint32_t>(), Pn, staging.as<R4>(), h->vm_mu.as<uint32_t>(),
                                            h->vm_LT.as<typename Vec2<Real>::type>(), s);
         });
         CK(cudaStreamSynchronize(s));
@@ -748,12 +752,38 @@ MuonPassArgs<Real> muon_args(muto_handle* h, const Real* lam, bool cost) {
     return a;
 }
 
+// Choices of the muon-pass tuner, kept for the process: scans of the same
+// shape (precision, device, muons to within a factor of 2, mean path to
+// within 8 voxels) reuse the choice instead of timing again.
+struct TuneShape {
+    int fp64, device, log2n, path8;
+    bool operator<(const TuneShape& o) const {
+        return std::tie(fp64, device, log2n, path8) < std::tie(o.fp64, o.device, o.log2n, o.path8);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneShape, std::pair<int, int>> g_tune_choice;
+
 // In-project autotuner: time the candidate muon-pass variants on this scan's
 // own lists (one warm-up and two timed launches each) and keep the fastest.
 template <typename Real>
 void autotune_muon_pass(muto_handle* h) {
     if (h->N == 0) return;
     HostPhase ph(h, "autotune");
+    int log2n = 0;
+    while ((h->N >> log2n) > 1) ++log2n;
+    const TuneShape shape{h->fp64() ? 1 : 0, h->device, log2n,
+                          static_cast<int>(static_cast<double>(h->npairs) / static_cast<double>(h->N) / 8.0)};
+    if (h->P.muon_pass == 0) {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        const auto it = g_tune_choice.find(shape);
+        if (it != g_tune_choice.end()) {
+            h->muon_kind = it->second.first;
+            h->muon_group = it->second.second;
+            if (h->muon_kind == 2) h->warp_blocks = em_muon_warp_blocks<Real>(h->muon_group) * h->num_sms;
+            return;
+        }
+    }
     struct Cand {
         int kind, group;
     };
@@ -806,6 +836,10 @@ void autotune_muon_pass(muto_handle* h) {
     cudaEventDestroy(e1);
     h->launches += 3 * cands.size();
     apply(pick);
+    if (h->P.muon_pass == 0) {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_choice[shape] = {pick.kind, pick.group};
+    }
     CK(cudaMemcpyAsync(h->ctr(), &saved, sizeof(Counters), cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
 }

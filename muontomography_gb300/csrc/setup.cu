@@ -202,13 +202,24 @@ __global__ void k_voxel_hist(const uint32_t* __restrict__ vidx, uint64_t P, uint
     warp_count(&ctr->bounds, bad);
 }
 
-// warp per muon: its pairs, read coalesced, go to the voxel-major lists in
-// their voxels' segments (a slot per pair from the voxel's cursor)
+template <typename Real> __device__ __forceinline__ Real index_bits(uint32_t i);
+template <> __device__ __forceinline__ float index_bits<float>(uint32_t i) { return __uint_as_float(i); }
+template <> __device__ __forceinline__ double index_bits<double>(uint32_t i) {
+    return __longlong_as_double(static_cast<long long>(i));
+}
+__device__ __forceinline__ uint32_t bits_index(float x) { return __float_as_uint(x); }
+__device__ __forceinline__ uint32_t bits_index(double x) { return static_cast<uint32_t>(__double_as_longlong(x)); }
+
+// Voxel-major lists in two steps.  First a warp per muon reads its pairs
+// coalesced and scatters each as one record (muon, L, T) to its slot in its
+// voxel's segment (one aligned store per pair: scattered partial stores of
+// the separate arrays cost twice as much).  Then a coalesced pass splits the
+// records into the muon and (L, T) arrays the voxel pass streams.
 template <typename Real>
 __global__ void k_build_voxel_major(const uint64_t* __restrict__ off, uint64_t n, const uint32_t* __restrict__ vidx,
                                     const Real* __restrict__ L, const Real* __restrict__ T, uint32_t V,
                                     const uint64_t* __restrict__ start, uint32_t* __restrict__ cursor,
-                                    uint32_t* __restrict__ vm_mu, typename Vec2<Real>::type* __restrict__ vm_LT) {
+                                    typename Vec4<Real>::type* __restrict__ rec) {
     const uint64_t i = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= n) return;
@@ -217,12 +228,26 @@ __global__ void k_build_voxel_major(const uint64_t* __restrict__ off, uint64_t n
         const uint32_t j = vidx[p];
         if (j >= V) continue;  // counted by k_voxel_hist
         const uint64_t at = start[j] + atomicAdd(&cursor[j], 1u);
-        vm_mu[at] = static_cast<uint32_t>(i);
-        typename Vec2<Real>::type lt;
-        lt.x = L[p];
-        lt.y = T[p];
-        vm_LT[at] = lt;
+        typename Vec4<Real>::type r;
+        r.x = index_bits<Real>(static_cast<uint32_t>(i));  // the index's bits, moved, never computed on
+        r.y = L[p];
+        r.z = T[p];
+        r.w = Real(0);
+        rec[at] = r;
     }
+}
+
+template <typename Real>
+__global__ void k_split_records(const typename Vec4<Real>::type* __restrict__ rec, uint64_t P,
+                                uint32_t* __restrict__ vm_mu, typename Vec2<Real>::type* __restrict__ vm_LT) {
+    const uint64_t p = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const typename Vec4<Real>::type r = rec[p];
+    vm_mu[p] = bits_index(r.x);
+    typename Vec2<Real>::type lt;
+    lt.x = r.y;
+    lt.y = r.z;
+    vm_LT[p] = lt;
 }
 
 struct BatchSink {
@@ -354,18 +379,22 @@ void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* m
 
 template <typename Real>
 void launch_build_voxel_major(const uint64_t* off, uint64_t n, const uint32_t* vidx, const Real* L, const Real* T,
-                              uint32_t V, const uint64_t* start, uint32_t* cursor, uint32_t* vm_mu,
-                              typename Vec2<Real>::type* vm_LT, cudaStream_t s) {
+                              uint32_t V, const uint64_t* start, uint32_t* cursor, uint64_t P,
+                              typename Vec4<Real>::type* rec, uint32_t* vm_mu, typename Vec2<Real>::type* vm_LT,
+                              cudaStream_t s) {
     if (n == 0) return;
-    k_build_voxel_major<Real><<<blocks_for(n * 32), kThreads, 0, s>>>(off, n, vidx, L, T, V, start, cursor, vm_mu,
-                                                                      vm_LT);
+    k_build_voxel_major<Real><<<blocks_for(n * 32), kThreads, 0, s>>>(off, n, vidx, L, T, V, start, cursor, rec);
+    count_launches(1);
+    if (P == 0) return;
+    k_split_records<Real><<<blocks_for(P), kThreads, 0, s>>>(rec, P, vm_mu, vm_LT);
     count_launches(1);
 }
 template void launch_build_voxel_major<float>(const uint64_t*, uint64_t, const uint32_t*, const float*, const float*,
-                                              uint32_t, const uint64_t*, uint32_t*, uint32_t*, float2*, cudaStream_t);
+                                              uint32_t, const uint64_t*, uint32_t*, uint64_t, float4*, uint32_t*,
+                                              float2*, cudaStream_t);
 template void launch_build_voxel_major<double>(const uint64_t*, uint64_t, const uint32_t*, const double*,
-                                               const double*, uint32_t, const uint64_t*, uint32_t*, uint32_t*,
-                                               double2*, cudaStream_t);
+                                               const double*, uint32_t, const uint64_t*, uint32_t*, uint64_t,
+                                               double4*, uint32_t*, double2*, cudaStream_t);
 
 void launch_siddon_batch(muto_grid g, const double* p1, const double* p2, uint64_t n, uint32_t cap, uint32_t* xyz,
                          double* len, uint32_t* counts, cudaStream_t s) {
