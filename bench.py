@@ -127,7 +127,7 @@ TRAFFIC_PER_PAIR = {"muon": 868.4e6 / 68700086, "voxel": 964.4e6 / 68700086}
 
 # set-up kernels and host phases reported by the library's profiler
 SETUP_KERNELS = ["keep_flags", "scan", "compact", "muon_info", "siddon_count", "siddon_fill", "voxel_offset",
-                 "voxel_hist", "voxel_major", "voxel_classes"]
+                 "voxel_hist", "voxel_major", "voxel_classes", "path_bound", "path_compact"]
 SETUP_PHASES = ["gather", "info_count", "offsets", "fill", "voxel_major", "classes", "tiles", "image", "autotune"]
 
 

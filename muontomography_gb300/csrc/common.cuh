@@ -82,7 +82,7 @@ struct Counters {
     double cost_sum;                // cost of the current iteration
     double cost_last;               // mean cost of the last finished iteration
     double cost_prev;               // mean cost of the one before
-    double pad2;
+    unsigned long long over_bound;  // paths longer than their set-up bound (then counted exactly)
 };
 
 // ---------------------------------------------------------------------------
@@ -105,6 +105,21 @@ void launch_path_count(const muto_ray* rays, const uint32_t* kept, const double*
 template <typename Real>
 void launch_path_fill(const muto_ray* rays, const uint32_t* kept, const double* scat, const uint64_t* off, uint64_t n,
                       muto_grid g, int straight, uint32_t* vidx, double* l64, Real* L, Real* T, cudaStream_t s);
+// Single-walk set-up: an upper bound on every kept muon's merged path
+// (index spans of the pieces on the grid, FP32, with a margin of 2 per axis
+// and end), the walk into slots sized by those bounds with the actual
+// counts, and the compaction to slots sized by the counts.  A path longer
+// than its bound (never expected) is counted in ctr->over_bound and the
+// caller falls back to the exact count walk.
+void launch_path_bound(const muto_ray* rays, const uint32_t* kept, const double* scat, uint64_t n, muto_grid g,
+                       int straight, uint32_t* bounds, cudaStream_t s);
+template <typename Real>
+void launch_path_fill_bounded(const muto_ray* rays, const uint32_t* kept, const double* scat, const uint64_t* boff,
+                              uint64_t n, muto_grid g, int straight, uint32_t* vidx, double* l64, Real* L, Real* T,
+                              uint32_t* counts, Counters* ctr, cudaStream_t s);
+template <typename Real>
+void launch_path_compact(const uint64_t* boff, const uint64_t* off, uint64_t n, const uint32_t* vidx_b,
+                         const Real* L_b, const Real* T_b, uint32_t* vidx, Real* L, Real* T, cudaStream_t s);
 // scan-local voxel indices j < V_scan become voff + j; others become 0xffffffff
 void launch_offset_voxels(uint32_t* vidx, uint64_t n, uint32_t v_scan, uint32_t voff, cudaStream_t s);
 void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* mult, Counters* ctr, cudaStream_t s);

@@ -527,6 +527,9 @@ void prepare_em(muto_handle* h) {
     h->pr2.alloc((N + kPad) * sizeof(Real), &h->dev_bytes);
     h->scat.alloc(std::max<uint64_t>(N, 1) * 3 * sizeof(double), &h->dev_bytes);
     h->pr64.alloc(std::max<uint64_t>(N, 1) * sizeof(double), &h->dev_bytes);
+    // --- merged paths: one walk per muon into slots sized by an upper bound
+    // on its path, then compaction to the exact slots (the walk is FP64 and
+    // the set-up's costliest step, so it is not run twice to count first) ---
     DevMem counts;
     counts.alloc(std::max<uint64_t>(N, 1) * sizeof(uint32_t), &h->dev_bytes);
     ph.reset(new HostPhase(h, "info_count"));
@@ -541,17 +544,55 @@ void prepare_em(muto_handle* h) {
             launch_muon_info<Real>(r, kept, sc.N, sc.grid, P.eps, P.has_energy, h->sd.as<R4>() + sc.noff,
                                    h->pr2.as<Real>() + sc.noff, scat, h->pr64.as<double>() + sc.noff, s);
         });
-        // --- path lengths (count walk) ---
-        run(h, "siddon_count", [&] {
-            launch_path_count(r, kept, scat, sc.N, sc.grid, P.straight_line, counts.as<uint32_t>() + sc.noff,
-                              h->ctr(), s);
+        run(h, "path_bound", [&] {
+            launch_path_bound(r, kept, scat, sc.N, sc.grid, P.straight_line, counts.as<uint32_t>() + sc.noff, s);
         });
     }
     flags.release();
     pos.clear();
     if (scratch.bytes() < scan_scratch_bytes(std::max<uint64_t>(N, V) + 1))
         scratch.alloc(scan_scratch_bytes(std::max<uint64_t>(N, V) + 1), &h->dev_bytes);
-    ph.reset(new HostPhase(h, "offsets"));
+    ph.reset(new HostPhase(h, "fill"));
+    DevMem boff;
+    boff.alloc((N + 1) * sizeof(uint64_t), &h->dev_bytes);
+    run(h, "scan", [&] { scan_u32_to_u64(counts.as<uint32_t>(), boff.as<uint64_t>(), N, scratch.as<void>(), s); });
+    uint64_t Pb = 0;
+    CK(cudaMemcpyAsync(&Pb, boff.as<uint64_t>() + N, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const bool real64 = std::is_same<Real, double>::value;
+    DevMem vidx_b, l64_b, L_b, T_b;
+    vidx_b.alloc((Pb + kPad) * sizeof(uint32_t), &h->dev_bytes);
+    l64_b.alloc((Pb + kPad) * sizeof(double), &h->dev_bytes);
+    if (!real64) L_b.alloc((Pb + kPad) * sizeof(Real), &h->dev_bytes);
+    T_b.alloc((Pb + kPad) * sizeof(Real), &h->dev_bytes);
+    Real* Lb = real64 ? reinterpret_cast<Real*>(l64_b.as<double>()) : L_b.as<Real>();
+    for (size_t k = 0; k < S; ++k) {
+        const auto& sc = h->scans[k];
+        run(h, "siddon_fill", [&] {
+            launch_path_fill_bounded<Real>(h->scan_rays(k), h->kept.as<uint32_t>() + sc.noff,
+                                           h->scat.as<double>() + 3 * sc.noff, boff.as<uint64_t>() + sc.noff, sc.N,
+                                           sc.grid, P.straight_line, vidx_b.as<uint32_t>(), l64_b.as<double>(), Lb,
+                                           T_b.as<Real>(), counts.as<uint32_t>() + sc.noff, h->ctr(), s);
+        });
+    }
+    unsigned long long over_bound = 0;
+    CK(cudaMemcpyAsync(&over_bound, &h->ctr()->over_bound, sizeof(over_bound), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (over_bound > 0) {  // a bound was short (never expected): count exactly, walk again below
+        vidx_b.release();
+        l64_b.release();
+        L_b.release();
+        T_b.release();
+        CK(cudaMemsetAsync(&h->ctr()->overflow, 0, sizeof(unsigned long long), s));
+        for (size_t k = 0; k < S; ++k) {
+            const auto& sc = h->scans[k];
+            run(h, "siddon_count", [&] {
+                launch_path_count(h->scan_rays(k), h->kept.as<uint32_t>() + sc.noff,
+                                  h->scat.as<double>() + 3 * sc.noff, sc.N, sc.grid, P.straight_line,
+                                  counts.as<uint32_t>() + sc.noff, h->ctr(), s);
+            });
+        }
+    }
     h->off.alloc((N + 1 + kPad) * sizeof(uint64_t), &h->dev_bytes);
     run(h, "scan", [&] { scan_u32_to_u64(counts.as<uint32_t>(), h->off.as<uint64_t>(), N, scratch.as<void>(), s); });
     counts.release();
@@ -570,14 +611,18 @@ void prepare_em(muto_handle* h) {
     const uint64_t Pn = scan_off[S];
     h->npairs = Pn;
 
-    ph.reset(new HostPhase(h, "fill"));
     h->vidx.alloc((Pn + kPad) * sizeof(uint32_t), &h->dev_bytes);
     h->L.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
     h->T.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
-    {
+    if (over_bound == 0) {
+        run(h, "path_compact", [&] {
+            launch_path_compact<Real>(boff.as<uint64_t>(), h->off.as<uint64_t>(), N, vidx_b.as<uint32_t>(), Lb,
+                                      T_b.as<Real>(), h->vidx.as<uint32_t>(), h->L.as<Real>(), h->T.as<Real>(), s);
+        });
+    } else {
         DevMem l64tmp;
         double* l64 = reinterpret_cast<double*>(h->L.as<Real>());
-        if (!std::is_same<Real, double>::value) {
+        if (!real64) {
             l64tmp.alloc(std::max<uint64_t>(Pn, 1) * sizeof(double), &h->dev_bytes);
             l64 = l64tmp.as<double>();
         }
@@ -589,17 +634,26 @@ void prepare_em(muto_handle* h) {
                                        sc.grid, P.straight_line, h->vidx.as<uint32_t>(), l64, h->L.as<Real>(),
                                        h->T.as<Real>(), s);
             });
-            // scan-local voxel indices into the batch's voxel space
-            if (h->batch) {
-                const uint64_t pb = scan_off[k], pe = scan_off[k + 1];
-                run(h, "voxel_offset", [&] {
-                    launch_offset_voxels(h->vidx.as<uint32_t>() + pb, pe - pb, static_cast<uint32_t>(sc.V),
-                                         static_cast<uint32_t>(sc.voff), s);
-                });
-            }
         }
         CK(cudaStreamSynchronize(s));
     }
+    // scan-local voxel indices into the batch's voxel space
+    if (h->batch) {
+        for (size_t k = 0; k < S; ++k) {
+            const auto& sc = h->scans[k];
+            const uint64_t pb = scan_off[k], pe = scan_off[k + 1];
+            run(h, "voxel_offset", [&] {
+                launch_offset_voxels(h->vidx.as<uint32_t>() + pb, pe - pb, static_cast<uint32_t>(sc.V),
+                                     static_cast<uint32_t>(sc.voff), s);
+            });
+        }
+    }
+    CK(cudaStreamSynchronize(s));
+    vidx_b.release();
+    l64_b.release();
+    L_b.release();
+    T_b.release();
+    boff.release();
 
     // --- multiplicity M_j and the voxel-major copy of the lists ---------------
     ph.reset(new HostPhase(h, "voxel_major"));

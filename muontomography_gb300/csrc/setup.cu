@@ -182,6 +182,101 @@ __global__ void k_path_fill(const muto_ray* __restrict__ rays, const uint32_t* _
     }
 }
 
+// voxels a walk of a -> b can record: 1 + the index span on each axis of
+// the endpoints clamped to the grid (the pieces on the grid lie between
+// them), +2 per axis for rounding at either end
+__device__ __forceinline__ uint32_t walk_bound(const DevGrid& g, const double* a, const double* b) {
+    uint32_t n = 1;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float lo = static_cast<float>(g.lo[k]), w = static_cast<float>(g.w[k]);
+        const float top = static_cast<float>(g.n[k] - 1);
+        const float ia = fminf(fmaxf(floorf((static_cast<float>(a[k]) - lo) / w), 0.f), top);
+        const float ib = fminf(fmaxf(floorf((static_cast<float>(b[k]) - lo) / w), 0.f), top);
+        n += static_cast<uint32_t>(fabsf(ia - ib)) + 2u;
+    }
+    return n;
+}
+
+__global__ void k_path_bound(const muto_ray* __restrict__ rays, const uint32_t* __restrict__ kept,
+                             const double* __restrict__ scat, uint64_t n, DevGrid g, int straight,
+                             uint32_t* __restrict__ bounds) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const muto_ray& r = rays[kept[i]];
+    if (straight) {
+        bounds[i] = walk_bound(g, r.pin, r.pout);
+    } else {
+        const double ps[3] = {scat[3 * i], scat[3 * i + 1], scat[3 * i + 2]};
+        bounds[i] = walk_bound(g, r.pin, ps) + walk_bound(g, ps, r.pout);
+    }
+}
+
+// the fill walk into bounded slots [boff[i], boff[i+1]); counts[i] = the
+// path's length (0 for a walk that hit its step guard, as in the count walk)
+template <typename Real>
+__global__ void k_path_fill_bounded(const muto_ray* __restrict__ rays, const uint32_t* __restrict__ kept,
+                                    const double* __restrict__ scat, const uint64_t* __restrict__ boff, uint64_t n,
+                                    DevGrid g, int straight, uint32_t* __restrict__ vidx, double* __restrict__ l64,
+                                    Real* __restrict__ L, Real* __restrict__ T, uint32_t* __restrict__ counts,
+                                    Counters* ctr) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t b = boff[i], e = boff[i + 1];
+    const muto_ray& r = rays[kept[i]];
+    const double ps[3] = {scat[3 * i], scat[3 * i + 1], scat[3 * i + 2]};
+    const uint32_t nx = g.n[0], nxy = g.n[0] * g.n[1];
+    uint64_t end;
+    bool overflow = false;
+    if (straight) {
+        StraightSink s{vidx, l64, b, e, nx, nxy};
+        overflow = siddon_walk(g, r.pin, r.pout, s) < 0;
+        end = s.pos;
+    } else {
+        FillSink s{vidx, l64, b, e, nx, nxy};
+        const int ci = siddon_walk(g, r.pin, ps, s);
+        s.phase = 1;
+        const int co = siddon_walk(g, ps, r.pout, s);
+        if (s.pending) s.emit(s.pj, dadd(s.pl, 0.0));  // out-half empty: length += 0.0
+        overflow = ci < 0 || co < 0;
+        end = s.pos;
+    }
+    if (overflow) {  // dropped, like the count walk does
+        atomicAdd(&ctr->overflow, 1ull);
+        end = b;
+    }
+    if (end > e) {
+        atomicAdd(&ctr->over_bound, 1ull);
+        end = e;
+    }
+    counts[i] = static_cast<uint32_t>(end - b);
+    // tail lengths, summed backwards in FP64 like src/MutoMLSD.cpp:407-413
+    double t = 0.0;
+    for (uint64_t k = end; k-- > b;) {
+        const double lk = l64[k];
+        if (L != reinterpret_cast<Real*>(l64)) L[k] = static_cast<Real>(lk);
+        T[k] = static_cast<Real>(t);
+        t = dadd(t, lk);
+    }
+}
+
+// warp per muon: its path from the bounded slots to the exact ones
+template <typename Real>
+__global__ void k_path_compact(const uint64_t* __restrict__ boff, const uint64_t* __restrict__ off, uint64_t n,
+                               const uint32_t* __restrict__ vidx_b, const Real* __restrict__ L_b,
+                               const Real* __restrict__ T_b, uint32_t* __restrict__ vidx, Real* __restrict__ L,
+                               Real* __restrict__ T) {
+    const uint64_t i = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const uint64_t src = boff[i], dst = off[i], m = off[i + 1] - dst;
+    for (uint64_t k = lane; k < m; k += 32) {
+        vidx[dst + k] = vidx_b[src + k];
+        L[dst + k] = L_b[src + k];
+        T[dst + k] = T_b[src + k];
+    }
+}
+
 __global__ void k_offset_voxels(uint32_t* __restrict__ vidx, uint64_t n, uint32_t v_scan, uint32_t voff) {
     const uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (k < n) {
@@ -365,6 +460,41 @@ template void launch_path_fill<float>(const muto_ray*, const uint32_t*, const do
                                       muto_grid, int, uint32_t*, double*, float*, float*, cudaStream_t);
 template void launch_path_fill<double>(const muto_ray*, const uint32_t*, const double*, const uint64_t*, uint64_t,
                                        muto_grid, int, uint32_t*, double*, double*, double*, cudaStream_t);
+
+void launch_path_bound(const muto_ray* rays, const uint32_t* kept, const double* scat, uint64_t n, muto_grid g,
+                       int straight, uint32_t* bounds, cudaStream_t s) {
+    if (n == 0) return;
+    k_path_bound<<<blocks_for(n), kThreads, 0, s>>>(rays, kept, scat, n, make_dev_grid(g), straight, bounds);
+    count_launches(1);
+}
+
+template <typename Real>
+void launch_path_fill_bounded(const muto_ray* rays, const uint32_t* kept, const double* scat, const uint64_t* boff,
+                              uint64_t n, muto_grid g, int straight, uint32_t* vidx, double* l64, Real* L, Real* T,
+                              uint32_t* counts, Counters* ctr, cudaStream_t s) {
+    if (n == 0) return;
+    k_path_fill_bounded<Real><<<blocks_for(n, 128), 128, 0, s>>>(rays, kept, scat, boff, n, make_dev_grid(g), straight,
+                                                                  vidx, l64, L, T, counts, ctr);
+    count_launches(1);
+}
+template void launch_path_fill_bounded<float>(const muto_ray*, const uint32_t*, const double*, const uint64_t*,
+                                              uint64_t, muto_grid, int, uint32_t*, double*, float*, float*, uint32_t*,
+                                              Counters*, cudaStream_t);
+template void launch_path_fill_bounded<double>(const muto_ray*, const uint32_t*, const double*, const uint64_t*,
+                                               uint64_t, muto_grid, int, uint32_t*, double*, double*, double*,
+                                               uint32_t*, Counters*, cudaStream_t);
+
+template <typename Real>
+void launch_path_compact(const uint64_t* boff, const uint64_t* off, uint64_t n, const uint32_t* vidx_b,
+                         const Real* L_b, const Real* T_b, uint32_t* vidx, Real* L, Real* T, cudaStream_t s) {
+    if (n == 0) return;
+    k_path_compact<Real><<<blocks_for(n * 32), kThreads, 0, s>>>(boff, off, n, vidx_b, L_b, T_b, vidx, L, T);
+    count_launches(1);
+}
+template void launch_path_compact<float>(const uint64_t*, const uint64_t*, uint64_t, const uint32_t*, const float*,
+                                         const float*, uint32_t*, float*, float*, cudaStream_t);
+template void launch_path_compact<double>(const uint64_t*, const uint64_t*, uint64_t, const uint32_t*, const double*,
+                                          const double*, uint32_t*, double*, double*, cudaStream_t);
 
 void launch_offset_voxels(uint32_t* vidx, uint64_t n, uint32_t v_scan, uint32_t voff, cudaStream_t s) {
     if (n == 0) return;
