@@ -135,7 +135,8 @@ int muto_set_image(muto_handle* h, const double* img, uint64_t len);
 
 /* Batched MutoSiddon::getVoxelPath (src/MutoSiddon.cpp:9-141) on the GPU.
  * Host buffers.  Ray r's voxels go to xyz[(r*cap+k)*3 + {0,1,2}] and
- * len[r*cap+k] for k < min(counts[r], cap); counts[r] is the full count. */
+ * len[r*cap+k] for k < min(counts[r], cap); counts[r] is the full count;
+ * the slots past it are 0. */
 int muto_siddon_batch(const muto_grid* g, const double* p1, const double* p2, uint64_t n, uint32_t cap,
                       uint32_t* xyz, double* len, uint32_t* counts);
 
@@ -147,7 +148,7 @@ int muto_siddon_batch(const muto_grid* g, const double* p1, const double* p2, ui
  * has none left to give, and a loop that keeps other streams of the device
  * busy (data acquisition, online monitoring) cannot take the device-wide
  * synchronisation that cudaFree performs.  Inputs, outputs and errors are
- * those of muto_siddon_batch; slots past min(counts[r], cap) come back 0.
+ * those of muto_siddon_batch.
  * The work runs on `stream` (a cudaStream_t; NULL is the legacy default
  * stream) and the call returns when it is done.
  *

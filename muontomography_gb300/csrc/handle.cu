@@ -46,6 +46,31 @@ struct Error : std::runtime_error {
                         std::string(#call) + ": " + cudaGetErrorString(e_));                           \
     } while (0)
 
+// Device memory comes from one pool per device that keeps freed blocks
+// mapped, so the next handle (the next scan) reuses them instead of paying
+// for new mappings; the pool grows to the largest working set seen.  Frees
+// keep cudaFree's ordering: they wait for the device to be idle first.
+cudaMemPool_t device_pool(int dev) {
+    constexpr int kMaxDevices = 64;
+    static std::once_flag once[kMaxDevices];
+    static cudaMemPool_t pools[kMaxDevices];
+    static cudaError_t errs[kMaxDevices];
+    if (dev < 0 || dev >= kMaxDevices) throw Error(MUTO_ERR_CUDA, "device ordinal out of range");
+    std::call_once(once[dev], [dev] {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        errs[dev] = cudaMemPoolCreate(&pools[dev], &props);
+        if (errs[dev] == cudaSuccess) {
+            unsigned long long keep = ~0ull;
+            errs[dev] = cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    });
+    CK(errs[dev]);
+    return pools[dev];
+}
+
 // Owned device allocation.
 class DevMem {
 public:
@@ -56,14 +81,18 @@ public:
     void alloc(size_t bytes, std::atomic<uint64_t>* tally) {
         release();
         if (bytes == 0) bytes = 16;
-        CK(cudaMalloc(&p_, bytes));
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaMallocFromPoolAsync(&p_, bytes, device_pool(dev), 0));
+        CK(cudaStreamSynchronize(0));  // usable from any stream once this returns
         bytes_ = bytes;
         tally_ = tally;
         if (tally_) *tally_ += bytes_;
     }
     void release() {
         if (p_) {
-            cudaFree(p_);
+            cudaDeviceSynchronize();
+            cudaFreeAsync(p_, 0);
             if (tally_) *tally_ -= bytes_;
         }
         p_ = nullptr;
@@ -1419,6 +1448,10 @@ int muto_siddon_batch(const muto_grid* g, const double* p1, const double* p2, ui
         dx.alloc(std::max<uint64_t>(n * cap, 1) * 3 * sizeof(uint32_t), nullptr);
         dl.alloc(std::max<uint64_t>(n * cap, 1) * sizeof(double), nullptr);
         dc.alloc(n * sizeof(uint32_t), nullptr);
+        if (cap > 0) {  // slots past a ray's count read as 0
+            CK(cudaMemsetAsync(dx.as<void>(), 0, n * cap * 3 * sizeof(uint32_t), s));
+            CK(cudaMemsetAsync(dl.as<void>(), 0, n * cap * sizeof(double), s));
+        }
         CK(cudaMemcpyAsync(d1.as<void>(), p1, n * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(d2.as<void>(), p2, n * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
         launch_siddon_batch(*g, d1.as<double>(), d2.as<double>(), n, cap, dx.as<uint32_t>(), dl.as<double>(),
