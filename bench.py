@@ -284,7 +284,7 @@ def run_ours(args) -> int:
     # algorithmic bytes per launch (mixed: 4-byte index, L, T; fp64: 8-byte L, T)
     rb = 4 if args.precision == "mixed" else 8
     muon_bytes = (4 + 2 * rb) * pairs + (4 * rb + rb + 8 + 4 * rb) * kept + rb * V  # lists, S/D/pr2/off, k out, lambda
-    voxel_bytes = (4 + 2 * rb) * pairs + (16 + 2 * rb) * V                          # voxel-major lists, descriptor, lambda in/out
+    voxel_bytes = (4 + 2 * rb) * pairs + (16 + 6 * rb) * V  # voxel-major lists; descriptor, lambda in/out, window in/out
     pk = peaks()
     muon_ms = tm_ / max(nm_, 1)
     voxel_ms = tv / max(nv_, 1)  # the voxel pass: all class launches of one iteration
