@@ -235,14 +235,15 @@ struct alignas(16) VoxDesc {
 template <typename Real, typename OutT>
 void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists, const uint32_t* counts,
                      const int* resident_blocks, uint32_t streamed, cudaStream_t s);
-// descriptors of all voxels partitioned by class (voxel order within a
-// class): counts needs kVoxClasses * voxel_class_blocks(V) entries, first one
+// descriptors of all voxels partitioned by class (within a class in column
+// order of column_order's grid when it covers the V voxels, else in index
+// order): counts needs kVoxClasses * voxel_class_blocks(V) entries, first one
 // more (exclusive scan; class c starts at first[c * blocks]); scan_scratch
 // as for scan_u32_to_u64 of that length
 uint32_t voxel_class_blocks(uint64_t V);
 template <typename Real>
-void launch_voxel_classes(const uint32_t* mult, const uint64_t* start, uint32_t V, uint32_t* counts, uint64_t* first,
-                          void* scan_scratch, VoxDesc* out, cudaStream_t s);
+void launch_voxel_classes(const uint32_t* mult, const uint64_t* start, uint32_t V, const muto_grid* column_order,
+                          uint32_t* counts, uint64_t* first, void* scan_scratch, VoxDesc* out, cudaStream_t s);
 // classes that hold segments of more than `pairs` pairs: the streamed mask
 __host__ __device__ constexpr uint32_t vox_streamed_mask(uint32_t pairs) {
     uint32_t m = 0;

@@ -723,8 +723,8 @@ void prepare_em(muto_handle* h) {
         h->vclass.alloc(std::max<uint64_t>(V, 1) * sizeof(VoxDesc), &h->dev_bytes);
         run(h, "voxel_classes", [&] {
             launch_voxel_classes<Real>(h->mult.as<uint32_t>(), h->start.as<uint64_t>(), static_cast<uint32_t>(V),
-                                       ccount.as<uint32_t>(), cfirst.as<uint64_t>(), cscr.as<void>(),
-                                       h->vclass.as<VoxDesc>(), s);
+                                       h->batch ? nullptr : &h->grid, ccount.as<uint32_t>(), cfirst.as<uint64_t>(),
+                                       cscr.as<void>(), h->vclass.as<VoxDesc>(), s);
         });
         uint64_t bnd[kVoxClasses + 1];
         for (int c = 0; c <= kVoxClasses; ++c)

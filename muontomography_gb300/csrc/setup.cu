@@ -377,15 +377,26 @@ __global__ void k_siddon_batch(DevGrid g, const double* __restrict__ p1, const d
 // length class (one counting pass of a radix sort with kVoxClasses buckets).
 // Per block of 256 voxels: the class counts (class-major, so one exclusive
 // scan gives every block's first slot in every class), then the scatter of
-// each voxel's descriptor to its slot, in voxel order within a class.
+// each voxel's descriptor to its slot.  Within a class the voxels are in
+// column order (z fastest, then x, then y) when a grid is given, else in
+// index order: vertically adjacent voxels, which share many of their (mostly
+// steep) muons, are then processed side by side and their coefficient
+// gathers hit the same cache lines.
+__device__ __forceinline__ uint32_t class_order_voxel(uint32_t t, uint32_t nx, uint32_t ny, uint32_t nz) {
+    if (nz == 0) return t;
+    const uint32_t z = t % nz, r = t / nz;
+    return r % nx + nx * (r / nx + ny * z);
+}
+
 template <typename Real>
-__global__ void k_class_count(const uint32_t* __restrict__ mult, uint32_t V, uint32_t nblocks,
-                              uint32_t* __restrict__ counts) {
+__global__ void k_class_count(const uint32_t* __restrict__ mult, uint32_t V, uint32_t nblocks, uint32_t nx,
+                              uint32_t ny, uint32_t nz, uint32_t* __restrict__ counts) {
     __shared__ uint32_t c_s[kVoxClasses];
     if (threadIdx.x < kVoxClasses) c_s[threadIdx.x] = 0;
     __syncthreads();
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int cls = j < V ? vox_class_of<Real>(mult[j]) : -1;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t j = t < V ? class_order_voxel(t, nx, ny, nz) : 0u;
+    const int cls = t < V ? vox_class_of<Real>(mult[j]) : -1;
     const int lane = threadIdx.x & 31;
     for (int c = 0; c < kVoxClasses; ++c) {
         const uint32_t n = __popc(__ballot_sync(kFull, cls == c));
@@ -397,11 +408,13 @@ __global__ void k_class_count(const uint32_t* __restrict__ mult, uint32_t V, uin
 
 template <typename Real>
 __global__ void k_class_scatter(const uint32_t* __restrict__ mult, const uint64_t* __restrict__ start, uint32_t V,
-                                uint32_t nblocks, const uint64_t* __restrict__ first, VoxDesc* __restrict__ out) {
+                                uint32_t nblocks, uint32_t nx, uint32_t ny, uint32_t nz,
+                                const uint64_t* __restrict__ first, VoxDesc* __restrict__ out) {
     constexpr int W = kThreads / 32;
     __shared__ uint32_t wc[W][kVoxClasses];
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int cls = j < V ? vox_class_of<Real>(mult[j]) : -1;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t j = t < V ? class_order_voxel(t, nx, ny, nz) : 0u;
+    const int cls = t < V ? vox_class_of<Real>(mult[j]) : -1;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     uint32_t my_rank = 0;
     for (int c = 0; c < kVoxClasses; ++c) {
@@ -539,19 +552,25 @@ namespace muto {
 uint32_t voxel_class_blocks(uint64_t V) { return blocks_for(V); }
 
 template <typename Real>
-void launch_voxel_classes(const uint32_t* mult, const uint64_t* start, uint32_t V, uint32_t* counts, uint64_t* first,
-                          void* scan_scratch, VoxDesc* out, cudaStream_t s) {
+void launch_voxel_classes(const uint32_t* mult, const uint64_t* start, uint32_t V, const muto_grid* column_order,
+                          uint32_t* counts, uint64_t* first, void* scan_scratch, VoxDesc* out, cudaStream_t s) {
     if (V == 0) return;
     const uint32_t nb = blocks_for(V);
-    k_class_count<Real><<<nb, kThreads, 0, s>>>(mult, V, nb, counts);
+    uint32_t nx = 0, ny = 0, nz = 0;
+    if (column_order && static_cast<uint64_t>(column_order->nx) * column_order->ny * column_order->nz == V) {
+        nx = column_order->nx;
+        ny = column_order->ny;
+        nz = column_order->nz;
+    }
+    k_class_count<Real><<<nb, kThreads, 0, s>>>(mult, V, nb, nx, ny, nz, counts);
     count_launches(1);
     scan_u32_to_u64(counts, first, static_cast<uint64_t>(nb) * kVoxClasses, scan_scratch, s);
-    k_class_scatter<Real><<<nb, kThreads, 0, s>>>(mult, start, V, nb, first, out);
+    k_class_scatter<Real><<<nb, kThreads, 0, s>>>(mult, start, V, nb, nx, ny, nz, first, out);
     count_launches(1);
 }
-template void launch_voxel_classes<float>(const uint32_t*, const uint64_t*, uint32_t, uint32_t*, uint64_t*, void*,
-                                          VoxDesc*, cudaStream_t);
-template void launch_voxel_classes<double>(const uint32_t*, const uint64_t*, uint32_t, uint32_t*, uint64_t*, void*,
-                                           VoxDesc*, cudaStream_t);
+template void launch_voxel_classes<float>(const uint32_t*, const uint64_t*, uint32_t, const muto_grid*, uint32_t*,
+                                          uint64_t*, void*, VoxDesc*, cudaStream_t);
+template void launch_voxel_classes<double>(const uint32_t*, const uint64_t*, uint32_t, const muto_grid*, uint32_t*,
+                                           uint64_t*, void*, VoxDesc*, cudaStream_t);
 
 }  // namespace muto
