@@ -101,14 +101,14 @@ class ClockSampler:
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from muontomography_gb300.replicas import env
+
+    return env()
 
 
 def workload(args, rank: int):
     from muontomography_gb300 import workloads as W
+    from muontomography_gb300.replicas import replica_seed
 
     fn = {"config1": W.config1, "config2": W.config2, "config2_coarse": W.config2_coarse, "config3": W.config3,
           "config5": W.config5}[args.workload]
@@ -116,7 +116,7 @@ def workload(args, rank: int):
     if args.n_muons:
         kw["n_muons"] = args.n_muons
     wl = fn(**kw)
-    wl.seed = wl.seed + 1000 * rank  # every rank reconstructs its own scan (weak scaling)
+    wl.seed = replica_seed(wl.seed, rank)  # every rank reconstructs its own scan (weak scaling)
     return wl
 
 
@@ -189,32 +189,12 @@ def run_reference(args) -> int:
 def run_ours(args) -> int:
     import torch
 
+    from muontomography_gb300.replicas import Replicas
+
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist_mod
-
-        dist = dist_mod
-        dist.init_process_group("nccl")
-
-    def barrier():
-        if dist:
-            dist.barrier()
-
-    def allmax(x: float) -> float:
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
-
-    def allsum(x: float) -> float:
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        return float(t.item())
+    rep = Replicas("nccl")
+    barrier, allmax, allsum = rep.barrier, rep.max, rep.sum
 
     import muontomography_gb300 as M
     from muontomography_gb300 import _lib
@@ -412,8 +392,7 @@ def run_ours(args) -> int:
             "time_to_lambda": ttl,
         }
         print(json.dumps(line), flush=True)
-    if dist:
-        dist.destroy_process_group()
+    rep.close()
     return 0
 
 
