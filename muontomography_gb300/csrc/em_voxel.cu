@@ -311,15 +311,16 @@ __device__ __forceinline__ int window_pass(const Src& v, uint32_t n, uint32_t k,
 }
 
 // One sampling round: the (up to 32) samples are sorted in the warp and the
-// window is the keys within 6 sample ranks of rank k (window_pass).
+// window is the keys within `reach` (6) sample ranks of rank k (window_pass).
 template <typename K, class Src>
 __device__ __forceinline__ int sample_round(const Src& v, uint32_t n, uint32_t k, K* out, uint32_t out_rows,
-                                            int lane, Ragged<K>& res, uint32_t& below, Sel<K>* direct) {
+                                            int lane, Ragged<K>& res, uint32_t& below, Sel<K>* direct,
+                                            int reach = 6) {
     const K smp = v.sample();
     const uint32_t ns = __popc(__ballot_sync(kFull, smp != empty_key<K>()));
     const K s = sort32(smp, lane);  // empty samples sort last
     const int pos = static_cast<int>((static_cast<float>(k) * static_cast<float>(ns)) / static_cast<float>(n));
-    const int ql = pos - 6, qh = pos + 6;
+    const int ql = pos - reach, qh = pos + reach;
     const K slo = __shfl_sync(kFull, s, ql < 0 ? 0 : (ql > 31 ? 31 : ql));
     const K shi = __shfl_sync(kFull, s, qh > 31 ? 31 : (qh < 0 ? 0 : qh));
     const K lo = ql <= 0 ? K(0) : slo;
@@ -380,7 +381,8 @@ __device__ __noinline__ Sel<K> select_candidates(K* cur_buf, K* oth_buf, uint32_
 
 // Order statistic k (and usually k-1) of a key source of M keys, exact.
 // Short segments are staged and sorted; longer ones go through a first
-// sampling round into buffer a, then select_candidates.
+// sampling round into buffer a (once more, twice as wide, if it misses),
+// then select_candidates.
 template <typename K, class Src>
 __device__ Sel<K> kth_select(const Src& v, uint32_t M, uint32_t k, K* a, K* b, uint32_t cap_rows, int lane) {
     if (M <= 64) {
@@ -398,7 +400,11 @@ __device__ Sel<K> kth_select(const Src& v, uint32_t M, uint32_t k, K* a, K* b, u
     Ragged<K> cur;
     uint32_t b1;
     Sel<K> r;
-    const int st = sample_round<K>(v, M, k, a, cap_rows, lane, cur, b1, &r);
+    int st = sample_round<K>(v, M, k, a, cap_rows, lane, cur, b1, &r);
+    if (st == kWinFail) {  // the samples sit off-centre (a few % of segments): twice as wide a window
+        __syncwarp();
+        st = sample_round<K>(v, M, k, a, cap_rows, lane, cur, b1, &r, 12);
+    }
     if (st == kWinEqual) {
         __syncwarp();
         return r;
