@@ -235,6 +235,36 @@ struct alignas(16) VoxDesc {
 template <typename Real, typename OutT>
 void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists, const uint32_t* counts,
                      const int* resident_blocks, uint32_t streamed, cudaStream_t s);
+// Bricked voxel order for the muon pass's lambda gathers: 4x4x4 bricks of
+// 64 consecutive entries, so the neighbouring voxels of a muon's path share
+// cache lines instead of lying a grid row or plane apart.
+struct BrickDims {
+    uint32_t nx, ny, nz, nbx, nby, nbz;
+};
+__host__ __device__ inline BrickDims brick_dims(const muto_grid& g) {
+    return BrickDims{g.nx, g.ny, g.nz, (g.nx + 3) / 4, (g.ny + 3) / 4, (g.nz + 3) / 4};
+}
+__host__ __device__ inline uint64_t brick_volume(const BrickDims& b) {
+    return static_cast<uint64_t>(b.nbx) * b.nby * b.nbz * 64;
+}
+__host__ __device__ inline uint32_t brick_of(uint32_t j, const BrickDims& b) {
+    const uint32_t x = j % b.nx, t = j / b.nx, y = t % b.ny, z = t / b.ny;
+    return (((z >> 2) * b.nby + (y >> 2)) * b.nbx + (x >> 2)) * 64u + (((z & 3u) << 4) | ((y & 3u) << 2) | (x & 3u));
+}
+__host__ __device__ inline uint32_t unbrick(uint32_t jb, const BrickDims& b) {
+    const uint32_t in = jb & 63u, blk = jb >> 6;
+    const uint32_t bx = blk % b.nbx, t = blk / b.nbx, by = t % b.nby, bz = t / b.nby;
+    const uint32_t x = bx * 4 + (in & 3u), y = by * 4 + ((in >> 2) & 3u), z = bz * 4 + (in >> 4);
+    return x + b.nx * (y + b.ny * z);
+}
+// voxel indices to bricked ones in place (indices >= V are left alone)
+void launch_brick_indices(uint32_t* vidx, uint64_t n, BrickDims b, uint32_t V, cudaStream_t s);
+// bricked indices back to voxel indices
+void launch_unbrick_indices(const uint32_t* in, uint32_t* out, uint64_t n, BrickDims b, cudaStream_t s);
+// lambda (voxel order, V) to its bricked copy
+template <typename Real>
+void launch_brick_lambda(const Real* lam, uint32_t V, BrickDims b, Real* lam_b, cudaStream_t s);
+
 // descriptors of all voxels partitioned by class (within a class in column
 // order of column_order's grid when it covers the V voxels, else in index
 // order): counts needs kVoxClasses * voxel_class_blocks(V) entries, first one

@@ -323,6 +323,10 @@ struct muto_handle {
     uint64_t vclass_off[kVoxClasses] = {};
     DevMem mult, start, kvec, keys;   // keys: scratch for voxels beyond the register budget
     DevMem win;                       // per voxel: the last selection window (center, half-width)
+    bool brick = false;               // path voxel indices are bricked (single scans), see lam_b
+    BrickDims bdims{};
+    uint64_t vb = 0;                  // bricked index space (>= V)
+    DevMem lam_b;                     // lambda in bricked order, refreshed before every muon pass
     DevMem lam, lam_ml, cost_hist;
     DevMem tiles;
     uint32_t ntiles = 0;
@@ -789,6 +793,21 @@ void prepare_em(muto_handle* h) {
 
     // --- image ---------------------------------------------------------------
     ph.reset(new HostPhase(h, "image"));
+    // the muon pass gathers lambda through bricked indices (single scans)
+    h->brick = false;
+    h->lam_b.release();
+    if (!h->batch) {
+        h->bdims = brick_dims(h->grid);
+        h->vb = brick_volume(h->bdims);
+        if (h->vb < 0xffffffffull) {
+            h->brick = true;
+            h->lam_b.alloc(h->vb * sizeof(Real), &h->dev_bytes);
+            CK(cudaMemsetAsync(h->lam_b.as<void>(), 0, h->vb * sizeof(Real), s));
+            run(h, "brick_indices", [&] {
+                launch_brick_indices(h->vidx.as<uint32_t>(), Pn, h->bdims, static_cast<uint32_t>(V), s);
+            });
+        }
+    }
     h->lam.alloc(V * sizeof(Real), &h->dev_bytes);
     h->win.alloc(2 * V * sizeof(Real), &h->dev_bytes);
     CK(cudaMemsetAsync(h->win.as<void>(), 0, 2 * V * sizeof(Real), s));  // half-width 0: no prediction yet
@@ -803,7 +822,13 @@ void prepare_em(muto_handle* h) {
 }
 
 template <typename Real>
-void launch_muon_pass(muto_handle* h, const MuonPassArgs<Real>& a, cudaStream_t s) {
+void launch_muon_pass(muto_handle* h, const MuonPassArgs<Real>& a_in, cudaStream_t s) {
+    MuonPassArgs<Real> a = a_in;
+    if (h->brick) {  // a.lam is in voxel order; the pass gathers from the bricked copy
+        launch_brick_lambda<Real>(a_in.lam, static_cast<uint32_t>(h->V()), h->bdims, h->lam_b.as<Real>(), s);
+        a.lam = h->lam_b.as<Real>();
+        a.V = static_cast<uint32_t>(h->vb);
+    }
     if (h->muon_kind == 2)
         launch_em_muon_warp<Real>(a, static_cast<uint32_t>(h->N), h->warp_blocks, h->muon_group, s);
     else
@@ -1477,7 +1502,17 @@ int muto_export_paths(muto_handle* h, uint32_t* kept, double* info, uint64_t* of
         const uint64_t N = h->N, Pn = h->npairs;
         if (kept && N) CK(cudaMemcpyAsync(kept, h->kept.as<void>(), N * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         if (off) CK(cudaMemcpyAsync(off, h->off.as<void>(), (N + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-        if (idx && Pn) CK(cudaMemcpyAsync(idx, h->vidx.as<void>(), Pn * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        if (idx && Pn) {
+            if (h->brick) {  // the stored indices are bricked
+                DevMem tmp;
+                tmp.alloc(Pn * sizeof(uint32_t), nullptr);
+                launch_unbrick_indices(h->vidx.as<uint32_t>(), tmp.as<uint32_t>(), Pn, h->bdims, s);
+                CK(cudaMemcpyAsync(idx, tmp.as<void>(), Pn * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+            } else {
+                CK(cudaMemcpyAsync(idx, h->vidx.as<void>(), Pn * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+            }
+        }
         auto fetch = [&](const DevMem& m, double* dst, uint64_t count) {
             if (!dst || count == 0) return;
             if (h->fp64()) {

@@ -431,6 +431,29 @@ __global__ void k_class_scatter(const uint32_t* __restrict__ mult, const uint64_
     }
 }
 
+__global__ void k_brick_indices(uint32_t* __restrict__ vidx, uint64_t n, BrickDims b, uint32_t V) {
+    const uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k < n) {
+        const uint32_t j = vidx[k];
+        if (j < V) vidx[k] = brick_of(j, b);
+    }
+}
+
+__global__ void k_unbrick_indices(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint64_t n,
+                                  BrickDims b) {
+    const uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (k < n) {
+        const uint32_t jb = in[k];
+        out[k] = jb == 0xffffffffu ? jb : unbrick(jb, b);
+    }
+}
+
+template <typename Real>
+__global__ void k_brick_lambda(const Real* __restrict__ lam, uint32_t V, BrickDims b, Real* __restrict__ lam_b) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < V) lam_b[brick_of(j, b)] = lam[j];
+}
+
 }  // namespace
 
 void launch_keep_flags(const muto_ray* rays, uint64_t n_total, muto_grid g, double eps, uint32_t* flags,
@@ -572,5 +595,30 @@ template void launch_voxel_classes<float>(const uint32_t*, const uint64_t*, uint
                                           uint64_t*, void*, VoxDesc*, cudaStream_t);
 template void launch_voxel_classes<double>(const uint32_t*, const uint64_t*, uint32_t, const muto_grid*, uint32_t*,
                                            uint64_t*, void*, VoxDesc*, cudaStream_t);
+
+}  // namespace muto
+
+namespace muto {
+
+void launch_brick_indices(uint32_t* vidx, uint64_t n, BrickDims b, uint32_t V, cudaStream_t s) {
+    if (n == 0) return;
+    k_brick_indices<<<blocks_for(n), kThreads, 0, s>>>(vidx, n, b, V);
+    count_launches(1);
+}
+
+void launch_unbrick_indices(const uint32_t* in, uint32_t* out, uint64_t n, BrickDims b, cudaStream_t s) {
+    if (n == 0) return;
+    k_unbrick_indices<<<blocks_for(n), kThreads, 0, s>>>(in, out, n, b);
+    count_launches(1);
+}
+
+template <typename Real>
+void launch_brick_lambda(const Real* lam, uint32_t V, BrickDims b, Real* lam_b, cudaStream_t s) {
+    if (V == 0) return;
+    k_brick_lambda<Real><<<blocks_for(V), kThreads, 0, s>>>(lam, V, b, lam_b);
+    count_launches(1);
+}
+template void launch_brick_lambda<float>(const float*, uint32_t, BrickDims, float*, cudaStream_t);
+template void launch_brick_lambda<double>(const double*, uint32_t, BrickDims, double*, cudaStream_t);
 
 }  // namespace muto
