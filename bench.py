@@ -31,6 +31,15 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+# --workload choices: grid, voxel size and muon count of each scan
+WORKLOADS = {
+    "cube100_20mm": lambda W: W.cube100_20mm,  # 100^3 voxels of 20 mm, 10 M muons (default)
+    "cube50_40mm": lambda W: W.cube50_40mm,  # the same scene on 50^3 voxels of 40 mm, 2.5 M muons
+    "cube20_50mm": lambda W: W.cube20_50mm,  # 20^3 voxels of 50 mm, 100 k muons
+    "map128x128x64_15mm": lambda W: W.map128x128x64_15mm,  # 128x128x64 voxels of 15 mm, 20 M muons
+    "grid256x256x128_10mm": lambda W: W.grid256x256x128_10mm,  # 256x256x128 voxels of 10 mm, 100 M muons
+}
+
 METRIC = "EM-iter muon-voxel updates/s"
 UNIT = "muon-voxel updates/s"
 
@@ -110,8 +119,7 @@ def workload(args, rank: int):
     from muontomography_gb300 import workloads as W
     from muontomography_gb300.replicas import replica_seed
 
-    fn = {"config1": W.config1, "config2": W.config2, "config2_coarse": W.config2_coarse, "config3": W.config3,
-          "config5": W.config5}[args.workload]
+    fn = WORKLOADS[args.workload](W)
     kw = {}
     if args.n_muons:
         kw["n_muons"] = args.n_muons
@@ -272,7 +280,7 @@ def run_ours(args) -> int:
     v_ach = voxel_bytes / (voxel_ms / 1000.0) / 1e9 if nv_ else None
     # DRAM traffic (read + write) per launch: ncu's bytes per pair on the 50^3-voxel
     # case of the same scene, scaled by this run's pairs
-    measured = args.precision == "mixed" and args.mode == "median" and args.workload in ("config2", "config2_coarse")
+    measured = args.precision == "mixed" and args.mode == "median" and args.workload in ("cube100_20mm", "cube50_40mm")
     t_voxel = (args.ncu_traffic if args.ncu_traffic is not None
                else (TRAFFIC_PER_PAIR["voxel"] * pairs if measured else None))
     t_muon = TRAFFIC_PER_PAIR["muon"] * pairs if measured else None
@@ -403,7 +411,7 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config2_coarse", "config3", "config5"])
+    ap.add_argument("--workload", default="cube100_20mm", choices=list(WORKLOADS))
     ap.add_argument("--n-muons", type=int, default=0)
     ap.add_argument("--mode", choices=["median", "mean"], default="median")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")

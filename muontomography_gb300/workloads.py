@@ -57,47 +57,47 @@ def _random_blocks(rng, grid: Grid, materials, edge_lo, edge_hi, margin=0.1):
     return out
 
 
-def config1(n_muons: int = 100_000, seed: int = 1) -> Workload:
+def cube20_50mm(n_muons: int = 100_000, seed: int = 1) -> Workload:
     """20^3 voxels of 50 mm (1 m cube), iron 200 mm cube at the centre, lead 100 mm cube 250 mm along x."""
     g = Grid(20, 20, 20, -500.0, -500.0, -500.0, 50.0, 50.0, 50.0)
     blocks = [Block((-100.0, -100.0, -100.0), (100.0, 100.0, 100.0), X0_MM["iron"]),
               Block((200.0, -50.0, -50.0), (300.0, 50.0, 50.0), X0_MM["lead"])]
-    return Workload("config1_20cube_100k", g, blocks, n_muons, seed, False, 20)
+    return Workload("cube20_50mm_100k", g, blocks, n_muons, seed, False, 20)
 
 
-def config2(n_muons: int = 10_000_000, seed: int = 2) -> Workload:
+def cube100_20mm(n_muons: int = 10_000_000, seed: int = 2) -> Workload:
     """100^3 voxels of 20 mm (2 m cube): iron, lead, aluminium blocks (150-300 mm) and a 50 mm concrete slab."""
     g = Grid(100, 100, 100, -1000.0, -1000.0, -1000.0, 20.0, 20.0, 20.0)
     rng = np.random.default_rng(seed)
     blocks = _random_blocks(rng, g, ["iron", "lead", "aluminium"], 150.0, 300.0)
     z0 = float(rng.uniform(-800.0, -500.0))
     blocks.insert(0, Block((-800.0, -800.0, z0), (800.0, 800.0, z0 + 50.0), X0_MM["concrete"]))
-    return Workload("config2_100cube_10M", g, blocks, n_muons, seed, True, 50)
+    return Workload("cube100_20mm_10M", g, blocks, n_muons, seed, True, 50)
 
 
-def config2_coarse(n_muons: int = 2_500_000, seed: int = 2) -> Workload:
-    """config2's scene on 50^3 voxels of 40 mm with a quarter of the muons: the same
+def cube50_40mm(n_muons: int = 2_500_000, seed: int = 2) -> Workload:
+    """cube100_20mm's scene on 50^3 voxels of 40 mm with a quarter of the muons: the same
     pairs per voxel (about 550) in a quarter of the memory, for profiler captures."""
-    full = config2(seed=seed)
+    full = cube100_20mm(seed=seed)
     g = Grid(50, 50, 50, -1000.0, -1000.0, -1000.0, 40.0, 40.0, 40.0)
-    return Workload("config2_coarse_50cube_2.5M", g, full.blocks, n_muons, seed, True, 50)
+    return Workload("cube50_40mm_2.5M", g, full.blocks, n_muons, seed, True, 50)
 
 
-def config3(n_muons: int = 20_000_000, seed: int = 3) -> Workload:
+def map128x128x64_15mm(n_muons: int = 20_000_000, seed: int = 3) -> Workload:
     """128x128x64 voxels of 15 mm, MAP with the 26-neighbour prior."""
     g = Grid(128, 128, 64, -960.0, -960.0, -480.0, 15.0, 15.0, 15.0)
     rng = np.random.default_rng(seed)
     blocks = _random_blocks(rng, g, ["iron", "lead", "aluminium", "concrete"], 100.0, 300.0)
-    return Workload("config3_128x128x64_map", g, blocks, n_muons, seed, True, 20)
+    return Workload("map128x128x64_15mm_20M", g, blocks, n_muons, seed, True, 20)
 
 
-def config5(n_muons: int = 100_000_000, seed: int = 5) -> Workload:
+def grid256x256x128_10mm(n_muons: int = 100_000_000, seed: int = 5) -> Workload:
     """256x256x128 voxels of 10 mm, 12 mixed blocks."""
     g = Grid(256, 256, 128, -1280.0, -1280.0, -640.0, 10.0, 10.0, 10.0)
     rng = np.random.default_rng(seed)
     mats = ["iron", "lead", "aluminium", "concrete"] * 3
     blocks = _random_blocks(rng, g, mats, 100.0, 400.0)
-    return Workload("config5_256x256x128_100M", g, blocks, n_muons, seed, True, 30)
+    return Workload("grid256x256x128_10mm_100M", g, blocks, n_muons, seed, True, 30)
 
 
 def small(n_muons: int = 4000, seed: int = 11, n: int = 12) -> Workload:

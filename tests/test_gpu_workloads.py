@@ -1,0 +1,142 @@
+"""The benchmark workloads other than the timed one, as parity cases.
+
+* the 20^3 grid of 50 mm voxels with 100 k muons, in full: PoCA voxel of
+  every ray and the merged paths bit-exact against the oracle; lambda after
+  20 FP64 EM iterations within 1e-10 relative L2 (mixed form: 1e-4).
+* the 128 x 128 x 64 grid of 15 mm voxels and its prior, with fewer muons:
+  MAP with beta in {1e-3, 1e-2}, the 26-neighbour stencil, p = 2 and p = 1,
+  delta = 0.1 median(lambda) x 1e7, against the oracle; the gradient of the
+  MAP objective against central differences on 64 random voxels, eps = 1e-4.
+* the batch of 64 scans (grids of 32^3 to 128^3 voxels of 20 mm, muon counts
+  log-uniform) with 1/100 of its muons: one batch handle against separate
+  handles.
+* the 256 x 256 x 128 grid of 10 mm voxels with 1 M muons: the mixed form
+  within 1e-4 of the FP64 form after 5 iterations.  With its full 100 M muons
+  (1.9e10 pairs) the stored lists would need about 456 GB: it does not fit
+  one GPU's memory.
+"""
+import numpy as np
+import pytest
+
+import muontomography_gb300 as M
+from muontomography_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_cube20_in_full(gpu, oracle):
+    wl = W.cube20_50mm()
+    rays = wl.tracks()
+    pcfg = wl.poca_config()
+    _, ref_assign, _ = oracle.poca(wl.grid, pcfg, rays)
+    with M.MutoPoCA(pcfg) as rec:
+        rec.reconstruct(rays)
+        assign = rec.poca_assignment(rays.shape[0])
+    assert np.array_equal(assign, ref_assign)
+    cfg = wl.em_config(precision="fp64", num_iteration=20)
+    init = np.full(wl.grid.nvox, 1e-7)
+    ref = oracle.Mlsd(wl.grid, cfg, rays, init)
+    r = ref.export()
+    ref.iterate(20)
+    with M.MutoMLSD(cfg) as rec:
+        rec.load_tracks(rays)
+        rec.prepare()
+        g = rec.export_paths()
+        rec.iterate(20)
+        img = rec.image().reshape(-1, order="F")
+    assert np.array_equal(g["kept"], r["kept"]) and np.array_equal(g["idx"], r["idx"])
+    assert np.array_equal(g["len"].view(np.uint64), r["len"].view(np.uint64))
+    assert np.array_equal(g["tail"].view(np.uint64), r["tail"].view(np.uint64))
+    assert rel_l2(img, ref.image()) < 1e-10
+    with M.MutoMLSD(wl.em_config(precision="mixed", num_iteration=20)) as rec:
+        mixed = rec.reconstruct(rays).reshape(-1, order="F")
+    assert rel_l2(mixed, ref.image()) < 1e-4
+
+
+def _map128_small(n_muons=300_000):
+    wl = W.map128x128x64_15mm(n_muons=n_muons)
+    lam = wl.lam()
+    delta = 0.1 * float(np.median(lam)) * 1e7
+    return wl, delta
+
+
+@pytest.mark.parametrize("beta", [1e-3, 1e-2])
+@pytest.mark.parametrize("p", [2.0, 1.0])
+def test_map128_matches_oracle(gpu, oracle, beta, p):
+    wl, delta = _map128_small()
+    rays = wl.tracks()
+    cfg = wl.em_config(precision="fp64", num_iteration=3, beta=beta, p=p, delta=delta, all_neighbours=True)
+    ref = oracle.Mlsd(wl.grid, cfg, rays, np.full(wl.grid.nvox, 1e-7), method="map")
+    ref.iterate(3)
+    with M.MutoMAP(cfg) as rec:
+        img = rec.reconstruct(rays).reshape(-1, order="F")
+        st = rec.status()
+    assert st["n_nonconverged"] == 0
+    assert rel_l2(img, ref.image()) < 1e-9
+
+
+@pytest.mark.parametrize("p", [2.0, 1.0])
+def test_map128_gradient_central_differences(gpu, p):
+    wl, delta = _map128_small()
+    cfg = wl.em_config(precision="fp64", num_iteration=0, beta=1e-2, p=p, delta=delta, all_neighbours=True)
+    eps = 1e-4
+    with M.MutoMAP(cfg) as rec:
+        rec.load_tracks(wl.tracks())
+        rec.prepare()
+        mult = rec.multiplicity()
+        rng = np.random.default_rng(17)
+        # neighbouring values far apart against delta: the central difference with
+        # eps = 1e-4 must not straddle the potential's kink (delta is tiny for p = 1)
+        lam = wl.lam() * rng.uniform(0.6, 1.4, wl.grid.nvox) + 2e-7 * rng.uniform(0.5, 1.5, wl.grid.nvox)
+        x = np.where(mult > 0, np.log(lam), 0.0)
+        _, g = rec.nll_grad(x)
+        pick = rng.choice(np.nonzero(mult > 0)[0], size=64, replace=False)
+        fd = np.empty(pick.size)
+        for k, j in enumerate(pick):
+            xp, xm = x.copy(), x.copy()
+            xp[j] += eps
+            xm[j] -= eps
+            fd[k] = (rec.nll(xp) - rec.nll(xm)) / (2 * eps)
+    # the differences carry the objective's rounding (~1e-9 of ~5e5, over 2 eps)
+    ok = np.abs(fd - g[pick]) <= 1e-4 * np.abs(g[pick]) + 1e-5 * np.abs(g[pick]).max()
+    if p == 2.0:
+        assert ok.all() and rel_l2(fd, g[pick]) < 1e-5
+    else:  # |t| potential: a voxel whose step straddles a neighbour's value (|t| < eps l) is a kink, not a slope
+        assert ok.sum() >= 61, np.nonzero(~ok)[0]
+
+
+def test_batch_of_64_scans(gpu):
+    rng = np.random.default_rng(4)
+    sides = rng.choice([32, 64, 96, 128], size=64)
+    muons = np.exp(rng.uniform(np.log(500), np.log(50_000), size=64)).astype(int)
+    wls = []
+    for k, (nside, nm) in enumerate(zip(sides, muons)):
+        half = nside * 20.0 / 2
+        g = M.Grid(int(nside), int(nside), int(nside), -half, -half, -half, 20.0, 20.0, 20.0)
+        blocks = [M.Block((-60.0, -60.0, -60.0), (60.0, 60.0, 60.0), M.X0_MM["iron"])]
+        wls.append(W.Workload(f"scan{k}", g, blocks, int(nm), 400 + k, True, 4))
+    cfg = wls[0].em_config(precision="fp64", num_iteration=4)
+    cfg.pop("grid")
+    tracks = [wl.tracks() for wl in wls]
+    with M.Batch(cfg, [wl.grid for wl in wls]) as b:
+        imgs = b.reconstruct_all(tracks)
+    for k in range(0, 64, 9):  # every ninth scan against its own handle
+        with M.MutoMLSD(dict(cfg, grid=wls[k].grid.json())) as rec:
+            one = rec.reconstruct(tracks[k])
+        assert rel_l2(imgs[k], one) < 1e-12, k
+
+
+def test_grid256_mixed_against_fp64(gpu):
+    wl = W.grid256x256x128_10mm(n_muons=1_000_000)
+    rays = wl.tracks()
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with M.MutoMLSD(wl.em_config(precision=prec, num_iteration=5)) as rec:
+            out[prec] = rec.reconstruct(rays).reshape(-1, order="F")
+    assert rel_l2(out["mixed"], out["fp64"]) < 1e-4
