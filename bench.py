@@ -287,7 +287,7 @@ def run_ours(args) -> int:
     # the voxel pass takes about three quarters of an iteration: it is the dominant kernel
     roofline = {"bound": "hbm", "achieved": v_ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": (v_ach / pk["hbm_gbs"]) if v_ach else None, "traffic": t_voxel,
-                "kernel": "k_em_voxel (one launch per segment-length class)", "kernel_ms": voxel_ms,
+                "kernel": "k_pair_keys + k_em_voxel (one launch per segment-length class)", "kernel_ms": voxel_ms,
                 "algorithmic_bytes": voxel_bytes, "peak_source": pk["source"],
                 "muon_pass": {"kernel": "k_em_muon", "kernel_ms": muon_ms, "algorithmic_bytes": muon_bytes,
                               "achieved": achieved, "frac": (achieved / pk["hbm_gbs"]) if achieved else None,

@@ -199,7 +199,8 @@ struct VoxelPassArgs {
     OutT* out;                                // V new value (median / percentile / mean)
     double* grad;                             // V gradient (kVoxGradient)
     const double* lam64;                      // V lambda in FP64 (kVoxGradient)
-    typename KeyOf<Real>::type* scratch;      // P keys of segments beyond the register budget
+    typename KeyOf<Real>::type* keys;         // P order keys of g_ij, voxel-major (the key pass writes them)
+    uint64_t P;                               // pairs in the voxel-major lists
     Real* win;                                // 2V selection window per voxel (center, half), or NULL
 };
 // segments up to this many pairs are selected from registers

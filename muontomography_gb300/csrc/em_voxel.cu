@@ -2,13 +2,19 @@
 // (updateImageVoxel, run for every voxel at :197-200), and the MAP step of
 // src/MutoMAP.cpp:228-247.
 //
-// The pairs are also stored voxel-major (muon, L, T), built once at setup, so
-// one warp per voxel reads its M_j pairs with coalesced streaming loads,
-// gathers each muon's coefficients k_i (written by the muon pass, small enough
-// to stay in L2) and forms in registers
-//     s_ij = 2 l_j + (k0 W00 + k1 W01 + k2 W11) l_j^2,
-// the reference's 2 l + (1/2 xyS - tr(Sigma^-1 W)) pr^2 l^2.  No s_ij array is
-// written; nothing is accumulated with atomics.
+// The pairs are also stored voxel-major (muon, L, T), built once at setup.
+// Two steps:
+//   key pass     one thread per pair streams the lists, gathers its muon's
+//                coefficients k_i (written by the muon pass, small enough to
+//                stay in L2) and writes g_ij = k0 W00 + k1 W01 + k2 W11 as an
+//                order-preserving integer key, voxel-major.  The gather runs
+//                at full occupancy, apart from the selection.
+//   class pass   one warp per voxel reads its M_j keys (coalesced, 4 or 8 B
+//                each) and selects on them; s_ij = 2 l_j + g_ij l_j^2, the
+//                reference's 2 l + (1/2 xyS - tr(Sigma^-1 W)) pr^2 l^2, is
+//                non-decreasing in g_ij, so an order statistic of the keys is
+//                one of the s_ij, formed only for the values the update uses.
+// Nothing is accumulated with atomics.
 //   median       exact order statistics of the s_ij (nth_element semantics).
 //                Two rounds of sampling narrow the search: 32 samples of the
 //                segment are sorted in the warp, the keys within 6 sample ranks
@@ -36,8 +42,9 @@ constexpr int kWarps = kVoxThreads / 32;
 // Rows of 32 keys in each of a warp's two candidate buffers.  Segments held
 // in registers get enough for any first window (at most R rows per lane).
 // Streamed segments get about 0.6 R + 4, at most 28 (a first window keeps
-// about 3/8 of the keys); the scratch-array class keeps 48 (32-bit keys) or
-// 24 rows.  A first window that does not fit falls back to the scratch array.
+// about 3/8 of the keys); the class beyond the register budget keeps 48
+// (32-bit keys) or 24 rows.  A window that does not fit its buffer ends in
+// the radix search over the key array.
 template <typename K, int C, bool STREAMED>
 __host__ __device__ constexpr int cand_rows() {
     return STREAMED ? (vox_class_rows(C) == 0 || (vox_class_rows(C) * 5) / 8 + 4 > 28 ? 28
@@ -149,7 +156,7 @@ struct VoxKeys {
     }
 };
 
-// A long segment's keys in the global scratch array, contiguous.
+// A segment's keys in the global key array, contiguous.
 template <typename K>
 struct PtrKeys {
     const K* p;
@@ -554,52 +561,34 @@ __device__ __forceinline__ Real pair_g(const typename Vec4<Real>::type& k, Real 
     return k.x * l + k.y * (lt + l * l * Real(0.5)) + k.z * (l * l * l * Real(1.0 / 3.0) + (l + t) * lt);
 }
 
-// the voxel's pairs held in registers, R per lane
+// the voxel's keys held in registers, R per lane
 template <typename Real, int R, typename OutT>
 __device__ __forceinline__ void voxel_regs(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uint64_t base, uint32_t M,
                                            int lane, const CandBufs& cb) {
     using K = typename KeyOf<Real>::type;
-    using R2 = typename Vec2<Real>::type;
     const Real lam = a.lam[j];
-    const bool keys = a.mode == kVoxMedian || a.mode == kVoxPercentile;
     VoxKeys<Real, R> v;
     v.M = M;
     v.lane = lane;
-    Real gs = 0;
-    constexpr int C = R < 8 ? R : 8;  // loads in flight per lane per chunk
+    const K* kp = a.keys + base;
 #pragma unroll
-    for (int r0 = 0; r0 < R; r0 += C) {
-        uint32_t mu[C];
-        R2 lt[C];
-#pragma unroll
-        for (int u = 0; u < C; ++u) {
-            const uint32_t e = static_cast<uint32_t>((r0 + u) * 32 + lane);
-            if (r0 + u < R && e < M) {
-                mu[u] = __ldcs(a.vm_mu + base + e);
-                lt[u] = __ldcs(a.vm_LT + base + e);
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < C; ++u) {
-            if (r0 + u >= R) break;
-            const uint32_t e = static_cast<uint32_t>((r0 + u) * 32 + lane);
-            v.key[r0 + u] = empty_key<K>();
-            if (e < M) {
-                const Real g = pair_g<Real>(ldg4(a.kvec + mu[u]), lt[u].x, lt[u].y);
-                if (keys) v.key[r0 + u] = to_key(g);  // s_ij = 2 l + g l^2 is non-decreasing in g
-                else gs += g;
-            }
-        }
+    for (int r = 0; r < R; ++r) {
+        const uint32_t e = static_cast<uint32_t>(r * 32 + lane);
+        v.key[r] = e < M ? __ldcs(kp + e) : empty_key<K>();
     }
     Real out;
-    if (keys) {
-        auto val = [lam](K x) {
+    if (a.mode == kVoxMedian || a.mode == kVoxPercentile) {
+        auto val = [lam](K x) {  // s_ij = 2 l + g l^2 is non-decreasing in g
             const Real g = from_key(x);
             return Real(2) * lam + g * lam * lam;
         };
         out = order_update<Real>(v, M, a.mode, a.pct, cb, lane, val,
                                  a.win ? reinterpret_cast<Pred<Real>*>(a.win) + j : nullptr);
     } else {
+        Real gs = 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            if (static_cast<uint32_t>(r * 32 + lane) < M) gs += from_key(v.key[r]);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) gs += __shfl_xor_sync(kFull, gs, o);
         if (a.mode == kVoxGradient) {
@@ -611,29 +600,26 @@ __device__ __forceinline__ void voxel_regs(const VoxelPassArgs<Real, OutT>& a, u
     if (lane == 0) a.out[j] = static_cast<OutT>(out);
 }
 
-// segments longer than the register budget: the keys go once to the scratch
-// array (same offsets as the voxel-major lists) and the selection reads them there
+// segments longer than the register budget, and those of the streamed
+// classes: the selection reads the keys where the key pass left them
+// (contiguous, through L1) instead of holding them
 template <typename Real, typename OutT>
 __device__ void voxel_stream(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uint64_t base, uint32_t M, int lane,
                              const CandBufs& cb) {
     using K = typename KeyOf<Real>::type;
     const Real lam = a.lam[j];
-    const bool keys = a.mode == kVoxMedian || a.mode == kVoxPercentile;
-    K* kp = a.scratch + base;
-    Real gs = 0;
-    for (uint32_t i = lane; i < M; i += 32) {
-        const auto lt = __ldcs(a.vm_LT + base + i);
-        const Real g = pair_g<Real>(ldg4(a.kvec + __ldcs(a.vm_mu + base + i)), lt.x, lt.y);
-        if (keys) kp[i] = to_key(Real(2) * lam + g * lam * lam);
-        else gs += g;
-    }
+    const PtrKeys<K> src{a.keys + base, M, lane};
     Real out;
-    if (keys) {
-        __syncwarp();  // the lanes' key stores are visible to the whole warp
-        const PtrKeys<K> src{kp, M, lane};
-        out = order_update<Real>(src, M, a.mode, a.pct, cb, lane, [](K x) { return from_key(x); },
-                                 static_cast<Pred<Real>*>(nullptr));
+    if (a.mode == kVoxMedian || a.mode == kVoxPercentile) {
+        auto val = [lam](K x) {
+            const Real g = from_key(x);
+            return Real(2) * lam + g * lam * lam;
+        };
+        out = order_update<Real>(src, M, a.mode, a.pct, cb, lane, val,
+                                 a.win ? reinterpret_cast<Pred<Real>*>(a.win) + j : nullptr);
     } else {
+        Real gs = 0;
+        src.each([&](K x) { gs += from_key(x); });
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) gs += __shfl_xor_sync(kFull, gs, o);
         if (a.mode == kVoxGradient) {
@@ -645,168 +631,49 @@ __device__ void voxel_stream(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uin
     if (lane == 0) a.out[j] = static_cast<OutT>(out);
 }
 
-// The keys of a voxel's pairs recomputed from the lists, C rows of 32 at a
-// time; f(key, element) is called for each element below M.
-template <typename Real, int C, typename OutT, class F>
-__device__ __forceinline__ void for_each_key(const VoxelPassArgs<Real, OutT>& a, uint64_t base, uint32_t M, Real lam,
-                                             int lane, F f) {
+// The key pass: every pair's order key to_key(g_ij), g_ij = k_i . W(L, T),
+// written in voxel-major order for the class kernels.  One thread per pair,
+// U pairs of a thread in flight at once; the lists stream through (loads
+// and stores marked evict-first) while the per-muon coefficients k_i, read
+// at random, stay in L2.
+constexpr int kKeyThreads = 256;
+template <typename Real>
+__global__ void __launch_bounds__(kKeyThreads)
+    k_pair_keys(const uint32_t* __restrict__ vm_mu, const typename Vec2<Real>::type* __restrict__ vm_LT,
+                const typename Vec4<Real>::type* __restrict__ kvec, typename KeyOf<Real>::type* __restrict__ keys,
+                uint64_t P) {
     using R2 = typename Vec2<Real>::type;
-    for (uint32_t r0 = 0; r0 * 32 < M; r0 += C) {
-        uint32_t mu[C];
-        R2 lt[C];
+    constexpr int U = 4;
+    constexpr uint64_t kTile = uint64_t(kKeyThreads) * U;
+    for (uint64_t t0 = uint64_t(blockIdx.x) * kTile; t0 < P; t0 += uint64_t(gridDim.x) * kTile) {
+        uint32_t mu[U];
+        R2 lt[U];
 #pragma unroll
-        for (int u = 0; u < C; ++u) {
-            const uint32_t e = (r0 + u) * 32 + lane;
-            if (e < M) {
-                mu[u] = __ldcs(a.vm_mu + base + e);
-                lt[u] = __ldcs(a.vm_LT + base + e);
+        for (int u = 0; u < U; ++u) {
+            const uint64_t i = t0 + uint64_t(u) * kKeyThreads + threadIdx.x;
+            if (i < P) {
+                mu[u] = __ldcs(vm_mu + i);
+                lt[u] = __ldcs(vm_LT + i);
             }
-        }
-#pragma unroll
-        for (int u = 0; u < C; ++u) {
-            const uint32_t e = (r0 + u) * 32 + lane;
-            if (e < M) {
-                const Real g = pair_g<Real>(ldg4(a.kvec + mu[u]), lt[u].x, lt[u].y);
-                f(to_key(Real(2) * lam + g * lam * lam), e);
-            }
-        }
-    }
-}
-
-// Segments selected without holding their keys: the first 32 keys are
-// sorted as samples, then one pass over the lists recomputes every key,
-// counts those below the window and appends those inside it to the warp's
-// ragged candidate buffer.  Rounds on the candidates follow
-// (select_candidates).  A window that misses, overflows the buffer or keeps
-// everything sends the segment to the scratch array (keys written once,
-// selected there).  Registers then hold only the loads in flight, whatever
-// the segment length.
-template <typename Real, typename OutT>
-__device__ void voxel_streamed(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uint64_t base, uint32_t M, int lane,
-                               const CandBufs& cb) {
-    using K = typename KeyOf<Real>::type;
-    using R2 = typename Vec2<Real>::type;
-    constexpr int C = 8;
-    const Real lam = a.lam[j];
-    if (a.mode == kVoxMean || a.mode == kVoxGradient) {
-        Real gs = 0;
-        for (uint32_t i = lane; i < M; i += 32) {
-            const R2 lt = __ldcs(a.vm_LT + base + i);
-            gs += pair_g<Real>(ldg4(a.kvec + __ldcs(a.vm_mu + base + i)), lt.x, lt.y);
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) gs += __shfl_xor_sync(kFull, gs, o);
-        if (a.mode == kVoxGradient) {
-            if (lane == 0) a.grad[j] = -a.lam64[j] * static_cast<double>(gs);
-        } else if (lane == 0) {
-            a.out[j] = static_cast<OutT>(lam + lam * lam * gs / (Real(2) * static_cast<Real>(M)));
-        }
-        return;
-    }
-    // rank of the wanted order statistic (src/MutoMLSD.cpp:500-516)
-    uint32_t k, jm = 0;
-    if (a.mode == kVoxMedian) {
-        k = M / 2;
-    } else {
-        jm = u32_cast_x86(a.pct / 100.0 * M);
-        if (jm < 1) jm = 1;
-        if (jm > M) jm = M;
-        k = jm - 1;
-    }
-    K* ba = static_cast<K*>(cb.a);
-    K* bb = static_cast<K*>(cb.b);
-    Sel<K> sel;
-    bool done = false;
-    {
-        // samples: the segment's first 32 keys (M > 64: all present)
-        const R2 lt0 = __ldcs(a.vm_LT + base + lane);
-        const Real g0 = pair_g<Real>(ldg4(a.kvec + __ldcs(a.vm_mu + base + lane)), lt0.x, lt0.y);
-        const K s = sort32(to_key(Real(2) * lam + g0 * lam * lam), lane);
-        const int pos = static_cast<int>((static_cast<float>(k) * 32.0f) / static_cast<float>(M));
-        const int ql = pos - 6, qh = pos + 6;
-        const K slo = __shfl_sync(kFull, s, ql < 0 ? 0 : (ql > 31 ? 31 : ql));
-        const K shi = __shfl_sync(kFull, s, qh > 31 ? 31 : (qh < 0 ? 0 : qh));
-        const K lo = ql <= 0 ? K(0) : slo;
-        const K hi = qh >= 31 ? empty_key<K>() - 1 : shi;
-        uint32_t c_lo = 0, t = 0;
-        const uint32_t cap = cb.rows;
-        for_each_key<Real, C>(a, base, M, lam, lane, [&](K x, uint32_t) {
-            if (x < lo) {
-                ++c_lo;
-            } else if (x <= hi) {
-                if (t < cap) ba[t * 32 + lane] = x;
-                ++t;
-            }
-        });
-        const uint32_t below = __reduce_add_sync(kFull, c_lo);
-        const uint32_t n_in = __reduce_add_sync(kFull, t);
-        const uint32_t rows = __reduce_max_sync(kFull, t);
-        __syncwarp();
-        if (rows <= cap && below <= k && k < below + n_in && n_in < M) {
-            sel = select_candidates<K>(ba, bb, cap, t, rows, n_in, k - below, lane);
-            done = true;
+        for (int u = 0; u < U; ++u) {
+            const uint64_t i = t0 + uint64_t(u) * kKeyThreads + threadIdx.x;
+            if (i < P) __stcs(keys + i, to_key(pair_g<Real>(ldg4(kvec + mu[u]), lt[u].x, lt[u].y)));
         }
     }
-    if (!done) {  // the scratch array, at the segment's own offsets
-        K* kp = a.scratch + base;
-        for_each_key<Real, C>(a, base, M, lam, lane, [&](K x, uint32_t e) { kp[e] = x; });
-        __syncwarp();
-        const PtrKeys<K> src{kp, M, lane};
-        sel = kth_select<K>(src, M, k, ba, bb, cb.rows, lane);
-    }
-    Real out;
-    if (a.mode == kVoxMedian) {
-        const Real v1 = from_key(sel.kth);
-        if (M % 2 == 0) {
-            Real v0;
-            if (sel.have_prev) {
-                v0 = from_key(sel.prev);
-            } else {  // v1 itself or the largest key below it
-                uint32_t c = 0;
-                K mb = K(0);
-                for_each_key<Real, C>(a, base, M, lam, lane, [&](K x, uint32_t) {
-                    if (x < sel.kth) {
-                        ++c;
-                        mb = x > mb ? x : mb;
-                    }
-                });
-                c = __reduce_add_sync(kFull, c);
-                mb = warp_max_k(mb);
-                v0 = c < M / 2 ? v1 : from_key(mb);
-            }
-            out = (v1 + v0) * Real(0.25);
-        } else {
-            out = v1 * Real(0.5);
-        }
-    } else {  // mean of the lowest jm values
-        const Real tk = from_key(sel.kth);
-        Real sum = 0;
-        uint32_t c = 0;
-        for_each_key<Real, C>(a, base, M, lam, lane, [&](K x, uint32_t) {
-            if (x < sel.kth) {
-                sum += from_key(x);
-                ++c;
-            }
-        });
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
-        c = __reduce_add_sync(kFull, c);
-        sum += static_cast<Real>(jm - c) * tk;
-        out = sum / static_cast<Real>(jm) * Real(0.5);
-    }
-    if (lane == 0) a.out[j] = static_cast<OutT>(out);
 }
 
 // Voxels of class C, one warp per voxel: registers hold vox_class_rows(C)
-// keys per lane (the last class selects from the scratch array).  Each warp
-// also prefetches into L2 the pair lists of the voxel `ahead` places further
-// down the class list, which a warp of the next wave of resident blocks will
-// read.  Dynamic shared memory: two candidate buffers per warp.
+// keys per lane (the last class, and streamed classes, select from the key
+// array).  Each warp also prefetches into L2 the keys of the voxel `ahead`
+// places further down the class list, which a warp of the next wave of
+// resident blocks will read.  Dynamic shared memory: two candidate buffers
+// per warp.
 template <typename Real, typename OutT, int C, bool STREAMED>
 __global__ void __launch_bounds__(kVoxThreads, vox_min_blocks(C, STREAMED))
     k_em_voxel(VoxelPassArgs<Real, OutT> a, const VoxDesc* __restrict__ desc, uint32_t n, uint32_t ahead) {
     using K = typename KeyOf<Real>::type;
-    using R2 = typename Vec2<Real>::type;
     constexpr int R = vox_class_rows(C);
     constexpr int RB = cand_rows<K, C, STREAMED>();
     if constexpr (R * 32 > static_cast<int>(voxel_register_cap<Real>()) || (STREAMED && !streamable(C))) {
@@ -821,10 +688,7 @@ __global__ void __launch_bounds__(kVoxThreads, vox_min_blocks(C, STREAMED))
         const VoxDesc d = desc[w];
         if (lane == 0 && w + ahead < n) {
             const VoxDesc f = desc[w + ahead];
-            if (f.M > 0) {
-                prefetch_l2(a.vm_mu + f.start, size_t(f.M) * sizeof(uint32_t));
-                prefetch_l2(a.vm_LT + f.start, size_t(f.M) * sizeof(R2));
-            }
+            if (f.M > 0) prefetch_l2(a.keys + f.start, size_t(f.M) * sizeof(K));
         }
         if (d.M == 0) {  // no muon crossed the voxel, src/MutoMLSD.cpp:494-496
             if (lane == 0) {
@@ -833,9 +697,8 @@ __global__ void __launch_bounds__(kVoxThreads, vox_min_blocks(C, STREAMED))
             }
             return;
         }
-        if constexpr (STREAMED) voxel_streamed<Real, OutT>(a, d.j, d.start, d.M, lane, cb);
-        else if constexpr (R > 0) voxel_regs<Real, R>(a, d.j, d.start, d.M, lane, cb);
-        else voxel_stream<Real, OutT>(a, d.j, d.start, d.M, lane, cb);
+        if constexpr (STREAMED || R == 0) voxel_stream<Real, OutT>(a, d.j, d.start, d.M, lane, cb);
+        else voxel_regs<Real, R>(a, d.j, d.start, d.M, lane, cb);
     }
 }
 
@@ -1011,6 +874,12 @@ template <typename Real, typename OutT, int... C>
 void launch_all(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists, const uint32_t* counts,
                 const int* resident_blocks, uint32_t streamed, cudaStream_t s, std::integer_sequence<int, C...>) {
     using K = typename KeyOf<Real>::type;
+    if (a.P > 0) {
+        constexpr uint64_t kTile = uint64_t(kKeyThreads) * 4;
+        const uint64_t nb = std::min<uint64_t>((a.P + kTile - 1) / kTile, uint64_t(1) << 22);
+        k_pair_keys<Real><<<static_cast<unsigned>(nb), kKeyThreads, 0, s>>>(a.vm_mu, a.vm_LT, a.kvec, a.keys, a.P);
+        count_launches(1);
+    }
     auto one = [&](auto cc) {
         constexpr int c = decltype(cc)::value;
         if (counts[c] == 0) return;

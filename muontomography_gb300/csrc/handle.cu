@@ -321,7 +321,7 @@ struct muto_handle {
     int vox_blocks_real[2 * kVoxClasses] = {}, vox_blocks_f64[2 * kVoxClasses] = {};  // resident blocks per class kernel
     uint32_t vox_streamed = 0;  // classes selected by the streamed path
     uint64_t vclass_off[kVoxClasses] = {};
-    DevMem mult, start, kvec, keys;   // keys: scratch for voxels beyond the register budget
+    DevMem mult, start, kvec, keys;   // keys: the voxel pass's order key of every pair
     DevMem win;                       // per voxel: the last selection window (center, half-width)
     bool brick = false;               // path voxel indices are bricked (single scans), see lam_b
     BrickDims bdims{};
@@ -740,14 +740,11 @@ void prepare_em(muto_handle* h) {
             h->vclass_off[c] = bnd[c];
             h->vclass_n[c] = static_cast<uint32_t>(bnd[c + 1] - bnd[c]);
         }
-        // segments beyond the register budget, and the fall-back of streamed
-        // ones, select from a scratch key array
+        // the voxel pass's key array (kPad past the end: the class kernels'
+        // L2 prefetches round out to 16 bytes)
         h->vox_streamed = P.voxel_stream_above < 0 ? 0u
                           : vox_streamed_mask(static_cast<uint32_t>(std::min<long long>(P.voxel_stream_above, 0xffffffffLL)));
-        bool need_keys = h->vclass_n[kVoxClasses - 1] > 0;
-        for (int c = 0; c < kVoxClasses; ++c)
-            if (((h->vox_streamed >> c) & 1u) && h->vclass_n[c] > 0) need_keys = true;
-        if (need_keys) h->keys.alloc(std::max<uint64_t>(Pn, 1) * sizeof(typename KeyOf<Real>::type), &h->dev_bytes);
+        h->keys.alloc((Pn + kPad) * sizeof(typename KeyOf<Real>::type), &h->dev_bytes);
         em_voxel_occupancy<Real, Real>(h->vox_blocks_real);
         em_voxel_occupancy<Real, double>(h->vox_blocks_f64);
         for (int c = 0; c < 2 * kVoxClasses; ++c) {
@@ -968,7 +965,8 @@ VoxelPassArgs<Real, OutT> voxel_args(muto_handle* h, const Real* lam, int mode, 
     v.out = out;
     v.grad = nullptr;
     v.lam64 = nullptr;
-    v.scratch = h->keys.empty() ? nullptr : h->keys.as<typename KeyOf<Real>::type>();
+    v.keys = h->keys.as<typename KeyOf<Real>::type>();
+    v.P = h->npairs;
     v.win = (mode == kVoxMedian || mode == kVoxPercentile) && !h->win.empty() ? h->win.as<Real>() : nullptr;
     return v;
 }
@@ -1184,13 +1182,11 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
         kv[i].y = kv[i].z = kv[i].w = Real(0);
     }
     std::vector<VoxDesc> cls[kVoxClasses];
-    uint32_t mmax = 0;
     for (uint32_t j = 0; j < n_segs; ++j) {
         const uint64_t m64 = seg_off[j + 1] - seg_off[j];
         if (seg_off[j + 1] < seg_off[j] || seg_off[j + 1] > n || m64 > 0xffffffffull)
             throw Error(MUTO_ERR_ARG, "segment offsets must be non-decreasing and within the values");
         const uint32_t m = static_cast<uint32_t>(m64);
-        mmax = std::max(mmax, m);
         cls[vox_class_of<Real>(m)].push_back(VoxDesc{j, m, seg_off[j]});
     }
     std::vector<Real> lam(n_segs, Real(1));
@@ -1202,8 +1198,7 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
     d_lam.alloc(std::max<uint64_t>(n_segs, 1) * sizeof(Real), nullptr);
     d_out.alloc(std::max<uint64_t>(n_segs, 1) * sizeof(Real), nullptr);
     d_desc.alloc(std::max<uint64_t>(n_segs, 1) * sizeof(VoxDesc), nullptr);
-    if (mmax > voxel_register_cap<Real>() || (streamed && mmax > 256u))
-        d_keys.alloc(np * sizeof(typename KeyOf<Real>::type), nullptr);
+    d_keys.alloc(np * sizeof(typename KeyOf<Real>::type), nullptr);
     d_win.alloc(std::max<uint64_t>(n_segs, 1) * 2 * sizeof(Real), nullptr);
     CK(cudaMemsetAsync(d_win.as<void>(), 0, std::max<uint64_t>(n_segs, 1) * 2 * sizeof(Real), s));
     if (n) {
@@ -1237,7 +1232,8 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
     v.mode = mode;
     v.pct = pct;
     v.out = d_out.as<Real>();
-    v.scratch = d_keys.empty() ? nullptr : d_keys.as<typename KeyOf<Real>::type>();
+    v.keys = d_keys.as<typename KeyOf<Real>::type>();
+    v.P = n;
     v.win = mode == kVoxMedian || mode == kVoxPercentile ? d_win.as<Real>() : nullptr;
     for (uint32_t rep = 0; rep < repeat; ++rep) {  // each pass its own values; windows carry over
         for (uint64_t i = 0; i < n; ++i) kv[i].x = static_cast<Real>(values[rep * n + i]);
