@@ -228,14 +228,25 @@ struct alignas(16) VoxDesc {
     uint32_t j, M;
     unsigned long long start;
 };
-// lists[c], counts[c]: the descriptors of class c; resident_blocks[c] and
-// [kVoxClasses + c]: blocks of class c's register and streamed kernels
-// resident on the whole GPU at once; bit c of `streamed`: class c (M > 256
-// only) is selected without holding its keys in registers, which needs the
-// scratch array for its fallback.
+// Side streams the class kernels of a voxel pass are spread over (they touch
+// disjoint voxels), with the events that fork them from the launching stream
+// and join them back; inside stream capture they become parallel branches.
+struct ClassFan {
+    static constexpr int kSide = 3;
+    cudaStream_t side[kSide];
+    cudaEvent_t fork, join[kSide];
+    int n = 0;  // side streams in use (0: every class on the launching stream)
+};
+// The key pass over a.P pairs, then the class kernels.  lists[c], counts[c]:
+// the descriptors of class c; resident_blocks[c] and [kVoxClasses + c]:
+// blocks of class c's register and streamed kernels resident on the whole
+// GPU at once; bit c of `streamed`: class c (M > 256 only) selects from the
+// key array instead of holding its keys in registers; num_sms sizes the key
+// pass's grid.
 template <typename Real, typename OutT>
 void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists, const uint32_t* counts,
-                     const int* resident_blocks, uint32_t streamed, cudaStream_t s);
+                     const int* resident_blocks, uint32_t streamed, int num_sms, const ClassFan* fan,
+                     cudaStream_t s);
 // Bricked voxel order for the muon pass's lambda gathers: 4x4x4 bricks of
 // 64 consecutive entries, so the neighbouring voxels of a muon's path share
 // cache lines instead of lying a grid row or plane apart.
@@ -272,6 +283,12 @@ void launch_brick_lambda(const Real* lam, uint32_t V, BrickDims b, Real* lam_b, 
 // more (exclusive scan; class c starts at first[c * blocks]); scan_scratch
 // as for scan_u32_to_u64 of that length
 uint32_t voxel_class_blocks(uint64_t V);
+// start (V+1) of each voxel's voxel-major segment from the pair counts:
+// segments laid out in the column order of column_order's grid when it
+// covers the V voxels (mcol: V, scol: V+1 entries of scratch), else in index
+// order; scan_scratch as for scan_u32_to_u64 of V
+void launch_segment_starts(const uint32_t* mult, uint32_t V, const muto_grid* column_order, uint32_t* mcol,
+                           uint64_t* scol, void* scan_scratch, uint64_t* start, cudaStream_t s);
 template <typename Real>
 void launch_voxel_classes(const uint32_t* mult, const uint64_t* start, uint32_t V, const muto_grid* column_order,
                           uint32_t* counts, uint64_t* first, void* scan_scratch, VoxDesc* out, cudaStream_t s);

@@ -633,25 +633,30 @@ __device__ void voxel_stream(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uin
 
 // The key pass: every pair's order key to_key(g_ij), g_ij = k_i . W(L, T),
 // written in voxel-major order for the class kernels.  One thread per pair,
-// U pairs of a thread in flight at once; the lists stream through (loads
-// and stores marked evict-first) while the per-muon coefficients k_i, read
-// at random, stay in L2.
-constexpr int kKeyThreads = 256;
+// U pairs of a thread in flight at once.  Each block streams one contiguous
+// range of the lists, tile after tile, so the segments of vertically
+// adjacent voxels (laid out next to each other) go through the same SM: a
+// steep muon's coefficients k_i, gathered for one segment, are still in L1
+// for the next.  The lists and the keys pass through marked evict-first.
+constexpr int kKeyThreads = 1024;
+constexpr int kKeyUnroll = 8;
+constexpr uint64_t kKeyTile = uint64_t(kKeyThreads) * kKeyUnroll;
 template <typename Real>
 __global__ void __launch_bounds__(kKeyThreads)
     k_pair_keys(const uint32_t* __restrict__ vm_mu, const typename Vec2<Real>::type* __restrict__ vm_LT,
                 const typename Vec4<Real>::type* __restrict__ kvec, typename KeyOf<Real>::type* __restrict__ keys,
-                uint64_t P) {
+                uint64_t P, uint64_t range) {
     using R2 = typename Vec2<Real>::type;
-    constexpr int U = 4;
-    constexpr uint64_t kTile = uint64_t(kKeyThreads) * U;
-    for (uint64_t t0 = uint64_t(blockIdx.x) * kTile; t0 < P; t0 += uint64_t(gridDim.x) * kTile) {
+    constexpr int U = kKeyUnroll;
+    const uint64_t r0 = uint64_t(blockIdx.x) * range;
+    const uint64_t r1 = r0 + range < P ? r0 + range : P;
+    for (uint64_t t0 = r0; t0 < r1; t0 += kKeyTile) {
         uint32_t mu[U];
         R2 lt[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const uint64_t i = t0 + uint64_t(u) * kKeyThreads + threadIdx.x;
-            if (i < P) {
+            if (i < r1) {
                 mu[u] = __ldcs(vm_mu + i);
                 lt[u] = __ldcs(vm_LT + i);
             }
@@ -659,7 +664,7 @@ __global__ void __launch_bounds__(kKeyThreads)
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const uint64_t i = t0 + uint64_t(u) * kKeyThreads + threadIdx.x;
-            if (i < P) __stcs(keys + i, to_key(pair_g<Real>(ldg4(kvec + mu[u]), lt[u].x, lt[u].y)));
+            if (i < r1) __stcs(keys + i, to_key(pair_g<Real>(ldg4(kvec + mu[u]), lt[u].x, lt[u].y)));
         }
     }
 }
@@ -872,17 +877,50 @@ void occupancy_all(int* regs, int* streamed, std::integer_sequence<int, C...>) {
 
 template <typename Real, typename OutT, int... C>
 void launch_all(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists, const uint32_t* counts,
-                const int* resident_blocks, uint32_t streamed, cudaStream_t s, std::integer_sequence<int, C...>) {
+                const int* resident_blocks, uint32_t streamed, int num_sms, const ClassFan* fan, cudaStream_t s,
+                std::integer_sequence<int, C...>) {
     using K = typename KeyOf<Real>::type;
-    if (a.P > 0) {
-        constexpr uint64_t kTile = uint64_t(kKeyThreads) * 4;
-        const uint64_t nb = std::min<uint64_t>((a.P + kTile - 1) / kTile, uint64_t(1) << 22);
-        k_pair_keys<Real><<<static_cast<unsigned>(nb), kKeyThreads, 0, s>>>(a.vm_mu, a.vm_LT, a.kvec, a.keys, a.P);
+    if (a.P > 0) {  // one block per SM, each a contiguous range of whole tiles
+        const uint64_t tiles = (a.P + kKeyTile - 1) / kKeyTile;
+        const uint64_t want = static_cast<uint64_t>(num_sms > 0 ? num_sms : 1);
+        const uint64_t per = (tiles + want - 1) / want;
+        const uint64_t nb = (tiles + per - 1) / per;
+        k_pair_keys<Real><<<static_cast<unsigned>(nb), kKeyThreads, 0, s>>>(a.vm_mu, a.vm_LT, a.kvec, a.keys, a.P,
+                                                                           per * kKeyTile);
         count_launches(1);
+    }
+    // classes to streams: the heaviest first, each to the least loaded stream
+    // (work ~ voxels x a typical segment length of the class)
+    cudaStream_t on[kVoxClasses];
+    for (int c = 0; c < kVoxClasses; ++c) on[c] = s;
+    const int ns = fan ? 1 + std::min(fan->n, ClassFan::kSide) : 1;
+    if (ns > 1) {
+        double work[kVoxClasses], load[1 + ClassFan::kSide] = {};
+        int order[kVoxClasses];
+        for (int c = 0; c < kVoxClasses; ++c) {
+            const double lo = c == 0 ? 0.0 : vox_class_hi(c - 1);
+            const double m = c == kVoxClasses - 1 ? 4.0 * lo : 0.5 * (lo + vox_class_hi(c));
+            work[c] = static_cast<double>(counts[c]) * (m + 32.0);
+            order[c] = c;
+        }
+        std::sort(order, order + kVoxClasses, [&](int x, int y) { return work[x] > work[y]; });
+        // failures here surface through cudaGetLastError after the pass
+        (void)cudaEventRecord(fan->fork, s);
+        for (int k = 1; k < ns; ++k) (void)cudaStreamWaitEvent(fan->side[k - 1], fan->fork, 0);
+        for (int q = 0; q < kVoxClasses; ++q) {
+            const int c = order[q];
+            if (counts[c] == 0) continue;
+            int best = 0;
+            for (int k = 1; k < ns; ++k)
+                if (load[k] < load[best]) best = k;
+            load[best] += work[c];
+            on[c] = best == 0 ? s : fan->side[best - 1];
+        }
     }
     auto one = [&](auto cc) {
         constexpr int c = decltype(cc)::value;
         if (counts[c] == 0) return;
+        cudaStream_t s = on[c];
         const bool st = streamable(c) && ((streamed >> c) & 1u);
         const unsigned nb = blocks_for(static_cast<uint64_t>(counts[c]) * 32u, kVoxThreads);
         const uint32_t ahead = static_cast<uint32_t>(resident_blocks[st ? kVoxClasses + c : c]) * kWarps;
@@ -895,6 +933,12 @@ void launch_all(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists,
         count_launches(1);
     };
     (one(std::integral_constant<int, C>{}), ...);
+    if (ns > 1) {
+        for (int k = 1; k < ns; ++k) {
+            (void)cudaEventRecord(fan->join[k - 1], fan->side[k - 1]);
+            (void)cudaStreamWaitEvent(s, fan->join[k - 1], 0);
+        }
+    }
 }
 
 template <typename Real, typename OutT>
@@ -908,16 +952,20 @@ template void em_voxel_occupancy<double, double>(int*);
 
 template <typename Real, typename OutT>
 void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists, const uint32_t* counts,
-                     const int* resident_blocks, uint32_t streamed, cudaStream_t s) {
-    launch_all<Real, OutT>(a, lists, counts, resident_blocks, streamed, s,
+                     const int* resident_blocks, uint32_t streamed, int num_sms, const ClassFan* fan,
+                     cudaStream_t s) {
+    launch_all<Real, OutT>(a, lists, counts, resident_blocks, streamed, num_sms, fan, s,
                            std::make_integer_sequence<int, kVoxClasses>{});
 }
 template void launch_em_voxel<float, float>(const VoxelPassArgs<float, float>&, const VoxDesc* const*,
-                                            const uint32_t*, const int*, uint32_t, cudaStream_t);
+                                            const uint32_t*, const int*, uint32_t, int, const ClassFan*,
+                                            cudaStream_t);
 template void launch_em_voxel<float, double>(const VoxelPassArgs<float, double>&, const VoxDesc* const*,
-                                             const uint32_t*, const int*, uint32_t, cudaStream_t);
+                                             const uint32_t*, const int*, uint32_t, int, const ClassFan*,
+                                             cudaStream_t);
 template void launch_em_voxel<double, double>(const VoxelPassArgs<double, double>&, const VoxDesc* const*,
-                                              const uint32_t*, const int*, uint32_t, cudaStream_t);
+                                              const uint32_t*, const int*, uint32_t, int, const ClassFan*,
+                                              cudaStream_t);
 
 void launch_finalize_cost(Counters* ctr, double n_muons, double* hist, uint32_t cap, cudaStream_t s) {
     k_finalize_cost<<<1, 1, 0, s>>>(ctr, n_muons, hist, cap);

@@ -282,6 +282,7 @@ struct muto_handle {
     Params P;
     muto_grid grid{};          // current grid (may be adopted from the initial image)
     cudaStream_t stream = nullptr;
+    ClassFan fan;                 // side streams of the voxel pass's class kernels
     int device = 0, num_sms = 148;
     size_t smem_optin = 0;
     std::atomic<uint64_t> dev_bytes{0};
@@ -361,6 +362,11 @@ struct muto_handle {
     }
     ~muto_handle() {
         drop_graph();
+        for (int k = 0; k < fan.n; ++k) {
+            cudaStreamDestroy(fan.side[k]);
+            cudaEventDestroy(fan.join[k]);
+        }
+        if (fan.n) cudaEventDestroy(fan.fork);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -694,7 +700,18 @@ void prepare_em(muto_handle* h) {
     CK(cudaMemsetAsync(h->mult.as<void>(), 0, V * sizeof(uint32_t), s));
     run(h, "voxel_hist", [&] { launch_voxel_hist(h->vidx.as<uint32_t>(), Pn, static_cast<uint32_t>(V), h->mult.as<uint32_t>(), h->ctr(), s); });
     h->start.alloc((V + 1) * sizeof(uint64_t), &h->dev_bytes);
-    run(h, "scan", [&] { scan_u32_to_u64(h->mult.as<uint32_t>(), h->start.as<uint64_t>(), V, scratch.as<void>(), s); });
+    {
+        DevMem mcol, scol;
+        if (!h->batch) {
+            mcol.alloc(std::max<uint64_t>(V, 1) * sizeof(uint32_t), &h->dev_bytes);
+            scol.alloc((V + 1) * sizeof(uint64_t), &h->dev_bytes);
+        }
+        run(h, "scan", [&] {
+            launch_segment_starts(h->mult.as<uint32_t>(), static_cast<uint32_t>(V), h->batch ? nullptr : &h->grid,
+                                  mcol.as<uint32_t>(), scol.as<uint64_t>(), scratch.as<void>(), h->start.as<uint64_t>(), s);
+        });
+        CK(cudaStreamSynchronize(s));
+    }
     {
         DevMem cursor;
         cursor.alloc(V * sizeof(uint32_t), &h->dev_bytes);
@@ -977,7 +994,7 @@ void launch_voxel_pass(muto_handle* h, const VoxelPassArgs<Real, OutT>& v, cudaS
     for (int c = 0; c < kVoxClasses; ++c) lists[c] = h->vclass.as<VoxDesc>() + h->vclass_off[c];
     launch_em_voxel<Real, OutT>(v, lists, h->vclass_n,
                                 std::is_same<OutT, Real>::value ? h->vox_blocks_real : h->vox_blocks_f64,
-                                h->vox_streamed, s);
+                                h->vox_streamed, h->num_sms, &h->fan, s);
 }
 
 int voxel_mode(const Params& P) {
@@ -1238,7 +1255,7 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
     for (uint32_t rep = 0; rep < repeat; ++rep) {  // each pass its own values; windows carry over
         for (uint64_t i = 0; i < n; ++i) kv[i].x = static_cast<Real>(values[rep * n + i]);
         if (n) CK(cudaMemcpyAsync(d_kv.as<void>(), kv.data(), n * sizeof(R4), cudaMemcpyHostToDevice, s));
-        launch_em_voxel<Real, Real>(v, lists, counts, resident, streamed, s);
+        launch_em_voxel<Real, Real>(v, lists, counts, resident, streamed, sms, nullptr, s);
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(s));  // kv is rewritten by the next pass
     }
@@ -1273,6 +1290,12 @@ int muto_create(const char* method, const char* config_json, muto_handle** out) 
         CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
         h->smem_optin = static_cast<size_t>(optin);
         CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&h->fan.fork, cudaEventDisableTiming));
+        for (int k = 0; k < ClassFan::kSide; ++k) {
+            CK(cudaStreamCreateWithFlags(&h->fan.side[k], cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&h->fan.join[k], cudaEventDisableTiming));
+            h->fan.n = k + 1;
+        }
         alloc_counters(h.get());
         CK(cudaStreamSynchronize(h->stream));
     });

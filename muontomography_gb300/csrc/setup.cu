@@ -388,6 +388,23 @@ __device__ __forceinline__ uint32_t class_order_voxel(uint32_t t, uint32_t nx, u
     return r % nx + nx * (r / nx + ny * z);
 }
 
+// Segment starts in column order: the voxel-major segments of vertically
+// adjacent voxels sit next to each other, so a stream through the lists
+// meets a steep muon in several consecutive segments (its coefficients are
+// still in L1 the second time).  mcol[t] = M of the t-th voxel in column
+// order; after the scan, start[j] = scol[t] for that voxel.
+__global__ void k_column_mult(const uint32_t* __restrict__ mult, uint32_t V, uint32_t nx, uint32_t ny, uint32_t nz,
+                              uint32_t* __restrict__ mcol) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < V) mcol[t] = mult[class_order_voxel(t, nx, ny, nz)];
+}
+__global__ void k_column_starts(const uint64_t* __restrict__ scol, uint32_t V, uint32_t nx, uint32_t ny, uint32_t nz,
+                                uint64_t* __restrict__ start) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < V) start[class_order_voxel(t, nx, ny, nz)] = scol[t];
+    if (t == 0) start[V] = scol[V];
+}
+
 template <typename Real>
 __global__ void k_class_count(const uint32_t* __restrict__ mult, uint32_t V, uint32_t nblocks, uint32_t nx,
                               uint32_t ny, uint32_t nz, uint32_t* __restrict__ counts) {
@@ -573,6 +590,21 @@ void launch_siddon_batch(muto_grid g, const double* p1, const double* p2, uint64
 namespace muto {
 
 uint32_t voxel_class_blocks(uint64_t V) { return blocks_for(V); }
+
+void launch_segment_starts(const uint32_t* mult, uint32_t V, const muto_grid* column_order, uint32_t* mcol,
+                           uint64_t* scol, void* scan_scratch, uint64_t* start, cudaStream_t s) {
+    if (!column_order || static_cast<uint64_t>(column_order->nx) * column_order->ny * column_order->nz != V ||
+        V == 0) {
+        scan_u32_to_u64(mult, start, V, scan_scratch, s);
+        return;
+    }
+    const uint32_t nx = column_order->nx, ny = column_order->ny, nz = column_order->nz;
+    k_column_mult<<<blocks_for(V), kThreads, 0, s>>>(mult, V, nx, ny, nz, mcol);
+    count_launches(1);
+    scan_u32_to_u64(mcol, scol, V, scan_scratch, s);
+    k_column_starts<<<blocks_for(V), kThreads, 0, s>>>(scol, V, nx, ny, nz, start);
+    count_launches(1);
+}
 
 template <typename Real>
 void launch_voxel_classes(const uint32_t* mult, const uint64_t* start, uint32_t V, const muto_grid* column_order,
