@@ -82,9 +82,11 @@ typedef struct muto_handle muto_handle;
  * Reconstruction handles
  * ------------------------------------------------------------------------- */
 
-/* Create a reconstruction: method is "poca", "mlsd" or "map"; config_json is
- * the JSON object of that method (the value of the "poca"/"mlsd"/"map" key,
- * as passed to the constructors MutoPoCA(json) src/MutoPoCA.cpp:74,
+/* Create a reconstruction: method is "poca", "pocut", "mlsd" or "map";
+ * config_json is the JSON object of that method (the value of the
+ * "poca"/"pocut"/"mlsd"/"map" key, as passed to the constructors
+ * MutoPoCA(json) src/MutoPoCA.cpp:74, MutoPoCut(json) src/MutoPoCut.cpp:12
+ * (PoCA's keys plus "cut_percentile", 1.0; straight_line is always off),
  * MutoMLSD(json) src/MutoMLSD.cpp:47, MutoMAP(json) src/MutoMAP.cpp:75).
  * The reference's keys and defaults apply; extra keys: "precision"
  * ("mixed" default, or "fp64"), "use_graph" (true), "random_seed",

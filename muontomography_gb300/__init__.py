@@ -24,7 +24,7 @@ from . import _lib
 from ._lib import MutoError, check
 
 __all__ = [
-    "Grid", "Block", "X0_MM", "RAY_FIELDS", "MutoError", "Reconstruction", "MutoPoCA", "MutoMLSD", "MutoMAP",
+    "Grid", "Block", "X0_MM", "RAY_FIELDS", "MutoError", "Reconstruction", "MutoPoCA", "MutoPoCut", "MutoMLSD", "MutoMAP",
     "phantom", "generate", "lambda_from_x0", "save_image", "load_image", "siddon_batch", "library", "Batch",
 ]
 
@@ -124,7 +124,7 @@ def _flat(img: np.ndarray) -> np.ndarray:
 
 
 class Reconstruction:
-    """One reconstruction handle (``muto_create``).  method: poca | mlsd | map."""
+    """One reconstruction handle (``muto_create``).  method: poca | pocut | mlsd | map."""
 
     def __init__(self, method: str, config: dict | str | None = None):
         self._lib = library()
@@ -178,7 +178,7 @@ class Reconstruction:
         # the output size follows the grid after the initial image is resolved: stage it
         self.load_tracks(rays)
         self.prepare()
-        if self.method != "poca":
+        if self.method not in ("poca", "pocut"):
             self.iterate(self.config_iterations())
         return self.image()
 
@@ -285,6 +285,14 @@ class MutoPoCA(Reconstruction):
 
     def __init__(self, config: dict | None = None):
         super().__init__("poca", config)
+
+
+class MutoPoCut(Reconstruction):
+    """MutoPoCut(json) / reconstruct (src/MutoPoCut.cpp:12-121): PoCA keeping, per
+    voxel, the lowest ``cut_percentile`` of the scattering values (default 1.0)."""
+
+    def __init__(self, config: dict | None = None):
+        super().__init__("pocut", config)
 
 
 class MutoMLSD(Reconstruction):

@@ -66,6 +66,10 @@ Image MutoGpuReconstruction::fetchImage() {
 // ---------------------------------------------------------------------------
 MutoPoCA::MutoPoCA() : MutoGpuReconstruction("poca", empty_object()) {}
 MutoPoCA::MutoPoCA(json config) : MutoGpuReconstruction("poca", config) {}
+MutoPoCA::MutoPoCA(const char* method, json config) : MutoGpuReconstruction(method, config) {}
+
+MutoPoCut::MutoPoCut() : MutoPoCA("pocut", empty_object()) {}
+MutoPoCut::MutoPoCut(json config) : MutoPoCA("pocut", config) {}
 
 Image MutoPoCA::reconstruct(const MutoMuonData& rays) {
     if (!fHandle) return Image{};

@@ -2,6 +2,7 @@
 // the C ABI (include/muto_gb300.h):
 //   MutoVReconstruction   include/MutoVReconstruction.h:11-16
 //   MutoPoCA(json)        include/MutoPoCA.h:17-50
+//   MutoPoCut(json)       include/MutoPoCut.h:13-28 (derives from MutoPoCA)
 //   MutoMLSD(json)        include/MutoMLSD.h:27-107
 //   MutoMAP(json)         include/MutoMAP.h:16-63 (derives from MutoMLSD)
 // Constructors take the method's JSON object with the reference's keys and
@@ -51,6 +52,16 @@ public:
     MutoPoCA();
     explicit MutoPoCA(json config);
     Image reconstruct(const MutoMuonData& rays) override;
+
+protected:
+    MutoPoCA(const char* method, json config);
+};
+
+// PoCA keeping, per voxel, the lowest cut_percentile of the scattering values
+class MutoPoCut : public MutoPoCA {
+public:
+    MutoPoCut();
+    explicit MutoPoCut(json config);
 };
 
 class MutoMLSD : public MutoGpuReconstruction {

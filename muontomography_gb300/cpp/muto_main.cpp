@@ -1,6 +1,6 @@
 // Command-line driver (the reference's MuToTest.cpp:15-83): reads a JSON
 // config, loads the raw-hit data files, reconstructs with the method whose
-// key is present ("poca", "mlsd" or "map") on the GPU and writes the image.
+// key is present ("poca", "mlsd", "map" or "pocut") on the GPU and writes the image.
 //
 // Top-level keys: data_files, detector_height, detector_middle, output_file;
 // optional data_precision (4 = float32 records, the default; 8 = float64).
@@ -57,8 +57,12 @@ int main(int argc, char** argv) {
         method = "map";
         rec.reset(new MutoMAP(config.get("map")));
         header.nIter = iterations("map");
+    } else if (config.exist("pocut")) {
+        method = "pocut";
+        rec.reset(new MutoPoCut(config.get("pocut")));
+        header.nIter = 1;
     } else {
-        std::cerr << "No supported reconstruction key (poca, mlsd, map) in " << path << std::endl;
+        std::cerr << "No supported reconstruction key (poca, mlsd, map, pocut) in " << path << std::endl;
         return 1;
     }
     if (!rec->ok()) return 1;

@@ -140,13 +140,35 @@ struct PocaArgs {
     muto_grid g;
     double eps, mag;
     int has_energy, straight, length_weighted;
-    double* img;
+    double* img;        // PoCA: the summed values (null for PoCut)
     double* weight;
     long long* assign;  // 3 per ray, optional
     Counters* ctr;
+    uint32_t* vox;      // PoCut: per ray its voxel, 0xffffffff when rejected (null for PoCA)
+    double* value;      // PoCut: per ray its value (angle^2, times p^2 with momentum)
 };
 void launch_poca(const PocaArgs& a, cudaStream_t s);
 void launch_poca_normalize(double* img, const double* weight, uint64_t V, double eps, cudaStream_t s);
+// PoCut's per-voxel step (src/MutoPoCut.cpp:113-118), after launch_poca:
+// the kept values grouped by voxel (counts, then offsets, then a scatter of
+// order keys into the voxels' segments), sorted per voxel and the lowest
+// floor(M cut) summed in ascending order.
+void launch_pocut_hist(const uint32_t* vox, uint64_t n, uint32_t* counts, cudaStream_t s);
+void launch_pocut_scatter(const uint32_t* vox, const double* value, uint64_t n, const uint64_t* off,
+                          uint32_t* cursor, unsigned long long* keys, cudaStream_t s);
+// voxels of no value: img = weight < eps ? 0 : 0 / weight
+void launch_pocut_empty(const uint32_t* counts, const double* weight, double* img, uint64_t V, double eps,
+                        cudaStream_t s);
+// voxels of at most 32 values, one warp each (list: voxel indices)
+void launch_pocut_small(const uint32_t* list, uint32_t n, const uint64_t* off, const uint32_t* counts,
+                        const unsigned long long* keys, const double* weight, double* img, double eps, double cut,
+                        cudaStream_t s);
+// voxels of more, one block each: sorted in shared memory up to kPocutSmemKeys
+// values, else in scratch (scratch_off[i]: first of next_pow2(M) slots)
+constexpr uint32_t kPocutSmemKeys = 4096;
+void launch_pocut_big(const uint32_t* list, uint32_t n, const uint64_t* off, const uint32_t* counts,
+                      const unsigned long long* keys, const uint64_t* scratch_off, unsigned long long* scratch,
+                      const double* weight, double* img, double eps, double cut, cudaStream_t s);
 
 // em_muon.cu: the muon pass (per-muon coefficients k)
 template <typename Real>

@@ -125,8 +125,10 @@ struct Params {
     double angle_unit_mag = 1.0, eps = 1.0e-8;
     double beta = 1.0, p = 1.0, delta = 0.1;
     bool add_object_prior = false, all_neighbours = false;
-    // PoCA, src/MutoPoCA.cpp:74-97
+    // PoCA, src/MutoPoCA.cpp:74-97; PoCut, src/MutoPoCut.cpp:12-15
     bool length_weighted = false;
+    bool pocut = false;          // PoCut: the PoCA handle keeps a percentile of the values per voxel
+    double cut_percentile = 1.0;
     // this library
     int precision = 0;  // 0 mixed, 1 fp64
     bool use_graph = true;
@@ -139,7 +141,7 @@ struct Params {
     long long voxel_stream_above = -1;  // segments longer than this are selected without registers (-1: none)
 };
 
-Params parse_params(Method m, const std::string& text) {
+Params parse_params(Method m, const std::string& text, bool pocut = false) {
     Params P;
     P.grid = muto_grid{100, 100, 100, 0, 0.0, 0.0, 0.0, 10.0, 10.0, 10.0};
     json cfg;
@@ -176,6 +178,11 @@ Params parse_params(Method m, const std::string& text) {
         P.eps = cfg.value("eps", 1.0e-8);
         if (m == kPoca) {
             P.length_weighted = cfg.value("length_weighted", false);
+            if (pocut) {  // MutoPoCut(json): MutoPoCA's keys, then straight_line off and cut_percentile
+                P.pocut = true;
+                P.straight_line = false;
+                P.cut_percentile = cfg.value("cut_percentile", 1.0);
+            }
         } else {
             P.update_with_mean = cfg.value("update_with_mean", false);
             P.early_stop = cfg.value("early_stop", false);
@@ -491,8 +498,83 @@ void prepare_poca(muto_handle* h) {
     a.weight = h->weight.as<double>();
     a.assign = h->assign.as<long long>();
     a.ctr = h->ctr();
-    run(h, "poca", [&] { launch_poca(a, h->stream); });
-    run(h, "poca_normalize", [&] { launch_poca_normalize(h->img64.as<double>(), h->weight.as<double>(), V, h->P.eps, h->stream); });
+    a.vox = nullptr;
+    a.value = nullptr;
+    if (!h->P.pocut) {
+        run(h, "poca", [&] { launch_poca(a, h->stream); });
+        run(h, "poca_normalize", [&] { launch_poca_normalize(h->img64.as<double>(), h->weight.as<double>(), V, h->P.eps, h->stream); });
+        return;
+    }
+    // PoCut (src/MutoPoCut.cpp:19-121): the same ray kernel keeping each value
+    // and voxel, then the values grouped by voxel, sorted, cut and summed
+    cudaStream_t s = h->stream;
+    DevMem vox, value, counts, off, cursor, keys, scan_scr, small, big, big_off, scratch;
+    vox.alloc(std::max<uint64_t>(nt, 1) * sizeof(uint32_t), &h->dev_bytes);
+    value.alloc(std::max<uint64_t>(nt, 1) * sizeof(double), &h->dev_bytes);
+    counts.alloc(std::max<uint64_t>(V, 1) * sizeof(uint32_t), &h->dev_bytes);
+    cursor.alloc(std::max<uint64_t>(V, 1) * sizeof(uint32_t), &h->dev_bytes);
+    off.alloc((V + 1) * sizeof(uint64_t), &h->dev_bytes);
+    scan_scr.alloc(scan_scratch_bytes(V + 1), &h->dev_bytes);
+    CK(cudaMemsetAsync(counts.as<void>(), 0, std::max<uint64_t>(V, 1) * sizeof(uint32_t), s));
+    CK(cudaMemsetAsync(cursor.as<void>(), 0, std::max<uint64_t>(V, 1) * sizeof(uint32_t), s));
+    a.img = nullptr;
+    a.vox = vox.as<uint32_t>();
+    a.value = value.as<double>();
+    run(h, "poca", [&] { launch_poca(a, s); });
+    run(h, "pocut_group", [&] {
+        launch_pocut_hist(vox.as<uint32_t>(), nt, counts.as<uint32_t>(), s);
+        scan_u32_to_u64(counts.as<uint32_t>(), off.as<uint64_t>(), V, scan_scr.as<void>(), s);
+    });
+    uint64_t nkeys = 0;
+    CK(cudaMemcpyAsync(&nkeys, off.as<uint64_t>() + V, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    std::vector<uint32_t> cnt(V);
+    if (V) CK(cudaMemcpyAsync(cnt.data(), counts.as<void>(), V * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    keys.alloc(std::max<uint64_t>(nkeys, 1) * sizeof(unsigned long long), &h->dev_bytes);
+    run(h, "pocut_group", [&] {
+        launch_pocut_scatter(vox.as<uint32_t>(), value.as<double>(), nt, off.as<uint64_t>(), cursor.as<uint32_t>(),
+                             keys.as<unsigned long long>(), s);
+    });
+    // voxels of up to 32 values: a warp each; more: a block each, sorting in
+    // shared memory, or in scratch of next_pow2(M) keys beyond kPocutSmemKeys
+    std::vector<uint32_t> small_h, big_h;
+    std::vector<uint64_t> big_off_h;
+    uint64_t nscratch = 0;
+    for (uint64_t j = 0; j < V; ++j) {
+        const uint32_t m = cnt[j];
+        if (m == 0) continue;
+        if (m <= 32) {
+            small_h.push_back(static_cast<uint32_t>(j));
+            continue;
+        }
+        big_h.push_back(static_cast<uint32_t>(j));
+        uint64_t n2 = 1;
+        while (n2 < m) n2 <<= 1;
+        big_off_h.push_back(nscratch);
+        if (n2 > kPocutSmemKeys) nscratch += n2;
+    }
+    small.alloc(std::max<size_t>(small_h.size(), 1) * sizeof(uint32_t), &h->dev_bytes);
+    big.alloc(std::max<size_t>(big_h.size(), 1) * sizeof(uint32_t), &h->dev_bytes);
+    big_off.alloc(std::max<size_t>(big_off_h.size(), 1) * sizeof(uint64_t), &h->dev_bytes);
+    scratch.alloc(std::max<uint64_t>(nscratch, 1) * sizeof(unsigned long long), &h->dev_bytes);
+    if (!small_h.empty())
+        CK(cudaMemcpyAsync(small.as<void>(), small_h.data(), small_h.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    if (!big_h.empty()) {
+        CK(cudaMemcpyAsync(big.as<void>(), big_h.data(), big_h.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(big_off.as<void>(), big_off_h.data(), big_off_h.size() * sizeof(uint64_t),
+                           cudaMemcpyHostToDevice, s));
+    }
+    const double eps = h->P.eps, cut = h->P.cut_percentile;
+    run(h, "pocut_select", [&] {
+        launch_pocut_empty(counts.as<uint32_t>(), h->weight.as<double>(), h->img64.as<double>(), V, eps, s);
+        launch_pocut_small(small.as<uint32_t>(), static_cast<uint32_t>(small_h.size()), off.as<uint64_t>(),
+                           counts.as<uint32_t>(), keys.as<unsigned long long>(), h->weight.as<double>(),
+                           h->img64.as<double>(), eps, cut, s);
+        launch_pocut_big(big.as<uint32_t>(), static_cast<uint32_t>(big_h.size()), off.as<uint64_t>(),
+                         counts.as<uint32_t>(), keys.as<unsigned long long>(), big_off.as<uint64_t>(),
+                         scratch.as<unsigned long long>(), h->weight.as<double>(), h->img64.as<double>(), eps, cut, s);
+    });
+    CK(cudaStreamSynchronize(s));  // the scratch arrays go out of scope
 }
 
 template <typename Real>
@@ -1277,12 +1359,13 @@ int muto_create(const char* method, const char* config_json, muto_handle** out) 
     *out = nullptr;
     std::unique_ptr<muto_handle> h(new muto_handle());
     const std::string m(method);
-    if (m == "poca") h->method = kPoca;
+    const bool pocut = m == "pocut";
+    if (m == "poca" || pocut) h->method = kPoca;
     else if (m == "mlsd") h->method = kMlsd;
     else if (m == "map") h->method = kMap;
     else return MUTO_ERR_ARG;
     const int rc = guarded(h.get(), [&] {
-        h->P = parse_params(h->method, config_json ? config_json : "");
+        h->P = parse_params(h->method, config_json ? config_json : "", pocut);
         h->grid = h->P.grid;
         CK(cudaGetDevice(&h->device));
         CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));

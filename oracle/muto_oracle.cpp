@@ -12,6 +12,7 @@
 //   scat_angle_square    src/MutoPoCA.cpp:165-174
 //   displacement         src/MutoMLSD.cpp:356-376
 //   Poca::run            src/MutoPoCA.cpp:51-134
+//   PoCut::run           src/MutoPoCut.cpp:19-121
 //   Mlsd::gather         src/MutoMLSD.cpp:268-326
 //   Mlsd::path_and_tail  src/MutoMLSD.cpp:382-415
 //   Mlsd::weights        src/MutoMLSD.cpp:417-430
@@ -249,17 +250,23 @@ int oracle_siddon_batch(const Grid* g, const double* p1, const double* p2, uint6
     return 0;
 }
 
-// PoCA reconstruction, src/MutoPoCA.cpp:51-134.
-// img: V doubles (column-major, x fastest).  assign (optional): 3 int64 per
-// ray, the PoCA voxel of each ray or -1 when the ray was rejected.
-// counters (optional): [n_total, n_not_parallel, n_scat_in_grid].
-int oracle_poca(const Grid* gp, const oracle_cfg* cfg, const Ray* rays, uint64_t n_rays, double* img,
-                int64_t* assign, uint64_t* counters) {
+// PoCA reconstruction, src/MutoPoCA.cpp:51-134, and PoCut, src/MutoPoCut.cpp:19-121
+// (cut != nullptr: the percentile *cut).  PoCut differs in two places: the
+// path is always the two halves around the PoCA point (its constructor sets
+// fStraightLine = false, :11-15), and instead of summing the scattering
+// values per voxel it keeps them, sorts each voxel's values ascending and
+// sums the lowest floor(count * cut) of them in that order from 0.0
+// (:113-117).  A cut that would take more values than the voxel holds (the
+// reference would read past the end) takes all of them.
+static int poca_run(const Grid* gp, const oracle_cfg* cfg, const double* cut, const Ray* rays, uint64_t n_rays,
+                    double* img, int64_t* assign, uint64_t* counters) {
     const Grid& g = *gp;
     const uint64_t V = static_cast<uint64_t>(g.nx) * g.ny * g.nz;
     std::vector<double> weight(V, 0.0);
+    std::vector<std::vector<double>> values(cut ? V : 0);  // PoCut: the values of each voxel
     std::fill(img, img + V, 0.0);
     if (n_rays == 0) return 0;
+    const bool straight = cut ? false : cfg->straight_line != 0;
     uint64_t n_total = cfg->total_num_rays > 0 ? static_cast<uint64_t>(cfg->total_num_rays) : n_rays;
     if (n_total > n_rays) n_total = n_rays;  // the reference would read past the end
     uint64_t not_parallel = 0, in_grid = 0;
@@ -284,28 +291,55 @@ int oracle_poca(const Grid* gp, const oracle_cfg* cfg, const Ray* rays, uint64_t
         }
         ++in_grid;
         if (assign) { assign[3 * i] = xs; assign[3 * i + 1] = ys; assign[3 * i + 2] = zs; }
-        img[at(xs, ys, zs)] += cfg->has_energy ? a2 * r.ein * r.ein : a2;  // :134-138
+        const double v = cfg->has_energy ? a2 * r.ein * r.ein : a2;  // :134-138 (PoCut :60-64)
+        if (cut) values[at(xs, ys, zs)].push_back(v);
+        else img[at(xs, ys, zs)] += v;
         // a walk inside the grid never yields an out-of-range voxel; the check
         // only keeps a malformed input from writing outside the image
-        auto addw = [&](const Voxel& v, double w) {
-            if (v.x < g.nx && v.y < g.ny && v.z < g.nz) weight[at(v.x, v.y, v.z)] += w;
+        auto addw = [&](const Voxel& w, double l) {
+            if (w.x < g.nx && w.y < g.ny && w.z < g.nz) weight[at(w.x, w.y, w.z)] += l;
         };
-        if (cfg->straight_line) {  // :141-149
+        if (straight) {  // :141-149
             siddon_path(g, r.pin, r.pout, vin);
-            for (const Voxel& v : vin) addw(v, cfg->length_weighted ? v.length : g.dz);
+            for (const Voxel& w : vin) addw(w, cfg->length_weighted ? w.length : g.dz);
         } else {  // :150-171
             siddon_path(g, r.pin, ps, vin);
             siddon_path(g, ps, r.pout, vout);
-            for (const Voxel& v : vin) addw(v, cfg->length_weighted ? v.length : g.dz);
-            for (const Voxel& v : vout) {
-                if (cfg->length_weighted) addw(v, v.length);
-                else if (v.x != xs || v.y != ys || v.z != zs) addw(v, g.dz);
+            for (const Voxel& w : vin) addw(w, cfg->length_weighted ? w.length : g.dz);
+            for (const Voxel& w : vout) {
+                if (cfg->length_weighted) addw(w, w.length);
+                else if (w.x != xs || w.y != ys || w.z != zs) addw(w, g.dz);
             }
         }
     }
-    for (uint64_t j = 0; j < V; ++j) img[j] = weight[j] < cfg->eps ? 0 : img[j] / weight[j];  // :180-182
+    if (cut) {  // src/MutoPoCut.cpp:113-118
+        for (uint64_t j = 0; j < V; ++j) {
+            std::vector<double>& s = values[j];
+            std::sort(s.begin(), s.end());
+            uint64_t t = u32_cast_x86(static_cast<double>(s.size()) * *cut);
+            if (t > s.size()) t = s.size();
+            const double sum = std::accumulate(s.begin(), s.begin() + static_cast<std::ptrdiff_t>(t), 0.0);
+            img[j] = weight[j] < cfg->eps ? 0 : sum / weight[j];
+        }
+    } else {
+        for (uint64_t j = 0; j < V; ++j) img[j] = weight[j] < cfg->eps ? 0 : img[j] / weight[j];  // :180-182
+    }
     if (counters) { counters[0] = n_total; counters[1] = not_parallel; counters[2] = in_grid; }
     return 0;
+}
+
+// img: V doubles (column-major, x fastest).  assign (optional): 3 int64 per
+// ray, the PoCA voxel of each ray or -1 when the ray was rejected.
+// counters (optional): [n_total, n_not_parallel, n_scat_in_grid].
+int oracle_poca(const Grid* gp, const oracle_cfg* cfg, const Ray* rays, uint64_t n_rays, double* img,
+                int64_t* assign, uint64_t* counters) {
+    return poca_run(gp, cfg, nullptr, rays, n_rays, img, assign, counters);
+}
+
+// PoCut with percentile cut (the "cut_percentile" key); outputs as oracle_poca.
+int oracle_pocut(const Grid* gp, const oracle_cfg* cfg, double cut, const Ray* rays, uint64_t n_rays, double* img,
+                 int64_t* assign, uint64_t* counters) {
+    return poca_run(gp, cfg, &cut, rays, n_rays, img, assign, counters);
 }
 
 }  // extern "C"

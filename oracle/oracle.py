@@ -54,6 +54,7 @@ def lib() -> C.CDLL:
             C.POINTER(C.c_int64)
         L.oracle_siddon_batch.argtypes = [C.POINTER(Grid), D, D, C.c_uint64, C.c_uint32, U32, D, U32]
         L.oracle_poca.argtypes = [C.POINTER(Grid), C.POINTER(Cfg), P, C.c_uint64, D, I64, U64]
+        L.oracle_pocut.argtypes = [C.POINTER(Grid), C.POINTER(Cfg), C.c_double, P, C.c_uint64, D, I64, U64]
         L.oracle_mlsd_create.restype = P
         L.oracle_mlsd_create.argtypes = [C.POINTER(Grid), C.POINTER(Cfg), P, C.c_uint64, D, C.c_int]
         L.oracle_mlsd_destroy.argtypes = [P]
@@ -115,6 +116,21 @@ def poca(grid, cfg: dict, rays: np.ndarray):
     c = make_cfg(cfg, "poca")
     lib().oracle_poca(C.byref(g), C.byref(c), rays.ctypes.data_as(C.c_void_p), n, _d(img),
                       assign.ctypes.data_as(C.POINTER(C.c_int64)), counters.ctypes.data_as(C.POINTER(C.c_uint64)))
+    return img, assign, counters
+
+
+def pocut(grid, cfg: dict, rays: np.ndarray):
+    """PoCut (src/MutoPoCut.cpp:19-121); cfg["cut_percentile"] defaults to 1.0 (:14)."""
+    rays = np.ascontiguousarray(rays, np.float64)
+    n = rays.shape[0]
+    img = np.zeros(grid.nx * grid.ny * grid.nz, np.float64)
+    assign = np.zeros((n, 3), np.int64)
+    counters = np.zeros(3, np.uint64)
+    g = make_grid(grid)
+    c = make_cfg(cfg, "poca")
+    lib().oracle_pocut(C.byref(g), C.byref(c), float(cfg.get("cut_percentile", 1.0)), rays.ctypes.data_as(C.c_void_p),
+                       n, _d(img), assign.ctypes.data_as(C.POINTER(C.c_int64)),
+                       counters.ctypes.data_as(C.POINTER(C.c_uint64)))
     return img, assign, counters
 
 

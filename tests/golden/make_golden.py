@@ -1,7 +1,7 @@
 """Generate the golden vectors in tests/golden/ from the reference itself.
 
 The reference's reconstruction sources (src/MutoSiddon.cpp, src/MutoPoCA.cpp,
-src/MutoMLSD.cpp, src/MutoMAP.cpp) are compiled in place by
+src/MutoMLSD.cpp, src/MutoMAP.cpp, src/MutoPoCut.cpp) are compiled in place by
 oracle/build_ref.sh and called through oracle/reference.py; the inputs
 (segments, synthetic tracks) are stored next to the outputs so the tests need
 neither the reference nor the generator.  Run where the reference tree is
@@ -57,6 +57,15 @@ def track_case():
                       "poca_dz": wl.poca_config(length_weighted=False),
                       "poca_straight": wl.poca_config(straight_line=True)}.items():
         img, _ = R.reconstruct("poca", cfg, rays, g.nvox)
+        out[name] = img
+        configs[name] = cfg
+    # PoCut: cut percentiles 1, 0.9, 0.5 and 0, both weightings, with and without momentum
+    for name, cfg in {"pocut_lw_100": wl.poca_config(length_weighted=True, cut_percentile=1.0),
+                      "pocut_dz_90": wl.poca_config(length_weighted=False, cut_percentile=0.9),
+                      "pocut_lw_50_energy": wl.poca_config(length_weighted=True, has_energy=True,
+                                                           cut_percentile=0.5),
+                      "pocut_dz_0": wl.poca_config(length_weighted=False, cut_percentile=0.0)}.items():
+        img, _ = R.reconstruct("pocut", cfg, rays, g.nvox)
         out[name] = img
         configs[name] = cfg
     cfg = wl.em_config()

@@ -54,6 +54,15 @@ def test_oracle_poca_matches_golden(oracle, name):
     assert np.array_equal(bits(img), bits(T[name]))
 
 
+POCUT_CASES = [k for k in CFG if k.startswith("pocut_")]
+
+
+@pytest.mark.parametrize("name", POCUT_CASES)
+def test_oracle_pocut_matches_golden(oracle, name):
+    img, _, _ = oracle.pocut(grid_of(T["grid"]), CFG[name], T["rays"])
+    assert np.array_equal(bits(img), bits(T[name]))
+
+
 def test_oracle_paths_match_golden(oracle):
     g = grid_of(T["grid"])
     e = oracle.Mlsd(g, CFG["paths"], T["rays"], np.full(g.nvox, 1e-7)).export()
@@ -101,6 +110,17 @@ def test_gpu_poca_matches_golden(gpu, name):
     with M.MutoPoCA(CFG[name]) as rec:
         img = rec.reconstruct(T["rays"]).reshape(-1, order="F")
     assert rel_l2(img, T[name]) < 1e-12
+    assert np.array_equal(img > 0, T[name] > 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", POCUT_CASES)
+def test_gpu_pocut_matches_golden(gpu, name):
+    # the kept values are summed in the reference's order (ascending, from 0);
+    # the weights are FP64 atomics, as for PoCA
+    with M.MutoPoCut(CFG[name]) as rec:
+        img = rec.reconstruct(T["rays"]).reshape(-1, order="F")
+    assert rel_l2(img, T[name]) < 1e-12 if np.any(T[name]) else not np.any(img)
     assert np.array_equal(img > 0, T[name] > 0)
 
 

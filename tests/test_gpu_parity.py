@@ -101,6 +101,32 @@ def _mlsd_pair(oracle, wl, rays, cfg, init, n_iter, method="mlsd"):
     return ref
 
 
+@pytest.mark.parametrize("n,n_muons,seed", [(12, 6000, 71), (4, 30000, 72), (2, 120000, 73)])
+@pytest.mark.parametrize("cut,lw,energy", [(1.0, True, False), (0.9, False, False), (0.37, True, True),
+                                           (0.0, False, False)])
+def test_pocut_matches_oracle(gpu, oracle, n, n_muons, seed, cut, lw, energy):
+    # src/MutoPoCut.cpp:19-121: 12^3 voxels hold a few values each (warp sorts); 4^3 voxels
+    # hundreds to thousands (block sorts in shared memory); 2^3 voxels more than 4096
+    # (block sorts in scratch).  The values are summed in the reference's order, so only
+    # the FP64 weight atomics differ: 1e-12 relative.
+    wl = W.small(n_muons=n_muons, seed=seed, n=n)
+    rays = wl.tracks()
+    cfg = wl.poca_config(length_weighted=lw, has_energy=energy, cut_percentile=cut, straight_line=True)
+    ref, ref_assign, ref_ctr = oracle.pocut(wl.grid, cfg, rays)  # straight_line is ignored by PoCut
+    with M.MutoPoCut(cfg) as rec:
+        img = rec.reconstruct(rays).reshape(-1, order="F")
+        st = rec.status()
+        assign = rec.poca_assignment(rays.shape[0])
+    assert np.array_equal(assign, ref_assign)
+    assert st["n_scat_in_grid"] == int(ref_ctr[2])
+    if n == 2 and cut == 1.0:
+        assert np.bincount(np.ravel_multi_index(assign[assign[:, 0] >= 0].T, (2, 2, 2), order="F")).max() > 4096
+    if np.any(ref):
+        assert rel_l2(img, ref) < 1e-12
+    assert np.array_equal(img > 0, ref > 0)
+    assert np.all(img[ref == 0] == 0)
+
+
 @pytest.mark.parametrize("straight", [False, True])
 def test_mlsd_paths_bit_exact(gpu, oracle, straight):
     wl = W.small(n_muons=6000, seed=31)
