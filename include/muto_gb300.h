@@ -82,12 +82,15 @@ typedef struct muto_handle muto_handle;
  * Reconstruction handles
  * ------------------------------------------------------------------------- */
 
-/* Create a reconstruction: method is "poca", "pocut", "mlsd" or "map";
- * config_json is the JSON object of that method (the value of the
- * "poca"/"pocut"/"mlsd"/"map" key, as passed to the constructors
- * MutoPoCA(json) src/MutoPoCA.cpp:74, MutoPoCut(json) src/MutoPoCut.cpp:12
- * (PoCA's keys plus "cut_percentile", 1.0; straight_line is always off),
- * MutoMLSD(json) src/MutoMLSD.cpp:47, MutoMAP(json) src/MutoMAP.cpp:75).
+/* Create a reconstruction: method is "poca", "pocut", "slr", "slr_iter",
+ * "mlsd" or "map"; config_json is the JSON object of that method (the value
+ * of the key of the same name, as passed to the constructors MutoPoCA(json)
+ * src/MutoPoCA.cpp:74, MutoPoCut(json) src/MutoPoCut.cpp:12 (PoCA's keys
+ * plus "cut_percentile", 1.0; straight_line is always off), MutoSLR(json)
+ * src/MutoSLR.cpp:21, MutoSLRIter(json) src/MutoSLRIter.cpp:8 (plus
+ * "num_iteration", 1), MutoMLSD(json) src/MutoMLSD.cpp:47, MutoMAP(json)
+ * src/MutoMAP.cpp:75).  poca, pocut, slr and slr_iter compute their image in
+ * muto_prepare.
  * The reference's keys and defaults apply; extra keys: "precision"
  * ("mixed" default, or "fp64"), "use_graph" (true), "random_seed",
  * "compute_cost" (computed when early_stop/log_results is set, or when true),

@@ -24,7 +24,7 @@ from . import _lib
 from ._lib import MutoError, check
 
 __all__ = [
-    "Grid", "Block", "X0_MM", "RAY_FIELDS", "MutoError", "Reconstruction", "MutoPoCA", "MutoPoCut", "MutoMLSD", "MutoMAP",
+    "Grid", "Block", "X0_MM", "RAY_FIELDS", "MutoError", "Reconstruction", "MutoPoCA", "MutoPoCut", "MutoSLR", "MutoSLRIter", "MutoMLSD", "MutoMAP",
     "phantom", "generate", "lambda_from_x0", "save_image", "load_image", "siddon_batch", "library", "Batch",
 ]
 
@@ -123,8 +123,12 @@ def _flat(img: np.ndarray) -> np.ndarray:
     return np.ascontiguousarray(img, dtype=np.float64)
 
 
+# methods whose image comes out of prepare (no EM iterations)
+ONE_SHOT = ("poca", "pocut", "slr", "slr_iter")
+
+
 class Reconstruction:
-    """One reconstruction handle (``muto_create``).  method: poca | pocut | mlsd | map."""
+    """One reconstruction handle (``muto_create``).  method: poca | pocut | slr | slr_iter | mlsd | map."""
 
     def __init__(self, method: str, config: dict | str | None = None):
         self._lib = library()
@@ -178,7 +182,7 @@ class Reconstruction:
         # the output size follows the grid after the initial image is resolved: stage it
         self.load_tracks(rays)
         self.prepare()
-        if self.method not in ("poca", "pocut"):
+        if self.method not in ONE_SHOT:
             self.iterate(self.config_iterations())
         return self.image()
 
@@ -293,6 +297,22 @@ class MutoPoCut(Reconstruction):
 
     def __init__(self, config: dict | None = None):
         super().__init__("pocut", config)
+
+
+class MutoSLR(Reconstruction):
+    """MutoSLR(json) / reconstruct (src/MutoSLR.cpp:21-103): straight-line back-projection
+    of the squared scattering angles over the voxels between the grid's top and bottom."""
+
+    def __init__(self, config: dict | None = None):
+        super().__init__("slr", config)
+
+
+class MutoSLRIter(Reconstruction):
+    """MutoSLRIter(json) / reconstruct (src/MutoSLRIter.cpp:8-83): SLR repeated
+    ``num_iteration`` times (default 1), later passes in place and in muon order."""
+
+    def __init__(self, config: dict | None = None):
+        super().__init__("slr_iter", config)
 
 
 class MutoMLSD(Reconstruction):

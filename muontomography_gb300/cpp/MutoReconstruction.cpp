@@ -9,7 +9,8 @@ namespace {
 json empty_object() { return json::parse("{}"); }
 }  // namespace
 
-MutoGpuReconstruction::MutoGpuReconstruction(const char* method, const json& config) : fConfig(config) {
+MutoGpuReconstruction::MutoGpuReconstruction(const char* method, const json& config)
+    : fConfig(config), fMethod(method) {
     const std::string text = config.is_object() ? config.dump() : std::string("{}");
     try {
         fLogPrint = config.is_object() && config.value("log_results", false);
@@ -71,6 +72,13 @@ MutoPoCA::MutoPoCA(const char* method, json config) : MutoGpuReconstruction(meth
 MutoPoCut::MutoPoCut() : MutoPoCA("pocut", empty_object()) {}
 MutoPoCut::MutoPoCut(json config) : MutoPoCA("pocut", config) {}
 
+MutoSLR::MutoSLR() : MutoPoCA("slr", empty_object()) {}
+MutoSLR::MutoSLR(json config) : MutoPoCA("slr", config) {}
+MutoSLR::MutoSLR(const char* method, json config) : MutoPoCA(method, config) {}
+
+MutoSLRIter::MutoSLRIter() : MutoSLR("slr_iter", empty_object()) {}
+MutoSLRIter::MutoSLRIter(json config) : MutoSLR("slr_iter", config) {}
+
 Image MutoPoCA::reconstruct(const MutoMuonData& rays) {
     if (!fHandle) return Image{};
     fTimeStart = std::chrono::steady_clock::now();
@@ -79,12 +87,17 @@ Image MutoPoCA::reconstruct(const MutoMuonData& rays) {
     if (!check(muto_prepare(fHandle), "muto_prepare")) return Image{};
     if (fLogPrint) {  // logResults, src/MutoPoCA.cpp:176-183
         const muto_status s = status();
+        const bool slr = fMethod.compare(0, 3, "slr") == 0;  // src/MutoSLR.cpp:111-116
         std::cout << "==================================================" << std::endl;
-        std::cout << "|| PoCA reconstruction results                  ||" << std::endl;
+        std::cout << (slr ? "|| SLR reconstruction results                  ||"
+                          : "|| PoCA reconstruction results                  ||")
+                  << std::endl;
         std::cout << "==================================================" << std::endl;
         std::cout << "number of rays processed: " << s.n_total << std::endl;
-        std::cout << "number of unparalleled rays: " << s.n_not_parallel << std::endl;
-        std::cout << "number of interactions in voxels: " << s.n_scat_in_grid << std::endl;
+        if (!slr) {
+            std::cout << "number of unparalleled rays: " << s.n_not_parallel << std::endl;
+            std::cout << "number of interactions in voxels: " << s.n_scat_in_grid << std::endl;
+        }
     }
     return fetchImage();
 }

@@ -3,6 +3,8 @@
 //   MutoVReconstruction   include/MutoVReconstruction.h:11-16
 //   MutoPoCA(json)        include/MutoPoCA.h:17-50
 //   MutoPoCut(json)       include/MutoPoCut.h:13-28 (derives from MutoPoCA)
+//   MutoSLR(json)         include/MutoSLR.h:13-41
+//   MutoSLRIter(json)     include/MutoSLRIter.h:9-23 (derives from MutoSLR)
 //   MutoMLSD(json)        include/MutoMLSD.h:27-107
 //   MutoMAP(json)         include/MutoMAP.h:16-63 (derives from MutoMLSD)
 // Constructors take the method's JSON object with the reference's keys and
@@ -43,6 +45,7 @@ protected:
 
     muto_handle* fHandle = nullptr;
     json fConfig;
+    std::string fMethod;
     bool fLogPrint = false;
     std::chrono::steady_clock::time_point fTimeStart;
 };
@@ -62,6 +65,23 @@ class MutoPoCut : public MutoPoCA {
 public:
     MutoPoCut();
     explicit MutoPoCut(json config);
+};
+
+// straight-line back-projection between the grid's top and bottom planes
+class MutoSLR : public MutoPoCA {
+public:
+    MutoSLR();
+    explicit MutoSLR(json config);
+
+protected:
+    MutoSLR(const char* method, json config);
+};
+
+// SLR repeated num_iteration times, later passes in place in muon order
+class MutoSLRIter : public MutoSLR {
+public:
+    MutoSLRIter();
+    explicit MutoSLRIter(json config);
 };
 
 class MutoMLSD : public MutoGpuReconstruction {

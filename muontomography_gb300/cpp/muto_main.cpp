@@ -1,6 +1,6 @@
 // Command-line driver (the reference's MuToTest.cpp:15-83): reads a JSON
 // config, loads the raw-hit data files, reconstructs with the method whose
-// key is present ("poca", "mlsd", "map" or "pocut") on the GPU and writes the image.
+// key is present ("poca", "mlsd", "map", "slr", "slr_iter" or "pocut") on the GPU and writes the image.
 //
 // Top-level keys: data_files, detector_height, detector_middle, output_file;
 // optional data_precision (4 = float32 records, the default; 8 = float64).
@@ -57,12 +57,21 @@ int main(int argc, char** argv) {
         method = "map";
         rec.reset(new MutoMAP(config.get("map")));
         header.nIter = iterations("map");
+    } else if (config.exist("slr")) {
+        method = "slr";
+        rec.reset(new MutoSLR(config.get("slr")));
+        header.nIter = 1;
+    } else if (config.exist("slr_iter")) {
+        method = "slr_iter";
+        rec.reset(new MutoSLRIter(config.get("slr_iter")));
+        header.nIter = 1;
     } else if (config.exist("pocut")) {
         method = "pocut";
         rec.reset(new MutoPoCut(config.get("pocut")));
         header.nIter = 1;
     } else {
-        std::cerr << "No supported reconstruction key (poca, mlsd, map, pocut) in " << path << std::endl;
+        std::cerr << "No supported reconstruction key (poca, mlsd, map, slr, slr_iter, pocut) in " << path
+                  << std::endl;
         return 1;
     }
     if (!rec->ok()) return 1;

@@ -149,6 +149,27 @@ struct PocaArgs {
 };
 void launch_poca(const PocaArgs& a, cudaStream_t s);
 void launch_poca_normalize(double* img, const double* weight, uint64_t V, double eps, cudaStream_t s);
+// slr.cu: straight-line reconstruction (src/MutoSLR.cpp:47-103) and the
+// iterative form's passes (src/MutoSLRIter.cpp:15-83)
+struct SlrArgs {
+    const muto_ray* rays;
+    uint64_t n;
+    muto_grid g;
+    double mag;
+    int has_energy, length_weighted;
+    double* img;     // summed values
+    double* weight;  // summed weights
+};
+// the first pass: every ray at once (atomics)
+void launch_slr(const SlrArgs& a, cudaStream_t s);
+// the walked straight lines: off == null: counts[i] = voxels of ray i; else
+// ray i's voxels (x + nx (y + ny z)) and lengths at vox/len + off[i]
+void launch_slr_paths(const SlrArgs& a, const uint64_t* off, uint32_t* counts, uint32_t* vox, double* len,
+                      cudaStream_t s);
+// one later, in-place pass over the walked lines, muon after muon
+void launch_slr_iter_pass(const SlrArgs& a, const uint64_t* off, const uint32_t* vox, const double* len,
+                          cudaStream_t s);
+
 // PoCut's per-voxel step (src/MutoPoCut.cpp:113-118), after launch_poca:
 // the kept values grouped by voxel (counts, then offsets, then a scatter of
 // order keys into the voxels' segments), sorted per voxel and the lowest

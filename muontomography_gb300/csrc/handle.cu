@@ -129,6 +129,9 @@ struct Params {
     bool length_weighted = false;
     bool pocut = false;          // PoCut: the PoCA handle keeps a percentile of the values per voxel
     double cut_percentile = 1.0;
+    // SLR, src/MutoSLR.cpp:21-45; SLRIter, src/MutoSLRIter.cpp:8-11
+    int slr = 0;                 // 1 straight-line reconstruction, 2 its iterative form
+    int slr_iterations = 1;
     // this library
     int precision = 0;  // 0 mixed, 1 fp64
     bool use_graph = true;
@@ -141,7 +144,8 @@ struct Params {
     long long voxel_stream_above = -1;  // segments longer than this are selected without registers (-1: none)
 };
 
-Params parse_params(Method m, const std::string& text, bool pocut = false) {
+// variant of the one-shot (PoCA) handle: 0 PoCA, 1 PoCut, 2 SLR, 3 SLRIter
+Params parse_params(Method m, const std::string& text, int variant = 0) {
     Params P;
     P.grid = muto_grid{100, 100, 100, 0, 0.0, 0.0, 0.0, 10.0, 10.0, 10.0};
     json cfg;
@@ -178,10 +182,14 @@ Params parse_params(Method m, const std::string& text, bool pocut = false) {
         P.eps = cfg.value("eps", 1.0e-8);
         if (m == kPoca) {
             P.length_weighted = cfg.value("length_weighted", false);
-            if (pocut) {  // MutoPoCut(json): MutoPoCA's keys, then straight_line off and cut_percentile
+            if (variant == 1) {  // MutoPoCut(json): MutoPoCA's keys, then straight_line off and cut_percentile
                 P.pocut = true;
                 P.straight_line = false;
                 P.cut_percentile = cfg.value("cut_percentile", 1.0);
+            } else if (variant >= 2) {  // MutoSLR(json): the grid and the common keys; SLRIter: num_iteration
+                P.slr = variant - 1;
+                if (P.slr == 2) P.slr_iterations = cfg.value("num_iteration", 1);
+                if (P.slr_iterations < 0) throw Error(MUTO_ERR_CONFIG, "num_iteration must be >= 0");
             }
         } else {
             P.update_with_mean = cfg.value("update_with_mean", false);
@@ -474,6 +482,49 @@ void alloc_counters(muto_handle* h) {
     CK(cudaMemsetAsync(h->ctr_mem.as<void>(), 0, sizeof(Counters), h->stream));
 }
 
+// SLR (src/MutoSLR.cpp:47-103) and SLRIter (src/MutoSLRIter.cpp:15-83): the
+// first pass over every ray at once; the iterative form's later passes, in
+// place and in muon order, over the walked straight lines kept on the device
+void prepare_slr(muto_handle* h, uint64_t nt) {
+    const uint64_t V = h->V();
+    cudaStream_t s = h->stream;
+    SlrArgs a;
+    a.rays = h->rays.as<muto_ray>();
+    a.n = nt;
+    a.g = h->grid;
+    a.mag = h->P.angle_unit_mag;
+    a.has_energy = h->P.has_energy;
+    a.length_weighted = h->P.length_weighted;
+    a.img = h->img64.as<double>();
+    a.weight = h->weight.as<double>();
+    const int passes = h->P.slr == 2 ? h->P.slr_iterations : 1;
+    if (passes >= 1) run(h, "slr", [&] { launch_slr(a, s); });
+    if (passes >= 2 && nt > 0) {
+        DevMem counts, off, vox, len, scan_scr;
+        counts.alloc(nt * sizeof(uint32_t), &h->dev_bytes);
+        off.alloc((nt + 1) * sizeof(uint64_t), &h->dev_bytes);
+        scan_scr.alloc(scan_scratch_bytes(nt + 1), &h->dev_bytes);
+        run(h, "slr_paths", [&] {
+            launch_slr_paths(a, nullptr, counts.as<uint32_t>(), nullptr, nullptr, s);
+            scan_u32_to_u64(counts.as<uint32_t>(), off.as<uint64_t>(), nt, scan_scr.as<void>(), s);
+        });
+        uint64_t np = 0;
+        CK(cudaMemcpyAsync(&np, off.as<uint64_t>() + nt, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        vox.alloc(std::max<uint64_t>(np, 1) * sizeof(uint32_t), &h->dev_bytes);
+        len.alloc(std::max<uint64_t>(np, 1) * sizeof(double), &h->dev_bytes);
+        run(h, "slr_paths", [&] {
+            launch_slr_paths(a, off.as<uint64_t>(), nullptr, vox.as<uint32_t>(), len.as<double>(), s);
+        });
+        for (int p = 1; p < passes; ++p)
+            run(h, "slr_iter_pass", [&] {
+                launch_slr_iter_pass(a, off.as<uint64_t>(), vox.as<uint32_t>(), len.as<double>(), s);
+            });
+        CK(cudaStreamSynchronize(s));  // the path arrays go out of scope
+    }
+    run(h, "poca_normalize", [&] { launch_poca_normalize(h->img64.as<double>(), h->weight.as<double>(), V, h->P.eps, s); });
+}
+
 void prepare_poca(muto_handle* h) {
     const uint64_t V = h->V();
     h->img64.alloc(V * sizeof(double), &h->dev_bytes);
@@ -500,6 +551,10 @@ void prepare_poca(muto_handle* h) {
     a.ctr = h->ctr();
     a.vox = nullptr;
     a.value = nullptr;
+    if (h->P.slr) {
+        prepare_slr(h, nt);
+        return;
+    }
     if (!h->P.pocut) {
         run(h, "poca", [&] { launch_poca(a, h->stream); });
         run(h, "poca_normalize", [&] { launch_poca_normalize(h->img64.as<double>(), h->weight.as<double>(), V, h->P.eps, h->stream); });
@@ -1359,13 +1414,13 @@ int muto_create(const char* method, const char* config_json, muto_handle** out) 
     *out = nullptr;
     std::unique_ptr<muto_handle> h(new muto_handle());
     const std::string m(method);
-    const bool pocut = m == "pocut";
-    if (m == "poca" || pocut) h->method = kPoca;
+    const int variant = m == "pocut" ? 1 : m == "slr" ? 2 : m == "slr_iter" ? 3 : 0;
+    if (m == "poca" || variant > 0) h->method = kPoca;
     else if (m == "mlsd") h->method = kMlsd;
     else if (m == "map") h->method = kMap;
     else return MUTO_ERR_ARG;
     const int rc = guarded(h.get(), [&] {
-        h->P = parse_params(h->method, config_json ? config_json : "", pocut);
+        h->P = parse_params(h->method, config_json ? config_json : "", variant);
         h->grid = h->P.grid;
         CK(cudaGetDevice(&h->device));
         CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));

@@ -1,0 +1,183 @@
+// Straight-line reconstruction (MutoSLR::reconstruct, src/MutoSLR.cpp:47-103)
+// and the first pass of its iterative form (MutoSLRIter, src/MutoSLRIter.cpp:
+// 15-83), one thread per ray: the incoming and outgoing lines cut at the
+// grid's top and bottom planes, the Siddon walk of the straight line between
+// the two points (bit-exact, as for the other methods), and per voxel the
+// mean squared projected angle shared by length^2 or equally.  Sums are FP64
+// atomics.  The later passes of the iterative form are order-dependent (each
+// muon sees the image the muons before it left): they run muon after muon on
+// one warp over the walked paths (k_slr_iter_pass).
+#include "common.cuh"
+#include "geometry.cuh"
+
+namespace muto {
+namespace {
+
+// per-ray quantities of :63-77
+struct SlrRay {
+    double a2;        // axz^2 + ayz^2
+    double p_in[3], p_out[3];
+    double l_total;   // |p_in - p_out|
+};
+
+__device__ __forceinline__ SlrRay slr_ray(const muto_ray& r, const DevGrid& g, double z_lo, double z_hi, double mag) {
+    SlrRay o;
+    const double axz = dmul(dsub(atan2(r.din[0], r.din[2]), atan2(r.dout[0], r.dout[2])), mag);
+    const double ayz = dmul(dsub(atan2(r.din[1], r.din[2]), atan2(r.dout[1], r.dout[2])), mag);
+    o.a2 = dadd(dmul(axz, axz), dmul(ayz, ayz));
+    const double t_in = ddiv(dsub(z_hi, r.pin[2]), r.din[2]);
+    const double t_out = ddiv(dsub(z_lo, r.pout[2]), r.dout[2]);
+    double d[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        o.p_in[k] = dadd(r.pin[k], dmul(t_in, r.din[k]));
+        o.p_out[k] = dadd(r.pout[k], dmul(t_out, r.dout[k]));
+        d[k] = dsub(o.p_in[k], o.p_out[k]);
+    }
+    o.l_total = __dsqrt_rn(dot3(d, d));
+    (void)g;
+    return o;
+}
+
+struct CountSink {
+    uint32_t n = 0;
+    __device__ void operator()(uint32_t, uint32_t, uint32_t, double) { ++n; }
+};
+
+struct SlrSink {
+    double* img;
+    double* weight;
+    uint32_t nx, ny, nz;
+    double dz, a2, l_total, share, e2;  // share: a2 / 2 / n^2 (equal shares)
+    int length_weighted, has_energy;
+    __device__ void operator()(uint32_t x, uint32_t y, uint32_t z, double l) {
+        if (x >= nx || y >= ny || z >= nz) return;  // never for a walk inside the grid
+        const uint64_t j = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * (y + static_cast<uint64_t>(ny) * z);
+        double iv;
+        if (length_weighted) {  // :80-83
+            atomicAdd(weight + j, ddiv(l, dz));
+            const double f = ddiv(l, l_total);
+            iv = dmul(dmul(dmul(a2, 0.5), f), f);
+        } else {  // :84-86
+            atomicAdd(weight + j, 1.0);
+            iv = share;
+        }
+        if (has_energy) iv = dmul(iv, e2);  // :87-89
+        atomicAdd(img + j, iv);
+    }
+};
+
+__global__ void k_slr(SlrArgs a) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const DevGrid g = make_dev_grid(a.g);
+    const muto_ray r = a.rays[i];
+    const double z_lo = a.g.z_min;                                               // :57
+    const double z_hi = dadd(a.g.z_min, dmul(a.g.dz, static_cast<double>(a.g.nz)));  // :58
+    const SlrRay s = slr_ray(r, g, z_lo, z_hi, a.mag);
+    double share = 0.0;
+    if (!a.length_weighted) {  // the equal share needs the path's voxel count first
+        CountSink c;
+        siddon_walk(g, s.p_in, s.p_out, c);
+        const uint64_t n = c.n;
+        share = ddiv(dmul(s.a2, 0.5), static_cast<double>(n * n));
+    }
+    SlrSink sink{a.img, a.weight, g.n[0], g.n[1], g.n[2], a.g.dz, s.a2, s.l_total, share, dmul(r.ein, r.ein),
+                 a.length_weighted, a.has_energy};
+    siddon_walk(g, s.p_in, s.p_out, sink);
+}
+
+// The walked straight lines, for the in-place passes: per ray its voxel
+// count (first call) or its voxels and lengths at off[i] (second call).
+struct PathSink {
+    uint32_t* vox;
+    double* len;
+    uint32_t nx, ny;
+    uint32_t k = 0;
+    __device__ void operator()(uint32_t x, uint32_t y, uint32_t z, double l) {
+        if (vox) {
+            vox[k] = x + nx * (y + ny * z);
+            len[k] = l;
+        }
+        ++k;
+    }
+};
+
+__global__ void k_slr_paths(SlrArgs a, const uint64_t* __restrict__ off, uint32_t* __restrict__ counts,
+                            uint32_t* __restrict__ vox, double* __restrict__ len) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const DevGrid g = make_dev_grid(a.g);
+    const double z_lo = a.g.z_min;
+    const double z_hi = dadd(a.g.z_min, dmul(a.g.dz, static_cast<double>(a.g.nz)));
+    const SlrRay s = slr_ray(a.rays[i], g, z_lo, z_hi, a.mag);
+    PathSink p{off ? vox + off[i] : nullptr, off ? len + off[i] : nullptr, g.n[0], g.n[1]};
+    siddon_walk(g, s.p_in, s.p_out, p);
+    if (!off) counts[i] = p.k;
+}
+
+// One later pass of the iterative form (src/MutoSLRIter.cpp:40-71 with
+// iter != 0), muon after muon on a single warp: the warp reads the image on
+// the muon's path, sums it, and adds to each voxel its share times the
+// voxel's part of that sum.  A muon's stores are ordered before the next
+// muon's loads by __syncwarp; no other warp touches the image.
+__global__ void k_slr_iter_pass(SlrArgs a, const uint64_t* __restrict__ off, const uint32_t* __restrict__ vox,
+                                const double* __restrict__ len) {
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x >= 32) return;
+    const DevGrid g = make_dev_grid(a.g);
+    const double z_lo = a.g.z_min;
+    const double z_hi = dadd(a.g.z_min, dmul(a.g.dz, static_cast<double>(a.g.nz)));
+    for (uint64_t i = 0; i < a.n; ++i) {
+        const muto_ray r = a.rays[i];
+        const SlrRay s = slr_ray(r, g, z_lo, z_hi, a.mag);
+        const uint64_t p0 = off[i];
+        const uint32_t n = static_cast<uint32_t>(off[i + 1] - p0);
+        double part = 0.0;  // :49-52, lanes' partial sums, then the warp's
+        for (uint32_t k = lane; k < n; k += 32) part = dadd(part, a.img[vox[p0 + k]]);
+        const double total = warp_sum(part);
+        const double share = ddiv(dmul(s.a2, 0.5), static_cast<double>(static_cast<uint64_t>(n) * n));
+        const double e2 = dmul(r.ein, r.ein);
+        for (uint32_t k = lane; k < n; k += 32) {
+            const uint32_t j = vox[p0 + k];
+            const double l = len[p0 + k];
+            double iv;
+            if (a.length_weighted) {
+                a.weight[j] = dadd(a.weight[j], ddiv(l, a.g.dz));
+                const double f = ddiv(l, s.l_total);
+                iv = dmul(dmul(dmul(s.a2, 0.5), f), f);
+            } else {
+                a.weight[j] = dadd(a.weight[j], 1.0);
+                iv = share;
+            }
+            iv = dmul(iv, ddiv(a.img[j], total));  // :64-66
+            if (a.has_energy) iv = dmul(iv, e2);
+            a.img[j] = dadd(a.img[j], iv);
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+void launch_slr(const SlrArgs& a, cudaStream_t s) {
+    if (a.n == 0) return;
+    k_slr<<<static_cast<unsigned>((a.n + 127) / 128), 128, 0, s>>>(a);
+    count_launches(1);
+}
+
+void launch_slr_paths(const SlrArgs& a, const uint64_t* off, uint32_t* counts, uint32_t* vox, double* len,
+                      cudaStream_t s) {
+    if (a.n == 0) return;
+    k_slr_paths<<<static_cast<unsigned>((a.n + 127) / 128), 128, 0, s>>>(a, off, counts, vox, len);
+    count_launches(1);
+}
+
+void launch_slr_iter_pass(const SlrArgs& a, const uint64_t* off, const uint32_t* vox, const double* len,
+                          cudaStream_t s) {
+    if (a.n == 0) return;
+    k_slr_iter_pass<<<1, 32, 0, s>>>(a, off, vox, len);
+    count_launches(1);
+}
+
+}  // namespace muto

@@ -10,6 +10,6 @@ mkdir -p "$HERE/_ref"
 g++ -O2 -std=c++14 -fPIC -shared -fopenmp -ffp-contract=off -fno-fast-math -w \
     -I "$HERE/ref_shim" -I "$REF/include" \
     "$REF/src/MutoSiddon.cpp" "$REF/src/MutoPoCA.cpp" "$REF/src/MutoMLSD.cpp" "$REF/src/MutoMAP.cpp" \
-    "$REF/src/MutoPoCut.cpp" \
+    "$REF/src/MutoPoCut.cpp" "$REF/src/MutoSLR.cpp" "$REF/src/MutoSLRIter.cpp" \
     "$HERE/ref_harness.cpp" -o "$HERE/_ref/libmuto_ref.so"
 echo "built $HERE/_ref/libmuto_ref.so"

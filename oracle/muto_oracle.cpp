@@ -13,6 +13,7 @@
 //   displacement         src/MutoMLSD.cpp:356-376
 //   Poca::run            src/MutoPoCA.cpp:51-134
 //   PoCut::run           src/MutoPoCut.cpp:19-121
+//   slr_run              src/MutoSLR.cpp:47-103, src/MutoSLRIter.cpp:15-83
 //   Mlsd::gather         src/MutoMLSD.cpp:268-326
 //   Mlsd::path_and_tail  src/MutoMLSD.cpp:382-415
 //   Mlsd::weights        src/MutoMLSD.cpp:417-430
@@ -334,6 +335,72 @@ static int poca_run(const Grid* gp, const oracle_cfg* cfg, const double* cut, co
 int oracle_poca(const Grid* gp, const oracle_cfg* cfg, const Ray* rays, uint64_t n_rays, double* img,
                 int64_t* assign, uint64_t* counters) {
     return poca_run(gp, cfg, nullptr, rays, n_rays, img, assign, counters);
+}
+
+// Straight-line reconstruction, src/MutoSLR.cpp:47-103 (n_iter = 0), and its
+// iterative form, src/MutoSLRIter.cpp:15-83 (n_iter >= 1 passes, in place:
+// every muon sees the image as the muons before it left it, and each pass
+// adds its weights again).  Each muon's incoming and outgoing lines are cut
+// at the grid's top and bottom planes and the straight line between the two
+// points is walked; its voxels get the mean squared projected angle, shared
+// by length^2 (length_weighted) or equally.
+static int slr_run(const Grid* gp, const oracle_cfg* cfg, int n_iter, const Ray* rays, uint64_t n_rays, double* img) {
+    const Grid& g = *gp;
+    const uint64_t V = static_cast<uint64_t>(g.nx) * g.ny * g.nz;
+    std::vector<double> weight(V, 0.0);
+    std::fill(img, img + V, 0.0);
+    uint64_t n_total = cfg->total_num_rays > 0 ? static_cast<uint64_t>(cfg->total_num_rays) : n_rays;
+    if (n_total > n_rays) n_total = n_rays;  // the reference would read past the end
+    const double z_lo = g.z_min;                                   // :57
+    const double z_hi = g.z_min + g.dz * static_cast<double>(g.nz);  // :58
+    const double mag = cfg->angle_unit_mag;
+    auto at = [&](const Voxel& v) -> uint64_t {
+        return static_cast<uint64_t>(v.x) + static_cast<uint64_t>(g.nx) * (static_cast<uint64_t>(v.y) + static_cast<uint64_t>(g.ny) * v.z);
+    };
+    std::vector<Voxel> path;
+    const int passes = n_iter > 0 ? n_iter : 1;
+    for (int iter = 0; iter < passes; ++iter) {
+        for (uint64_t i = 0; i < n_total; ++i) {
+            const Ray& r = rays[i];
+            const double axz = (std::atan2(r.din[0], r.din[2]) - std::atan2(r.dout[0], r.dout[2])) * mag;  // :63-64
+            const double ayz = (std::atan2(r.din[1], r.din[2]) - std::atan2(r.dout[1], r.dout[2])) * mag;
+            const double t_in = (z_hi - r.pin[2]) / r.din[2];  // :67-70
+            const double t_out = (z_lo - r.pout[2]) / r.dout[2];
+            double p_in[3], p_out[3], d[3];
+            for (int k = 0; k < 3; ++k) {
+                p_in[k] = r.pin[k] + t_in * r.din[k];
+                p_out[k] = r.pout[k] + t_out * r.dout[k];
+                d[k] = p_in[k] - p_out[k];
+            }
+            siddon_path(g, p_in, p_out, path);
+            const double l_total = std::sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);  // :77
+            double val_total = 0.0;  // src/MutoSLRIter.cpp:49-52
+            if (n_iter > 0)
+                for (const Voxel& v : path) val_total += img[at(v)];
+            const double a2 = axz * axz + ayz * ayz;
+            for (const Voxel& v : path) {
+                const uint64_t j = at(v);
+                double iv;
+                if (cfg->length_weighted) {  // :80-86
+                    weight[j] += v.length / g.dz;
+                    iv = a2 * 0.5 * (v.length / l_total) * (v.length / l_total);
+                } else {
+                    weight[j] += 1.0;
+                    iv = a2 * 0.5 / static_cast<double>(path.size() * path.size());
+                }
+                if (n_iter > 0 && iter != 0) iv *= img[j] / val_total;  // src/MutoSLRIter.cpp:64-66
+                if (cfg->has_energy) iv *= r.ein * r.ein;                 // :87-89
+                img[j] += iv;
+            }
+        }
+    }
+    for (uint64_t j = 0; j < V; ++j) img[j] = weight[j] < cfg->eps ? 0 : img[j] / weight[j];  // :98-100
+    return 0;
+}
+
+// SLR (n_iter = 0) or SLRIter (n_iter = its "num_iteration", >= 1).
+int oracle_slr(const Grid* gp, const oracle_cfg* cfg, int n_iter, const Ray* rays, uint64_t n_rays, double* img) {
+    return slr_run(gp, cfg, n_iter, rays, n_rays, img);
 }
 
 // PoCut with percentile cut (the "cut_percentile" key); outputs as oracle_poca.

@@ -55,6 +55,7 @@ def lib() -> C.CDLL:
         L.oracle_siddon_batch.argtypes = [C.POINTER(Grid), D, D, C.c_uint64, C.c_uint32, U32, D, U32]
         L.oracle_poca.argtypes = [C.POINTER(Grid), C.POINTER(Cfg), P, C.c_uint64, D, I64, U64]
         L.oracle_pocut.argtypes = [C.POINTER(Grid), C.POINTER(Cfg), C.c_double, P, C.c_uint64, D, I64, U64]
+        L.oracle_slr.argtypes = [C.POINTER(Grid), C.POINTER(Cfg), C.c_int, P, C.c_uint64, D]
         L.oracle_mlsd_create.restype = P
         L.oracle_mlsd_create.argtypes = [C.POINTER(Grid), C.POINTER(Cfg), P, C.c_uint64, D, C.c_int]
         L.oracle_mlsd_destroy.argtypes = [P]
@@ -132,6 +133,20 @@ def pocut(grid, cfg: dict, rays: np.ndarray):
                        n, _d(img), assign.ctypes.data_as(C.POINTER(C.c_int64)),
                        counters.ctypes.data_as(C.POINTER(C.c_uint64)))
     return img, assign, counters
+
+
+def slr(grid, cfg: dict, rays: np.ndarray, iterative: bool = False):
+    """SLR (src/MutoSLR.cpp:47-103) or, iterative, SLRIter (src/MutoSLRIter.cpp:15-83;
+    cfg["num_iteration"] defaults to 1, :10)."""
+    rays = np.ascontiguousarray(rays, np.float64)
+    img = np.zeros(grid.nx * grid.ny * grid.nz, np.float64)
+    g = make_grid(grid)
+    c = make_cfg(cfg, "poca")
+    n_iter = max(int(cfg.get("num_iteration", 1)), 0) if iterative else 0
+    if iterative and n_iter == 0:  # no pass at all: nothing added, every voxel 0
+        return img
+    lib().oracle_slr(C.byref(g), C.byref(c), n_iter, rays.ctypes.data_as(C.c_void_p), rays.shape[0], _d(img))
+    return img
 
 
 def cubic(p3: float, p2: float, p1: float, p0: float, tol: float = 1e-8):

@@ -1,6 +1,7 @@
 // C entry points over the reference's own reconstruction classes, compiled
 // from its sources in place (src/MutoSiddon.cpp, src/MutoPoCA.cpp,
-// src/MutoMLSD.cpp, src/MutoMAP.cpp, src/MutoPoCut.cpp) against the stand-in headers in
+// src/MutoMLSD.cpp, src/MutoMAP.cpp, src/MutoPoCut.cpp, src/MutoSLR.cpp,
+// src/MutoSLRIter.cpp) against the stand-in headers in
 // oracle/ref_shim.  TEST INFRASTRUCTURE ONLY: used to generate the golden
 // vectors under tests/golden/ and to cross-check oracle/muto_oracle.cpp.
 //
@@ -17,6 +18,8 @@
 #include "MutoMLSD.h"
 #include "MutoPoCA.h"
 #include "MutoPoCut.h"
+#include "MutoSLR.h"
+#include "MutoSLRIter.h"
 #include "MutoSiddon.h"
 
 static_assert(sizeof(RayData) == 14 * sizeof(double), "RayData must be 14 doubles");
@@ -119,7 +122,8 @@ int ref_siddon(const uint32_t* n, const double* f, const double* p1, const doubl
     return 0;
 }
 
-// method: "poca", "pocut", "mlsd" or "map"; config: that method's JSON object.  out
+// method: "poca", "pocut", "slr", "slr_iter", "mlsd" or "map"; config: that
+// method's JSON object.  out
 // gets nx*ny*nz doubles of the grid the object ends with (out_n: its dims).
 int ref_reconstruct(const char* method, const char* config, const double* rays, uint64_t n, double* out,
                     uint64_t cap, uint32_t* out_n) {
@@ -134,6 +138,14 @@ int ref_reconstruct(const char* method, const char* config, const double* rays, 
         g = r.getCurrentGrid();
     } else if (m == "pocut") {
         MutoPoCut r(cfg);
+        img = r.reconstruct(data);
+        g = r.getCurrentGrid();
+    } else if (m == "slr") {
+        MutoSLR r(cfg);
+        img = r.reconstruct(data);
+        g = r.getCurrentGrid();
+    } else if (m == "slr_iter") {
+        MutoSLRIter r(cfg);
         img = r.reconstruct(data);
         g = r.getCurrentGrid();
     } else if (m == "mlsd") {

@@ -1,7 +1,8 @@
 """Generate the golden vectors in tests/golden/ from the reference itself.
 
 The reference's reconstruction sources (src/MutoSiddon.cpp, src/MutoPoCA.cpp,
-src/MutoMLSD.cpp, src/MutoMAP.cpp, src/MutoPoCut.cpp) are compiled in place by
+src/MutoMLSD.cpp, src/MutoMAP.cpp, src/MutoPoCut.cpp, src/MutoSLR.cpp,
+src/MutoSLRIter.cpp) are compiled in place by
 oracle/build_ref.sh and called through oracle/reference.py; the inputs
 (segments, synthetic tracks) are stored next to the outputs so the tests need
 neither the reference nor the generator.  Run where the reference tree is
@@ -68,6 +69,16 @@ def track_case():
         img, _ = R.reconstruct("pocut", cfg, rays, g.nvox)
         out[name] = img
         configs[name] = cfg
+    # SLR and SLRIter: both weightings, with momentum, 1 and 3 in-place passes
+    for name, (method, cfg) in {"slr_lw": ("slr", wl.poca_config(length_weighted=True)),
+                                "slr_eq": ("slr", wl.poca_config(length_weighted=False)),
+                                "slr_lw_energy": ("slr", wl.poca_config(length_weighted=True, has_energy=True)),
+                                "slr_iter_1": ("slr_iter", wl.poca_config(length_weighted=True, num_iteration=1)),
+                                "slr_iter_3": ("slr_iter", wl.poca_config(length_weighted=False, has_energy=True,
+                                                                          num_iteration=3))}.items():
+        img, _ = R.reconstruct(method, cfg, rays, g.nvox)
+        out[name] = img
+        configs[name] = {"method": method, **cfg}
     cfg = wl.em_config()
     p = R.mlsd_paths(cfg, rays)
     for k, v in p.items():

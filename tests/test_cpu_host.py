@@ -40,7 +40,9 @@ def test_python_bindings_cover_the_header():
     ("map", '{"num_iteration": -1}', 2),
     ("mlsd", '{"update_with_mean": 3}', 2),
     ("mlsd", '[1, 2]', 2),
-    ("slr", "{}", 1),
+    ("slr_v2", "{}", 1),
+    ("slr_iter", '{"num_iteration": -1}', 2),
+    ("pocut", '{"cut_percentile": "most"}', 2),
 ])
 def test_config_errors_are_reported_before_any_device_call(lib, method, cfg, code):
     h = C.c_void_p()

@@ -63,6 +63,16 @@ def test_oracle_pocut_matches_golden(oracle, name):
     assert np.array_equal(bits(img), bits(T[name]))
 
 
+SLR_CASES = [k for k in CFG if k.startswith("slr_")]
+
+
+@pytest.mark.parametrize("name", SLR_CASES)
+def test_oracle_slr_matches_golden(oracle, name):
+    cfg = CFG[name]
+    img = oracle.slr(grid_of(T["grid"]), cfg, T["rays"], iterative=cfg["method"] == "slr_iter")
+    assert np.array_equal(bits(img), bits(T[name]))
+
+
 def test_oracle_paths_match_golden(oracle):
     g = grid_of(T["grid"])
     e = oracle.Mlsd(g, CFG["paths"], T["rays"], np.full(g.nvox, 1e-7)).export()
@@ -121,6 +131,20 @@ def test_gpu_pocut_matches_golden(gpu, name):
     with M.MutoPoCut(CFG[name]) as rec:
         img = rec.reconstruct(T["rays"]).reshape(-1, order="F")
     assert rel_l2(img, T[name]) < 1e-12 if np.any(T[name]) else not np.any(img)
+    assert np.array_equal(img > 0, T[name] > 0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", SLR_CASES)
+def test_gpu_slr_matches_golden(gpu, name):
+    # voxel walks bit-exact; atan2 (CUDA's, within 2 ulp of the correctly rounded
+    # one) and the FP64 atomics of the first pass leave rounding differences
+    cfg = dict(CFG[name])
+    method = cfg.pop("method")
+    rec = M.MutoSLRIter(cfg) if method == "slr_iter" else M.MutoSLR(cfg)
+    with rec:
+        img = rec.reconstruct(T["rays"]).reshape(-1, order="F")
+    assert rel_l2(img, T[name]) < 1e-12
     assert np.array_equal(img > 0, T[name] > 0)
 
 

@@ -127,6 +127,32 @@ def test_pocut_matches_oracle(gpu, oracle, n, n_muons, seed, cut, lw, energy):
     assert np.all(img[ref == 0] == 0)
 
 
+@pytest.mark.parametrize("n,n_muons,seed", [(12, 5000, 81), (30, 20000, 82)])
+@pytest.mark.parametrize("lw,energy,iters", [(True, False, 0), (False, False, 0), (True, True, 0), (True, False, 1),
+                                             (False, True, 3), (True, False, 0.5)])
+def test_slr_matches_oracle(gpu, oracle, n, n_muons, seed, lw, energy, iters):
+    # src/MutoSLR.cpp:47-103 (iters 0) and src/MutoSLRIter.cpp:15-83 (iters passes; 0.5
+    # stands for SLRIter with num_iteration 0: an empty image).  Voxel walks are bit-exact;
+    # atan2 and the first pass's FP64 atomics leave rounding differences.
+    wl = W.small(n_muons=n_muons, seed=seed, n=n)
+    rays = wl.tracks()
+    cfg = wl.poca_config(length_weighted=lw, has_energy=energy)
+    if iters:
+        cfg["num_iteration"] = int(iters)
+        ref = oracle.slr(wl.grid, cfg, rays, iterative=True)
+        rec = M.MutoSLRIter(cfg)
+    else:
+        ref = oracle.slr(wl.grid, cfg, rays)
+        rec = M.MutoSLR(cfg)
+    with rec:
+        img = rec.reconstruct(rays).reshape(-1, order="F")
+    if not np.any(ref):
+        assert not np.any(img)
+        return
+    assert rel_l2(img, ref) < 1e-12
+    assert np.array_equal(img > 0, ref > 0)
+
+
 @pytest.mark.parametrize("straight", [False, True])
 def test_mlsd_paths_bit_exact(gpu, oracle, straight):
     wl = W.small(n_muons=6000, seed=31)
