@@ -54,7 +54,7 @@ __host__ __device__ constexpr int cand_rows() {
 }
 // resident blocks per SM each class kernel is compiled for (its register cap)
 __host__ __device__ constexpr int vox_min_blocks(int C, bool streamed) {
-    return streamed ? 4 : C <= 4 ? 5 : C <= 6 ? 4 : C == 7 ? 3 : C <= 9 ? 2 : 5;
+    return streamed ? 4 : C <= 4 ? 5 : C <= 6 ? 4 : C == 7 ? 4 : C == 8 ? 3 : C == 9 ? 2 : 5;
 }
 // classes whose segments are long enough (M > 256) to be selected by the
 // streamed path
