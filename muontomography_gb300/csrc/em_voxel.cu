@@ -147,7 +147,19 @@ struct VoxKeys {
     static constexpr bool kBounded = true;  // a lane never has more than R keys
     __device__ __forceinline__ uint32_t rows() const { return R; }
     __device__ __forceinline__ K get(int r) const { return key[r]; }
-    __device__ __forceinline__ K sample() const { return key[0]; }  // element `lane`: slot order is random
+    // one key per lane from rows spread over the segment (row lane*R/32, or
+    // the last row holding an element of this lane), so that the samples do
+    // not all come from the segment's first 32 elements
+    __device__ __forceinline__ K sample() const {
+        uint32_t t = (static_cast<uint32_t>(lane) * R) >> 5;
+        const uint32_t last = M > static_cast<uint32_t>(lane) ? (M - 1 - lane) >> 5 : 0;
+        if (t > last) t = last;
+        K s = key[0];
+#pragma unroll
+        for (int r = 1; r < R; ++r)
+            if (static_cast<uint32_t>(r) == t) s = key[r];
+        return s;
+    }
     template <class F>
     __device__ __forceinline__ void each(F f) const {
 #pragma unroll
