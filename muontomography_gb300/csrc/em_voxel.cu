@@ -479,14 +479,15 @@ struct Pred {
 };
 
 // Next window: centred on the order statistic just found, wide enough for
-// about 40 keys at the density of the final sorted candidates, and for
+// about 24 keys at the density of the final sorted candidates (so that most
+// windows end in the 32-key warp sort), and for
 // twice the drift since the last prediction (twice the old width after a
 // miss).  0: no prediction (sampling next time).
 template <typename Real, typename K>
 __device__ __forceinline__ Pred<Real> next_window(const Sel<K>& sel, bool used, bool hit, const Pred<Real>& old) {
     const Real c = from_key(sel.kth);
     Real h = 0;
-    if (sel.nfin >= 2) h = (from_key(sel.whi) - from_key(sel.wlo)) * Real(20) / static_cast<Real>(sel.nfin);
+    if (sel.nfin >= 2) h = (from_key(sel.whi) - from_key(sel.wlo)) * Real(12) / static_cast<Real>(sel.nfin);
     if (used) {
         const Real drift = c > old.center ? c - old.center : old.center - c;
         h = h > Real(2) * drift ? h : Real(2) * drift;
