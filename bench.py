@@ -140,7 +140,8 @@ SETUP_PHASES = ["gather", "info_count", "offsets", "fill", "voxel_major", "class
 
 
 def em_config(wl, args, precision: str, n_iter: int) -> dict:
-    over = {"precision": precision, "num_iteration": n_iter, "muon_pass": args.muon_pass}
+    over = {"precision": precision, "num_iteration": n_iter, "muon_pass": args.muon_pass,
+            "muon_layout": args.muon_layout}
     if getattr(args, "voxel_stream_above", None) is not None:
         over["voxel_stream_above"] = args.voxel_stream_above
     if args.mode == "mean":
@@ -420,6 +421,7 @@ def main() -> int:
     ap.add_argument("--ttl-iters", type=int, default=50)
     ap.add_argument("--cpu-sample", type=int, default=150_000)
     ap.add_argument("--muon-pass", choices=["auto", "tile", "warp"], default="auto")
+    ap.add_argument("--muon-layout", choices=["auto", "columns", "index"], default="auto")
     ap.add_argument("--voxel-stream-above", type=int, default=None,
                     help="segments longer than this are selected without holding their keys (-1: never)")
     ap.add_argument("--ncu-traffic", type=float, default=None,

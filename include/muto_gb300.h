@@ -98,6 +98,9 @@ typedef struct muto_handle muto_handle;
  * "muon_pass" ("auto": the warp-batched variant, its group size chosen by
  * timing on the scan's data at prepare and reused for later scans of the
  * same shape in the process; "tile" or "warp" force one),
+ * "muon_layout" ("auto": the per-muon coefficient table in column order of
+ * the muons' PoCA points when it would take more than a third of L2, else
+ * in muon order; "columns" or "index" force one),
  * "voxel_stream_above" (-1: every segment up to 1536 pairs (768 in fp64)
  * is selected from registers; n >= 256: segments longer than n are
  * selected without holding their keys). */

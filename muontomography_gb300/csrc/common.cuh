@@ -125,11 +125,21 @@ void launch_offset_voxels(uint32_t* vidx, uint64_t n, uint32_t v_scan, uint32_t 
 void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* mult, Counters* ctr, cudaStream_t s);
 // voxel-major copy of the pair lists: (muon, L, T) at start[j] + rank within voxel j
 // (rec: P staging records, free after the call's work is done)
+// kslot (optional): vm_mu holds kslot[muon] instead of the muon's index
 template <typename Real>
 void launch_build_voxel_major(const uint64_t* off, uint64_t n, const uint32_t* vidx, const Real* L, const Real* T,
                               uint32_t V, const uint64_t* start, uint32_t* cursor, uint64_t P,
                               typename Vec4<Real>::type* rec, uint32_t* vm_mu, typename Vec2<Real>::type* vm_LT,
-                              cudaStream_t s);
+                              const uint32_t* kslot, cudaStream_t s);
+// Rows of the per-muon coefficient table in column order of the muons' PoCA
+// points (x, y cell of the grid, clamped): the muons crossing a column of
+// voxels then sit in a compact block of rows, so the key pass's gathers for
+// a run of columns touch a slice of the table that stays in L2 even when the
+// whole table does not.  cell: n scratch; hist, cursor: nx*ny + 1 scratch
+// (zeroed here); cstart: nx*ny + 1; scan_scratch as for scan_u32_to_u64 of
+// nx*ny
+void launch_muon_slots(const double* scat, uint64_t n, muto_grid g, uint32_t* cell, uint32_t* hist,
+                       uint64_t* cstart, uint32_t* cursor, void* scan_scratch, uint32_t* kslot, cudaStream_t s);
 void launch_siddon_batch(muto_grid g, const double* p1, const double* p2, uint64_t n, uint32_t cap, uint32_t* xyz,
                          double* len, uint32_t* counts, cudaStream_t s);
 
@@ -204,6 +214,7 @@ struct MuonPassArgs {
     const Real* pr2;                          // N (+ padding)
     const Real* lam;                          // V: lambda gathered by the muons
     typename Vec4<Real>::type* kout;          // N: (k0, k1, k2, 0)
+    const uint32_t* kslot;                    // N: the row of kout each muon writes (null: its own index)
     uint32_t V;
     double E00, E01, E11;
     int compute_cost;

@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_em_muon(MuonPassArgs<Real> a, i
             } else {
                 ++singular_local;  // inverse left at zero: s_ij = 2 l_j
             }
-            a.kout[mb + m] = kv;
+            a.kout[a.kslot ? a.kslot[mb + m] : mb + m] = kv;
         }
         __syncthreads();  // closes the tile: its stage buffer may be refilled
     }
@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(kThreads) k_em_muon_warp(MuonPassArgs<Real> a,
             } else {
                 ++singular_local;
             }
-            a.kout[m] = kv;
+            a.kout[a.kslot ? a.kslot[m] : m] = kv;
         }
     }
     const double c = warp_sum(cost_local);

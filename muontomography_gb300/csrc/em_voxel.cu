@@ -183,7 +183,16 @@ struct PtrKeys {
     __device__ __forceinline__ K sample() const { return p[(lane * n) >> 5]; }
     template <class F>
     __device__ __forceinline__ void each(F f) const {
-        for (uint32_t i = lane; i < n; i += 32) f(p[i]);
+        constexpr uint32_t B = 8;  // eight loads in flight
+        uint32_t i = lane;
+        for (; i + 32 * (B - 1) < n; i += 32 * B) {
+            K x[B];
+#pragma unroll
+            for (uint32_t b = 0; b < B; ++b) x[b] = p[i + 32 * b];
+#pragma unroll
+            for (uint32_t b = 0; b < B; ++b) f(x[b]);
+        }
+        for (; i < n; i += 32) f(p[i]);
     }
 };
 
@@ -299,15 +308,28 @@ __device__ __forceinline__ int window_pass(const Src& v, uint32_t n, uint32_t k,
                                            Sel<K>* direct) {
     uint32_t c_lo = 0, t = 0;
     const uint32_t nr = v.rows();
-#pragma unroll
-    for (uint32_t r = 0; r < nr; ++r) {
-        const K x = v.get(r);
+    auto one = [&](K x) {
         const bool lt = x < lo;
         c_lo += lt ? 1u : 0u;
         if (!lt && x <= hi) {
             if (Src::kBounded || t < out_rows) out[t * 32 + lane] = x;
             ++t;
         }
+    };
+    if constexpr (Src::kBounded) {  // keys in registers
+#pragma unroll
+        for (uint32_t r = 0; r < nr; ++r) one(v.get(r));
+    } else {  // keys in memory: eight rows' loads in flight before their stores
+        constexpr uint32_t B = 8;
+        uint32_t r = 0;
+        for (; r + B <= nr; r += B) {
+            K x[B];
+#pragma unroll
+            for (uint32_t b = 0; b < B; ++b) x[b] = v.get(r + b);
+#pragma unroll
+            for (uint32_t b = 0; b < B; ++b) one(x[b]);
+        }
+        for (; r < nr; ++r) one(v.get(r));
     }
     below = __reduce_add_sync(kFull, c_lo);
     const uint32_t n_in = __reduce_add_sync(kFull, t);

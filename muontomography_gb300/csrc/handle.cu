@@ -142,6 +142,7 @@ struct Params {
     int tile_pairs = 0;
     int muon_pass = 0;  // 0 autotune, 1 tile (TMA), 2 warp-batched
     long long voxel_stream_above = -1;  // segments longer than this are selected without registers (-1: none)
+    int muon_layout = 0;  // coefficient rows: 0 auto (column order when the table outgrows L2), 1 columns, 2 index
 };
 
 // variant of the one-shot (PoCA) handle: 0 PoCA, 1 PoCut, 2 SLR, 3 SLRIter
@@ -230,6 +231,11 @@ Params parse_params(Method m, const std::string& text, int variant = 0) {
         else if (mp == "warp") P.muon_pass = 2;
         else throw Error(MUTO_ERR_CONFIG, "muon_pass must be \"auto\", \"tile\" or \"warp\"");
         P.voxel_stream_above = cfg.value("voxel_stream_above", static_cast<int64_t>(-1));
+        const std::string ml = cfg.value("muon_layout", "auto");
+        if (ml == "auto") P.muon_layout = 0;
+        else if (ml == "columns") P.muon_layout = 1;
+        else if (ml == "index") P.muon_layout = 2;
+        else throw Error(MUTO_ERR_CONFIG, "muon_layout must be \"auto\", \"columns\" or \"index\"");
         if (P.newton_max_iter < 1) throw Error(MUTO_ERR_CONFIG, "newton_max_iter must be >= 1");
     } catch (const json::type_error& e) {
         throw Error(MUTO_ERR_CONFIG, std::string("config value of the wrong type: ") + e.what());
@@ -299,6 +305,7 @@ struct muto_handle {
     cudaStream_t stream = nullptr;
     ClassFan fan;                 // side streams of the voxel pass's class kernels
     int device = 0, num_sms = 148;
+    uint64_t l2_bytes = 0;         // the device's L2 size
     size_t smem_optin = 0;
     std::atomic<uint64_t> dev_bytes{0};
     Profiler prof;
@@ -337,6 +344,7 @@ struct muto_handle {
     int vox_blocks_real[2 * kVoxClasses] = {}, vox_blocks_f64[2 * kVoxClasses] = {};  // resident blocks per class kernel
     uint32_t vox_streamed = 0;  // classes selected by the streamed path
     uint64_t vclass_off[kVoxClasses] = {};
+    DevMem kslot;                     // per kept muon: its row of kvec (empty: its own index)
     DevMem mult, start, kvec, keys;   // keys: the voxel pass's order key of every pair
     DevMem win;                       // per voxel: the last selection window (center, half-width)
     bool brick = false;               // path voxel indices are bricked (single scans), see lam_b
@@ -857,11 +865,32 @@ void prepare_em(muto_handle* h) {
         h->vm_LT.alloc((Pn + kPad) * sizeof(typename Vec2<Real>::type), &h->dev_bytes);
         DevMem staging;
         staging.alloc(std::max<uint64_t>(Pn, 1) * sizeof(R4), &h->dev_bytes);
+        // coefficient rows in column order of the PoCA points, when asked or
+        // when the table would take more than a third of L2
+        h->kslot.release();
+        const bool columns = P.muon_layout == 1 || (P.muon_layout == 0 && N * sizeof(R4) > h->l2_bytes / 3);
+        if (columns && !h->batch && N > 0) {
+            const uint64_t nc = static_cast<uint64_t>(h->grid.nx) * h->grid.ny;
+            DevMem cell, hist, cstart, ccur, cscr;
+            h->kslot.alloc(N * sizeof(uint32_t), &h->dev_bytes);
+            cell.alloc(N * sizeof(uint32_t), &h->dev_bytes);
+            hist.alloc((nc + 1) * sizeof(uint32_t), &h->dev_bytes);
+            ccur.alloc((nc + 1) * sizeof(uint32_t), &h->dev_bytes);
+            cstart.alloc((nc + 1) * sizeof(uint64_t), &h->dev_bytes);
+            cscr.alloc(scan_scratch_bytes(nc + 1), &h->dev_bytes);
+            run(h, "muon_slots", [&] {
+                launch_muon_slots(h->scat.as<double>(), N, h->grid, cell.as<uint32_t>(), hist.as<uint32_t>(),
+                                  cstart.as<uint64_t>(), ccur.as<uint32_t>(), cscr.as<void>(), h->kslot.as<uint32_t>(),
+                                  s);
+            });
+            CK(cudaStreamSynchronize(s));
+        }
         run(h, "voxel_major", [&] {
             launch_build_voxel_major<Real>(h->off.as<uint64_t>(), N, h->vidx.as<uint32_t>(), h->L.as<Real>(),
                                            h->T.as<Real>(), static_cast<uint32_t>(V), h->start.as<uint64_t>(),
                                            cursor.as<uint32_t>(), Pn, staging.as<R4>(), h->vm_mu.as<uint32_t>(),
-                                           h->vm_LT.as<typename Vec2<Real>::type>(), s);
+                                           h->vm_LT.as<typename Vec2<Real>::type>(),
+                                           h->kslot.empty() ? nullptr : h->kslot.as<uint32_t>(), s);
         });
         CK(cudaStreamSynchronize(s));
     }
@@ -1002,6 +1031,7 @@ MuonPassArgs<Real> muon_args(muto_handle* h, const Real* lam, bool cost) {
     a.pr2 = h->pr2.as<Real>();
     a.lam = lam;
     a.kout = h->kvec.as<R4>();
+    a.kslot = h->kslot.empty() ? nullptr : h->kslot.as<uint32_t>();
     a.V = static_cast<uint32_t>(h->V());
     a.E00 = 4.0 * exy * exy / (ezo * ezo);
     a.E11 = 2.0 * exy * exy * (1.0 + (ezi / ezo + 1.0) * ezi / ezo);
@@ -1424,6 +1454,9 @@ int muto_create(const char* method, const char* config_json, muto_handle** out) 
         h->grid = h->P.grid;
         CK(cudaGetDevice(&h->device));
         CK(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device));
+        int l2 = 0;
+        CK(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, h->device));
+        h->l2_bytes = static_cast<uint64_t>(l2);
         int optin = 0;
         CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
         h->smem_optin = static_cast<size_t>(optin);

@@ -334,11 +334,13 @@ __global__ void k_build_voxel_major(const uint64_t* __restrict__ off, uint64_t n
 
 template <typename Real>
 __global__ void k_split_records(const typename Vec4<Real>::type* __restrict__ rec, uint64_t P,
-                                uint32_t* __restrict__ vm_mu, typename Vec2<Real>::type* __restrict__ vm_LT) {
+                                uint32_t* __restrict__ vm_mu, typename Vec2<Real>::type* __restrict__ vm_LT,
+                                const uint32_t* __restrict__ kslot) {
     const uint64_t p = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (p >= P) return;
     const typename Vec4<Real>::type r = rec[p];
-    vm_mu[p] = bits_index(r.x);
+    const uint32_t m = bits_index(r.x);
+    vm_mu[p] = kslot ? kslot[m] : m;
     typename Vec2<Real>::type lt;
     lt.x = r.y;
     lt.y = r.z;
@@ -564,20 +566,58 @@ template <typename Real>
 void launch_build_voxel_major(const uint64_t* off, uint64_t n, const uint32_t* vidx, const Real* L, const Real* T,
                               uint32_t V, const uint64_t* start, uint32_t* cursor, uint64_t P,
                               typename Vec4<Real>::type* rec, uint32_t* vm_mu, typename Vec2<Real>::type* vm_LT,
-                              cudaStream_t s) {
+                              const uint32_t* kslot, cudaStream_t s) {
     if (n == 0) return;
     k_build_voxel_major<Real><<<blocks_for(n * 32), kThreads, 0, s>>>(off, n, vidx, L, T, V, start, cursor, rec);
     count_launches(1);
     if (P == 0) return;
-    k_split_records<Real><<<blocks_for(P), kThreads, 0, s>>>(rec, P, vm_mu, vm_LT);
+    k_split_records<Real><<<blocks_for(P), kThreads, 0, s>>>(rec, P, vm_mu, vm_LT, kslot);
     count_launches(1);
 }
 template void launch_build_voxel_major<float>(const uint64_t*, uint64_t, const uint32_t*, const float*, const float*,
                                               uint32_t, const uint64_t*, uint32_t*, uint64_t, float4*, uint32_t*,
-                                              float2*, cudaStream_t);
+                                              float2*, const uint32_t*, cudaStream_t);
 template void launch_build_voxel_major<double>(const uint64_t*, uint64_t, const uint32_t*, const double*,
                                                const double*, uint32_t, const uint64_t*, uint32_t*, uint64_t,
-                                               double4*, uint32_t*, double2*, cudaStream_t);
+                                               double4*, uint32_t*, double2*, const uint32_t*, cudaStream_t);
+
+// the (x, y) cell of each kept muon's PoCA point, clamped to the grid, and
+// the muons per cell
+__global__ void k_muon_cells(const double* __restrict__ scat, uint64_t n, DevGrid g, uint32_t* __restrict__ cell,
+                             uint32_t* __restrict__ hist) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t c[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const double u = (scat[3 * i + k] - g.lo[k]) / g.w[k];
+        c[k] = u >= 0.0 ? (u < static_cast<double>(g.n[k]) ? static_cast<uint32_t>(u) : g.n[k] - 1) : 0u;
+    }
+    const uint32_t x = c[0] + g.n[0] * c[1];
+    cell[i] = x;
+    atomicAdd(hist + x, 1u);
+}
+
+__global__ void k_muon_slots(const uint32_t* __restrict__ cell, uint64_t n, const uint64_t* __restrict__ cstart,
+                             uint32_t* __restrict__ cursor, uint32_t* __restrict__ kslot) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t x = cell[i];
+    kslot[i] = static_cast<uint32_t>(cstart[x] + atomicAdd(cursor + x, 1u));
+}
+
+void launch_muon_slots(const double* scat, uint64_t n, muto_grid g, uint32_t* cell, uint32_t* hist,
+                       uint64_t* cstart, uint32_t* cursor, void* scan_scratch, uint32_t* kslot, cudaStream_t s) {
+    if (n == 0) return;
+    const uint64_t nc = static_cast<uint64_t>(g.nx) * g.ny;
+    (void)cudaMemsetAsync(hist, 0, (nc + 1) * sizeof(uint32_t), s);
+    (void)cudaMemsetAsync(cursor, 0, (nc + 1) * sizeof(uint32_t), s);
+    k_muon_cells<<<blocks_for(n), kThreads, 0, s>>>(scat, n, make_dev_grid(g), cell, hist);
+    count_launches(1);
+    scan_u32_to_u64(hist, cstart, nc, scan_scratch, s);
+    k_muon_slots<<<blocks_for(n), kThreads, 0, s>>>(cell, n, cstart, cursor, kslot);
+    count_launches(1);
+}
 
 void launch_siddon_batch(muto_grid g, const double* p1, const double* p2, uint64_t n, uint32_t cap, uint32_t* xyz,
                          double* len, uint32_t* counts, cudaStream_t s) {
