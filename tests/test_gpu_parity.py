@@ -312,6 +312,28 @@ def test_long_segments_match_oracle(gpu, oracle, precision, tol, mode):
     assert rel_l2(img.reshape(-1, order="F"), ref.image()) < tol
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("method", ["mlsd", "map"])
+def test_muon_layouts_agree(gpu, oracle, precision, method):
+    # the per-muon coefficient table in muon order or in column order of the PoCA
+    # points (chosen automatically for large tables, forced here): the keys are the
+    # same, so the medians are identical; both match the oracle
+    wl = W.small(n_muons=8000, seed=171, n=12)
+    rays = wl.tracks()
+    extra = {"beta": 0.01, "p": 1.0, "delta": 0.1, "all_neighbours": True} if method == "map" else {}
+    out = []
+    for layout in ("index", "columns"):
+        cfg = wl.em_config(precision=precision, num_iteration=4, muon_layout=layout, **extra)
+        rec = M.MutoMAP(cfg) if method == "map" else M.MutoMLSD(cfg)
+        with rec:
+            out.append(rec.reconstruct(rays))
+    assert np.array_equal(out[0].view(np.uint64), out[1].view(np.uint64))
+    ref = _mlsd_pair(oracle, wl, rays, wl.em_config(precision=precision, num_iteration=4, **extra),
+                     np.full(wl.grid.nvox, 1e-7), 4, method=method)
+    tol = FP64_TOL if precision == "fp64" else MIXED_TOL
+    assert rel_l2(out[1].reshape(-1, order="F"), ref.image()) < (1e-9 if method == "map" and precision == "fp64" else tol)
+
+
 @pytest.mark.parametrize("variant", ["tile", "warp"])
 def test_muon_pass_variants_agree(gpu, oracle, variant):
     wl = W.small(n_muons=8000, seed=121)
