@@ -139,9 +139,16 @@ SETUP_KERNELS = ["keep_flags", "scan", "compact", "muon_info", "siddon_count", "
 SETUP_PHASES = ["gather", "info_count", "offsets", "fill", "voxel_major", "classes", "tiles", "image", "autotune"]
 
 
+def method_of(args) -> str:
+    """MAP for the MAP workload (128x128x64 voxels of 15 mm), MLSD otherwise."""
+    return "map" if args.workload.startswith("map") else "mlsd"
+
+
 def em_config(wl, args, precision: str, n_iter: int) -> dict:
     over = {"precision": precision, "num_iteration": n_iter, "muon_pass": args.muon_pass,
             "muon_layout": args.muon_layout}
+    if method_of(args) == "map":  # beta 0.01, p = 1, the 26-neighbour stencil, delta = 0.1 median(lambda) 1e7
+        over.update(beta=0.01, p=1.0, all_neighbours=True, delta=0.1 * float(np.median(wl.lam())) * 1e7)
     if getattr(args, "voxel_stream_above", None) is not None:
         over["voxel_stream_above"] = args.voxel_stream_above
     if args.mode == "mean":
@@ -159,7 +166,7 @@ def cpu_port(wl, args, n_sample: int, n_iter: int, threads: int) -> dict:
     cfg = em_config(wl, args, "fp64", n_iter)
     init = np.full(wl.grid.nvox, 1e-7)
     t0 = time.perf_counter()
-    ref = O.Mlsd(wl.grid, cfg, rays, init, keep_paths=False)
+    ref = O.Mlsd(wl.grid, cfg, rays, init, keep_paths=False, method=method_of(args))
     t_setup = time.perf_counter() - t0
     pairs = ref.counts()["n_pairs"]
     times = []
@@ -184,7 +191,7 @@ def run_reference(args) -> int:
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * sum(t) / len(t), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": wl.name, "grid": list(wl.grid.shape), "mode": args.mode,
+        "config": {"workload": wl.name, "method": method_of(args), "grid": list(wl.grid.shape), "mode": args.mode,
                    "sample_muons": n_sample, "sample_pairs": r["pairs"]},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{n_sample} muons of {wl.name}: one EM iteration per step "
@@ -224,7 +231,7 @@ def run_ours(args) -> int:
 
     # ---- value: EM iterations with the tracks resident in HBM ---------------
     cfg = em_config(wl, args, args.precision, args.warmup + args.steps)
-    rec = M.Reconstruction("mlsd", cfg)
+    rec = M.Reconstruction(method_of(args), cfg)
     rec.load_tracks(None, on_device_ptr=d_rays.data_ptr(), n=n)
     rec.set_profiling(True)
     t0 = time.perf_counter()
@@ -306,7 +313,7 @@ def run_ours(args) -> int:
         out = np.empty(V, np.float64)
         times = []
         for k in range(args.e2e_steps + 1):  # the first call is a warm-up
-            r2 = M.Reconstruction("mlsd", ecfg)
+            r2 = M.Reconstruction(method_of(args), ecfg)
             lib.muto_get_stream(r2._h, C.byref(sp))
             s2 = torch.cuda.ExternalStream(sp.value)
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -321,7 +328,7 @@ def run_ours(args) -> int:
                 times.append(a.elapsed_time(b))
             r2.close()
         # the set-up of one more reconstruct, untimed, by phase (modules loaded)
-        r2 = M.Reconstruction("mlsd", ecfg)
+        r2 = M.Reconstruction(method_of(args), ecfg)
         r2.set_profiling(True)
         t0 = time.perf_counter()
         r2.load_tracks(host.numpy())
@@ -354,7 +361,7 @@ def run_ours(args) -> int:
         for prec in ("fp64", "mixed"):
             d = torch.empty((n, 14), dtype=torch.float64, device="cuda")
             d.copy_(host)
-            r3 = M.Reconstruction("mlsd", em_config(wl, args, prec, args.ttl_iters))
+            r3 = M.Reconstruction(method_of(args), em_config(wl, args, prec, args.ttl_iters))
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             r3.load_tracks(None, on_device_ptr=d.data_ptr(), n=n)
@@ -387,7 +394,8 @@ def run_ours(args) -> int:
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64",
             "data": "synthetic",
-            "config": {"workload": wl.name, "grid": list(wl.grid.shape), "voxel_mm": wl.grid.dx, "muons": n,
+            "config": {"workload": wl.name, "method": method_of(args), "grid": list(wl.grid.shape),
+                       "voxel_mm": wl.grid.dx, "muons": n,
                        "kept_muons": kept, "pairs_per_iteration": pairs, "mode": args.mode,
                        "precision": args.precision, "per_muon_2x2": "f64", "graph": True,
                        "parallelism": f"replicas x{world} (one scan per GPU)",
