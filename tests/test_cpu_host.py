@@ -43,6 +43,8 @@ def test_python_bindings_cover_the_header():
     ("slr_v2", "{}", 1),
     ("slr_iter", '{"num_iteration": -1}', 2),
     ("pocut", '{"cut_percentile": "most"}', 2),
+    ("mlsd", '{"muon_layout": "spiral"}', 2),
+    ("mlsd", '{"muon_pass": "fast"}', 2),
 ])
 def test_config_errors_are_reported_before_any_device_call(lib, method, cfg, code):
     h = C.c_void_p()
