@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_em_muon(MuonPassArgs<Real> a, i
 template <typename Real, int GROUP>
 __global__ void __launch_bounds__(kThreads) k_em_muon_warp(MuonPassArgs<Real> a, uint32_t n_muons) {
     using R4 = typename Vec4<Real>::type;
-    constexpr int U = 4;                    // pair loads in flight per lane per round
+    constexpr int U = 5;                    // pair loads in flight per lane per round
     constexpr int kPer = 32 / GROUP;        // muons summed at once per warp
     const int lane = threadIdx.x & 31;
     const int sub = lane / GROUP, glane = lane % GROUP;
