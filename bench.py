@@ -130,8 +130,8 @@ def workload(args, rank: int):
 
 # DRAM bytes per pair per launch, measured by ncu (--set full) on the 50^3-voxel
 # 2.5 M-muon case of the default scene (median EM, mixed form): muon pass
-# 868.4 MB and voxel pass (key pass and all classes) 1377.1 MB for 68 700 086 pairs
-TRAFFIC_PER_PAIR = {"muon": 868.4e6 / 68700086, "voxel": 1377.1e6 / 68700086}
+# 868.4 MB and voxel pass (key pass and all classes) 1378.5 MB for 68 700 086 pairs
+TRAFFIC_PER_PAIR = {"muon": 868.4e6 / 68700086, "voxel": 1378.5e6 / 68700086}
 
 # set-up kernels and host phases reported by the library's profiler
 SETUP_KERNELS = ["keep_flags", "scan", "compact", "muon_info", "siddon_count", "siddon_fill", "voxel_offset",
