@@ -5,10 +5,11 @@
 // The pairs are also stored voxel-major (muon, L, T), built once at setup.
 // Two steps:
 //   key pass     one thread per pair streams the lists, gathers its muon's
-//                coefficients k_i (written by the muon pass, small enough to
-//                stay in L2) and writes g_ij = k0 W00 + k1 W01 + k2 W11 as an
-//                order-preserving integer key, voxel-major.  The gather runs
-//                at full occupancy, apart from the selection.
+//                coefficients k_i (written by the muon pass; rows in column
+//                order of the PoCA points when the table outgrows L2) and
+//                writes g_ij = k0 W00 + k1 W01 + k2 W11 as an order-preserving
+//                integer key, voxel-major.  The gather runs at full
+//                occupancy, apart from the selection.
 //   class pass   one warp per voxel reads its M_j keys (coalesced, 4 or 8 B
 //                each) and selects on them; s_ij = 2 l_j + g_ij l_j^2, the
 //                reference's 2 l + (1/2 xyS - tr(Sigma^-1 W)) pr^2 l^2, is
@@ -16,12 +17,15 @@
 //                one of the s_ij, formed only for the values the update uses.
 // Nothing is accumulated with atomics.
 //   median       exact order statistics of the s_ij (nth_element semantics).
-//                Two rounds of sampling narrow the search: 32 samples of the
-//                segment are sorted in the warp, the keys within 6 sample ranks
-//                of the target are counted and compacted into shared memory,
-//                the same is done once more on the compacted keys, and the
-//                survivors (<= 64) are sorted by a warp bitonic sort.  A window
-//                that misses the target falls back to a bitwise radix search.
+//                Each voxel starts from the window its previous selection
+//                left (one pass: keys below it counted, keys inside kept in
+//                shared memory, sorted by a warp bitonic sort when <= 64).
+//                Without one, or when it misses, rounds of sampling narrow
+//                the search: 32 samples spread over the segment are sorted in
+//                the warp, the keys within 6 sample ranks of the target are
+//                counted and kept, the same is done on the kept keys, and the
+//                survivors (<= 64) are sorted.  A window that misses the
+//                target twice falls back to a bitwise radix search.
 //   percentile   mean of the lowest floor(pct/100 M) values: the order
 //                statistic t plus the sum of the values below it.
 //   mean         l + l^2 (sum_i g_ij) / (2 M)  ==  (sum_i s_ij) / M / 2.
