@@ -672,11 +672,13 @@ __device__ void voxel_stream(const VoxelPassArgs<Real, OutT>& a, uint32_t j, uin
 
 // The key pass: every pair's order key to_key(g_ij), g_ij = k_i . W(L, T),
 // written in voxel-major order for the class kernels.  One thread per pair,
-// U pairs of a thread in flight at once.  Each block streams one contiguous
-// range of the lists, tile after tile, so the segments of vertically
-// adjacent voxels (laid out next to each other) go through the same SM: a
-// steep muon's coefficients k_i, gathered for one segment, are still in L1
-// for the next.  The lists and the keys pass through marked evict-first.
+// U pairs of a thread in flight at once.  Persistent blocks, one per SM,
+// take the tiles of the column-ordered lists round robin, so the whole GPU
+// advances through a window of a few dozen adjacent columns: the muons
+// those columns share are gathered while their coefficients are in L2 (and
+// within a tile, the vertically adjacent segments of one column go through
+// the same SM's L1), whatever the size of the coefficient table.  The lists
+// and the keys pass through marked evict-first.
 constexpr int kKeyThreads = 1024;
 constexpr int kKeyUnroll = 8;
 constexpr uint64_t kKeyTile = uint64_t(kKeyThreads) * kKeyUnroll;
@@ -684,12 +686,11 @@ template <typename Real>
 __global__ void __launch_bounds__(kKeyThreads)
     k_pair_keys(const uint32_t* __restrict__ vm_mu, const typename Vec2<Real>::type* __restrict__ vm_LT,
                 const typename Vec4<Real>::type* __restrict__ kvec, typename KeyOf<Real>::type* __restrict__ keys,
-                uint64_t P, uint64_t range) {
+                uint64_t P) {
     using R2 = typename Vec2<Real>::type;
     constexpr int U = kKeyUnroll;
-    const uint64_t r0 = uint64_t(blockIdx.x) * range;
-    const uint64_t r1 = r0 + range < P ? r0 + range : P;
-    for (uint64_t t0 = r0; t0 < r1; t0 += kKeyTile) {
+    const uint64_t r1 = P;
+    for (uint64_t t0 = uint64_t(blockIdx.x) * kKeyTile; t0 < P; t0 += uint64_t(gridDim.x) * kKeyTile) {
         uint32_t mu[U];
         R2 lt[U];
 #pragma unroll
@@ -933,13 +934,11 @@ void launch_all(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists,
                 const int* resident_blocks, uint32_t streamed, int num_sms, const ClassFan* fan, cudaStream_t s,
                 std::integer_sequence<int, C...>) {
     using K = typename KeyOf<Real>::type;
-    if (a.P > 0) {  // one block per SM, each a contiguous range of whole tiles
+    if (a.P > 0) {  // one persistent block per SM, tiles round robin
         const uint64_t tiles = (a.P + kKeyTile - 1) / kKeyTile;
         const uint64_t want = static_cast<uint64_t>(num_sms > 0 ? num_sms : 1);
-        const uint64_t per = (tiles + want - 1) / want;
-        const uint64_t nb = (tiles + per - 1) / per;
-        k_pair_keys<Real><<<static_cast<unsigned>(nb), kKeyThreads, 0, s>>>(a.vm_mu, a.vm_LT, a.kvec, a.keys, a.P,
-                                                                           per * kKeyTile);
+        const unsigned nb = static_cast<unsigned>(tiles < want ? tiles : want);
+        k_pair_keys<Real><<<nb, kKeyThreads, 0, s>>>(a.vm_mu, a.vm_LT, a.kvec, a.keys, a.P);
         count_launches(1);
     }
     // classes to streams: the heaviest first, each to the least loaded stream
