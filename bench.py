@@ -131,7 +131,7 @@ def workload(args, rank: int):
 # DRAM bytes per pair per launch, measured by ncu (--set full) on the 50^3-voxel
 # 2.5 M-muon case of the default scene (median EM, mixed form): muon pass
 # 868.4 MB and voxel pass (key pass and all classes) 1378.5 MB for 68 700 086 pairs
-TRAFFIC_PER_PAIR = {"muon": 868.4e6 / 68700086, "voxel": 1378.5e6 / 68700086}
+TRAFFIC_PER_PAIR = {"muon": 868.4e6 / 68700086, "voxel": 1371.0e6 / 68700086}
 
 # set-up kernels and host phases reported by the library's profiler
 SETUP_KERNELS = ["keep_flags", "scan", "compact", "muon_info", "siddon_count", "siddon_fill", "voxel_offset",
@@ -292,7 +292,7 @@ def run_ours(args) -> int:
     t_voxel = (args.ncu_traffic if args.ncu_traffic is not None
                else (TRAFFIC_PER_PAIR["voxel"] * pairs if measured else None))
     t_muon = TRAFFIC_PER_PAIR["muon"] * pairs if measured else None
-    # the voxel pass takes about three quarters of an iteration: it is the dominant kernel
+    # the voxel pass takes about two thirds of an iteration: it is the dominant kernel
     roofline = {"bound": "hbm", "achieved": v_ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": (v_ach / pk["hbm_gbs"]) if v_ach else None, "traffic": t_voxel,
                 "kernel": "k_pair_keys + k_em_voxel (one launch per segment-length class)", "kernel_ms": voxel_ms,
