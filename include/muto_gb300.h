@@ -292,6 +292,23 @@ int muto_generate(const muto_grid* g, const double* lambda, const muto_gen_param
 int muto_generate_device(const muto_grid* g, const double* lambda_dev, const muto_gen_params* p, uint64_t first,
                          uint64_t n, muto_ray* out_dev, void* stream);
 
+/* Batched line fit of raw detector records on the GPU, one thread per
+ * record: the per-record step of MutoFile::getMuonData (src/MutoFile.cpp:
+ * 58-78 and getRayDataFromTemp, :248-304).  records holds n records of
+ * 2*nz+2 values {ein, x0, y0, ..., x_{nz-1}, y_{nz-1}, eout}, float32 when
+ * precision is 4, float64 when 8, at z = z_layers[0..nz-1] (nz <= 64).
+ * Layers 0..n_middle-1 give the incoming line and n_middle..nz-1 the
+ * outgoing one (n_middle >= 2 and nz - n_middle >= 2): each line is the
+ * principal axis of its hits (the first right singular vector the
+ * reference takes from JacobiSVD), oriented with d_z > 0, with pin on
+ * layer n_middle-1 and pout on layer n_middle.  Records holding a NaN are
+ * dropped (:71-76).  Host buffers: out must hold n tracks; it receives the
+ * kept records' tracks in record order and *n_out their number.  The
+ * result is bit for bit that of muto_read_muon_data (include/muto_io.h),
+ * which reads the same records from files on the host. */
+int muto_fit_tracks(const void* records, int precision, uint64_t n, const double* z_layers, int nz, int n_middle,
+                    muto_ray* out, uint64_t* n_out);
+
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their
  * own work (events, copies) with the handle's. */
 int muto_get_stream(muto_handle* h, void** out);

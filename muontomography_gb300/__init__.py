@@ -25,7 +25,7 @@ from ._lib import MutoError, check
 
 __all__ = [
     "Grid", "Block", "X0_MM", "RAY_FIELDS", "MutoError", "Reconstruction", "MutoPoCA", "MutoPoCut", "MutoSLR", "MutoSLRIter", "MutoMLSD", "MutoMAP",
-    "phantom", "generate", "lambda_from_x0", "save_image", "load_image", "siddon_batch", "library", "Batch",
+    "phantom", "generate", "lambda_from_x0", "save_image", "load_image", "siddon_batch", "fit_tracks", "library", "Batch",
 ]
 
 RAY_FIELDS = ("ein", "eout", "pin", "pout", "din", "dout")
@@ -390,6 +390,26 @@ def siddon_batch(grid: Grid, p1: np.ndarray, p2: np.ndarray, cap: int) -> tuple[
     check(lib.muto_siddon_batch(C.byref(g), _lib.dptr(p1), _lib.dptr(p2), n, cap, _lib.u32ptr(xyz), _lib.dptr(ln),
                                 _lib.u32ptr(cnt)), "muto_siddon_batch")
     return xyz, ln, cnt
+
+
+def fit_tracks(records: np.ndarray, z_layers, n_middle: int) -> np.ndarray:
+    """MutoFile::getMuonData's per-record line fit on the GPU (src/MutoFile.cpp:248-304).
+
+    records: (n, 2*nz+2) float32 or float64 rows {ein, x0, y0, ..., eout}; rows
+    holding a NaN are dropped.  Returns (kept, 14) tracks in the muto_ray layout."""
+    lib = library()
+    rec = np.ascontiguousarray(records)
+    if rec.dtype not in (np.float32, np.float64):
+        rec = rec.astype(np.float64)
+    z = np.ascontiguousarray(z_layers, np.float64)
+    if rec.ndim != 2 or rec.shape[1] != 2 * z.size + 2:
+        raise ValueError(f"records need 2*nz+2 = {2 * z.size + 2} columns, got shape {rec.shape}")
+    n = rec.shape[0]
+    out = np.zeros((n, 14), np.float64)
+    kept = C.c_uint64()
+    check(lib.muto_fit_tracks(rec.ctypes.data_as(C.c_void_p), rec.itemsize, n, _lib.dptr(z), z.size, n_middle,
+                              out.ctypes.data_as(C.c_void_p), C.byref(kept)), "muto_fit_tracks")
+    return out[: kept.value]
 
 
 def save_image(path: str, img: np.ndarray, grid: Grid, method: str, n_ray: int, n_iter: int, precision: int = 4) -> None:

@@ -69,6 +69,8 @@ SIGNATURES = {
     "muto_get_image": (C.c_int, [_P, _D, C.c_uint64]),
     "muto_set_image": (C.c_int, [_P, _D, C.c_uint64]),
     "muto_siddon_batch": (C.c_int, [C.POINTER(muto_grid), _D, _D, C.c_uint64, C.c_uint32, _U32, _D, _U32]),
+    "muto_fit_tracks": (C.c_int, [C.c_void_p, C.c_int, C.c_uint64, _D, C.c_int, C.c_int, C.c_void_p,
+                                  C.POINTER(C.c_uint64)]),
     "muto_siddon_batch_noalloc": (C.c_int, [C.POINTER(muto_grid), _D, _D, C.c_uint64, C.c_uint32, _U32, _D, _U32,
                                              _P]),
     "muto_select_probe": (C.c_int, [C.c_int, _D, C.c_uint64, _U64, C.c_uint32, C.c_int, C.c_int, C.c_longlong,

@@ -9,6 +9,7 @@
 #include <iostream>
 
 #include "muto_gb300.h"
+#include "trackfit.h"
 
 namespace {
 
@@ -26,67 +27,10 @@ muto_grid to_c(const VoxelGrid& g) {
     return c;
 }
 
-// Eigen-decomposition of a symmetric 3x3 matrix by cyclic Jacobi rotations;
-// returns the unit eigenvector of the largest eigenvalue.
-void principal_axis(double a[3][3], double* out) {
-    double v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-    for (int sweep = 0; sweep < 50; ++sweep) {
-        const double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
-        if (off < 1e-30 * (a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2]) || off == 0.0) break;
-        for (int p = 0; p < 2; ++p)
-            for (int q = p + 1; q < 3; ++q) {
-                if (a[p][q] == 0.0) continue;
-                const double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
-                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < 3; ++k) {  // A <- A J
-                    const double akp = a[k][p], akq = a[k][q];
-                    a[k][p] = c * akp - s * akq;
-                    a[k][q] = s * akp + c * akq;
-                }
-                for (int k = 0; k < 3; ++k) {  // A <- J^T A
-                    const double apk = a[p][k], aqk = a[q][k];
-                    a[p][k] = c * apk - s * aqk;
-                    a[q][k] = s * apk + c * aqk;
-                }
-                for (int k = 0; k < 3; ++k) {  // V <- V J
-                    const double vkp = v[k][p], vkq = v[k][q];
-                    v[k][p] = c * vkp - s * vkq;
-                    v[k][q] = s * vkp + c * vkq;
-                }
-            }
-    }
-    int best = 0;
-    for (int k = 1; k < 3; ++k)
-        if (a[k][k] > a[best][best]) best = k;
-    for (int k = 0; k < 3; ++k) out[k] = v[k][best];
-}
-
 }  // namespace
 
 void MutoFile::fitLine(const double* x, const double* y, const double* z, int n, double* c, double* d) {
-    c[0] = c[1] = c[2] = 0.0;
-    for (int i = 0; i < n; ++i) {
-        c[0] += x[i];
-        c[1] += y[i];
-        c[2] += z[i];
-    }
-    for (int k = 0; k < 3; ++k) c[k] /= (n > 0 ? n : 1);
-    double a[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-    for (int i = 0; i < n; ++i) {
-        const double r[3] = {x[i] - c[0], y[i] - c[1], z[i] - c[2]};
-        for (int p = 0; p < 3; ++p)
-            for (int q = 0; q < 3; ++q) a[p][q] += r[p] * r[q];
-    }
-    principal_axis(a, d);
-    const double nrm = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    if (!(nrm > 0)) {
-        d[0] = d[1] = 0.0;
-        d[2] = 1.0;
-        return;
-    }
-    const double sgn = d[2] < 0 ? -1.0 : 1.0;  // the SVD leaves the sign open; d_z > 0 here
-    for (int k = 0; k < 3; ++k) d[k] = sgn * d[k] / nrm;
+    muto::fit::fit_line(x, y, z, n, c, d);
 }
 
 MutoMuonData MutoFile::getMuonData(std::vector<std::string> flist, std::vector<MTfloat> zlayers, int nMiddle,
@@ -101,9 +45,12 @@ MutoMuonData MutoFile::getMuonData(std::vector<std::string> flist, std::vector<M
         std::cerr << "Error: at least two layers of detectors for both up and down area. " << std::endl;
         return data;
     }
+    if (nz > muto::fit::kMaxLayers) {
+        std::cerr << "Error: at most " << muto::fit::kMaxLayers << " layers of detectors. " << std::endl;
+        return data;
+    }
     const size_t nEach = 2 * static_cast<size_t>(nz) + 2;  // two extra values for in and out energy
     std::vector<double> rec(nEach);
-    std::vector<double> hx(nz), hy(nz);
     for (const std::string& name : flist) {
         std::ifstream file(name.c_str(), std::ios::in | std::ios::binary);
         if (file.fail()) {
@@ -119,7 +66,6 @@ MutoMuonData MutoFile::getMuonData(std::vector<std::string> flist, std::vector<M
         for (uint64_t r = 0; r < nRay; ++r) {
             file.read(raw.data(), static_cast<std::streamsize>(raw.size()));
             if (!file) break;
-            bool nan = false;
             for (size_t k = 0; k < nEach; ++k) {
                 if (fPrecision == 4) {
                     float f;
@@ -128,25 +74,12 @@ MutoMuonData MutoFile::getMuonData(std::vector<std::string> flist, std::vector<M
                 } else {
                     std::memcpy(&rec[k], raw.data() + 8 * k, 8);
                 }
-                nan = nan || std::isnan(rec[k]);
             }
-            if (nan) continue;
-            for (int i = 0; i < nz; ++i) {
-                hx[i] = rec[1 + 2 * i];
-                hy[i] = rec[2 + 2 * i];
-            }
+            muto_ray c;
+            if (!muto::fit::fit_record(rec.data(), zlayers.data(), nz, nMiddle, &c)) continue;  // a NaN
             RayData ray;
-            ray.ein = rec[0];
-            ray.eout = rec[2 * nz + 1];
-            double c[3], d[3];
-            fitLine(hx.data(), hy.data(), zlayers.data(), nMiddle, c, d);  // upper layers
-            double t = (zlayers[nMiddle - 1] - c[2]) / d[2];
-            ray.din = Vector3(d[0], d[1], d[2]);
-            ray.pin = Vector3(t * d[0] + c[0], t * d[1] + c[1], zlayers[nMiddle - 1]);
-            fitLine(hx.data() + nMiddle, hy.data() + nMiddle, zlayers.data() + nMiddle, nz - nMiddle, c, d);  // lower
-            t = (zlayers[nMiddle] - c[2]) / d[2];
-            ray.dout = Vector3(d[0], d[1], d[2]);
-            ray.pout = Vector3(t * d[0] + c[0], t * d[1] + c[1], zlayers[nMiddle]);
+            static_assert(sizeof(RayData) == sizeof(muto_ray), "RayData mirrors muto_ray");
+            std::memcpy(&ray, &c, sizeof(c));
             data.push_back(ray);
         }
     }
@@ -252,7 +185,7 @@ extern "C" int muto_read_muon_data(const char* const* files, int n_files, const 
                                    int n_middle, int precision, muto_ray* out, uint64_t cap, uint64_t* n_out) {
     if (!n_out || (n_files > 0 && !files) || nz <= 0 || !z_layers) return MUTO_ERR_ARG;
     if (precision != 4 && precision != 8) return MUTO_ERR_ARG;
-    if (n_middle < 2 || nz - n_middle < 2) return MUTO_ERR_ARG;
+    if (n_middle < 2 || nz - n_middle < 2 || nz > muto::fit::kMaxLayers) return MUTO_ERR_ARG;
     std::vector<std::string> fl;
     for (int i = 0; i < n_files; ++i) fl.push_back(files[i] ? files[i] : "");
     const std::vector<MTfloat> z(z_layers, z_layers + nz);

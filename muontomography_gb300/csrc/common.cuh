@@ -381,6 +381,18 @@ void launch_prior(const double* lam64, const uint32_t* mult, DevGrid g, MapParam
 void launch_generate(const muto_grid& g, const double* lambda, const muto_gen_params& p, uint64_t first, uint64_t n,
                      muto_ray* out, cudaStream_t s);
 
+// fit.cu: the detector layers of a batched line fit (nz <= 64)
+struct FitLayers {
+    double z[64];
+    int nz, n_middle;
+};
+// rec: n records of 2*nz+2 values (float when precision is 4, else double);
+// all, keep: n tracks and flags; pos: n+1 slots; scan_scratch as for
+// scan_u32_to_u64 of n.  out receives the kept tracks in record order and
+// pos[n] their number.
+void launch_fit_records(const void* rec, int precision, uint64_t n, const FitLayers& zl, muto_ray* all,
+                        uint32_t* keep, uint64_t* pos, void* scan_scratch, muto_ray* out, cudaStream_t s);
+
 // Kernel launches issued by the library (all handles), for the launch count.
 void count_launches(unsigned long long n);
 unsigned long long launches_so_far();

@@ -1965,4 +1965,48 @@ int muto_generate_device(const muto_grid* g, const double* lambda_dev, const mut
     });
 }
 
+int muto_fit_tracks(const void* records, int precision, uint64_t n, const double* z_layers, int nz, int n_middle,
+                    muto_ray* out, uint64_t* n_out) {
+    if (!n_out || !z_layers || (n > 0 && (!records || !out))) return MUTO_ERR_ARG;
+    if (precision != 4 && precision != 8) return MUTO_ERR_ARG;
+    if (nz > static_cast<int>(sizeof(FitLayers::z) / sizeof(double)) || n_middle < 2 || nz - n_middle < 2)
+        return MUTO_ERR_ARG;
+    return guarded(nullptr, [&] {
+        *n_out = 0;
+        if (n == 0) return;
+        FitLayers zl{};
+        for (int i = 0; i < nz; ++i) zl.z[i] = z_layers[i];
+        zl.nz = nz;
+        zl.n_middle = n_middle;
+        const uint64_t rec_bytes = (2 * static_cast<uint64_t>(nz) + 2) * static_cast<uint64_t>(precision);
+        const uint64_t chunk = std::min<uint64_t>(n, uint64_t(1) << 20);  // records per round trip
+        cudaStream_t s;
+        CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        DevMem rec, all, keep, pos, scr, kept;
+        rec.alloc(chunk * rec_bytes, nullptr);
+        all.alloc(chunk * sizeof(muto_ray), nullptr);
+        keep.alloc(chunk * sizeof(uint32_t), nullptr);
+        pos.alloc((chunk + 1) * sizeof(uint64_t), nullptr);
+        scr.alloc(scan_scratch_bytes(chunk), nullptr);
+        kept.alloc(chunk * sizeof(muto_ray), nullptr);
+        uint64_t written = 0;
+        for (uint64_t r0 = 0; r0 < n; r0 += chunk) {
+            const uint64_t m = std::min(chunk, n - r0);
+            CK(cudaMemcpyAsync(rec.as<void>(), static_cast<const char*>(records) + r0 * rec_bytes, m * rec_bytes,
+                               cudaMemcpyHostToDevice, s));
+            launch_fit_records(rec.as<void>(), precision, m, zl, all.as<muto_ray>(), keep.as<uint32_t>(),
+                               pos.as<uint64_t>(), scr.as<void>(), kept.as<muto_ray>(), s);
+            CK(cudaGetLastError());
+            uint64_t k = 0;
+            CK(cudaMemcpyAsync(&k, pos.as<uint64_t>() + m, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            if (k) CK(cudaMemcpyAsync(out + written, kept.as<void>(), k * sizeof(muto_ray), cudaMemcpyDeviceToHost, s));
+            written += k;
+        }
+        CK(cudaStreamSynchronize(s));
+        CK(cudaStreamDestroy(s));
+        *n_out = written;
+    });
+}
+
 }  // extern "C"

@@ -226,3 +226,32 @@ class Mlsd:
         g = np.zeros(self.V, np.float64)
         v = lib().oracle_mlsd_nll(self._h, _d(lam), _d(g))
         return v, g
+
+
+def fit_records(records: np.ndarray, z_layers, n_middle: int) -> np.ndarray:
+    """MutoFile::getMuonData's record loop (src/MutoFile.cpp:58-78) and its
+    per-record fit getRayDataFromTemp (:248-304), restated with numpy's SVD
+    in place of Eigen's JacobiSVD: each half's hits are centred, the first
+    right singular vector is the direction (oriented here with d_z > 0, which
+    the SVD leaves open), and the line is evaluated at layer n_middle-1 (in)
+    and n_middle (out).  Records holding a NaN are dropped.  Returns
+    (kept, 14) rows {ein, eout, pin, pout, din, dout}."""
+    rec = np.asarray(records, np.float64)
+    z = np.asarray(z_layers, np.float64)
+    nz = z.size
+    out = []
+    for row in rec:
+        if np.isnan(row).any():
+            continue
+        hits = np.stack([row[1:2 * nz + 1:2], row[2:2 * nz + 2:2], z], axis=1)
+        ray = [row[0], row[2 * nz + 1]]
+        lines = []
+        for part, zt in ((hits[:n_middle], z[n_middle - 1]), (hits[n_middle:], z[n_middle])):
+            c = part.mean(axis=0)
+            d = np.linalg.svd(part - c, full_matrices=False)[2][0]
+            d = d if d[2] >= 0 else -d
+            t = (zt - c[2]) / d[2]
+            lines.append((np.array([c[0] + t * d[0], c[1] + t * d[1], zt]), d))
+        ray += list(lines[0][0]) + list(lines[1][0]) + list(lines[0][1]) + list(lines[1][1])
+        out.append(ray)
+    return np.asarray(out, np.float64).reshape(-1, 14)

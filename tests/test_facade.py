@@ -116,3 +116,38 @@ def test_cli_end_to_end(gpu, facade, tmp_path, method):
         rec._n_iter = section.get("num_iteration", 1)
         want = rec.reconstruct(tracks)
     assert np.array_equal(img, want.astype(np.float32).astype(np.float64))
+
+
+@pytest.mark.parametrize("precision", [8, 4])
+def test_reader_matches_oracle_svd_fit(facade, oracle, tmp_path, precision):
+    # smeared hits: the principal-axis fit against the oracle's SVD restatement
+    g = M.Grid(10, 10, 10, -500.0, -500.0, -500.0, 100.0, 100.0, 100.0)
+    rays = M.generate(g, np.full(g.nvox, 1e-7), 300, seed=8)
+    rec = hits_from_tracks(rays)
+    rng = np.random.default_rng(8)
+    rec[:, 1:-1] += rng.standard_normal((rec.shape[0], rec.shape[1] - 2))
+    rec[[4, 250], [0, 9]] = np.nan
+    rec = rec.astype(np.float64 if precision == 8 else np.float32)
+    f = tmp_path / "hits.bin"
+    rec.tofile(f)
+    got = read(facade, [f], precision=precision)
+    want = oracle.fit_records(rec, Z, N_MIDDLE)
+    assert got.shape == want.shape == (298, 14)
+    np.testing.assert_array_equal(got[:, :2], want[:, :2])
+    np.testing.assert_allclose(got[:, 2:8], want[:, 2:8], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(got[:, 8:], want[:, 8:], rtol=0, atol=1e-12)
+
+
+def test_fit_tracks_rejects_bad_layouts(facade):
+    lib = M.library()
+    zz = np.asarray(Z, np.float64)
+    n = C.c_uint64()
+    rec = np.zeros((2, 14))
+    p = rec.ctypes.data_as(C.c_void_p)
+    out = np.zeros((2, 14)).ctypes.data_as(C.c_void_p)
+    assert lib.muto_fit_tracks(p, 2, 2, _lib.dptr(zz), 6, 3, out, C.byref(n)) == 1      # precision
+    assert lib.muto_fit_tracks(p, 8, 2, _lib.dptr(zz), 6, 1, out, C.byref(n)) == 1      # one upper layer
+    assert lib.muto_fit_tracks(p, 8, 2, _lib.dptr(zz), 6, 5, out, C.byref(n)) == 1      # one lower layer
+    assert lib.muto_fit_tracks(p, 8, 2, _lib.dptr(zz), 65, 3, out, C.byref(n)) == 1     # > 64 layers
+    assert lib.muto_fit_tracks(p, 8, 2, _lib.dptr(zz), 6, 3, None, C.byref(n)) == 1     # no output
+    assert lib.muto_fit_tracks(p, 8, 2, _lib.dptr(zz), 6, 3, out, None) == 1            # no count
