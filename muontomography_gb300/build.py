@@ -4,7 +4,7 @@
   ``include/muto_gb300.h`` (sm_103a kernels + host code).
 * ``muontomography_gb300/lib/libmuto_facade.so`` and ``lib/muto`` -- the C++
   reconstruction classes (MutoPoCA / MutoMLSD / MutoMAP / MutoFile /
-  MutoConfig) over the C ABI, and the command-line driver.
+  MutoConfig) over the C ABI, and the command-line program.
 
 Translation units compile in parallel; a unit is rebuilt only when it or a
 header it may include is newer than its object.

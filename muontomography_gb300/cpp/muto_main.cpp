@@ -1,4 +1,4 @@
-// Command-line driver (the reference's MuToTest.cpp:15-83): reads a JSON
+// Command-line program (the reference's MuToTest.cpp:15-83): reads a JSON
 // config, loads the raw-hit data files, reconstructs with the method whose
 // key is present ("poca", "mlsd", "map", "slr", "slr_iter" or "pocut") on the GPU and writes the image.
 //

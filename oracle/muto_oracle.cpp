@@ -2,7 +2,7 @@
 //
 // TEST INFRASTRUCTURE ONLY.  Nothing in the product links or calls this file;
 // only the tests, `__graft_entry__.smoke()` and the CPU-baseline leg of
-// `bench.py` load it (through oracle/oracle.py), and only as the checker.
+// `bench.py` load it (through oracle/oracle.py), and only to check results.
 //
 // It restates, function by function, the reference's reconstruction code
 // (LasDes/MuonTomography) with every quirk kept:

@@ -1,8 +1,8 @@
 """ctypes view of the FP64 CPU oracle (oracle/muto_oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and
-the CPU-baseline / reference leg of ``bench.py`` -- as the checker, never as the
-product path.  ``build()`` compiles the oracle into ``oracle/_build`` with
+the CPU-baseline / reference leg of ``bench.py`` -- to check results, never as
+the product path.  ``build()`` compiles the oracle into ``oracle/_build`` with
 ``g++ -O3 -fopenmp -ffp-contract=off``.
 """
 from __future__ import annotations

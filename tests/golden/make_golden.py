@@ -53,13 +53,13 @@ def track_case():
     rays = wl.tracks()
     g = wl.grid
     out = {"grid": np.array([g.nx, g.ny, g.nz, g.x_min, g.y_min, g.z_min, g.dx, g.dy, g.dz]), "rays": rays}
-    configs = {}
+    cases = {}
     for name, cfg in {"poca_lw": wl.poca_config(length_weighted=True),
                       "poca_dz": wl.poca_config(length_weighted=False),
                       "poca_straight": wl.poca_config(straight_line=True)}.items():
         img, _ = R.reconstruct("poca", cfg, rays, g.nvox)
         out[name] = img
-        configs[name] = cfg
+        cases[name] = cfg
     # PoCut: cut percentiles 1, 0.9, 0.5 and 0, both weightings, with and without momentum
     for name, cfg in {"pocut_lw_100": wl.poca_config(length_weighted=True, cut_percentile=1.0),
                       "pocut_dz_90": wl.poca_config(length_weighted=False, cut_percentile=0.9),
@@ -68,7 +68,7 @@ def track_case():
                       "pocut_dz_0": wl.poca_config(length_weighted=False, cut_percentile=0.0)}.items():
         img, _ = R.reconstruct("pocut", cfg, rays, g.nvox)
         out[name] = img
-        configs[name] = cfg
+        cases[name] = cfg
     # SLR and SLRIter: both weightings, with momentum, 1 and 3 in-place passes
     for name, (method, cfg) in {"slr_lw": ("slr", wl.poca_config(length_weighted=True)),
                                 "slr_eq": ("slr", wl.poca_config(length_weighted=False)),
@@ -78,12 +78,12 @@ def track_case():
                                                                           num_iteration=3))}.items():
         img, _ = R.reconstruct(method, cfg, rays, g.nvox)
         out[name] = img
-        configs[name] = {"method": method, **cfg}
+        cases[name] = {"method": method, **cfg}
     cfg = wl.em_config()
     p = R.mlsd_paths(cfg, rays)
     for k, v in p.items():
         out["paths_" + k] = v
-    configs["paths"] = cfg
+    cases["paths"] = cfg
     em = {"mlsd_median": ("mlsd", wl.em_config(num_iteration=6)),
           "mlsd_mean": ("mlsd", wl.em_config(num_iteration=6, update_with_mean=True)),
           "mlsd_pct90": ("mlsd", wl.em_config(num_iteration=6, update_with_mean=True, mean_percentile=90)),
@@ -96,8 +96,8 @@ def track_case():
     for name, (method, cfg) in em.items():
         img, _ = R.reconstruct(method, cfg, rays, g.nvox)
         out[name] = img
-        configs[name] = {"method": method, **cfg}
-    # PoCA-seeded EM through an initial image (initialize_method 0), as the example configs chain them
+        cases[name] = {"method": method, **cfg}
+    # PoCA-seeded EM through an initial image (initialize_method 0), as the example JSON files chain them
     seed_img = out["poca_lw"].astype(np.float32).astype(np.float64)
     R.set_initial_image(seed_img, g)
     cfg = wl.em_config(num_iteration=5, initialize_method=0, initial_image_file="poca.bin")
@@ -105,8 +105,8 @@ def track_case():
     R.set_initial_image(None)
     out["mlsd_poca_seeded"] = img
     out["poca_seed_image"] = seed_img
-    configs["mlsd_poca_seeded"] = {"method": "mlsd", **cfg}
-    return out, configs
+    cases["mlsd_poca_seeded"] = {"method": "mlsd", **cfg}
+    return out, cases
 
 
 def main() -> None:
@@ -114,9 +114,9 @@ def main() -> None:
         raise SystemExit("reference sources are not mounted here")
     R.build()
     np.savez_compressed(HERE / "siddon.npz", **siddon_case())
-    tracks, configs = track_case()
+    tracks, cases = track_case()
     np.savez_compressed(HERE / "tracks.npz", **tracks)
-    (HERE / "configs.json").write_text(json.dumps(configs, indent=1, sort_keys=True))
+    (HERE / "configs.json").write_text(json.dumps(cases, indent=1, sort_keys=True))
     print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
 
 

@@ -1,5 +1,5 @@
 """The C++ host layer: raw-hit reader (MutoFile::getMuonData), the image file
-format through MutoFile, and the command-line driver (MuToTest.cpp's
+format through MutoFile, and the command-line program (MuToTest.cpp's
 replacement) running the reconstruction classes on the GPU."""
 import ctypes as C
 import json

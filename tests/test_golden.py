@@ -97,7 +97,7 @@ def test_reference_build_still_matches_oracle_when_mounted(oracle):
     from oracle import reference as R
 
     if not R.available():
-        pytest.skip("reference sources not mounted (GPU box)")
+        pytest.skip("reference sources not mounted")
     g = grid_of(S["grid"])
     a = R.siddon(g, S["p1"], S["p2"], S["xyz"].shape[1])
     assert np.array_equal(a[2], S["count"]) and np.array_equal(bits(a[1]), bits(S["len"]))
