@@ -108,6 +108,17 @@ private:
     std::atomic<uint64_t>* tally_ = nullptr;
 };
 
+// A non-blocking stream owned by one call, destroyed on every way out.
+struct OwnedStream {
+    cudaStream_t s = nullptr;
+    OwnedStream() { CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
+    ~OwnedStream() {
+        if (s) cudaStreamDestroy(s);
+    }
+    OwnedStream(const OwnedStream&) = delete;
+    OwnedStream& operator=(const OwnedStream&) = delete;
+};
+
 enum Method { kPoca, kMlsd, kMap };
 
 struct Params {
@@ -1354,8 +1365,8 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
                       uint32_t streamed, uint32_t repeat, double* out) {
     using R2 = typename Vec2<Real>::type;
     using R4 = typename Vec4<Real>::type;
-    cudaStream_t s;
-    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    OwnedStream owned;
+    cudaStream_t s = owned.s;
     std::vector<uint32_t> mu(n);
     std::vector<R2> lt(n);
     std::vector<R4> kv(n);
@@ -1429,7 +1440,6 @@ void select_probe_run(const double* values, uint64_t n, const uint64_t* seg_off,
     std::vector<Real> o(n_segs);
     CK(cudaMemcpyAsync(o.data(), d_out.as<void>(), n_segs * sizeof(Real), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    CK(cudaStreamDestroy(s));
     for (uint32_t j = 0; j < n_segs; ++j) out[j] = static_cast<double>(o[j]);
 }
 
@@ -1655,8 +1665,8 @@ int muto_siddon_batch(const muto_grid* g, const double* p1, const double* p2, ui
     if (!g || (n > 0 && (!p1 || !p2 || !counts)) || (cap > 0 && n > 0 && (!xyz || !len))) return MUTO_ERR_ARG;
     return guarded(nullptr, [&] {
         if (n == 0) return;
-        cudaStream_t s;
-        CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        OwnedStream owned;
+        cudaStream_t s = owned.s;
         DevMem d1, d2, dx, dl, dc;
         d1.alloc(n * 3 * sizeof(double), nullptr);
         d2.alloc(n * 3 * sizeof(double), nullptr);
@@ -1678,7 +1688,6 @@ int muto_siddon_batch(const muto_grid* g, const double* p1, const double* p2, ui
         }
         CK(cudaMemcpyAsync(counts, dc.as<void>(), n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
-        CK(cudaStreamDestroy(s));
     });
 }
 
@@ -1980,8 +1989,8 @@ int muto_fit_tracks(const void* records, int precision, uint64_t n, const double
         zl.n_middle = n_middle;
         const uint64_t rec_bytes = (2 * static_cast<uint64_t>(nz) + 2) * static_cast<uint64_t>(precision);
         const uint64_t chunk = std::min<uint64_t>(n, uint64_t(1) << 20);  // records per round trip
-        cudaStream_t s;
-        CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        OwnedStream owned;
+        cudaStream_t s = owned.s;
         DevMem rec, all, keep, pos, scr, kept;
         rec.alloc(chunk * rec_bytes, nullptr);
         all.alloc(chunk * sizeof(muto_ray), nullptr);
@@ -2004,7 +2013,6 @@ int muto_fit_tracks(const void* records, int precision, uint64_t n, const double
             written += k;
         }
         CK(cudaStreamSynchronize(s));
-        CK(cudaStreamDestroy(s));
         *n_out = written;
     });
 }
