@@ -11,9 +11,10 @@
   log-uniform) with 1/100 of its muons: one batch handle against separate
   handles.
 * the 256 x 256 x 128 grid of 10 mm voxels with 1 M muons: the mixed form
-  within 1e-4 of the FP64 form after 5 iterations.  With its full 100 M muons
-  (1.9e10 pairs) the stored lists would need about 456 GB: it does not fit
-  one GPU's memory.
+  within 1e-4 of the FP64 form after 5 iterations.  Its full 100 M muons
+  (about 44 M kept and 9.8e9 pairs with this generator) would need about
+  275 GB of stored lists after set-up and about 390 GB at the set-up's
+  peak: more than one GPU's memory.
 """
 import numpy as np
 import pytest
