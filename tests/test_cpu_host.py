@@ -109,3 +109,38 @@ def test_phantom_voxel_centres():
     img = lam.reshape(g.shape, order="F")
     assert np.all(img[:2, :2, :2] == M.lambda_from_x0(M.X0_MM["lead"]))
     assert img[2, 0, 0] == M.lambda_from_x0(M.X0_MM["air"])
+
+
+def _bench(*argv, env=None):
+    import json
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parents[1]
+    e = dict(os.environ, **(env or {}))
+    out = subprocess.run([sys.executable, str(root / "bench.py"), *argv], cwd=root, env=e, capture_output=True,
+                         text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    return [json.loads(ln) for ln in lines]
+
+
+def test_reference_arm_prints_one_contract_line():
+    # the CPU reference arm on a small sample: one JSON line with the bench's keys
+    (line,) = _bench("--impl", "reference", "--steps", "1", "--warmup", "0", "--cpu-sample", "3000")
+    assert line["impl"] == "reference"
+    assert line["metric"] == "EM-iter muon-voxel updates/s" and line["higher_is_better"] is True
+    assert line["value"] > 0 and line["steps"] == 1 and line["n_gpus"] == 1
+    assert line["config"]["workload"] == "cube100_20mm_10M"
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and "3000 muons" in cb["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_other_ranks_exit_without_work():
+    env = {"RANK": "1", "LOCAL_RANK": "1", "WORLD_SIZE": "2", "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": "29533"}
+    assert _bench("--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-sample", "3000",
+                  env=env) == []
