@@ -1,6 +1,7 @@
 #!/bin/sh
 # Compile the reference's reconstruction sources in place against the
-# stand-in headers in oracle/ref_shim, into oracle/_ref/libmuto_ref.so.
+# stand-in headers in oracle/ref_shim, into oracle/_ref/libmuto_ref.so (and
+# its MutoFile into oracle/_ref/libmuto_ref_file.so).
 # Only possible where the reference tree is mounted; test infrastructure only.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -12,4 +13,9 @@ g++ -O2 -std=c++14 -fPIC -shared -fopenmp -ffp-contract=off -fno-fast-math -w \
     "$REF/src/MutoSiddon.cpp" "$REF/src/MutoPoCA.cpp" "$REF/src/MutoMLSD.cpp" "$REF/src/MutoMAP.cpp" \
     "$REF/src/MutoPoCut.cpp" "$REF/src/MutoSLR.cpp" "$REF/src/MutoSLRIter.cpp" \
     "$HERE/ref_harness.cpp" -o "$HERE/_ref/libmuto_ref.so"
-echo "built $HERE/_ref/libmuto_ref.so"
+# the reference's MutoFile (raw-hit reader and image files) on its own: the
+# reconstruction harness above provides its own loadImage
+g++ -O2 -std=c++14 -fPIC -shared -ffp-contract=off -fno-fast-math -w \
+    -I "$HERE/ref_shim" -I "$REF/include" \
+    "$REF/src/MutoFile.cpp" "$HERE/ref_file_harness.cpp" -o "$HERE/_ref/libmuto_ref_file.so"
+echo "built $HERE/_ref/libmuto_ref.so $HERE/_ref/libmuto_ref_file.so"

@@ -1,5 +1,6 @@
 """ctypes view of the reference's own reconstruction code built by
-oracle/build_ref.sh (oracle/_ref/libmuto_ref.so).
+oracle/build_ref.sh (oracle/_ref/libmuto_ref.so, and its MutoFile in
+oracle/_ref/libmuto_ref_file.so).
 
 TEST INFRASTRUCTURE ONLY.  Available only where the reference sources are
 mounted; used by tests/golden/make_golden.py to produce the committed golden
@@ -18,6 +19,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_ref" / "libmuto_ref.so"
+FILE_LIB = HERE / "_ref" / "libmuto_ref_file.so"
 REF = Path(os.environ.get("MUTO_REFERENCE", "/root/reference"))
 
 
@@ -26,9 +28,13 @@ def available() -> bool:
 
 
 def build() -> Path:
-    srcs = [REF / "src" / f for f in ("MutoSiddon.cpp", "MutoPoCA.cpp", "MutoMLSD.cpp", "MutoMAP.cpp")]
-    deps = srcs + [HERE / "ref_harness.cpp"] + list((HERE / "ref_shim").rglob("*"))
-    if not LIB.exists() or any(p.is_file() and p.stat().st_mtime > LIB.stat().st_mtime for p in deps):
+    srcs = [REF / "src" / f for f in ("MutoSiddon.cpp", "MutoPoCA.cpp", "MutoMLSD.cpp", "MutoMAP.cpp",
+                                      "MutoPoCut.cpp", "MutoSLR.cpp", "MutoSLRIter.cpp", "MutoFile.cpp")]
+    deps = srcs + [HERE / "ref_harness.cpp", HERE / "ref_file_harness.cpp", HERE / "build_ref.sh"] \
+        + list((HERE / "ref_shim").rglob("*"))
+    stale = [lib for lib in (LIB, FILE_LIB) if not lib.exists()
+             or any(p.is_file() and p.stat().st_mtime > lib.stat().st_mtime for p in deps)]
+    if stale:
         subprocess.run(["sh", str(HERE / "build_ref.sh")], check=True, capture_output=True)
     return LIB
 
@@ -112,3 +118,56 @@ def mlsd_paths(cfg: dict, rays: np.ndarray) -> dict:
     L.ref_mlsd_paths(text, _d(rays), rays.shape[0], sizes.ctypes.data_as(C.POINTER(C.c_uint64)), _u32(kept), _d(info),
                      off.ctypes.data_as(C.POINTER(C.c_uint64)), _u32(idx), _d(ln), _d(tl))
     return {"kept": kept, "info": info, "off": off, "idx": idx, "len": ln, "tail": tl}
+
+
+_file_lib = None
+
+
+def file_lib() -> C.CDLL:
+    global _file_lib
+    if _file_lib is None:
+        build()
+        L = C.CDLL(str(FILE_LIB))
+        D, U32 = C.POINTER(C.c_double), C.POINTER(C.c_uint32)
+        L.ref_read_muon_data.restype = C.c_uint64
+        L.ref_read_muon_data.argtypes = [C.c_char_p, D, C.c_int, C.c_int, C.c_int, D, C.c_uint64]
+        L.ref_save_image.argtypes = [C.c_char_p, D, U32, D, C.c_char_p, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.ref_load_image.argtypes = [C.c_char_p, D, C.c_uint64, U32, D, C.c_char_p, U32, U32, U32]
+        _file_lib = L
+    return _file_lib
+
+
+def read_muon_data(path, z_layers, n_middle: int, precision: int) -> np.ndarray:
+    """MutoFile::getMuonData on one file: (n, 14) tracks as the reference fits them."""
+    z = np.ascontiguousarray(z_layers, np.float64)
+    L = file_lib()
+    n = L.ref_read_muon_data(str(path).encode(), _d(z), z.size, n_middle, precision, None, 0)
+    out = np.zeros((n, 14), np.float64)
+    L.ref_read_muon_data(str(path).encode(), _d(z), z.size, n_middle, precision, _d(out), n)
+    return out
+
+
+def save_image(path, img: np.ndarray, grid, method: str, n_ray: int, n_iter: int, precision: int) -> None:
+    """MutoFile::saveImage; img is (nx, ny, nz) or flat in column-major order."""
+    n, f = _grid(grid)
+    x = np.ascontiguousarray(np.asarray(img, np.float64).reshape(-1, order="F"))
+    rc = file_lib().ref_save_image(str(path).encode(), _d(x), _u32(n), _d(f), method.encode(), n_ray, n_iter,
+                                   precision)
+    if rc != 0:
+        raise RuntimeError(f"reference saveImage failed for {path}")
+
+
+def load_image(path, cap: int) -> tuple[np.ndarray, dict]:
+    """MutoFile::loadImage: (flat column-major image, header fields)."""
+    img = np.zeros(cap, np.float64)
+    n = np.zeros(3, np.uint32)
+    f = np.zeros(6, np.float64)
+    m = C.create_string_buffer(16)
+    nr, ni, pr = (np.zeros(1, np.uint32) for _ in range(3))
+    rc = file_lib().ref_load_image(str(path).encode(), _d(img), cap, _u32(n), _d(f), m, _u32(nr), _u32(ni), _u32(pr))
+    if rc != 0:
+        raise RuntimeError(f"reference loadImage failed for {path}")
+    v = int(n[0]) * int(n[1]) * int(n[2])
+    hdr = {"n": [int(k) for k in n], "f": [float(k) for k in f], "method": m.raw.split(b"\0", 1)[0].decode(),
+           "n_ray": int(nr[0]), "n_iter": int(ni[0]), "precision": int(pr[0])}
+    return img[:v], hdr

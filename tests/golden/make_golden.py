@@ -2,8 +2,8 @@
 
 The reference's reconstruction sources (src/MutoSiddon.cpp, src/MutoPoCA.cpp,
 src/MutoMLSD.cpp, src/MutoMAP.cpp, src/MutoPoCut.cpp, src/MutoSLR.cpp,
-src/MutoSLRIter.cpp) are compiled in place by
-oracle/build_ref.sh and called through oracle/reference.py; the inputs
+src/MutoSLRIter.cpp) and its file code (src/MutoFile.cpp) are compiled in
+place by oracle/build_ref.sh and called through oracle/reference.py; the inputs
 (segments, synthetic tracks) are stored next to the outputs so the tests need
 neither the reference nor the generator.  Run where the reference tree is
 mounted:  python tests/golden/make_golden.py
@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import json
 import sys
+import tempfile
 from pathlib import Path
 
 import numpy as np
@@ -109,6 +110,41 @@ def track_case():
     return out, cases
 
 
+Z_LAYERS = [1500.0, 1000.0, 500.0, -500.0, -1000.0, -1500.0]  # input/example_mlsd.json:3-4
+
+
+def file_case(tmp: Path):
+    """MutoFile: the raw-hit reader on smeared records (float64 and float32
+    files, one NaN record) and the image files it writes (both precisions)."""
+    g = M.Grid(10, 10, 10, -500.0, -500.0, -500.0, 100.0, 100.0, 100.0)
+    n = 400
+    rays = M.generate(g, np.full(g.nvox, 1e-7), n, seed=21)
+    rng = np.random.default_rng(21)
+    rec = np.empty((n, 2 * len(Z_LAYERS) + 2))
+    rec[:, 0], rec[:, -1] = rays[:, 0], rays[:, 1]
+    for k, zk in enumerate(Z_LAYERS):
+        p, d = (rays[:, 2:5], rays[:, 8:11]) if k < 3 else (rays[:, 5:8], rays[:, 11:14])
+        t = (zk - p[:, 2]) / d[:, 2]
+        rec[:, 1 + 2 * k] = p[:, 0] + t * d[:, 0] + rng.standard_normal(n)
+        rec[:, 2 + 2 * k] = p[:, 1] + t * d[:, 1] + rng.standard_normal(n)
+    rec[[7, 301], [4, 13]] = np.nan
+    out = {"z_layers": np.asarray(Z_LAYERS), "n_middle": np.int64(3), "records64": rec,
+           "records32": rec.astype(np.float32)}
+    for prec, key in ((8, "records64"), (4, "records32")):
+        f = tmp / f"hits{prec}.bin"
+        out[key].tofile(f)
+        out[f"tracks{prec}"] = R.read_muon_data(f, Z_LAYERS, 3, prec)
+    ig = M.Grid(7, 5, 3, -350.5, -250.25, -150.125, 100.0, 80.0, 60.0)
+    img = rng.random((7, 5, 3)) * 1e-6
+    out["image"] = img
+    out["image_grid"] = np.array([7, 5, 3, -350.5, -250.25, -150.125, 100.0, 80.0, 60.0])
+    for prec in (8, 4):
+        f = tmp / f"image{prec}.bin"
+        R.save_image(f, img, ig, "mlsd", 123456, 50, prec)
+        out[f"image_file{prec}"] = np.frombuffer(f.read_bytes(), np.uint8)
+    return out
+
+
 def main() -> None:
     if not R.available():
         raise SystemExit("reference sources are not mounted here")
@@ -117,6 +153,8 @@ def main() -> None:
     tracks, cases = track_case()
     np.savez_compressed(HERE / "tracks.npz", **tracks)
     (HERE / "configs.json").write_text(json.dumps(cases, indent=1, sort_keys=True))
+    with tempfile.TemporaryDirectory() as tmp:
+        np.savez_compressed(HERE / "files.npz", **file_case(Path(tmp)))
     print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
 
 

@@ -5,6 +5,7 @@ import ctypes as C
 import json
 import re
 import subprocess
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -151,3 +152,49 @@ def test_fit_tracks_rejects_bad_layouts(facade):
     assert lib.muto_fit_tracks(p, 8, 2, _lib.dptr(zz), 65, 3, out, C.byref(n)) == 1     # > 64 layers
     assert lib.muto_fit_tracks(p, 8, 2, _lib.dptr(zz), 6, 3, None, C.byref(n)) == 1     # no output
     assert lib.muto_fit_tracks(p, 8, 2, _lib.dptr(zz), 6, 3, out, None) == 1            # no count
+
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.mark.parametrize("precision", [8, 4])
+def test_reader_matches_reference_reader(facade, tmp_path, precision):
+    # the reference's own MutoFile::getMuonData on the same records (tests/golden/files.npz)
+    F = np.load(GOLD / "files.npz")
+    rec = F["records64"] if precision == 8 else F["records32"]
+    f = tmp_path / "hits.bin"
+    rec.tofile(f)
+    got = read(facade, [f], z=list(F["z_layers"]), n_middle=int(F["n_middle"]), precision=precision)
+    ref = F[f"tracks{precision}"]
+    assert (ref[:, 10] < 0).any() and (ref[:, 13] < 0).any()  # the reference's fits point down at times
+    want = ref.copy()
+    for c in (8, 11):
+        want[:, c:c + 3] *= np.where(want[:, c + 2:c + 3] < 0, -1.0, 1.0)
+    assert got.shape == want.shape == (398, 14)
+    np.testing.assert_array_equal(got[:, :2], want[:, :2])
+    np.testing.assert_allclose(got[:, 2:8], want[:, 2:8], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(got[:, 8:], want[:, 8:], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("precision", [8, 4])
+def test_image_files_match_reference_files(tmp_path, precision):
+    # MutoFile::saveImage / loadImage (src/MutoFile.cpp:85-211) against files the reference wrote
+    F = np.load(GOLD / "files.npz")
+    a = F["image_grid"]
+    g = M.Grid(int(a[0]), int(a[1]), int(a[2]), *map(float, a[3:]))
+    ref = F[f"image_file{precision}"].tobytes()
+    p = tmp_path / "ours.bin"
+    M.save_image(str(p), F["image"], g, "mlsd", 123456, 50, precision)
+    ours = p.read_bytes()
+    assert len(ours) == len(ref) == 64 + precision * g.nvox
+    # bytes 2-17 hold the method copied from a std::string: past its NUL the
+    # reference writes whatever the string's buffer holds, the library zeros
+    assert ours[:7] == ref[:7] and ours[18:] == ref[18:]
+    assert ours[7:18] == bytes(11)
+    q = tmp_path / "ref.bin"
+    q.write_bytes(ref)
+    img, hdr = M.load_image(str(q))
+    want = F["image"] if precision == 8 else F["image"].astype(np.float32).astype(np.float64)
+    assert np.array_equal(img, want)
+    assert (hdr["method"], hdr["n_ray"], hdr["n_iter"], hdr["precision"]) == ("mlsd", 123456, 50, precision)
+    assert hdr["grid"] == g

@@ -103,6 +103,45 @@ def test_reference_build_still_matches_oracle_when_mounted(oracle):
     assert np.array_equal(a[2], S["count"]) and np.array_equal(bits(a[1]), bits(S["len"]))
 
 
+F = dict(np.load(GOLD / "files.npz"))
+
+
+def oriented(tracks):
+    """Directions flipped to d_z > 0: the reference's SVD leaves their sign
+    open (src/MutoFile.cpp:273,298); the points do not depend on it."""
+    t = np.array(tracks, np.float64, copy=True)
+    for c in (8, 11):
+        t[:, c:c + 3] *= np.where(t[:, c + 2:c + 3] < 0, -1.0, 1.0)
+    return t
+
+
+@pytest.mark.parametrize("prec", [8, 4])
+def test_oracle_line_fit_matches_golden(oracle, prec):
+    rec = F["records64"] if prec == 8 else F["records32"]
+    got = oracle.fit_records(rec, F["z_layers"], int(F["n_middle"]))
+    want = oriented(F[f"tracks{prec}"])
+    assert got.shape == want.shape == (398, 14)
+    np.testing.assert_array_equal(got[:, :2], want[:, :2])
+    np.testing.assert_allclose(got[:, 2:8], want[:, 2:8], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(got[:, 8:], want[:, 8:], rtol=0, atol=1e-12)
+
+
+def test_reference_file_code_still_matches_golden_when_mounted(tmp_path):
+    from oracle import reference as R
+
+    if not R.available():
+        pytest.skip("reference sources not mounted")
+    f = tmp_path / "hits.bin"
+    F["records64"].tofile(f)
+    got = R.read_muon_data(f, F["z_layers"], int(F["n_middle"]), 8)
+    assert np.array_equal(bits(got), bits(F["tracks8"]))
+    a = F["image_grid"]
+    R.save_image(tmp_path / "img.bin", F["image"], grid_of(a), "mlsd", 123456, 50, 8)
+    ref = F["image_file8"].tobytes()
+    ours = (tmp_path / "img.bin").read_bytes()
+    assert ours[:7] == ref[:7] and ours[18:] == ref[18:]
+
+
 # ------------------------------------------------------------------ GPU path
 @pytest.mark.gpu
 def test_gpu_siddon_matches_golden(gpu):
