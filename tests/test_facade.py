@@ -165,11 +165,7 @@ def test_reader_matches_reference_reader(facade, tmp_path, precision):
     f = tmp_path / "hits.bin"
     rec.tofile(f)
     got = read(facade, [f], z=list(F["z_layers"]), n_middle=int(F["n_middle"]), precision=precision)
-    ref = F[f"tracks{precision}"]
-    assert (ref[:, 10] < 0).any() and (ref[:, 13] < 0).any()  # the reference's fits point down at times
-    want = ref.copy()
-    for c in (8, 11):
-        want[:, c:c + 3] *= np.where(want[:, c + 2:c + 3] < 0, -1.0, 1.0)
+    want = F[f"tracks{precision}"]
     assert got.shape == want.shape == (398, 14)
     np.testing.assert_array_equal(got[:, :2], want[:, :2])
     np.testing.assert_allclose(got[:, 2:8], want[:, 2:8], rtol=0, atol=1e-9)
