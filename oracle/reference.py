@@ -20,6 +20,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_ref" / "libmuto_ref.so"
 FILE_LIB = HERE / "_ref" / "libmuto_ref_file.so"
+CLI = HERE / "_ref" / "muto_ref_cli"
 REF = Path(os.environ.get("MUTO_REFERENCE", "/root/reference"))
 
 
@@ -32,7 +33,8 @@ def build() -> Path:
                                       "MutoPoCut.cpp", "MutoSLR.cpp", "MutoSLRIter.cpp", "MutoFile.cpp")]
     deps = srcs + [HERE / "ref_harness.cpp", HERE / "ref_file_harness.cpp", HERE / "build_ref.sh"] \
         + list((HERE / "ref_shim").rglob("*"))
-    stale = [lib for lib in (LIB, FILE_LIB) if not lib.exists()
+    deps.append(REF / "MuToTest.cpp")
+    stale = [lib for lib in (LIB, FILE_LIB, CLI) if not lib.exists()
              or any(p.is_file() and p.stat().st_mtime > lib.stat().st_mtime for p in deps)]
     if stale:
         subprocess.run(["sh", str(HERE / "build_ref.sh")], check=True, capture_output=True)
@@ -171,3 +173,12 @@ def load_image(path, cap: int) -> tuple[np.ndarray, dict]:
     hdr = {"n": [int(k) for k in n], "f": [float(k) for k in f], "method": m.raw.split(b"\0", 1)[0].decode(),
            "n_ray": int(nr[0]), "n_iter": int(ni[0]), "precision": int(pr[0])}
     return img[:v], hdr
+
+
+def run_cli(config_path) -> str:
+    """The reference's command-line program (MuToTest.cpp) on a JSON config; returns its stdout."""
+    build()
+    r = subprocess.run([str(CLI), str(config_path)], capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference CLI failed: {r.stdout[-500:]} {r.stderr[-500:]}")
+    return r.stdout

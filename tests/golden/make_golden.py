@@ -2,8 +2,9 @@
 
 The reference's reconstruction sources (src/MutoSiddon.cpp, src/MutoPoCA.cpp,
 src/MutoMLSD.cpp, src/MutoMAP.cpp, src/MutoPoCut.cpp, src/MutoSLR.cpp,
-src/MutoSLRIter.cpp) and its file code (src/MutoFile.cpp) are compiled in
-place by oracle/build_ref.sh and called through oracle/reference.py; the inputs
+src/MutoSLRIter.cpp), its file code (src/MutoFile.cpp) and its command-line
+program (MuToTest.cpp) are compiled in place by oracle/build_ref.sh and
+called through oracle/reference.py; the inputs
 (segments, synthetic tracks) are stored next to the outputs so the tests need
 neither the reference nor the generator.  Run where the reference tree is
 mounted:  python tests/golden/make_golden.py
@@ -113,6 +114,16 @@ def track_case():
 Z_LAYERS = [1500.0, 1000.0, 500.0, -500.0, -1000.0, -1500.0]  # input/example_mlsd.json:3-4
 
 
+def image_bytes(path: Path) -> np.ndarray:
+    """An image file the reference wrote, with the method field's bytes past
+    its NUL zeroed: the reference copies 16 bytes out of a short std::string
+    (src/MutoFile.cpp:99), so those bytes are whatever its buffer held."""
+    b = bytearray(path.read_bytes())
+    end = b.index(0, 2, 18) if 0 in b[2:18] else 18
+    b[end:18] = bytes(18 - end)
+    return np.frombuffer(bytes(b), np.uint8)
+
+
 def file_case(tmp: Path):
     """MutoFile: the raw-hit reader on smeared records (float64 and float32
     files, one NaN record) and the image files it writes (both precisions)."""
@@ -141,7 +152,57 @@ def file_case(tmp: Path):
     for prec in (8, 4):
         f = tmp / f"image{prec}.bin"
         R.save_image(f, img, ig, "mlsd", 123456, 50, prec)
-        out[f"image_file{prec}"] = np.frombuffer(f.read_bytes(), np.uint8)
+        out[f"image_file{prec}"] = image_bytes(f)
+    return out
+
+
+CLI_METHODS = ("poca", "pocut", "slr", "slr_iter", "mlsd", "map")
+
+
+def cli_case(tmp: Path):
+    """The reference's command-line program (MuToTest.cpp) end to end on the
+    1 m cube of 50 mm voxels: a float32 hit file, one config per method, PoCA
+    written first and read back as the initial image of MLSD and MAP (as the
+    example JSON files chain them).  Configs hold "{dir}" for the folder."""
+    wl = W.cube20_50mm(n_muons=10_000, seed=31)
+    rays = wl.tracks()
+    rng = np.random.default_rng(31)
+    rec = np.empty((rays.shape[0], 2 * len(Z_LAYERS) + 2))
+    rec[:, 0], rec[:, -1] = rays[:, 0], rays[:, 1]
+    for k, zk in enumerate(Z_LAYERS):
+        p, d = (rays[:, 2:5], rays[:, 8:11]) if k < 3 else (rays[:, 5:8], rays[:, 11:14])
+        t = (zk - p[:, 2]) / d[:, 2]
+        rec[:, 1 + 2 * k] = p[:, 0] + t * d[:, 0] + 0.5 * rng.standard_normal(rays.shape[0])
+        rec[:, 2 + 2 * k] = p[:, 1] + t * d[:, 1] + 0.5 * rng.standard_normal(rays.shape[0])
+    rec = rec.astype(np.float32)
+    (tmp / "hits.bin").write_bytes(rec.tobytes())
+    g = wl.grid
+    grid = {"nx": g.nx, "ny": g.ny, "nz": g.nz, "x_min": g.x_min, "y_min": g.y_min, "z_min": g.z_min,
+            "dx": g.dx, "dy": g.dy, "dz": g.dz}
+    common = {"grid": grid, "has_energy": False, "total_num_rays": 0, "eps": 1.0e-8, "log_results": False}
+    em = dict(common, straight_line=False, update_with_mean=False, mean_percentile=98, early_stop=False,
+              initial_image_file="{dir}/poca.bin", initialize_method=0, initialize_value=1.0e-7,
+              error_xy=1.0, error_dz_outer=1000.0, error_dz_inner=1000.0)
+    sections = {
+        "poca": dict(common, straight_line=False, length_weighted=False),
+        "pocut": dict(common, length_weighted=False, cut_percentile=0.9),
+        "slr": dict(common, length_weighted=True),
+        "slr_iter": dict(common, length_weighted=False, num_iteration=2),
+        "mlsd": dict(em, num_iteration=5),
+        "map": dict(em, num_iteration=3, beta=0.01, p=1.0, delta=0.1, all_neighbours=True, add_object_prior=False),
+    }
+    out = {"records": rec, "z_layers": np.asarray(Z_LAYERS), "n_middle": np.int64(3),
+           "tracks": R.read_muon_data(tmp / "hits.bin", Z_LAYERS, 3, 4)}
+    configs = {}
+    for m in CLI_METHODS:
+        cfg = {"data_files": ["{dir}/hits.bin"], "detector_height": Z_LAYERS, "detector_middle": 3,
+               "output_file": "{dir}/" + m + ".bin", m: sections[m]}
+        configs[m] = cfg
+        text = json.dumps(cfg).replace("{dir}", str(tmp))
+        (tmp / f"{m}.json").write_text(text)
+        R.run_cli(tmp / f"{m}.json")
+        out[f"out_{m}"] = image_bytes(tmp / f"{m}.bin")
+    out["configs"] = np.frombuffer(json.dumps(configs, sort_keys=True).encode(), np.uint8)
     return out
 
 
@@ -155,6 +216,8 @@ def main() -> None:
     (HERE / "configs.json").write_text(json.dumps(cases, indent=1, sort_keys=True))
     with tempfile.TemporaryDirectory() as tmp:
         np.savez_compressed(HERE / "files.npz", **file_case(Path(tmp)))
+    with tempfile.TemporaryDirectory() as tmp:
+        np.savez_compressed(HERE / "cli.npz", **cli_case(Path(tmp)))
     print("wrote", sorted(p.name for p in HERE.glob("*.npz")))
 
 

@@ -133,6 +133,50 @@ def test_reference_file_code_still_matches_golden_when_mounted(tmp_path):
     assert ours[:7] == ref[:7] and ours[18:] == ref[18:]
 
 
+CLI = dict(np.load(GOLD / "cli.npz"))
+CLI_CFG = json.loads(CLI["configs"].tobytes())
+CLI_N_ITER = {"poca": 1, "pocut": 1, "slr": 1, "slr_iter": 1, "mlsd": 5, "map": 3}
+
+
+def image_file(b: bytes):
+    """Header fields and body of a MutoFile image (src/MutoFile.cpp:85-133)."""
+    u16 = lambda o: int.from_bytes(b[o:o + 2], "little")  # noqa: E731
+    hdr = {"length": b[0], "version": b[1], "method": b[2:18].split(b"\0", 1)[0].decode(),
+           "n_ray": int.from_bytes(b[18:22], "little"), "n_iter": u16(22), "precision": u16(24),
+           "n": (u16(26), u16(28), u16(30)), "f": tuple(np.frombuffer(b[32:56], np.float32)), "pad": b[56:64]}
+    return hdr, np.frombuffer(b[64:], np.float32 if hdr["precision"] == 4 else np.float64)
+
+
+@pytest.mark.parametrize("method", list(CLI_N_ITER))
+def test_oracle_reproduces_reference_cli(oracle, method):
+    # MuToTest.cpp end to end (reader, reconstruction, image file; MLSD and MAP
+    # start from the PoCA file): the oracle on the reference's fitted tracks
+    sec = CLI_CFG[method][method]
+    g = M.Grid(**sec["grid"])
+    rays = CLI["tracks"]
+    hdr, body = image_file(CLI[f"out_{method}"].tobytes())
+    assert (hdr["length"], hdr["version"], hdr["method"], hdr["n_ray"], hdr["precision"]) == (64, 1, method, 10000, 4)
+    assert hdr["n_iter"] == CLI_N_ITER[method] and hdr["n"] == (g.nx, g.ny, g.nz) and hdr["pad"] == bytes(8)
+    assert hdr["f"] == tuple(np.float32([g.x_min, g.y_min, g.z_min, g.dx, g.dy, g.dz]))
+    if method in ("poca", "pocut"):
+        img = getattr(oracle, method)(g, sec, rays)[0]
+    elif method in ("slr", "slr_iter"):
+        img = oracle.slr(g, sec, rays, iterative=method == "slr_iter")
+    else:
+        init = image_file(CLI["out_poca"].tobytes())[1].astype(np.float64)
+        o = oracle.Mlsd(g, sec, rays, init, method=method)
+        o.iterate(sec["num_iteration"])
+        img = o.image()
+    assert (body > 0).sum() > 400
+    assert np.array_equal(img.astype(np.float32), body)
+
+
+def test_oracle_line_fit_matches_reference_cli_tracks(oracle):
+    got = oracle.fit_records(CLI["records"], CLI["z_layers"], int(CLI["n_middle"]))
+    np.testing.assert_allclose(got[:, 2:8], CLI["tracks"][:, 2:8], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(got[:, 8:], CLI["tracks"][:, 8:], rtol=0, atol=1e-12)
+
+
 # ------------------------------------------------------------------ GPU path
 @pytest.mark.gpu
 def test_gpu_siddon_matches_golden(gpu):
