@@ -1,6 +1,7 @@
 // MutoFile: raw-hit reader and image files.  See MutoFile.h.
 #include "MutoFile.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -27,6 +28,46 @@ muto_grid to_c(const VoxelGrid& g) {
     return c;
 }
 
+// Reads each file's whole records, a chunk of at most 2^20 at a time, and
+// hands them to f(raw bytes, number of records); a file that cannot be
+// opened is reported and skipped (src/MutoFile.cpp:42-48).  Sizes are 64-bit.
+template <class F>
+void read_records(const std::vector<std::string>& flist, size_t rec_bytes, F&& f) {
+    const uint64_t chunk = uint64_t(1) << 20;
+    std::vector<char> raw;
+    for (const std::string& name : flist) {
+        std::ifstream file(name.c_str(), std::ios::in | std::ios::binary);
+        if (file.fail()) {
+            std::cout << "Reading muon data error for : " << name << std::endl;
+            continue;
+        }
+        file.seekg(0, std::ios::end);
+        const uint64_t filesize = static_cast<uint64_t>(file.tellg());
+        file.seekg(0, std::ios::beg);
+        const uint64_t nRay = filesize / rec_bytes;
+        for (uint64_t r0 = 0; r0 < nRay; r0 += chunk) {
+            const uint64_t m = std::min(chunk, nRay - r0);
+            raw.resize(static_cast<size_t>(m * rec_bytes));
+            file.read(raw.data(), static_cast<std::streamsize>(raw.size()));
+            const uint64_t got = static_cast<uint64_t>(file.gcount()) / rec_bytes;  // whole records read
+            if (got) f(raw.data(), got);
+            if (got < m) break;
+        }
+    }
+}
+
+void to_doubles(const char* raw, size_t n, int precision, double* out) {
+    for (size_t k = 0; k < n; ++k) {
+        if (precision == 4) {
+            float v;
+            std::memcpy(&v, raw + 4 * k, 4);
+            out[k] = v;
+        } else {
+            std::memcpy(&out[k], raw + 8 * k, 8);
+        }
+    }
+}
+
 }  // namespace
 
 void MutoFile::fitLine(const double* x, const double* y, const double* z, int n, double* c, double* d) {
@@ -50,39 +91,29 @@ MutoMuonData MutoFile::getMuonData(std::vector<std::string> flist, std::vector<M
         return data;
     }
     const size_t nEach = 2 * static_cast<size_t>(nz) + 2;  // two extra values for in and out energy
-    std::vector<double> rec(nEach);
-    for (const std::string& name : flist) {
-        std::ifstream file(name.c_str(), std::ios::in | std::ios::binary);
-        if (file.fail()) {
-            std::cout << "Reading muon data error for : " << name << std::endl;
-            continue;
+    std::vector<muto_ray> fitted;
+    std::vector<unsigned char> keep;
+    read_records(flist, nEach * static_cast<size_t>(fPrecision), [&](const char* raw, uint64_t n) {
+        // records are independent: each thread fits its own share, the kept
+        // tracks are then appended in record order
+        fitted.resize(n);
+        keep.resize(n);
+#pragma omp parallel for schedule(static)
+        for (long long i = 0; i < static_cast<long long>(n); ++i) {
+            double rec[2 * muto::fit::kMaxLayers + 2];
+            to_doubles(raw + static_cast<size_t>(i) * nEach * static_cast<size_t>(fPrecision), nEach, fPrecision,
+                       rec);
+            keep[i] = muto::fit::fit_record(rec, zlayers.data(), nz, nMiddle, &fitted[i]) ? 1 : 0;  // 0: a NaN
         }
-        file.seekg(0, std::ios::end);
-        const uint64_t filesize = static_cast<uint64_t>(file.tellg());  // 64-bit: files above 4 GB are fine
-        file.seekg(0, std::ios::beg);
-        const uint64_t nRay = filesize / nEach / static_cast<uint64_t>(fPrecision);
-        std::vector<char> raw(nEach * static_cast<size_t>(fPrecision));
-        data.reserve(data.size() + nRay);
-        for (uint64_t r = 0; r < nRay; ++r) {
-            file.read(raw.data(), static_cast<std::streamsize>(raw.size()));
-            if (!file) break;
-            for (size_t k = 0; k < nEach; ++k) {
-                if (fPrecision == 4) {
-                    float f;
-                    std::memcpy(&f, raw.data() + 4 * k, 4);
-                    rec[k] = f;
-                } else {
-                    std::memcpy(&rec[k], raw.data() + 8 * k, 8);
-                }
-            }
-            muto_ray c;
-            if (!muto::fit::fit_record(rec.data(), zlayers.data(), nz, nMiddle, &c)) continue;  // a NaN
+        static_assert(sizeof(RayData) == sizeof(muto_ray), "RayData mirrors muto_ray");
+        if (data.capacity() < data.size() + n) data.reserve(std::max<size_t>(2 * data.capacity(), data.size() + n));
+        for (uint64_t i = 0; i < n; ++i) {
+            if (!keep[i]) continue;
             RayData ray;
-            static_assert(sizeof(RayData) == sizeof(muto_ray), "RayData mirrors muto_ray");
-            std::memcpy(&ray, &c, sizeof(c));
+            std::memcpy(&ray, &fitted[i], sizeof(muto_ray));
             data.push_back(ray);
         }
-    }
+    });
     return data;
 }
 
@@ -188,12 +219,26 @@ extern "C" int muto_read_muon_data(const char* const* files, int n_files, const 
     if (n_middle < 2 || nz - n_middle < 2 || nz > muto::fit::kMaxLayers) return MUTO_ERR_ARG;
     std::vector<std::string> fl;
     for (int i = 0; i < n_files; ++i) fl.push_back(files[i] ? files[i] : "");
-    const std::vector<MTfloat> z(z_layers, z_layers + nz);
-    const MutoMuonData d = MutoFile::getMuonData(fl, z, n_middle, precision);
-    if (!out) {
-        *n_out = d.size();
+    if (!out) {  // count the records without a NaN, fitting nothing
+        const size_t each = 2 * static_cast<size_t>(nz) + 2;
+        uint64_t kept = 0;
+        read_records(fl, each * static_cast<size_t>(precision), [&](const char* raw, uint64_t n) {
+            uint64_t k = 0;
+#pragma omp parallel for schedule(static) reduction(+ : k)
+            for (long long i = 0; i < static_cast<long long>(n); ++i) {
+                double rec[2 * muto::fit::kMaxLayers + 2];
+                to_doubles(raw + static_cast<size_t>(i) * each * static_cast<size_t>(precision), each, precision, rec);
+                bool nan = false;
+                for (size_t j = 0; j < each; ++j) nan = nan || rec[j] != rec[j];
+                k += nan ? 0 : 1;
+            }
+            kept += k;
+        });
+        *n_out = kept;
         return MUTO_OK;
     }
+    const std::vector<MTfloat> z(z_layers, z_layers + nz);
+    const MutoMuonData d = MutoFile::getMuonData(fl, z, n_middle, precision);
     const uint64_t n = d.size() < cap ? d.size() : cap;
     if (n) std::memcpy(out, d.data(), n * sizeof(muto_ray));
     *n_out = n;
