@@ -157,3 +157,22 @@ def test_median_update_even_and_odd(oracle):
     c = ref.counts()
     assert np.all(np.isfinite(img)) and img.max() > 0
     assert c["iterations_done"] == 3 and c["n_singular"] == 0
+
+
+@pytest.mark.parametrize("lw", [False, True])
+@pytest.mark.parametrize("iters", [1, 3])
+def test_slr_iter_level_schedule_is_exact(oracle, lw, iters):
+    # SLRIter's passes are order-dependent (src/MutoSLRIter.cpp:45-67); run
+    # level by level (muons of a level share no voxel, every voxel sees its
+    # muons in index order, the latest index first inside a level) they give
+    # the same image bit for bit: the schedule a parallel form can use
+    g = M.Grid(12, 12, 12, -300.0, -300.0, -300.0, 50.0, 50.0, 50.0)
+    rays = M.generate(g, np.full(g.nvox, 2e-6), 3000, seed=12)
+    cfg = {"length_weighted": lw, "has_energy": True, "num_iteration": iters}
+    want = oracle.slr(g, cfg, rays, iterative=True)
+    got = oracle.slr_by_level(g, cfg, rays, iterative=True)
+    assert np.count_nonzero(want) > 1000
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+    # a schedule that breaks a voxel's order does change the result
+    perm = np.random.default_rng(0).permutation(rays.shape[0])
+    assert not np.array_equal(oracle.slr(g, cfg, rays[perm], iterative=True).view(np.uint64), want.view(np.uint64))
