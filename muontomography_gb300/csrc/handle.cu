@@ -2,6 +2,7 @@
 // configuration, device memory, the setup pipeline and the EM / MAP
 // iteration, captured once into a CUDA graph and replayed.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <atomic>
@@ -443,12 +444,27 @@ void run(muto_handle* h, const char* name, F&& f) {
 
 // wall time of a host-side set-up phase (including the device waits inside
 // it), kept with the kernel statistics under "host:<phase>" when profiling
+// An NVTX range over one entry point's call.
+struct NvtxRange {
+    nvtxRangeId_t id;
+    explicit NvtxRange(const char* n) : id(nvtxRangeStartA(n)) {}
+    ~NvtxRange() { nvtxRangeEnd(id); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
+// A host phase of the set-up: timed for the profiler and marked as an NVTX
+// range (start/end, not push/pop: phases are replaced while the next one
+// starts), which a profiler attached to the process shows on the timeline.
 struct HostPhase {
     muto_handle* h;
     const char* name;
     std::chrono::steady_clock::time_point t0;
-    HostPhase(muto_handle* hh, const char* n) : h(hh), name(n), t0(std::chrono::steady_clock::now()) {}
+    nvtxRangeId_t range;
+    HostPhase(muto_handle* hh, const char* n)
+        : h(hh), name(n), t0(std::chrono::steady_clock::now()), range(nvtxRangeStartA(n)) {}
     ~HostPhase() {
+        nvtxRangeEnd(range);
         if (!h->prof.on) return;
         const double ms =
             std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -1566,6 +1582,7 @@ int muto_load_tracks(muto_handle* h, const muto_ray* rays, uint64_t n, int on_de
 
 int muto_prepare(muto_handle* h) {
     if (!h) return MUTO_ERR_ARG;
+    NvtxRange nv("muto_prepare");
     return guarded(h, [&] {
         if (h->rays.empty()) throw Error(MUTO_ERR_STATE, "load tracks first");
         for (const auto& r : h->batch_rays)
@@ -1592,6 +1609,7 @@ int muto_prepare(muto_handle* h) {
 
 int muto_iterate(muto_handle* h, int n_iter) {
     if (!h) return MUTO_ERR_ARG;
+    NvtxRange nv("muto_iterate");
     return guarded(h, [&] {
         n_prepared_check(h);
         if (h->method == kPoca) return;  // PoCA has no iterations
