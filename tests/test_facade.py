@@ -194,3 +194,22 @@ def test_image_files_match_reference_files(tmp_path, precision):
     assert np.array_equal(img, want)
     assert (hdr["method"], hdr["n_ray"], hdr["n_iter"], hdr["precision"]) == ("mlsd", 123456, 50, precision)
     assert hdr["grid"] == g
+
+
+@pytest.mark.parametrize("precision", [8, 4])
+def test_reader_drops_a_truncated_last_record(facade, tmp_path, precision):
+    # a file cut inside its last record: the whole records are read, the rest
+    # ignored (nRay = filesize / nEach / precision, src/MutoFile.cpp:52-55)
+    F = np.load(GOLD / "files.npz")
+    rec = F["records64"] if precision == 8 else F["records32"]
+    f = tmp_path / "hits.bin"
+    f.write_bytes(rec.tobytes() + rec[:1].tobytes()[: 5 * precision + 3])
+    got = read(facade, [f], z=list(F["z_layers"]), n_middle=int(F["n_middle"]), precision=precision)
+    want = F[f"tracks{precision}"]
+    assert got.shape == want.shape
+    np.testing.assert_allclose(got[:, 2:], want[:, 2:], rtol=0, atol=1e-9)
+    # two files: the tracks of both, in file order; an empty file adds nothing
+    (tmp_path / "empty.bin").write_bytes(b"")
+    both = read(facade, [f, tmp_path / "empty.bin", f], z=list(F["z_layers"]), n_middle=int(F["n_middle"]),
+                precision=precision)
+    assert np.array_equal(both, np.concatenate([got, got]))
