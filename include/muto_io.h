@@ -9,8 +9,12 @@
  * give the incoming line and n_middle..nz-1 the outgoing one, each the
  * principal axis of its hits oriented with d_z > 0, with pin on layer
  * n_middle-1 and pout on layer n_middle.
- * Call with out == NULL to get the number of tracks in *n_out; otherwise at
- * most cap tracks are written and *n_out is the number written.
+ * Call with out == NULL to get the number of tracks in *n_out (the records
+ * without a NaN; nothing is fitted); otherwise at most cap tracks are
+ * written and *n_out is the number written.  Records are read 2^20 at a time
+ * and fitted in parallel (OpenMP threads of the calling process); the result
+ * does not depend on the thread count.  Files are opened by name (a file
+ * that cannot be opened is reported and skipped, as the reference does).
  */
 #ifndef MUTO_IO_H
 #define MUTO_IO_H
