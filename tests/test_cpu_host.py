@@ -144,3 +144,12 @@ def test_reference_arm_other_ranks_exit_without_work():
     env = {"RANK": "1", "LOCAL_RANK": "1", "WORLD_SIZE": "2", "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": "29533"}
     assert _bench("--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-sample", "3000",
                   env=env) == []
+
+
+@pytest.mark.parametrize("argv,method,mode", [
+    (("--workload", "map128x128x64_15mm"), "map", "median"),
+    (("--mode", "mean"), "mlsd", "mean"),
+])
+def test_reference_arm_other_workloads(argv, method, mode):
+    (line,) = _bench("--impl", "reference", "--steps", "1", "--warmup", "0", "--cpu-sample", "2000", *argv)
+    assert line["config"]["method"] == method and line["config"]["mode"] == mode and line["value"] > 0
