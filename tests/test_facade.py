@@ -213,3 +213,21 @@ def test_reader_drops_a_truncated_last_record(facade, tmp_path, precision):
     both = read(facade, [f, tmp_path / "empty.bin", f], z=list(F["z_layers"]), n_middle=int(F["n_middle"]),
                 precision=precision)
     assert np.array_equal(both, np.concatenate([got, got]))
+
+
+@pytest.mark.parametrize("cfg,message", [
+    (None, "Configuration file load error"),
+    ({"data_files": [], "detector_height": [1.0, 0.0, -1.0, -2.0], "detector_middle": 2, "output_file": "o.bin"},
+     "No supported reconstruction key"),
+    ({"detector_height": [1.0, 0.0, -1.0, -2.0]}, "Configuration error"),
+    ("{not json", "Configuration file load error"),
+])
+def test_cli_reports_configuration_errors(facade, tmp_path, cfg, message):
+    # the command-line program stops with status 1 before any device work
+    path = tmp_path / "cfg.json"
+    if cfg is not None:
+        path.write_text(cfg if isinstance(cfg, str) else json.dumps(cfg))
+    r = subprocess.run([str(B.cli_path()), str(path)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 1
+    assert message in r.stdout + r.stderr
+    assert not (tmp_path / "o.bin").exists()
