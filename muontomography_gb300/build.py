@@ -33,7 +33,7 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-fopenmp", "-Wa
 CUDA_UNITS = ["scan.cu", "setup.cu", "em_muon.cu", "em_voxel.cu", "poca.cu", "slr.cu", "adjoint.cu", "gen.cu",
               "fit.cu", "handle.cu", "noalloc.cu"]
 HOST_UNITS = ["host.cpp"]
-FACADE_UNITS = ["MutoFile.cpp", "MutoReconstruction.cpp"]
+FACADE_UNITS = ["MutoFile.cpp", "MutoReconstruction.cpp", "MutoSiddon.cpp"]
 
 
 def nvcc() -> str:

@@ -1,7 +1,10 @@
 // MutoFile: raw-hit reader and image files.  See MutoFile.h.
 #include "MutoFile.h"
 
+#include <unistd.h>
+
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -13,6 +16,12 @@
 #include "trackfit.h"
 
 namespace {
+
+std::string start_dir() {
+    char buf[PATH_MAX];
+    return getcwd(buf, sizeof(buf)) ? std::string(buf) : std::string();
+}
+const std::string g_start_dir = start_dir();
 
 muto_grid to_c(const VoxelGrid& g) {
     muto_grid c{};
@@ -69,6 +78,8 @@ void to_doubles(const char* raw, size_t n, int precision, double* out) {
 }
 
 }  // namespace
+
+std::string MutoFile::getCurrentPath() { return g_start_dir; }
 
 void MutoFile::fitLine(const double* x, const double* y, const double* z, int n, double* c, double* d) {
     muto::fit::fit_line(x, y, z, n, c, d);

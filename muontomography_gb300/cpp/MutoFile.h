@@ -5,6 +5,7 @@
 //   saveImagePure   the image alone (:136-157)
 //   loadImage       header + image (:160-211)
 //   loadImagePure   the image alone, grid given (:214-245)
+//   getCurrentPath  the start-up working directory (include/MutoFile.h:65)
 #pragma once
 
 #include <string>
@@ -28,6 +29,10 @@ public:
     // A file that cannot be read gives an empty image (size() == 0).
     static std::pair<Image, ImageHeader> loadImage(std::string filename);
     static Image loadImagePure(std::string filename, VoxelGrid grid, MTindex fPrecision = 4);
+
+    // The working directory when the library was loaded (the reference keeps
+    // it in a static member set at start-up, src/MutoFile.cpp:11-15).
+    static std::string getCurrentPath();
 
     // One line fit of getMuonData: centroid and unit direction (d_z >= 0) of
     // n points.

@@ -231,3 +231,37 @@ def test_cli_reports_configuration_errors(facade, tmp_path, cfg, message):
     assert r.returncode == 1
     assert message in r.stdout + r.stderr
     assert not (tmp_path / "o.bin").exists()
+
+
+USER_PROGRAM = r"""
+// a program written against the reference's headers (MuToTest.cpp style)
+#include <iostream>
+#include "MutoFile.h"
+#include "MutoReconstruction.h"
+#include "MutoSiddon.h"
+
+int main() {
+    VoxelGrid g{10, 10, 10, -50.0, -50.0, -50.0, 10.0, 10.0, 10.0};
+    MutoSiddon siddon(g);                      // include/MutoSiddon.h:14
+    std::vector<Vector3> none;
+    std::cout << siddon.getVoxelPaths(none, none).size() << "\n";  // no segments: no device work
+    std::cout << MutoFile::getCurrentPath() << "\n";                // include/MutoFile.h:65
+    MutoMuonData data = MutoFile::getMuonData({}, {1.0, 0.0, -1.0, -2.0}, 2);
+    std::cout << data.size() << "\n";
+    return 0;
+}
+"""
+
+
+def test_user_program_compiles_against_the_headers(facade, tmp_path):
+    src = tmp_path / "user.cpp"
+    src.write_text(USER_PROGRAM)
+    exe = tmp_path / "user"
+    lib = B.facade_lib_path().parent
+    root = lib.parent
+    subprocess.run(["g++", "-std=c++17", "-I", str(root.parent / "include"), "-I", str(root / "cpp"), "-I",
+                    str(root / "csrc"), str(src), "-o", str(exe), "-L", str(lib), "-lmuto_facade", "-lmuto_gb300",
+                    f"-Wl,-rpath,{lib}"], check=True, capture_output=True, timeout=120)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.split("\n")[:3] == ["0", str(tmp_path), "0"]
