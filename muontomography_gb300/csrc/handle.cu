@@ -442,8 +442,6 @@ void run(muto_handle* h, const char* name, F&& f) {
     CK(cudaGetLastError());
 }
 
-// wall time of a host-side set-up phase (including the device waits inside
-// it), kept with the kernel statistics under "host:<phase>" when profiling
 // An NVTX range over one entry point's call.
 struct NvtxRange {
     nvtxRangeId_t id;
@@ -453,9 +451,10 @@ struct NvtxRange {
     NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
-// A host phase of the set-up: timed for the profiler and marked as an NVTX
-// range (start/end, not push/pop: phases are replaced while the next one
-// starts), which a profiler attached to the process shows on the timeline.
+// Wall time of a host-side set-up phase (including the device waits inside
+// it), kept with the kernel statistics under "host:<phase>" when profiling,
+// and an NVTX range over it (start/end, not push/pop: a phase is replaced
+// while the next one starts) for a profiler attached to the process.
 struct HostPhase {
     muto_handle* h;
     const char* name;
