@@ -265,3 +265,10 @@ def test_user_program_compiles_against_the_headers(facade, tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
     assert r.returncode == 0, r.stderr
     assert r.stdout.split("\n")[:3] == ["0", str(tmp_path), "0"]
+
+
+def test_fit_tracks_host_checks():
+    # no records: nothing to fit, no device touched; a record of the wrong width is refused
+    assert M.fit_tracks(np.zeros((0, 14)), Z, N_MIDDLE).shape == (0, 14)
+    with pytest.raises(ValueError):
+        M.fit_tracks(np.zeros((3, 13)), Z, N_MIDDLE)
