@@ -14,6 +14,8 @@
 //   Poca::run            src/MutoPoCA.cpp:51-134
 //   PoCut::run           src/MutoPoCut.cpp:19-121
 //   slr_run              src/MutoSLR.cpp:47-103, src/MutoSLRIter.cpp:15-83
+//                        (by_level: the same passes in a level order, a
+//                        check of that schedule, not the reference's order)
 //   Mlsd::gather         src/MutoMLSD.cpp:268-326
 //   Mlsd::path_and_tail  src/MutoMLSD.cpp:382-415
 //   Mlsd::weights        src/MutoMLSD.cpp:417-430

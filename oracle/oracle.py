@@ -3,7 +3,8 @@
 TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and
 the CPU-baseline / reference leg of ``bench.py`` -- to check results, never as
 the product path.  ``build()`` compiles the oracle into ``oracle/_build`` with
-``g++ -O3 -fopenmp -ffp-contract=off``.
+``g++ -O3 -fopenmp -ffp-contract=off``.  ``fit_records`` (the raw-hit line
+fit, with numpy's SVD) is restated here in Python.
 """
 from __future__ import annotations
 
