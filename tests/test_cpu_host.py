@@ -131,7 +131,7 @@ def test_reference_arm_prints_one_contract_line():
     # the CPU reference arm on a small sample: one JSON line with the bench's keys
     (line,) = _bench("--impl", "reference", "--steps", "1", "--warmup", "0", "--cpu-sample", "3000")
     assert line["impl"] == "reference"
-    assert line["metric"] == "EM-iter muon-voxel updates/s" and line["higher_is_better"] is True
+    assert line["metric"] == "EM-iter muon\u00b7voxel updates/s" and line["higher_is_better"] is True
     assert line["value"] > 0 and line["steps"] == 1 and line["n_gpus"] == 1
     assert line["config"]["workload"] == "cube100_20mm_10M"
     cb = line["cpu_baseline"]
