@@ -69,10 +69,17 @@ typedef struct muto_status {
     double cost;                /* mean cost of the last iteration (when computed) */
     double cost_prev;           /* mean cost of the iteration before */
     uint64_t device_bytes;      /* device memory held by the handle */
-    int32_t muon_pass;          /* muon-pass variant in use: 1 TMA tiles, 2 warp-batched */
+    int32_t muon_pass;          /* muon-pass variant in use: 1 TMA tiles, 2 warp-batched, 3 the mean
+                                   update's one-pass form over stored lists, 4 its pass over recomputed
+                                   paths, 5 its split form (warp-batched muon pass, then a scatter pass) */
     int32_t muon_group;         /* lanes per muon in its covariance sums */
-    int32_t tile_pairs;         /* pairs per tile (TMA variant; 0 when it is not used) */
-    int32_t tile_muons;         /* muons per tile (TMA variant) */
+    int32_t tile_pairs;         /* pairs per tile (TMA variant), pairs per muon held in registers
+                                   (fused stored-list pass); 0 otherwise */
+    int32_t tile_muons;         /* muons per tile (TMA variant), muons per CTA batch (fused pass) */
+    int32_t path_lists;         /* how the pairs are kept: 1 muon-major lists and their voxel-major copy,
+                                   2 muon-major lists only, 3 none (paths walked every iteration);
+                                   0 for the one-shot methods */
+    int32_t reserved;
     char message[256];          /* text of the last error */
 } muto_status;
 
@@ -103,7 +110,26 @@ typedef struct muto_handle muto_handle;
  * in muon order; "columns" or "index" force one),
  * "voxel_stream_above" (-1: every segment up to 1536 pairs (768 in fp64)
  * is selected from registers; n >= 256: segments longer than n are
- * selected without holding their keys). */
+ * selected without holding their keys),
+ * "path_lists" (how the muon-voxel pairs are kept: "voxel_major" -- the
+ * muon-major lists plus a voxel-major copy, which the median and
+ * percentile updates need; "muon_major" -- the muon-major lists alone
+ * (12 bytes per pair mixed, 20 fp64), with the mean update's per-voxel
+ * sums formed by reductions to global memory; "recompute" -- no lists,
+ * every path walked again (FP64, bit-exact walk) twice per iteration, one
+ * scan per handle; "auto" (default): "muon_major" for the mean update
+ * (update_with_mean true, mean_percentile 100), else "voxel_major";
+ * "muon_major" and "recompute" require the mean update),
+ * "fused_variant" ("auto": the mean update's pass over muon-major lists
+ * takes the lanes per muon and pairs held per lane by timing the variants
+ * that suit the scan's mean path and the split form (the muon pass, then a
+ * second pass over the lists adding the terms) at prepare; "4x8", "8x4",
+ * "8x8", "8x16", "16x8", "16x16" or "split" force one), "fused_prefetch"
+ * (false; true: the one-pass form
+ * prefetches every CTA's next batch of pairs into L2),
+ * "setup_chunk_pairs" (0: the set-up walks the paths in chunks of muons
+ * whose bounded slots take at most a quarter of the free device memory,
+ * 12 GiB at most; n > 0: chunks of at most n bounded pairs). */
 int muto_create(const char* method, const char* config_json, muto_handle** out);
 int muto_destroy(muto_handle* h);
 

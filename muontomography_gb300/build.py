@@ -30,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-O3"] + ARCH
 CXX_FLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-fopenmp", "-Wall", "-Wno-unused-function"]
 
-CUDA_UNITS = ["scan.cu", "setup.cu", "em_muon.cu", "em_voxel.cu", "poca.cu", "slr.cu", "adjoint.cu", "gen.cu",
+CUDA_UNITS = ["scan.cu", "setup.cu", "em_muon.cu", "em_fused.cu", "em_voxel.cu", "poca.cu", "slr.cu", "adjoint.cu", "gen.cu",
               "fit.cu", "handle.cu", "noalloc.cu"]
 HOST_UNITS = ["host.cpp"]
 FACADE_UNITS = ["MutoFile.cpp", "MutoReconstruction.cpp", "MutoSiddon.cpp"]

@@ -92,6 +92,8 @@ struct Counters {
 // (out[n] = total).  scratch must hold scan_scratch_bytes(n) bytes.
 size_t scan_scratch_bytes(uint64_t n);
 void scan_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, void* scratch, cudaStream_t s);
+// a[i] += add for i < n
+void launch_add_u64(uint64_t* a, uint64_t n, uint64_t add, cudaStream_t s);
 
 // setup.cu
 void launch_keep_flags(const muto_ray* rays, uint64_t n_total, muto_grid g, double eps, uint32_t* flags,
@@ -110,16 +112,19 @@ void launch_path_fill(const muto_ray* rays, const uint32_t* kept, const double* 
 // and end), the walk into slots sized by those bounds with the actual
 // counts, and the compaction to slots sized by the counts.  A path longer
 // than its bound (never expected) is counted in ctr->over_bound and the
-// caller falls back to the exact count walk.
+// caller falls back to the exact count walk.  The bounded slots of muon i
+// are [boff[i], boff[i+1]) - slot_base, so a chunk of muons can be walked
+// into scratch sized for the chunk alone.
 void launch_path_bound(const muto_ray* rays, const uint32_t* kept, const double* scat, uint64_t n, muto_grid g,
                        int straight, uint32_t* bounds, cudaStream_t s);
 template <typename Real>
 void launch_path_fill_bounded(const muto_ray* rays, const uint32_t* kept, const double* scat, const uint64_t* boff,
-                              uint64_t n, muto_grid g, int straight, uint32_t* vidx, double* l64, Real* L, Real* T,
-                              uint32_t* counts, Counters* ctr, cudaStream_t s);
+                              uint64_t slot_base, uint64_t n, muto_grid g, int straight, uint32_t* vidx, double* l64,
+                              Real* L, Real* T, uint32_t* counts, Counters* ctr, cudaStream_t s);
 template <typename Real>
-void launch_path_compact(const uint64_t* boff, const uint64_t* off, uint64_t n, const uint32_t* vidx_b,
-                         const Real* L_b, const Real* T_b, uint32_t* vidx, Real* L, Real* T, cudaStream_t s);
+void launch_path_compact(const uint64_t* boff, uint64_t slot_base, const uint64_t* off, uint64_t n,
+                         const uint32_t* vidx_b, const Real* L_b, const Real* T_b, uint32_t* vidx, Real* L, Real* T,
+                         cudaStream_t s);
 // scan-local voxel indices j < V_scan become voff + j; others become 0xffffffff
 void launch_offset_voxels(uint32_t* vidx, uint64_t n, uint32_t v_scan, uint32_t voff, cudaStream_t s);
 void launch_voxel_hist(const uint32_t* vidx, uint64_t P, uint32_t V, uint32_t* mult, Counters* ctr, cudaStream_t s);
@@ -301,9 +306,12 @@ template <typename Real, typename OutT>
 void launch_em_voxel(const VoxelPassArgs<Real, OutT>& a, const VoxDesc* const* lists, const uint32_t* counts,
                      const int* resident_blocks, uint32_t streamed, int num_sms, const ClassFan* fan,
                      cudaStream_t s);
-// Bricked voxel order for the muon pass's lambda gathers: 4x4x4 bricks of
-// 64 consecutive entries, so the neighbouring voxels of a muon's path share
-// cache lines instead of lying a grid row or plane apart.
+// Bricked voxel order for the muon passes' lambda gathers and the per-voxel
+// sums: 4x4x4 bricks of 64 consecutive entries, each brick made of eight
+// 2x2x2 micro-blocks of 8 entries (one 32-byte sector in FP32), so the
+// consecutive voxels of a muon's path, which differ by one step on one
+// axis, fall into the same sector about half the time instead of lying a
+// grid row or plane apart.
 struct BrickDims {
     uint32_t nx, ny, nz, nbx, nby, nbz;
 };
@@ -313,14 +321,21 @@ __host__ __device__ inline BrickDims brick_dims(const muto_grid& g) {
 __host__ __device__ inline uint64_t brick_volume(const BrickDims& b) {
     return static_cast<uint64_t>(b.nbx) * b.nby * b.nbz * 64;
 }
+__host__ __device__ inline uint32_t brick_xyz(uint32_t x, uint32_t y, uint32_t z, const BrickDims& b) {
+    const uint32_t in = (((z >> 1) & 1u) << 5) | (((y >> 1) & 1u) << 4) | (((x >> 1) & 1u) << 3) | ((z & 1u) << 2) |
+                        ((y & 1u) << 1) | (x & 1u);
+    return (((z >> 2) * b.nby + (y >> 2)) * b.nbx + (x >> 2)) * 64u + in;
+}
 __host__ __device__ inline uint32_t brick_of(uint32_t j, const BrickDims& b) {
     const uint32_t x = j % b.nx, t = j / b.nx, y = t % b.ny, z = t / b.ny;
-    return (((z >> 2) * b.nby + (y >> 2)) * b.nbx + (x >> 2)) * 64u + (((z & 3u) << 4) | ((y & 3u) << 2) | (x & 3u));
+    return brick_xyz(x, y, z, b);
 }
 __host__ __device__ inline uint32_t unbrick(uint32_t jb, const BrickDims& b) {
     const uint32_t in = jb & 63u, blk = jb >> 6;
     const uint32_t bx = blk % b.nbx, t = blk / b.nbx, by = t % b.nby, bz = t / b.nby;
-    const uint32_t x = bx * 4 + (in & 3u), y = by * 4 + ((in >> 2) & 3u), z = bz * 4 + (in >> 4);
+    const uint32_t x = bx * 4 + (((in >> 3) & 1u) << 1) + (in & 1u);
+    const uint32_t y = by * 4 + (((in >> 4) & 1u) << 1) + ((in >> 1) & 1u);
+    const uint32_t z = bz * 4 + (((in >> 5) & 1u) << 1) + ((in >> 2) & 1u);
     return x + b.nx * (y + b.ny * z);
 }
 // voxel indices to bricked ones in place (indices >= V are left alone)
@@ -330,6 +345,60 @@ void launch_unbrick_indices(const uint32_t* in, uint32_t* out, uint64_t n, Brick
 // lambda (voxel order, V) to its bricked copy
 template <typename Real>
 void launch_brick_lambda(const Real* lam, uint32_t V, BrickDims b, Real* lam_b, cudaStream_t s);
+
+// em_fused.cu: the mean-update iteration over the muon-major lists (or over
+// paths walked again every iteration) with per-voxel sums G_j = sum_i g_ij
+// accumulated by reductions to global memory
+template <typename Real>
+struct FusedArgs {
+    const uint64_t* off;                      // N+1 pair offsets (stored lists)
+    const uint32_t* vidx;                     // voxel of each pair (bricked when lam/G are)
+    const Real* L;
+    const Real* T;
+    const typename Vec4<Real>::type* sd;      // N: Sx, Dx, Sy, Dy
+    const Real* pr2;                          // N
+    const Real* lam;                          // lambda gathered by the muons (bricked copy when brick)
+    Real* G;                                  // per-voxel sums of g_ij, zero on entry
+    uint32_t V;                               // entries of lam and G
+    uint32_t N;                               // kept muons
+    double E00, E01, E11;
+    int compute_cost;
+    int prefetch;                             // stored lists: prefetch every CTA's next batch into L2
+    Counters* ctr;
+    // recompute form: the walk's inputs
+    const muto_ray* rays;
+    const uint32_t* kept;
+    const double* scat;                       // 3N PoCA points
+    const double* ltot;                       // N in-grid path lengths (-1: dropped walk)
+    DevGrid g;
+    int straight;
+    BrickDims bdims;
+    int brick;
+};
+// stored-list variants: lanes per muon and pairs held in registers per muon
+constexpr int kFusedVariants = 6;
+int fused_variant_group(int v);
+int fused_variant_held(int v);
+template <typename Real>
+int em_fused_blocks(int variant);  // resident CTAs per SM
+template <typename Real>
+void launch_em_fused(const FusedArgs<Real>& a, int variant, int blocks, cudaStream_t s);
+template <typename Real>
+void launch_em_fused_walk(const FusedArgs<Real>& a, int num_sms, cudaStream_t s);
+// split form: g_ij of every pair from the muon pass's coefficients kvec, added to G
+template <typename Real>
+int em_scatter_blocks(int group);  // resident 256-thread CTAs per SM
+template <typename Real>
+void launch_em_scatter(const FusedArgs<Real>& a, const typename Vec4<Real>::type* kvec, int group, int blocks,
+                       cudaStream_t s);
+// recompute set-up: in-grid length per kept muon and pairs per voxel (mult zeroed by the caller)
+void launch_path_stats(const muto_ray* rays, const uint32_t* kept, const double* scat, uint64_t n, muto_grid g,
+                       int straight, double* ltot, uint32_t* mult, Counters* ctr, cudaStream_t s);
+// out_j = M_j ? l_j + l_j^2 G_j / (2 M_j) : 0, or grad_j = M_j ? -lam64_j G_j : 0 when grad is
+// given; G (bricked by `brick` when given) is cleared
+template <typename Real, typename OutT>
+void launch_mean_update(const Real* lam, Real* G, const uint32_t* mult, uint32_t V, const BrickDims* brick, OutT* out,
+                        double* grad, const double* lam64, cudaStream_t s);
 
 // descriptors of all voxels partitioned by class (within a class in column
 // order of column_order's grid when it covers the V voxels, else in index

@@ -155,7 +155,14 @@ struct Params {
     int muon_pass = 0;  // 0 autotune, 1 tile (TMA), 2 warp-batched
     long long voxel_stream_above = -1;  // segments longer than this are selected without registers (-1: none)
     int muon_layout = 0;  // coefficient rows: 0 auto (column order when the table outgrows L2), 1 columns, 2 index
+    int path_lists = 0;   // 0 auto, 1 voxel-major copy, 2 muon-major lists only, 3 recomputed every iteration
+    long long setup_chunk_pairs = 0;  // bounded pairs per set-up chunk (0: sized from free device memory)
+    int fused_variant = -1;           // stored-list fused pass: -1 autotune, else the variant index
+    bool fused_prefetch = false;      // stored-list fused pass: L2 prefetch of each CTA's next batch
 };
+
+// how an EM / MAP handle keeps its pair lists
+enum Lists { kListsVoxelMajor = 1, kListsMuonMajor = 2, kListsRecompute = 3 };
 
 // variant of the one-shot (PoCA) handle: 0 PoCA, 1 PoCut, 2 SLR, 3 SLRIter
 Params parse_params(Method m, const std::string& text, int variant = 0) {
@@ -249,6 +256,30 @@ Params parse_params(Method m, const std::string& text, int variant = 0) {
         else if (ml == "index") P.muon_layout = 2;
         else throw Error(MUTO_ERR_CONFIG, "muon_layout must be \"auto\", \"columns\" or \"index\"");
         if (P.newton_max_iter < 1) throw Error(MUTO_ERR_CONFIG, "newton_max_iter must be >= 1");
+        const std::string fv = cfg.value("fused_variant", "auto");
+        if (fv == "auto") P.fused_variant = -1;
+        else if (fv == "4x8") P.fused_variant = 0;
+        else if (fv == "8x8") P.fused_variant = 1;
+        else if (fv == "8x16") P.fused_variant = 2;
+        else if (fv == "16x8") P.fused_variant = 3;
+        else if (fv == "16x16") P.fused_variant = 4;
+        else if (fv == "8x4") P.fused_variant = 5;
+        else if (fv == "split") P.fused_variant = kFusedVariants;
+        else throw Error(MUTO_ERR_CONFIG, "fused_variant must be \"auto\", \"4x8\", \"8x4\", \"8x8\", \"8x16\", "
+                                          "\"16x8\", \"16x16\" or \"split\"");
+        P.fused_prefetch = cfg.value("fused_prefetch", false);
+        P.setup_chunk_pairs = cfg.value("setup_chunk_pairs", static_cast<int64_t>(0));
+        if (P.setup_chunk_pairs < 0) throw Error(MUTO_ERR_CONFIG, "setup_chunk_pairs must be >= 0");
+        const std::string pl = cfg.value("path_lists", "auto");
+        if (pl == "auto") P.path_lists = 0;
+        else if (pl == "voxel_major") P.path_lists = kListsVoxelMajor;
+        else if (pl == "muon_major") P.path_lists = kListsMuonMajor;
+        else if (pl == "recompute") P.path_lists = kListsRecompute;
+        else throw Error(MUTO_ERR_CONFIG, "path_lists must be \"auto\", \"voxel_major\", \"muon_major\" or \"recompute\"");
+        const bool mean_update = P.update_with_mean && P.mean_percentile == 100;
+        if (m != kPoca && P.path_lists >= kListsMuonMajor && !mean_update)
+            throw Error(MUTO_ERR_CONFIG, "path_lists \"muon_major\" and \"recompute\" take the mean update "
+                                         "(update_with_mean true, mean_percentile 100)");
     } catch (const json::type_error& e) {
         throw Error(MUTO_ERR_CONFIG, std::string("config value of the wrong type: ") + e.what());
     } catch (const json::out_of_range& e) {
@@ -359,6 +390,11 @@ struct muto_handle {
     DevMem kslot;                     // per kept muon: its row of kvec (empty: its own index)
     DevMem mult, start, kvec, keys;   // keys: the voxel pass's order key of every pair
     DevMem win;                       // per voxel: the last selection window (center, half-width)
+    int lists = kListsVoxelMajor;     // how the pair lists are kept (Lists)
+    DevMem gsum;                      // muon-major / recompute: per-voxel sums of g_ij (bricked like lam_b)
+    DevMem ltot;                      // recompute: in-grid path length per kept muon
+    int fused_variant = 1, fused_blocks = 0;  // stored-list fused pass: variant and persistent grid
+    int scatter_group = 32, scatter_blocks = 0;  // split form's scatter pass (fused_variant == kFusedVariants)
     bool brick = false;               // path voxel indices are bricked (single scans), see lam_b
     BrickDims bdims{};
     uint64_t vb = 0;                  // bricked index space (>= V)
@@ -666,6 +702,141 @@ void prepare_poca(muto_handle* h) {
     CK(cudaStreamSynchronize(s));  // the scratch arrays go out of scope
 }
 
+// The merged paths of all kept muons into the muon-major lists (vidx, L, T)
+// with their offsets.  Per chunk of muons: one FP64 walk into slots sized by
+// the FP32 path bounds (scratch for the chunk alone), then compaction to the
+// exact slots after the chunks before it.  The lists are allocated for the
+// bounds' total (a few percent above the pairs), so the set-up's peak is the
+// lists plus one chunk's scratch.  counts holds every muon's bound on entry
+// and its path length on return.  scan_off: each scan's first pair and the
+// total; off_h: every muon's offset when the TMA tile pass needs them.
+template <typename Real>
+void fill_lists(muto_handle* h, DevMem& counts, DevMem& scratch, std::vector<uint64_t>& scan_off,
+                std::vector<uint64_t>& off_h) {
+    const Params& P = h->P;
+    cudaStream_t s = h->stream;
+    const uint64_t N = h->N;
+    const size_t S = h->scans.size();
+    const bool real64 = std::is_same<Real, double>::value;
+    HostPhase ph(h, "fill");
+    DevMem boff;
+    boff.alloc((N + 1) * sizeof(uint64_t), &h->dev_bytes);
+    run(h, "scan", [&] { scan_u32_to_u64(counts.as<uint32_t>(), boff.as<uint64_t>(), N, scratch.as<void>(), s); });
+    uint64_t Pb = 0;
+    CK(cudaMemcpyAsync(&Pb, boff.as<uint64_t>() + N, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    h->off.alloc((N + 1 + kPad) * sizeof(uint64_t), &h->dev_bytes);
+    CK(cudaMemsetAsync(h->off.as<void>(), 0, (N + 1 + kPad) * sizeof(uint64_t), s));
+    h->vidx.alloc((Pb + kPad) * sizeof(uint32_t), &h->dev_bytes);
+    h->L.alloc((Pb + kPad) * sizeof(Real), &h->dev_bytes);
+    h->T.alloc((Pb + kPad) * sizeof(Real), &h->dev_bytes);
+    // one chunk's bounded slots: voxel, FP64 length (tails are summed in FP64), L, T
+    const uint64_t per_pair = sizeof(uint32_t) + sizeof(double) + (real64 ? 0 : sizeof(Real)) + sizeof(Real);
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const uint64_t budget = std::min<uint64_t>(free_b / 4, uint64_t(12) << 30);
+    uint64_t cap = std::min<uint64_t>(std::max<uint64_t>(Pb, 1), std::max<uint64_t>(budget / per_pair, uint64_t(1) << 20));
+    if (P.setup_chunk_pairs > 0) cap = static_cast<uint64_t>(P.setup_chunk_pairs);
+    DevMem vidx_b, l64_b, L_b, T_b;
+    vidx_b.alloc((cap + kPad) * sizeof(uint32_t), &h->dev_bytes);
+    l64_b.alloc((cap + kPad) * sizeof(double), &h->dev_bytes);
+    if (!real64) L_b.alloc((cap + kPad) * sizeof(Real), &h->dev_bytes);
+    T_b.alloc((cap + kPad) * sizeof(Real), &h->dev_bytes);
+    Real* Lb = real64 ? reinterpret_cast<Real*>(l64_b.as<double>()) : L_b.as<Real>();
+    const double avg = N ? static_cast<double>(Pb) / static_cast<double>(N) : 1.0;
+    const uint64_t chunk0 = std::max<uint64_t>(P.setup_chunk_pairs > 0 ? 1 : 1024,
+                                               static_cast<uint64_t>(static_cast<double>(cap) / (1.25 * avg + 1.0)));
+    uint64_t base = 0;
+    for (size_t k = 0; k < S; ++k) {
+        const auto& sc = h->scans[k];
+        const uint64_t end = sc.noff + sc.N;
+        for (uint64_t m = sc.noff; m < end;) {
+            uint64_t nc = std::min<uint64_t>(end - m, chunk0);
+            uint64_t b[2] = {0, 0};
+            for (;;) {  // the chunk's bounded slots must fit the scratch
+                CK(cudaMemcpyAsync(&b[0], boff.as<uint64_t>() + m, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+                CK(cudaMemcpyAsync(&b[1], boff.as<uint64_t>() + m + nc, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                if (b[1] - b[0] <= cap || nc == 1) break;
+                nc = (nc + 1) / 2;
+            }
+            if (b[1] - b[0] > cap) throw Error(MUTO_ERR_CAPACITY, "a muon's path bound exceeds the set-up scratch");
+            run(h, "siddon_fill", [&] {
+                launch_path_fill_bounded<Real>(h->scan_rays(k), h->kept.as<uint32_t>() + m, h->scat.as<double>() + 3 * m,
+                                               boff.as<uint64_t>() + m, b[0], nc, sc.grid, P.straight_line,
+                                               vidx_b.as<uint32_t>(), l64_b.as<double>(), Lb, T_b.as<Real>(),
+                                               counts.as<uint32_t>() + m, h->ctr(), s);
+            });
+            run(h, "scan", [&] {
+                scan_u32_to_u64(counts.as<uint32_t>() + m, h->off.as<uint64_t>() + m, nc, scratch.as<void>(), s);
+                launch_add_u64(h->off.as<uint64_t>() + m, nc + 1, base, s);
+            });
+            run(h, "path_compact", [&] {
+                launch_path_compact<Real>(boff.as<uint64_t>() + m, b[0], h->off.as<uint64_t>() + m, nc,
+                                          vidx_b.as<uint32_t>(), Lb, T_b.as<Real>(), h->vidx.as<uint32_t>(),
+                                          h->L.as<Real>(), h->T.as<Real>(), s);
+            });
+            CK(cudaMemcpyAsync(&base, h->off.as<uint64_t>() + m + nc, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            m += nc;
+        }
+    }
+    vidx_b.release();
+    l64_b.release();
+    L_b.release();
+    T_b.release();
+    boff.release();
+    unsigned long long over_bound = 0;
+    CK(cudaMemcpyAsync(&over_bound, &h->ctr()->over_bound, sizeof(over_bound), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (over_bound > 0) {  // a bound was short (never expected): count exactly, then walk into exact slots
+        CK(cudaMemsetAsync(&h->ctr()->overflow, 0, sizeof(unsigned long long), s));
+        for (size_t k = 0; k < S; ++k) {
+            const auto& sc = h->scans[k];
+            run(h, "siddon_count", [&] {
+                launch_path_count(h->scan_rays(k), h->kept.as<uint32_t>() + sc.noff, h->scat.as<double>() + 3 * sc.noff,
+                                  sc.N, sc.grid, P.straight_line, counts.as<uint32_t>() + sc.noff, h->ctr(), s);
+            });
+        }
+        run(h, "scan", [&] { scan_u32_to_u64(counts.as<uint32_t>(), h->off.as<uint64_t>(), N, scratch.as<void>(), s); });
+        uint64_t Pe = 0;
+        CK(cudaMemcpyAsync(&Pe, h->off.as<uint64_t>() + N, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        h->vidx.alloc((Pe + kPad) * sizeof(uint32_t), &h->dev_bytes);
+        h->L.alloc((Pe + kPad) * sizeof(Real), &h->dev_bytes);
+        h->T.alloc((Pe + kPad) * sizeof(Real), &h->dev_bytes);
+        DevMem l64tmp;
+        double* l64 = reinterpret_cast<double*>(h->L.as<Real>());
+        if (!real64) {
+            l64tmp.alloc(std::max<uint64_t>(Pe, 1) * sizeof(double), &h->dev_bytes);
+            l64 = l64tmp.as<double>();
+        }
+        for (size_t k = 0; k < S; ++k) {
+            const auto& sc = h->scans[k];
+            run(h, "siddon_fill", [&] {
+                launch_path_fill<Real>(h->scan_rays(k), h->kept.as<uint32_t>() + sc.noff,
+                                       h->scat.as<double>() + 3 * sc.noff, h->off.as<uint64_t>() + sc.noff, sc.N,
+                                       sc.grid, P.straight_line, h->vidx.as<uint32_t>(), l64, h->L.as<Real>(),
+                                       h->T.as<Real>(), s);
+            });
+        }
+        CK(cudaStreamSynchronize(s));
+    }
+    counts.release();
+    // pair offsets on the host: each scan's first pair and the total, and
+    // every muon's for the tile schedule
+    for (size_t k = 0; k < S; ++k)
+        CK(cudaMemcpyAsync(&scan_off[k], h->off.as<uint64_t>() + h->scans[k].noff, sizeof(uint64_t),
+                           cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&scan_off[S], h->off.as<uint64_t>() + N, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    if (P.muon_pass == 1 && h->lists == kListsVoxelMajor) {
+        off_h.resize(N + 1);
+        CK(cudaMemcpyAsync(off_h.data(), h->off.as<uint64_t>(), (N + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    h->npairs = scan_off[S];
+}
+
 template <typename Real>
 void prepare_em(muto_handle* h) {
     using R4 = typename Vec4<Real>::type;
@@ -737,6 +908,13 @@ void prepare_em(muto_handle* h) {
     h->pr2.alloc((N + kPad) * sizeof(Real), &h->dev_bytes);
     h->scat.alloc(std::max<uint64_t>(N, 1) * 3 * sizeof(double), &h->dev_bytes);
     h->pr64.alloc(std::max<uint64_t>(N, 1) * sizeof(double), &h->dev_bytes);
+    // --- how the lists are kept: the voxel-major copy for the median and
+    // percentile updates; for the mean update the muon-major lists alone, or
+    // none (the paths walked again every iteration) ---
+    h->lists = P.path_lists ? P.path_lists
+                            : (P.update_with_mean && P.mean_percentile == 100 ? kListsMuonMajor : kListsVoxelMajor);
+    if (h->lists == kListsRecompute && h->batch)
+        throw Error(MUTO_ERR_CONFIG, "path_lists \"recompute\" takes one scan per handle");
     // --- merged paths: one walk per muon into slots sized by an upper bound
     // on its path, then compaction to the exact slots (the walk is FP64 and
     // the set-up's costliest step, so it is not run twice to count first) ---
@@ -754,213 +932,150 @@ void prepare_em(muto_handle* h) {
             launch_muon_info<Real>(r, kept, sc.N, sc.grid, P.eps, P.has_energy, h->sd.as<R4>() + sc.noff,
                                    h->pr2.as<Real>() + sc.noff, scat, h->pr64.as<double>() + sc.noff, s);
         });
-        run(h, "path_bound", [&] {
-            launch_path_bound(r, kept, scat, sc.N, sc.grid, P.straight_line, counts.as<uint32_t>() + sc.noff, s);
-        });
+        if (h->lists != kListsRecompute)
+            run(h, "path_bound", [&] {
+                launch_path_bound(r, kept, scat, sc.N, sc.grid, P.straight_line, counts.as<uint32_t>() + sc.noff, s);
+            });
     }
     flags.release();
     pos.clear();
     if (scratch.bytes() < scan_scratch_bytes(std::max<uint64_t>(N, V) + 1))
         scratch.alloc(scan_scratch_bytes(std::max<uint64_t>(N, V) + 1), &h->dev_bytes);
-    ph.reset(new HostPhase(h, "fill"));
-    DevMem boff;
-    boff.alloc((N + 1) * sizeof(uint64_t), &h->dev_bytes);
-    run(h, "scan", [&] { scan_u32_to_u64(counts.as<uint32_t>(), boff.as<uint64_t>(), N, scratch.as<void>(), s); });
-    uint64_t Pb = 0;
-    CK(cudaMemcpyAsync(&Pb, boff.as<uint64_t>() + N, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    const bool real64 = std::is_same<Real, double>::value;
-    DevMem vidx_b, l64_b, L_b, T_b;
-    vidx_b.alloc((Pb + kPad) * sizeof(uint32_t), &h->dev_bytes);
-    l64_b.alloc((Pb + kPad) * sizeof(double), &h->dev_bytes);
-    if (!real64) L_b.alloc((Pb + kPad) * sizeof(Real), &h->dev_bytes);
-    T_b.alloc((Pb + kPad) * sizeof(Real), &h->dev_bytes);
-    Real* Lb = real64 ? reinterpret_cast<Real*>(l64_b.as<double>()) : L_b.as<Real>();
-    for (size_t k = 0; k < S; ++k) {
-        const auto& sc = h->scans[k];
-        run(h, "siddon_fill", [&] {
-            launch_path_fill_bounded<Real>(h->scan_rays(k), h->kept.as<uint32_t>() + sc.noff,
-                                           h->scat.as<double>() + 3 * sc.noff, boff.as<uint64_t>() + sc.noff, sc.N,
-                                           sc.grid, P.straight_line, vidx_b.as<uint32_t>(), l64_b.as<double>(), Lb,
-                                           T_b.as<Real>(), counts.as<uint32_t>() + sc.noff, h->ctr(), s);
-        });
-    }
-    unsigned long long over_bound = 0;
-    CK(cudaMemcpyAsync(&over_bound, &h->ctr()->over_bound, sizeof(over_bound), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (over_bound > 0) {  // a bound was short (never expected): count exactly, walk again below
-        vidx_b.release();
-        l64_b.release();
-        L_b.release();
-        T_b.release();
-        CK(cudaMemsetAsync(&h->ctr()->overflow, 0, sizeof(unsigned long long), s));
-        for (size_t k = 0; k < S; ++k) {
-            const auto& sc = h->scans[k];
-            run(h, "siddon_count", [&] {
-                launch_path_count(h->scan_rays(k), h->kept.as<uint32_t>() + sc.noff,
-                                  h->scat.as<double>() + 3 * sc.noff, sc.N, sc.grid, P.straight_line,
-                                  counts.as<uint32_t>() + sc.noff, h->ctr(), s);
-            });
-        }
-    }
-    h->off.alloc((N + 1 + kPad) * sizeof(uint64_t), &h->dev_bytes);
-    run(h, "scan", [&] { scan_u32_to_u64(counts.as<uint32_t>(), h->off.as<uint64_t>(), N, scratch.as<void>(), s); });
-    counts.release();
-    // pair offsets on the host: each scan's first pair and the total, and
-    // every muon's for the tile schedule
-    std::vector<uint64_t> scan_off(S + 1), off_h;
-    for (size_t k = 0; k < S; ++k)
-        CK(cudaMemcpyAsync(&scan_off[k], h->off.as<uint64_t>() + h->scans[k].noff, sizeof(uint64_t),
-                           cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(&scan_off[S], h->off.as<uint64_t>() + N, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-    if (P.muon_pass == 1) {
-        off_h.resize(N + 1);
-        CK(cudaMemcpyAsync(off_h.data(), h->off.as<uint64_t>(), (N + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-    }
-    CK(cudaStreamSynchronize(s));
-    const uint64_t Pn = scan_off[S];
-    h->npairs = Pn;
-
-    h->vidx.alloc((Pn + kPad) * sizeof(uint32_t), &h->dev_bytes);
-    h->L.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
-    h->T.alloc((Pn + kPad) * sizeof(Real), &h->dev_bytes);
-    if (over_bound == 0) {
-        run(h, "path_compact", [&] {
-            launch_path_compact<Real>(boff.as<uint64_t>(), h->off.as<uint64_t>(), N, vidx_b.as<uint32_t>(), Lb,
-                                      T_b.as<Real>(), h->vidx.as<uint32_t>(), h->L.as<Real>(), h->T.as<Real>(), s);
-        });
-    } else {
-        DevMem l64tmp;
-        double* l64 = reinterpret_cast<double*>(h->L.as<Real>());
-        if (!real64) {
-            l64tmp.alloc(std::max<uint64_t>(Pn, 1) * sizeof(double), &h->dev_bytes);
-            l64 = l64tmp.as<double>();
-        }
-        for (size_t k = 0; k < S; ++k) {
-            const auto& sc = h->scans[k];
-            run(h, "siddon_fill", [&] {
-                launch_path_fill<Real>(h->scan_rays(k), h->kept.as<uint32_t>() + sc.noff,
-                                       h->scat.as<double>() + 3 * sc.noff, h->off.as<uint64_t>() + sc.noff, sc.N,
-                                       sc.grid, P.straight_line, h->vidx.as<uint32_t>(), l64, h->L.as<Real>(),
-                                       h->T.as<Real>(), s);
-            });
-        }
-        CK(cudaStreamSynchronize(s));
-    }
-    // scan-local voxel indices into the batch's voxel space
-    if (h->batch) {
-        for (size_t k = 0; k < S; ++k) {
-            const auto& sc = h->scans[k];
-            const uint64_t pb = scan_off[k], pe = scan_off[k + 1];
-            run(h, "voxel_offset", [&] {
-                launch_offset_voxels(h->vidx.as<uint32_t>() + pb, pe - pb, static_cast<uint32_t>(sc.V),
-                                     static_cast<uint32_t>(sc.voff), s);
-            });
-        }
-    }
-    CK(cudaStreamSynchronize(s));
-    vidx_b.release();
-    l64_b.release();
-    L_b.release();
-    T_b.release();
-    boff.release();
-
-    // --- multiplicity M_j and the voxel-major copy of the lists ---------------
-    ph.reset(new HostPhase(h, "voxel_major"));
     h->mult.alloc(V * sizeof(uint32_t), &h->dev_bytes);
     CK(cudaMemsetAsync(h->mult.as<void>(), 0, V * sizeof(uint32_t), s));
-    run(h, "voxel_hist", [&] { launch_voxel_hist(h->vidx.as<uint32_t>(), Pn, static_cast<uint32_t>(V), h->mult.as<uint32_t>(), h->ctr(), s); });
-    h->start.alloc((V + 1) * sizeof(uint64_t), &h->dev_bytes);
-    {
-        DevMem mcol, scol;
-        if (!h->batch) {
-            mcol.alloc(std::max<uint64_t>(V, 1) * sizeof(uint32_t), &h->dev_bytes);
-            scol.alloc((V + 1) * sizeof(uint64_t), &h->dev_bytes);
+    std::vector<uint64_t> scan_off(S + 1), off_h;
+    if (h->lists == kListsRecompute) {
+        // no lists: every kept muon's in-grid length and the pairs per voxel,
+        // from one walk of every path
+        counts.release();
+        ph.reset(new HostPhase(h, "path_stats"));
+        h->ltot.alloc(std::max<uint64_t>(N, 1) * sizeof(double), &h->dev_bytes);
+        const auto& sc = h->scans[0];
+        run(h, "path_stats", [&] {
+            launch_path_stats(h->scan_rays(0), h->kept.as<uint32_t>(), h->scat.as<double>(), sc.N, sc.grid,
+                              P.straight_line, h->ltot.as<double>(), h->mult.as<uint32_t>(), h->ctr(), s);
+        });
+        DevMem moff;
+        moff.alloc((V + 1) * sizeof(uint64_t), &h->dev_bytes);
+        run(h, "scan", [&] { scan_u32_to_u64(h->mult.as<uint32_t>(), moff.as<uint64_t>(), V, scratch.as<void>(), s); });
+        CK(cudaMemcpyAsync(&h->npairs, moff.as<uint64_t>() + V, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    } else {
+        fill_lists<Real>(h, counts, scratch, scan_off, off_h);
+        // scan-local voxel indices into the batch's voxel space
+        if (h->batch) {
+            for (size_t k = 0; k < S; ++k) {
+                const auto& sc = h->scans[k];
+                const uint64_t pb = scan_off[k], pe = scan_off[k + 1];
+                run(h, "voxel_offset", [&] {
+                    launch_offset_voxels(h->vidx.as<uint32_t>() + pb, pe - pb, static_cast<uint32_t>(sc.V),
+                                         static_cast<uint32_t>(sc.voff), s);
+                });
+            }
         }
-        run(h, "scan", [&] {
-            launch_segment_starts(h->mult.as<uint32_t>(), static_cast<uint32_t>(V), h->batch ? nullptr : &h->grid,
-                                  mcol.as<uint32_t>(), scol.as<uint64_t>(), scratch.as<void>(), h->start.as<uint64_t>(), s);
+        run(h, "voxel_hist", [&] {
+            launch_voxel_hist(h->vidx.as<uint32_t>(), h->npairs, static_cast<uint32_t>(V), h->mult.as<uint32_t>(),
+                              h->ctr(), s);
         });
         CK(cudaStreamSynchronize(s));
     }
-    {
-        DevMem cursor;
-        cursor.alloc(V * sizeof(uint32_t), &h->dev_bytes);
-        CK(cudaMemsetAsync(cursor.as<void>(), 0, V * sizeof(uint32_t), s));
-        h->vm_mu.alloc((Pn + kPad) * sizeof(uint32_t), &h->dev_bytes);
-        h->vm_LT.alloc((Pn + kPad) * sizeof(typename Vec2<Real>::type), &h->dev_bytes);
-        DevMem staging;
-        staging.alloc(std::max<uint64_t>(Pn, 1) * sizeof(R4), &h->dev_bytes);
-        // coefficient rows in column order of the PoCA points, when asked or
-        // when the table would take more than a third of L2
-        h->kslot.release();
-        const bool columns = P.muon_layout == 1 || (P.muon_layout == 0 && N * sizeof(R4) > h->l2_bytes / 3);
-        if (columns && !h->batch && N > 0) {
-            const uint64_t nc = static_cast<uint64_t>(h->grid.nx) * h->grid.ny;
-            DevMem cell, hist, cstart, ccur, cscr;
-            h->kslot.alloc(N * sizeof(uint32_t), &h->dev_bytes);
-            cell.alloc(N * sizeof(uint32_t), &h->dev_bytes);
-            hist.alloc((nc + 1) * sizeof(uint32_t), &h->dev_bytes);
-            ccur.alloc((nc + 1) * sizeof(uint32_t), &h->dev_bytes);
-            cstart.alloc((nc + 1) * sizeof(uint64_t), &h->dev_bytes);
-            cscr.alloc(scan_scratch_bytes(nc + 1), &h->dev_bytes);
-            run(h, "muon_slots", [&] {
-                launch_muon_slots(h->scat.as<double>(), N, h->grid, cell.as<uint32_t>(), hist.as<uint32_t>(),
-                                  cstart.as<uint64_t>(), ccur.as<uint32_t>(), cscr.as<void>(), h->kslot.as<uint32_t>(),
-                                  s);
+    const uint64_t Pn = h->npairs;
+
+    // --- the voxel-major copy of the lists (median / percentile updates) -----
+    if (h->lists == kListsVoxelMajor) {
+        ph.reset(new HostPhase(h, "voxel_major"));
+        h->start.alloc((V + 1) * sizeof(uint64_t), &h->dev_bytes);
+        {
+            DevMem mcol, scol;
+            if (!h->batch) {
+                mcol.alloc(std::max<uint64_t>(V, 1) * sizeof(uint32_t), &h->dev_bytes);
+                scol.alloc((V + 1) * sizeof(uint64_t), &h->dev_bytes);
+            }
+            run(h, "scan", [&] {
+                launch_segment_starts(h->mult.as<uint32_t>(), static_cast<uint32_t>(V), h->batch ? nullptr : &h->grid,
+                                      mcol.as<uint32_t>(), scol.as<uint64_t>(), scratch.as<void>(), h->start.as<uint64_t>(), s);
             });
             CK(cudaStreamSynchronize(s));
         }
-        run(h, "voxel_major", [&] {
-            launch_build_voxel_major<Real>(h->off.as<uint64_t>(), N, h->vidx.as<uint32_t>(), h->L.as<Real>(),
-                                           h->T.as<Real>(), static_cast<uint32_t>(V), h->start.as<uint64_t>(),
-                                           cursor.as<uint32_t>(), Pn, staging.as<R4>(), h->vm_mu.as<uint32_t>(),
-                                           h->vm_LT.as<typename Vec2<Real>::type>(),
-                                           h->kslot.empty() ? nullptr : h->kslot.as<uint32_t>(), s);
-        });
-        CK(cudaStreamSynchronize(s));
+        {
+            DevMem cursor;
+            cursor.alloc(V * sizeof(uint32_t), &h->dev_bytes);
+            CK(cudaMemsetAsync(cursor.as<void>(), 0, V * sizeof(uint32_t), s));
+            h->vm_mu.alloc((Pn + kPad) * sizeof(uint32_t), &h->dev_bytes);
+            h->vm_LT.alloc((Pn + kPad) * sizeof(typename Vec2<Real>::type), &h->dev_bytes);
+            DevMem staging;
+            staging.alloc(std::max<uint64_t>(Pn, 1) * sizeof(R4), &h->dev_bytes);
+            // coefficient rows in column order of the PoCA points, when asked or
+            // when the table would take more than a third of L2
+            h->kslot.release();
+            const bool columns = P.muon_layout == 1 || (P.muon_layout == 0 && N * sizeof(R4) > h->l2_bytes / 3);
+            if (columns && !h->batch && N > 0) {
+                const uint64_t nc = static_cast<uint64_t>(h->grid.nx) * h->grid.ny;
+                DevMem cell, hist, cstart, ccur, cscr;
+                h->kslot.alloc(N * sizeof(uint32_t), &h->dev_bytes);
+                cell.alloc(N * sizeof(uint32_t), &h->dev_bytes);
+                hist.alloc((nc + 1) * sizeof(uint32_t), &h->dev_bytes);
+                ccur.alloc((nc + 1) * sizeof(uint32_t), &h->dev_bytes);
+                cstart.alloc((nc + 1) * sizeof(uint64_t), &h->dev_bytes);
+                cscr.alloc(scan_scratch_bytes(nc + 1), &h->dev_bytes);
+                run(h, "muon_slots", [&] {
+                    launch_muon_slots(h->scat.as<double>(), N, h->grid, cell.as<uint32_t>(), hist.as<uint32_t>(),
+                                      cstart.as<uint64_t>(), ccur.as<uint32_t>(), cscr.as<void>(), h->kslot.as<uint32_t>(),
+                                      s);
+                });
+                CK(cudaStreamSynchronize(s));
+            }
+            run(h, "voxel_major", [&] {
+                launch_build_voxel_major<Real>(h->off.as<uint64_t>(), N, h->vidx.as<uint32_t>(), h->L.as<Real>(),
+                                               h->T.as<Real>(), static_cast<uint32_t>(V), h->start.as<uint64_t>(),
+                                               cursor.as<uint32_t>(), Pn, staging.as<R4>(), h->vm_mu.as<uint32_t>(),
+                                               h->vm_LT.as<typename Vec2<Real>::type>(),
+                                               h->kslot.empty() ? nullptr : h->kslot.as<uint32_t>(), s);
+            });
+            CK(cudaStreamSynchronize(s));
+        }
+        h->kvec.alloc((N + kPad) * sizeof(R4), &h->dev_bytes);
+        ph.reset(new HostPhase(h, "classes"));
+        {
+            // voxel classes by segment length, one voxel-pass kernel each, built on
+            // the device; a descriptor carries the voxel, its pair count and its
+            // first voxel-major pair
+            const uint32_t nb = voxel_class_blocks(V);
+            const uint64_t nc = static_cast<uint64_t>(nb) * kVoxClasses;
+            DevMem ccount, cfirst, cscr;
+            ccount.alloc(nc * sizeof(uint32_t), &h->dev_bytes);
+            cfirst.alloc((nc + 1) * sizeof(uint64_t), &h->dev_bytes);
+            cscr.alloc(scan_scratch_bytes(nc + 1), &h->dev_bytes);
+            h->vclass.alloc(std::max<uint64_t>(V, 1) * sizeof(VoxDesc), &h->dev_bytes);
+            run(h, "voxel_classes", [&] {
+                launch_voxel_classes<Real>(h->mult.as<uint32_t>(), h->start.as<uint64_t>(), static_cast<uint32_t>(V),
+                                           h->batch ? nullptr : &h->grid, ccount.as<uint32_t>(), cfirst.as<uint64_t>(),
+                                           cscr.as<void>(), h->vclass.as<VoxDesc>(), s);
+            });
+            uint64_t bnd[kVoxClasses + 1];
+            for (int c = 0; c <= kVoxClasses; ++c)
+                CK(cudaMemcpyAsync(&bnd[c], cfirst.as<uint64_t>() + static_cast<uint64_t>(c) * nb, sizeof(uint64_t),
+                                   cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            if (bnd[kVoxClasses] != V) throw Error(MUTO_ERR_STATE, "voxel classes do not cover the voxels");
+            for (int c = 0; c < kVoxClasses; ++c) {
+                h->vclass_off[c] = bnd[c];
+                h->vclass_n[c] = static_cast<uint32_t>(bnd[c + 1] - bnd[c]);
+            }
+            // the voxel pass's key array (kPad past the end: the class kernels'
+            // L2 prefetches round out to 16 bytes)
+            h->vox_streamed = P.voxel_stream_above < 0 ? 0u
+                              : vox_streamed_mask(static_cast<uint32_t>(std::min<long long>(P.voxel_stream_above, 0xffffffffLL)));
+            h->keys.alloc((Pn + kPad) * sizeof(typename KeyOf<Real>::type), &h->dev_bytes);
+            em_voxel_occupancy<Real, Real>(h->vox_blocks_real);
+            em_voxel_occupancy<Real, double>(h->vox_blocks_f64);
+            for (int c = 0; c < 2 * kVoxClasses; ++c) {
+                h->vox_blocks_real[c] *= h->num_sms;
+                h->vox_blocks_f64[c] *= h->num_sms;
+            }
+        }
     }
     scratch.release();
-    h->kvec.alloc((N + kPad) * sizeof(R4), &h->dev_bytes);
-    ph.reset(new HostPhase(h, "classes"));
-    {
-        // voxel classes by segment length, one voxel-pass kernel each, built on
-        // the device; a descriptor carries the voxel, its pair count and its
-        // first voxel-major pair
-        const uint32_t nb = voxel_class_blocks(V);
-        const uint64_t nc = static_cast<uint64_t>(nb) * kVoxClasses;
-        DevMem ccount, cfirst, cscr;
-        ccount.alloc(nc * sizeof(uint32_t), &h->dev_bytes);
-        cfirst.alloc((nc + 1) * sizeof(uint64_t), &h->dev_bytes);
-        cscr.alloc(scan_scratch_bytes(nc + 1), &h->dev_bytes);
-        h->vclass.alloc(std::max<uint64_t>(V, 1) * sizeof(VoxDesc), &h->dev_bytes);
-        run(h, "voxel_classes", [&] {
-            launch_voxel_classes<Real>(h->mult.as<uint32_t>(), h->start.as<uint64_t>(), static_cast<uint32_t>(V),
-                                       h->batch ? nullptr : &h->grid, ccount.as<uint32_t>(), cfirst.as<uint64_t>(),
-                                       cscr.as<void>(), h->vclass.as<VoxDesc>(), s);
-        });
-        uint64_t bnd[kVoxClasses + 1];
-        for (int c = 0; c <= kVoxClasses; ++c)
-            CK(cudaMemcpyAsync(&bnd[c], cfirst.as<uint64_t>() + static_cast<uint64_t>(c) * nb, sizeof(uint64_t),
-                               cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        if (bnd[kVoxClasses] != V) throw Error(MUTO_ERR_STATE, "voxel classes do not cover the voxels");
-        for (int c = 0; c < kVoxClasses; ++c) {
-            h->vclass_off[c] = bnd[c];
-            h->vclass_n[c] = static_cast<uint32_t>(bnd[c + 1] - bnd[c]);
-        }
-        // the voxel pass's key array (kPad past the end: the class kernels'
-        // L2 prefetches round out to 16 bytes)
-        h->vox_streamed = P.voxel_stream_above < 0 ? 0u
-                          : vox_streamed_mask(static_cast<uint32_t>(std::min<long long>(P.voxel_stream_above, 0xffffffffLL)));
-        h->keys.alloc((Pn + kPad) * sizeof(typename KeyOf<Real>::type), &h->dev_bytes);
-        em_voxel_occupancy<Real, Real>(h->vox_blocks_real);
-        em_voxel_occupancy<Real, double>(h->vox_blocks_f64);
-        for (int c = 0; c < 2 * kVoxClasses; ++c) {
-            h->vox_blocks_real[c] *= h->num_sms;
-            h->vox_blocks_f64[c] *= h->num_sms;
-        }
-    }
 
     // --- tiles of consecutive muons fitting the shared-memory stage ----------
     // (only for the TMA tile pass)
@@ -970,7 +1085,7 @@ void prepare_em(muto_handle* h) {
     h->ntiles = 0;
     h->tile_pairs = 0;
     h->tile_muons = 0;
-    if (P.muon_pass == 1) {
+    if (P.muon_pass == 1 && h->lists == kListsVoxelMajor) {
         uint64_t maxpath = 0;
         for (uint64_t i = 0; i < N; ++i) maxpath = std::max<uint64_t>(maxpath, off_h[i + 1] - off_h[i]);
         int TP = P.tile_pairs > 0 ? P.tile_pairs : (std::is_same<Real, double>::value ? 1024 : 2048);
@@ -1009,14 +1124,26 @@ void prepare_em(muto_handle* h) {
             h->brick = true;
             h->lam_b.alloc(h->vb * sizeof(Real), &h->dev_bytes);
             CK(cudaMemsetAsync(h->lam_b.as<void>(), 0, h->vb * sizeof(Real), s));
-            run(h, "brick_indices", [&] {
-                launch_brick_indices(h->vidx.as<uint32_t>(), Pn, h->bdims, static_cast<uint32_t>(V), s);
-            });
+            if (h->lists != kListsRecompute)
+                run(h, "brick_indices", [&] {
+                    launch_brick_indices(h->vidx.as<uint32_t>(), Pn, h->bdims, static_cast<uint32_t>(V), s);
+                });
         }
     }
     h->lam.alloc(V * sizeof(Real), &h->dev_bytes);
-    h->win.alloc(2 * V * sizeof(Real), &h->dev_bytes);
-    CK(cudaMemsetAsync(h->win.as<void>(), 0, 2 * V * sizeof(Real), s));  // half-width 0: no prediction yet
+    h->gsum.release();
+    h->win.release();
+    if (h->lists == kListsVoxelMajor) {
+        h->win.alloc(2 * V * sizeof(Real), &h->dev_bytes);
+        CK(cudaMemsetAsync(h->win.as<void>(), 0, 2 * V * sizeof(Real), s));  // half-width 0: no prediction yet
+    } else {  // the per-voxel sums of g_ij, in the index space of the gathered lambda
+        const uint64_t ng = h->brick ? h->vb : V;
+        h->gsum.alloc((ng + kPad) * sizeof(Real), &h->dev_bytes);
+        CK(cudaMemsetAsync(h->gsum.as<void>(), 0, (ng + kPad) * sizeof(Real), s));
+        // the split form's per-muon coefficients
+        if (h->lists == kListsMuonMajor) h->kvec.alloc((N + kPad) * sizeof(R4), &h->dev_bytes);
+        h->kslot.release();
+    }
     {
         std::vector<Real> init_r(init.begin(), init.end());
         CK(cudaMemcpyAsync(h->lam.as<void>(), init_r.data(), V * sizeof(Real), cudaMemcpyHostToDevice, s));
@@ -1065,6 +1192,141 @@ MuonPassArgs<Real> muon_args(muto_handle* h, const Real* lam, bool cost) {
     a.compute_cost = cost ? 1 : 0;
     a.ctr = h->ctr();
     return a;
+}
+
+// The mean-update pass over muon-major lists or recomputed paths: lambda
+// (voxel order) is copied to its bricked order first when the path indices
+// are bricked; the pass adds every g_ij to h->gsum.
+template <typename Real>
+void launch_fused_pass(muto_handle* h, const Real* lam, bool cost, cudaStream_t s) {
+    using R4 = typename Vec4<Real>::type;
+    const Params& P = h->P;
+    const double exy = P.error_xy, ezo = P.error_dz_outer, ezi = P.error_dz_inner;  // src/MutoMLSD.cpp:168-170
+    FusedArgs<Real> a{};
+    a.off = h->off.as<uint64_t>();
+    a.vidx = h->vidx.as<uint32_t>();
+    a.L = h->L.as<Real>();
+    a.T = h->T.as<Real>();
+    a.sd = h->sd.as<R4>();
+    a.pr2 = h->pr2.as<Real>();
+    a.lam = lam;
+    a.V = static_cast<uint32_t>(h->V());
+    const bool split = h->lists == kListsMuonMajor && h->fused_variant == kFusedVariants;
+    if (h->brick) {  // (the split form's muon pass refreshes the bricked copy itself)
+        if (!split) launch_brick_lambda<Real>(lam, static_cast<uint32_t>(h->V()), h->bdims, h->lam_b.as<Real>(), s);
+        a.lam = h->lam_b.as<Real>();
+        a.V = static_cast<uint32_t>(h->vb);
+    }
+    a.G = h->gsum.as<Real>();
+    a.N = static_cast<uint32_t>(h->N);
+    a.E00 = 4.0 * exy * exy / (ezo * ezo);
+    a.E11 = 2.0 * exy * exy * (1.0 + (ezi / ezo + 1.0) * ezi / ezo);
+    a.E01 = 2.0 * exy * exy * ezi / (ezo * ezo);
+    a.compute_cost = cost ? 1 : 0;
+    a.prefetch = P.fused_prefetch ? 1 : 0;
+    a.ctr = h->ctr();
+    if (h->lists == kListsMuonMajor && h->fused_variant == kFusedVariants) {
+        // split form: the muon pass writes every muon's coefficients, the scatter adds g_ij
+        const MuonPassArgs<Real> m = muon_args<Real>(h, lam, cost);
+        launch_muon_pass<Real>(h, m, s);
+        launch_em_scatter<Real>(a, h->kvec.as<R4>(), h->scatter_group, h->scatter_blocks, s);
+        return;
+    }
+    if (h->lists == kListsRecompute) {
+        a.rays = h->rays.as<muto_ray>();
+        a.kept = h->kept.as<uint32_t>();
+        a.scat = h->scat.as<double>();
+        a.ltot = h->ltot.as<double>();
+        a.g = make_dev_grid(h->grid);
+        a.straight = P.straight_line ? 1 : 0;
+        a.bdims = h->bdims;
+        a.brick = h->brick ? 1 : 0;
+        launch_em_fused_walk<Real>(a, h->num_sms, s);
+    } else {
+        launch_em_fused<Real>(a, h->fused_variant, h->fused_blocks, s);
+    }
+}
+
+// the voxel side of a mean-update pass: out = l + l^2 G / (2M) (or the
+// gradient into grad); clears h->gsum
+template <typename Real, typename OutT>
+void launch_fused_update(muto_handle* h, const Real* lam, OutT* out, double* grad, const double* lam64,
+                         cudaStream_t s) {
+    launch_mean_update<Real, OutT>(lam, h->gsum.as<Real>(), h->mult.as<uint32_t>(), static_cast<uint32_t>(h->V()),
+                                   h->brick ? &h->bdims : nullptr, out, grad, lam64, s);
+}
+
+// In-project autotuner of the stored-list pass: the variants whose held
+// pairs suit the scan's mean path, timed on the scan's own lists (one
+// warm-up and two timed launches each); the per-voxel sums are cleared after.
+template <typename Real>
+void autotune_fused(muto_handle* h) {
+    if (h->lists != kListsMuonMajor || h->N == 0) return;
+    HostPhase ph(h, "autotune");
+    const double avg = static_cast<double>(h->npairs) / static_cast<double>(h->N);
+    std::vector<int> cands;
+    const bool forced = h->P.fused_variant >= 0;
+    if (forced) cands.push_back(h->P.fused_variant);
+    for (int v = 0; v < kFusedVariants && !forced; ++v) {
+        const int held = fused_variant_held(v);
+        // a one-pass variant is a candidate when its lanes per muon suit the
+        // mean path: 4 or 8 lanes below 48 pairs, 8 or 16 up to 160, 16 beyond
+        const int g = fused_variant_group(v);
+        const bool fit = avg < 48.0 ? g <= 8 && held <= 64 : avg < 160.0 ? g >= 8 && held <= 128 : g == 16;
+        if (fit) cands.push_back(v);
+    }
+    if (!forced) cands.push_back(kFusedVariants);  // the split form
+    auto apply = [&](int v) {
+        h->fused_variant = v;
+        if (v == kFusedVariants) {  // split: the warp-batched muon pass and the scatter pass
+            const int g = avg <= 32 ? 8 : (avg <= 64 ? 16 : 32);
+            h->muon_kind = 2;
+            h->muon_group = g;
+            h->warp_blocks = em_muon_warp_blocks<Real>(g) * h->num_sms;
+            h->scatter_group = g;
+            h->scatter_blocks = em_scatter_blocks<Real>(g) * h->num_sms;
+        } else {
+            h->fused_blocks = em_fused_blocks<Real>(v) * h->num_sms;
+        }
+    };
+    if (cands.size() == 1) {
+        apply(cands[0]);
+        return;
+    }
+    cudaStream_t s = h->stream;
+    Counters saved;
+    CK(cudaMemcpyAsync(&saved, h->ctr(), sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int pick = cands[0];
+    for (size_t i = 0; i < cands.size(); ++i) {
+        apply(cands[i]);
+        launch_fused_pass<Real>(h, h->lam.as<Real>(), false, s);
+        CK(cudaEventRecord(e0, s));
+        for (int r = 0; r < 2; ++r) launch_fused_pass<Real>(h, h->lam.as<Real>(), false, s);
+        CK(cudaEventRecord(e1, s));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaGetLastError());
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= 2.f;
+        if (i < 4) h->tune_ms[i] = ms;
+        if (ms < best) {
+            best = ms;
+            pick = cands[i];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    h->launches += 3 * cands.size() * (h->brick ? 2 : 1);
+    apply(pick);
+    const uint64_t ng = h->brick ? h->vb : h->V();
+    CK(cudaMemsetAsync(h->gsum.as<void>(), 0, (ng + kPad) * sizeof(Real), s));
+    CK(cudaMemcpyAsync(h->ctr(), &saved, sizeof(Counters), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
 }
 
 // Choices of the muon-pass tuner, kept for the process: scans of the same
@@ -1202,6 +1464,27 @@ template <typename Real>
 void enqueue_iteration(muto_handle* h) {
     const Params& P = h->P;
     cudaStream_t s = h->stream;
+    const uint32_t cap = static_cast<uint32_t>(h->cost_hist.bytes() / sizeof(double));
+    if (h->lists != kListsVoxelMajor) {  // the mean update over muon-major lists or recomputed paths
+        run(h, "em_fused", [&] { launch_fused_pass<Real>(h, h->lam.as<Real>(), h->want_cost(), s); });
+        if (h->method == kMap) {  // ML step into lambda_ML, then the MAP step (src/MutoMAP.cpp:138-184)
+            run(h, "em_update", [&] {
+                launch_fused_update<Real, double>(h, h->lam.as<Real>(), h->lam_ml.as<double>(), nullptr, nullptr, s);
+            });
+            MapParams mp{P.beta, P.p, P.delta, P.eps, P.all_neighbours, P.add_object_prior, P.newton_max_iter};
+            run(h, "map_voxel", [&] {
+                launch_map_voxel<Real>(h->lam.as<Real>(), h->lam_ml.as<double>(), h->mult.as<uint32_t>(),
+                                       make_dev_grid(h->grid), mp, h->ctr(), s);
+            });
+            run(h, "map_copy", [&] { launch_copy_to<Real>(h->lam_ml.as<double>(), h->lam.as<Real>(), h->V(), s); });
+        } else {  // each thread reads only its own voxel's lambda before writing it: in place
+            run(h, "em_update", [&] {
+                launch_fused_update<Real, Real>(h, h->lam.as<Real>(), h->lam.as<Real>(), nullptr, nullptr, s);
+            });
+        }
+        run(h, "cost", [&] { launch_finalize_cost(h->ctr(), static_cast<double>(h->N), h->cost_hist.as<double>(), cap, s); });
+        return;
+    }
     const MuonPassArgs<Real> a = muon_args<Real>(h, h->lam.as<Real>(), h->want_cost());
     run(h, "em_muon", [&] { launch_muon_pass<Real>(h, a, s); });
     const int mode = voxel_mode(P);
@@ -1218,7 +1501,6 @@ void enqueue_iteration(muto_handle* h) {
         const auto v = voxel_args<Real, Real>(h, h->lam.as<Real>(), mode, h->lam.as<Real>());
         run(h, "em_voxel", [&] { launch_voxel_pass<Real, Real>(h, v, s); });
     }
-    const uint32_t cap = static_cast<uint32_t>(h->cost_hist.bytes() / sizeof(double));
     run(h, "cost", [&] { launch_finalize_cost(h->ctr(), static_cast<double>(h->N), h->cost_hist.as<double>(), cap, s); });
 }
 
@@ -1327,15 +1609,24 @@ double nll_eval(muto_handle* h, const double* loglam_host, double* grad_host) {
     CK(cudaMemcpyAsync(&c0, h->ctr(), sizeof(Counters), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     CK(cudaMemsetAsync(&h->ctr()->cost_sum, 0, sizeof(double), s));
+    CK(cudaMemsetAsync(h->fval.as<void>(), 0, sizeof(double), s));
+    if (h->lists != kListsVoxelMajor) {
+        // one pass over the muon-major lists (or the paths walked again): the
+        // cost and the per-voxel sums of g_ij; d NLL / d log l_j = -l_j sum_i g_ij
+        run(h, grad_host ? "nll_backward" : "nll_forward", [&] { launch_fused_pass<Real>(h, lam_r, true, s); });
+        run(h, "em_update_grad", [&] {
+            launch_fused_update<Real, Real>(h, lam_r, nullptr, h->grad.as<double>(), h->lam64.as<double>(), s);
+        });
+    } else {
     const MuonPassArgs<Real> a = muon_args<Real>(h, lam_r, true);
     run(h, grad_host ? "nll_backward" : "nll_forward",
         [&] { launch_muon_pass<Real>(h, a, s); });
-    CK(cudaMemsetAsync(h->fval.as<void>(), 0, sizeof(double), s));
     if (grad_host) {  // d NLL / d log l_j = -l_j sum_i g_ij, per voxel
         auto v = voxel_args<Real, Real>(h, lam_r, kVoxGradient, nullptr);
         v.grad = h->grad.as<double>();
         v.lam64 = h->lam64.as<double>();
         run(h, "em_voxel_grad", [&] { launch_voxel_pass<Real, Real>(h, v, s); });
+    }
     }
     const Params& P = h->P;
     if (h->method == kMap) {
@@ -1541,6 +1832,23 @@ int muto_get_status(const muto_handle* hc, muto_status* out) {
     out->muon_group = h->muon_kind == 2 ? h->muon_group : h->group;
     out->tile_pairs = h->tile_pairs;
     out->tile_muons = h->tile_muons;
+    out->path_lists = h->method == kPoca ? 0 : h->lists;
+    if (h->method != kPoca && h->lists == kListsMuonMajor && h->fused_variant == kFusedVariants) {
+        out->muon_pass = 5;
+        out->muon_group = h->scatter_group;
+        out->tile_pairs = 0;
+        out->tile_muons = 0;
+    } else if (h->method != kPoca && h->lists == kListsMuonMajor) {
+        out->muon_pass = 3;
+        out->muon_group = fused_variant_group(h->fused_variant);
+        out->tile_pairs = fused_variant_held(h->fused_variant);
+        out->tile_muons = 32;
+    } else if (h->method != kPoca && h->lists == kListsRecompute) {
+        out->muon_pass = 4;
+        out->muon_group = 1;
+        out->tile_pairs = 0;
+        out->tile_muons = 0;
+    }
     std::snprintf(out->message, sizeof(out->message), "%s", h->last_msg.c_str());
     return MUTO_OK;
 }
@@ -1596,10 +1904,12 @@ int muto_prepare(muto_handle* h) {
             prepare_poca(h);
         } else if (h->fp64()) {
             prepare_em<double>(h);
-            autotune_muon_pass<double>(h);
+            if (h->lists == kListsVoxelMajor) autotune_muon_pass<double>(h);
+            else autotune_fused<double>(h);
         } else {
             prepare_em<float>(h);
-            autotune_muon_pass<float>(h);
+            if (h->lists == kListsVoxelMajor) autotune_muon_pass<float>(h);
+            else autotune_fused<float>(h);
         }
         sync_and_harvest(h, pf);
         h->prepared = true;
@@ -1714,6 +2024,8 @@ int muto_export_paths(muto_handle* h, uint32_t* kept, double* info, uint64_t* of
     return guarded(h, [&] {
         n_prepared_check(h);
         if (h->method == kPoca) throw Error(MUTO_ERR_STATE, "PoCA stores no paths");
+        if (h->lists == kListsRecompute && (idx || len || tail || off))
+            throw Error(MUTO_ERR_STATE, "path_lists \"recompute\" stores no paths");
         cudaStream_t s = h->stream;
         const uint64_t N = h->N, Pn = h->npairs;
         if (kept && N) CK(cudaMemcpyAsync(kept, h->kept.as<void>(), N * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));

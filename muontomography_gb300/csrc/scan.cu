@@ -124,3 +124,18 @@ void scan_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n, void* scratc
 }
 
 }  // namespace muto
+
+namespace muto {
+namespace {
+__global__ void k_add_u64(uint64_t* __restrict__ a, uint64_t n, uint64_t add) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) a[i] += add;
+}
+}  // namespace
+
+void launch_add_u64(uint64_t* a, uint64_t n, uint64_t add, cudaStream_t s) {
+    if (n == 0 || add == 0) return;
+    k_add_u64<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(a, n, add);
+    count_launches(1);
+}
+}  // namespace muto

@@ -212,17 +212,17 @@ __global__ void k_path_bound(const muto_ray* __restrict__ rays, const uint32_t* 
     }
 }
 
-// the fill walk into bounded slots [boff[i], boff[i+1]); counts[i] = the
-// path's length (0 for a walk that hit its step guard, as in the count walk)
+// the fill walk into bounded slots [boff[i], boff[i+1]) - slot_base; counts[i]
+// = the path's length (0 for a walk that hit its step guard, as in the count walk)
 template <typename Real>
 __global__ void k_path_fill_bounded(const muto_ray* __restrict__ rays, const uint32_t* __restrict__ kept,
                                     const double* __restrict__ scat, const uint64_t* __restrict__ boff, uint64_t n,
                                     DevGrid g, int straight, uint32_t* __restrict__ vidx, double* __restrict__ l64,
                                     Real* __restrict__ L, Real* __restrict__ T, uint32_t* __restrict__ counts,
-                                    Counters* ctr) {
+                                    Counters* ctr, uint64_t slot_base) {
     const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint64_t b = boff[i], e = boff[i + 1];
+    const uint64_t b = boff[i] - slot_base, e = boff[i + 1] - slot_base;
     const muto_ray& r = rays[kept[i]];
     const double ps[3] = {scat[3 * i], scat[3 * i + 1], scat[3 * i + 2]};
     const uint32_t nx = g.n[0], nxy = g.n[0] * g.n[1];
@@ -260,16 +260,16 @@ __global__ void k_path_fill_bounded(const muto_ray* __restrict__ rays, const uin
     }
 }
 
-// warp per muon: its path from the bounded slots to the exact ones
+// warp per muon: its path from the bounded slots (boff[i] - slot_base) to the exact ones
 template <typename Real>
-__global__ void k_path_compact(const uint64_t* __restrict__ boff, const uint64_t* __restrict__ off, uint64_t n,
-                               const uint32_t* __restrict__ vidx_b, const Real* __restrict__ L_b,
+__global__ void k_path_compact(const uint64_t* __restrict__ boff, uint64_t slot_base, const uint64_t* __restrict__ off,
+                               uint64_t n, const uint32_t* __restrict__ vidx_b, const Real* __restrict__ L_b,
                                const Real* __restrict__ T_b, uint32_t* __restrict__ vidx, Real* __restrict__ L,
                                Real* __restrict__ T) {
     const uint64_t i = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= n) return;
-    const uint64_t src = boff[i], dst = off[i], m = off[i + 1] - dst;
+    const uint64_t src = boff[i] - slot_base, dst = off[i], m = off[i + 1] - dst;
     for (uint64_t k = lane; k < m; k += 32) {
         vidx[dst + k] = vidx_b[src + k];
         L[dst + k] = L_b[src + k];
@@ -525,31 +525,33 @@ void launch_path_bound(const muto_ray* rays, const uint32_t* kept, const double*
 
 template <typename Real>
 void launch_path_fill_bounded(const muto_ray* rays, const uint32_t* kept, const double* scat, const uint64_t* boff,
-                              uint64_t n, muto_grid g, int straight, uint32_t* vidx, double* l64, Real* L, Real* T,
-                              uint32_t* counts, Counters* ctr, cudaStream_t s) {
+                              uint64_t slot_base, uint64_t n, muto_grid g, int straight, uint32_t* vidx, double* l64,
+                              Real* L, Real* T, uint32_t* counts, Counters* ctr, cudaStream_t s) {
     if (n == 0) return;
     k_path_fill_bounded<Real><<<blocks_for(n, 128), 128, 0, s>>>(rays, kept, scat, boff, n, make_dev_grid(g), straight,
-                                                                  vidx, l64, L, T, counts, ctr);
+                                                                  vidx, l64, L, T, counts, ctr, slot_base);
     count_launches(1);
 }
 template void launch_path_fill_bounded<float>(const muto_ray*, const uint32_t*, const double*, const uint64_t*,
-                                              uint64_t, muto_grid, int, uint32_t*, double*, float*, float*, uint32_t*,
-                                              Counters*, cudaStream_t);
+                                              uint64_t, uint64_t, muto_grid, int, uint32_t*, double*, float*, float*,
+                                              uint32_t*, Counters*, cudaStream_t);
 template void launch_path_fill_bounded<double>(const muto_ray*, const uint32_t*, const double*, const uint64_t*,
-                                               uint64_t, muto_grid, int, uint32_t*, double*, double*, double*,
-                                               uint32_t*, Counters*, cudaStream_t);
+                                               uint64_t, uint64_t, muto_grid, int, uint32_t*, double*, double*,
+                                               double*, uint32_t*, Counters*, cudaStream_t);
 
 template <typename Real>
-void launch_path_compact(const uint64_t* boff, const uint64_t* off, uint64_t n, const uint32_t* vidx_b,
-                         const Real* L_b, const Real* T_b, uint32_t* vidx, Real* L, Real* T, cudaStream_t s) {
+void launch_path_compact(const uint64_t* boff, uint64_t slot_base, const uint64_t* off, uint64_t n,
+                         const uint32_t* vidx_b, const Real* L_b, const Real* T_b, uint32_t* vidx, Real* L, Real* T,
+                         cudaStream_t s) {
     if (n == 0) return;
-    k_path_compact<Real><<<blocks_for(n * 32), kThreads, 0, s>>>(boff, off, n, vidx_b, L_b, T_b, vidx, L, T);
+    k_path_compact<Real><<<blocks_for(n * 32), kThreads, 0, s>>>(boff, slot_base, off, n, vidx_b, L_b, T_b, vidx, L,
+                                                                 T);
     count_launches(1);
 }
-template void launch_path_compact<float>(const uint64_t*, const uint64_t*, uint64_t, const uint32_t*, const float*,
-                                         const float*, uint32_t*, float*, float*, cudaStream_t);
-template void launch_path_compact<double>(const uint64_t*, const uint64_t*, uint64_t, const uint32_t*, const double*,
-                                          const double*, uint32_t*, double*, double*, cudaStream_t);
+template void launch_path_compact<float>(const uint64_t*, uint64_t, const uint64_t*, uint64_t, const uint32_t*,
+                                         const float*, const float*, uint32_t*, float*, float*, cudaStream_t);
+template void launch_path_compact<double>(const uint64_t*, uint64_t, const uint64_t*, uint64_t, const uint32_t*,
+                                          const double*, const double*, uint32_t*, double*, double*, cudaStream_t);
 
 void launch_offset_voxels(uint32_t* vidx, uint64_t n, uint32_t v_scan, uint32_t voff, cudaStream_t s) {
     if (n == 0) return;
