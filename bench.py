@@ -1,17 +1,26 @@
 #!/usr/bin/env python
 """MLSD EM iteration throughput (muon-voxel updates per second) on one scan.
 
-Default workload: the 100^3-voxel, 2 cm, 10M-muon scan (iron / lead /
-aluminium blocks and a concrete slab, momentum known per muon), median EM
-update (the reference's default), mixed precision, graph-captured iteration.
-A step is one EM iteration over all kept muons; value = muon-voxel pairs per
-iteration x steps / time.  Inputs are synthetic (seeded generator), resident
-in HBM before the timed region; the per-iteration working set (lists, S) is
-far larger than L2, so no flush is needed between steps.
+Default workload: the largest single scan -- 256x256x128 voxels of 10 mm
+(8.4 M voxels) with 100 M muons through 12 mixed iron / lead / aluminium /
+concrete blocks, momentum known per muon -- reconstructed with the mean EM
+update over stored muon-major lists (int32 voxel index, FP32 L and T), mixed
+precision, graph-captured iteration.  A step is one EM iteration over all
+kept muons; value = muon-voxel pairs per iteration x steps / time.  Inputs
+are synthetic (seeded generator), resident in HBM before the timed region;
+the lists read every iteration (118 GB) are far larger than L2, so no flush
+is needed between steps.  Beside it, the same line carries: the recomputed-
+paths variant, PoCA on the same tracks, an end-to-end reconstruct from
+pinned host tracks, time to lambda (mixed vs the FP64 GPU form) and the CPU
+port of the reference on a sample.
+
+--workload cube100_20mm runs the 100^3 scan with the median update (the
+reference's default) over the voxel-major lists.
 
 --impl reference times the reference's CPU implementation of the same path
 (the FP64 restatement in oracle/, serial muon loop + OpenMP voxel loop, all
-host cores) on a bounded sample of the same workload.
+host cores) on a bounded sample of the same workload, with tracks made by
+the oracle's own build of the generator (the product library is not loaded).
 """
 from __future__ import annotations
 
@@ -33,15 +42,41 @@ sys.path.insert(0, str(ROOT))
 
 # --workload choices: grid, voxel size and muon count of each scan
 WORKLOADS = {
-    "cube100_20mm": lambda W: W.cube100_20mm,  # 100^3 voxels of 20 mm, 10 M muons (default)
+    "grid256x256x128_10mm": lambda W: W.grid256x256x128_10mm,  # 256x256x128 voxels of 10 mm, 100 M muons (default)
+    "cube100_20mm": lambda W: W.cube100_20mm,  # 100^3 voxels of 20 mm, 10 M muons
     "cube50_40mm": lambda W: W.cube50_40mm,  # the same scene on 50^3 voxels of 40 mm, 2.5 M muons
     "cube20_50mm": lambda W: W.cube20_50mm,  # 20^3 voxels of 50 mm, 100 k muons
     "map128x128x64_15mm": lambda W: W.map128x128x64_15mm,  # 128x128x64 voxels of 15 mm, 20 M muons
-    "grid256x256x128_10mm": lambda W: W.grid256x256x128_10mm,  # 256x256x128 voxels of 10 mm, 100 M muons
+}
+# the EM update each workload is benchmarked with: the throughput scan with
+# the mean update (its per-voxel lists do not fit next to the muon-major
+# ones), the others with the reference's default median
+DEFAULT_MODE = {"grid256x256x128_10mm": "mean"}
+
+METRIC = "EM-iter muon·voxel updates/s"  # the headline metric's own wording
+UNIT = "muon·voxel updates/s"
+
+# DRAM bytes (read + write) per pair per launch from ncu captures of each
+# kernel (mixed form), scaled by a run's pairs: the full workloads are above
+# the capture size the profiler is run at.  Captures:
+# profiles/em_split_grid256x256x128_10mm_2M.md (the 256x256x128 grid with 2 M
+# muons, mean update, 195 962 860 pairs) and
+# profiles/em_passes_cube50_40mm_2.5M.md (the 100^3 scene on 50^3 voxels,
+# median update, 68 700 086 pairs).
+TRAFFIC_PER_PAIR = {
+    ("grid256", "em_muon"): (2.461415e9 + 7.902976e6) / 195962860,
+    ("grid256", "em_scatter"): (2.598490e9 + 10.157312e6) / 195962860,
+    ("cube", "em_muon"): 868.4e6 / 68700086,
+    ("cube", "em_voxel"): 1371.0e6 / 68700086,
 }
 
-METRIC = "EM-iter muon\u00b7voxel updates/s"  # the headline metric's own wording
-UNIT = "muon\u00b7voxel updates/s"
+# set-up kernels and host phases reported by the library's profiler
+SETUP_KERNELS = ["keep_flags", "scan", "compact", "muon_info", "siddon_count", "siddon_fill", "voxel_offset",
+                 "voxel_hist", "voxel_major", "voxel_classes", "path_bound", "path_compact", "path_stats"]
+SETUP_PHASES = ["gather", "info_count", "fill", "path_stats", "voxel_major", "classes", "tiles", "image",
+                "autotune"]
+ITER_KERNELS = ["em_muon", "em_scatter", "em_fused", "em_walk", "em_voxel", "em_update", "brick_lambda", "map_voxel",
+                "map_copy", "cost"]
 
 
 def peaks() -> dict:
@@ -50,6 +85,14 @@ def peaks() -> dict:
         d = json.loads(p.read_text())
         return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
     return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def host_cores() -> int:
+    """Cores this process may run on (affinity / cgroup cpuset), not the machine's count."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
 
 
 class ClockSampler:
@@ -128,27 +171,24 @@ def workload(args, rank: int):
     return wl
 
 
-# DRAM bytes per pair per launch, measured by ncu (--set full) on the 50^3-voxel
-# 2.5 M-muon case of the default scene (median EM, mixed form): muon pass
-# 868.4 MB and voxel pass (key pass and all classes) 1378.5 MB for 68 700 086 pairs
-TRAFFIC_PER_PAIR = {"muon": 868.4e6 / 68700086, "voxel": 1371.0e6 / 68700086}
-
-# set-up kernels and host phases reported by the library's profiler
-SETUP_KERNELS = ["keep_flags", "scan", "compact", "muon_info", "siddon_count", "siddon_fill", "voxel_offset",
-                 "voxel_hist", "voxel_major", "voxel_classes", "path_bound", "path_compact"]
-SETUP_PHASES = ["gather", "info_count", "offsets", "fill", "voxel_major", "classes", "tiles", "image", "autotune"]
-
-
 def method_of(args) -> str:
     """MAP for the MAP workload (128x128x64 voxels of 15 mm), MLSD otherwise."""
     return "map" if args.workload.startswith("map") else "mlsd"
 
 
-def em_config(wl, args, precision: str, n_iter: int) -> dict:
+def wl_lambda(wl) -> np.ndarray:
+    """The workload's phantom, rasterised without the product library."""
+    from muontomography_gb300 import X0_MM
+    from oracle import synthetic as S
+
+    return S.phantom(wl.grid, wl.blocks, X0_MM["air"], 3.0)
+
+
+def em_config(wl, args, precision: str, n_iter: int, lists: str | None = None) -> dict:
     over = {"precision": precision, "num_iteration": n_iter, "muon_pass": args.muon_pass,
-            "muon_layout": args.muon_layout}
+            "muon_layout": args.muon_layout, "path_lists": lists or args.lists}
     if method_of(args) == "map":  # beta 0.01, p = 1, the 26-neighbour stencil, delta = 0.1 median(lambda) 1e7
-        over.update(beta=0.01, p=1.0, all_neighbours=True, delta=0.1 * float(np.median(wl.lam())) * 1e7)
+        over.update(beta=0.01, p=1.0, all_neighbours=True, delta=0.1 * float(np.median(wl_lambda(wl))) * 1e7)
     if getattr(args, "voxel_stream_above", None) is not None:
         over["voxel_stream_above"] = args.voxel_stream_above
     if args.mode == "mean":
@@ -156,13 +196,11 @@ def em_config(wl, args, precision: str, n_iter: int) -> dict:
     return wl.em_config(**over)
 
 
-def cpu_port(wl, args, n_sample: int, n_iter: int, threads: int) -> dict:
-    """Time the CPU restatement of the reference path on a sample of the workload."""
+def cpu_port(wl, args, rays: np.ndarray, n_iter: int, threads: int) -> dict:
+    """Time the CPU restatement of the reference path on a sample of the workload's tracks."""
     os.environ["OMP_NUM_THREADS"] = str(threads)
-    import muontomography_gb300 as M
     from oracle import oracle as O
 
-    rays = M.generate(wl.grid, wl.lam(), n_sample, wl.seed)
     cfg = em_config(wl, args, "fp64", n_iter)
     init = np.full(wl.grid.nvox, 1e-7)
     t0 = time.perf_counter()
@@ -174,17 +212,29 @@ def cpu_port(wl, args, n_sample: int, n_iter: int, threads: int) -> dict:
         t0 = time.perf_counter()
         ref.iterate(1)
         times.append(time.perf_counter() - t0)
-    return {"pairs": pairs, "times": times, "setup_s": t_setup, "n_sample": n_sample}
+    return {"pairs": pairs, "times": times, "setup_s": t_setup, "n_sample": rays.shape[0]}
+
+
+def reference_sample(steps: int, warmup: int, cap: int) -> int:
+    """Muons of the reference leg's sample: about 150 s of EM iterations at the
+    port's ~1.5e7 pairs/s with ~100 pairs per sampled muon, at most `cap`."""
+    per_step_s = 150.0 / max(steps + warmup, 1)
+    return int(min(cap, max(20_000, per_step_s * 1.5e7 / 100.0)))
 
 
 def run_reference(args) -> int:
     rank, world, local = dist_env()
     if rank != 0:
         return 0
+    from oracle import synthetic as S
+
     wl = workload(args, 0)
-    threads = os.cpu_count() or 1
-    n_sample = args.cpu_sample
-    r = cpu_port(wl, args, n_sample, args.warmup + args.steps, threads)
+    threads = host_cores()
+    n_sample = args.cpu_sample if args.cpu_sample_fixed else reference_sample(args.steps, args.warmup, args.cpu_sample)
+    t0 = time.perf_counter()
+    rays = S.generate(wl.grid, wl_lambda(wl), n_sample, wl.seed)  # the first n_sample muons of the workload's stream
+    t_gen = time.perf_counter() - t0
+    r = cpu_port(wl, args, rays, args.warmup + args.steps, threads)
     t = r["times"][args.warmup:]
     value = r["pairs"] * len(t) / sum(t)
     line = {
@@ -192,14 +242,27 @@ def run_reference(args) -> int:
         "warmup": args.warmup, "ms_per_step": 1000 * sum(t) / len(t), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": wl.name, "method": method_of(args), "grid": list(wl.grid.shape), "mode": args.mode,
-                   "sample_muons": n_sample, "sample_pairs": r["pairs"]},
+                   "muons": wl.n_muons, "sample_muons": n_sample, "sample_pairs": r["pairs"]},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{n_sample} muons of {wl.name}: one EM iteration per step "
-                                   f"({r['pairs']} pairs), setup {r['setup_s']:.2f} s untimed"},
+                         "sample": f"the first {n_sample} of the {wl.n_muons} muons of {wl.name} "
+                                   f"({r['pairs']} pairs per EM iteration): one EM iteration per step; "
+                                   f"set-up {r['setup_s']:.1f} s and track generation {t_gen:.1f} s untimed"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def algorithmic_bytes(kernel: str, rb: int, P: int, N: int, V: int) -> int:
+    """Bytes a kernel must move per launch (rb: bytes of the storage precision)."""
+    lists = (4 + 2 * rb) * P  # voxel index, L, T of every pair, read once
+    return {
+        "em_muon": lists + (8 + 9 * rb) * N + rb * V,      # + offsets, (S, D), pr^2, k out; lambda gathered
+        "em_scatter": lists + (8 + 4 * rb) * N + rb * V,   # + offsets, k in; G reduced
+        "em_fused": lists + (8 + 5 * rb) * N + 2 * rb * V,  # + offsets, (S, D), pr^2; lambda in, G reduced
+        "em_voxel": lists + (16 + 6 * rb) * V,             # voxel-major lists; descriptor, lambda, window
+        "em_update": (4 + 4 * rb) * V,                     # lambda, M, G in, G cleared, lambda out
+    }.get(kernel, 0)
 
 
 def run_ours(args) -> int:
@@ -228,6 +291,20 @@ def run_ours(args) -> int:
                                         C.c_void_p(torch.cuda.current_stream().cuda_stream)), "generate")
     torch.cuda.synchronize()
     t_gen = time.perf_counter() - t0
+    del lam
+    sp = C.c_void_p()
+
+    def stream_of(rec):
+        lib.muto_get_stream(rec._h, C.byref(sp))
+        return torch.cuda.ExternalStream(sp.value)
+
+    def setup_stats(rec) -> dict:
+        out = {}
+        for name in SETUP_KERNELS + ["host:" + p for p in SETUP_PHASES]:
+            cnt, tot = rec.kernel_stats(name)
+            if cnt:
+                out[name] = round(tot, 3)
+        return out
 
     # ---- value: EM iterations with the tracks resident in HBM ---------------
     cfg = em_config(wl, args, args.precision, args.warmup + args.steps)
@@ -237,16 +314,10 @@ def run_ours(args) -> int:
     t0 = time.perf_counter()
     rec.prepare()
     t_setup = time.perf_counter() - t0
-    setup_ms = {}
-    for name in SETUP_KERNELS + ["host:" + p for p in SETUP_PHASES]:
-        cnt, tot = rec.kernel_stats(name)
-        if cnt:
-            setup_ms[name] = round(tot, 3)
+    setup_ms = setup_stats(rec)
     st = rec.status()
     pairs, kept, V = st["n_pairs"], st["n_scat_in_grid"], wl.grid.nvox
-    sp = C.c_void_p()
-    lib.muto_get_stream(rec._h, C.byref(sp))
-    stream = torch.cuda.ExternalStream(sp.value)
+    stream = stream_of(rec)
     for _ in range(args.warmup):
         rec.iterate(1)
     cnt, tot = rec.kernel_stats("host:graph_capture")
@@ -272,55 +343,58 @@ def run_ours(args) -> int:
     ms = allmax(ms_local)
     total_pairs = allsum(float(pairs))
     value = total_pairs * args.steps / (ms / 1000.0)
-    nm_, tm_ = rec.kernel_stats("em_muon")
-    nv_, tv = rec.kernel_stats("em_voxel")
+    kern = {}
+    for k in ITER_KERNELS:
+        c, t = rec.kernel_stats(k)
+        if c:
+            kern[k] = t / args.steps  # ms per iteration (all launches of that name in one iteration)
     rec.set_profiling(False)
     rec.close()
 
-    # algorithmic bytes per launch (mixed: 4-byte index, L, T; fp64: 8-byte L, T)
+    # ---- rooflines: every iteration kernel by its algorithmic bytes ----------
     rb = 4 if args.precision == "mixed" else 8
-    muon_bytes = (4 + 2 * rb) * pairs + (4 * rb + rb + 8 + 4 * rb) * kept + rb * V  # lists, S/D/pr2/off, k out, lambda
-    voxel_bytes = (4 + 2 * rb) * pairs + (16 + 6 * rb) * V  # voxel-major lists; descriptor, lambda in/out, window in/out
     pk = peaks()
-    muon_ms = tm_ / max(nm_, 1)
-    voxel_ms = tv / max(nv_, 1)  # the voxel pass: all class launches of one iteration
-    achieved = muon_bytes / (muon_ms / 1000.0) / 1e9 if nm_ else None
-    v_ach = voxel_bytes / (voxel_ms / 1000.0) / 1e9 if nv_ else None
-    # DRAM traffic (read + write) per launch: ncu's bytes per pair on the 50^3-voxel
-    # case of the same scene, scaled by this run's pairs
-    measured = args.precision == "mixed" and args.mode == "median" and args.workload in ("cube100_20mm", "cube50_40mm")
-    t_voxel = (args.ncu_traffic if args.ncu_traffic is not None
-               else (TRAFFIC_PER_PAIR["voxel"] * pairs if measured else None))
-    t_muon = TRAFFIC_PER_PAIR["muon"] * pairs if measured else None
-    # the voxel pass takes about two thirds of an iteration: it is the dominant kernel
-    roofline = {"bound": "hbm", "achieved": v_ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": (v_ach / pk["hbm_gbs"]) if v_ach else None, "traffic": t_voxel,
-                "kernel": "k_pair_keys + k_em_voxel (one launch per segment-length class)", "kernel_ms": voxel_ms,
-                "algorithmic_bytes": voxel_bytes, "peak_source": pk["source"],
-                "muon_pass": {"kernel": "k_em_muon", "kernel_ms": muon_ms, "algorithmic_bytes": muon_bytes,
-                              "achieved": achieved, "frac": (achieved / pk["hbm_gbs"]) if achieved else None,
-                              "traffic": t_muon}}
+    fam = "grid256" if args.workload.startswith("grid256") else "cube"
+    per_kernel = {}
+    for k, kms in kern.items():
+        b = algorithmic_bytes(k, rb, pairs, kept, V)
+        if not b:
+            continue
+        ach = b / (kms / 1000.0) / 1e9
+        tpp = TRAFFIC_PER_PAIR.get((fam, k)) if args.precision == "mixed" else None
+        per_kernel[k] = {"kernel_ms": kms, "algorithmic_bytes": b, "achieved": ach, "frac": ach / pk["hbm_gbs"],
+                         "traffic": tpp * pairs if tpp else None}
+    dom = max(per_kernel, key=lambda k: per_kernel[k]["kernel_ms"]) if per_kernel else None
+    # one iteration's algorithmic bytes: the lists once, per-muon inputs and cost, lambda in, G, lambda out
+    b_iter = (4 + 2 * rb) * pairs + 24 * kept + 12 * V
+    roofline = {"bound": "hbm", "peak": pk["hbm_gbs"], "unit": "GB/s", "peak_source": pk["source"]}
+    if dom:
+        d = per_kernel[dom]
+        roofline.update(kernel=dom, achieved=d["achieved"], frac=d["frac"], traffic=d["traffic"],
+                        kernel_ms=d["kernel_ms"], algorithmic_bytes=d["algorithmic_bytes"])
+    roofline["kernels"] = per_kernel
+    roofline["iteration"] = {"algorithmic_bytes": b_iter, "ms": ms / args.steps,
+                             "achieved": b_iter / (ms / args.steps / 1000.0) / 1e9,
+                             "frac": b_iter / (ms / args.steps / 1000.0) / 1e9 / pk["hbm_gbs"],
+                             "what": f"{4 + 2 * rb} B per pair (index, L, T) + 24 B per kept muon + 12 B per voxel"}
 
     # ---- e2e: full reconstruct through the C ABI from pinned host tracks ------
     e2e = None
     if args.e2e_steps > 0:
-        host = torch.empty((n, 14), dtype=torch.float64, pin_memory=True)
-        host.copy_(d_rays)
-        del d_rays
-        torch.cuda.empty_cache()
+        hst = torch.empty((n, 14), dtype=torch.float64, pin_memory=True)
+        hst.copy_(d_rays)
         e_iters = args.e2e_iters if args.e2e_iters > 0 else wl.n_iter  # the workload's reconstruct call
         ecfg = em_config(wl, args, args.precision, e_iters)
         out = np.empty(V, np.float64)
         times = []
         for k in range(args.e2e_steps + 1):  # the first call is a warm-up
             r2 = M.Reconstruction(method_of(args), ecfg)
-            lib.muto_get_stream(r2._h, C.byref(sp))
-            s2 = torch.cuda.ExternalStream(sp.value)
+            s2 = stream_of(r2)
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             barrier()
             torch.cuda.synchronize()
             a.record(s2)
-            rc = lib.muto_reconstruct(r2._h, C.c_void_p(host.data_ptr()), n, _lib.dptr(out), V)
+            rc = lib.muto_reconstruct(r2._h, C.c_void_p(hst.data_ptr()), n, _lib.dptr(out), V)
             b.record(s2)
             b.synchronize()
             _lib.check(rc, "muto_reconstruct")
@@ -331,62 +405,110 @@ def run_ours(args) -> int:
         r2 = M.Reconstruction(method_of(args), ecfg)
         r2.set_profiling(True)
         t0 = time.perf_counter()
-        r2.load_tracks(host.numpy())
+        r2.load_tracks(hst.numpy())
         setup_warm = {"load_tracks_h2d": round((time.perf_counter() - t0) * 1e3, 3)}
         t0 = time.perf_counter()
         r2.prepare()
         setup_warm["prepare"] = round((time.perf_counter() - t0) * 1e3, 3)
-        for name in SETUP_KERNELS + ["host:" + p for p in SETUP_PHASES]:
-            cnt, tot = r2.kernel_stats(name)
-            if cnt:
-                setup_warm[name] = round(tot, 3)
+        setup_warm.update(setup_stats(r2))
         r2.close()
+        del hst
         e_ms = allmax(statistics.mean(times))
         e2e = {"value": total_pairs * e_iters / (e_ms / 1000.0), "unit": UNIT,
-               "h2d_bytes_per_step": int(n * 14 * 8), "d2h_bytes_per_step": int(V * rb),
+               "h2d_bytes_per_step": int(n * 14 * 8), "d2h_bytes_per_step": int(V * 8),
                "ms_per_step": e_ms, "em_iterations_per_step": e_iters, "setup_ms": setup_warm,
                "what": "muto_reconstruct: H2D of pinned tracks, setup (gather, Siddon lists), "
                        f"{e_iters} EM iterations (the workload's num_iteration), D2H of the image"}
-    else:
-        host = None
+
+    # ---- stored lists against paths recomputed every iteration ----------------
+    recompute = None
+    if args.recompute_iters > 0 and args.mode == "mean" and rank == 0:
+        r4 = M.Reconstruction(method_of(args), em_config(wl, args, args.precision, 1 + args.recompute_iters,
+                                                         lists="recompute"))
+        r4.load_tracks(None, on_device_ptr=d_rays.data_ptr(), n=n)
+        t0 = time.perf_counter()
+        r4.prepare()
+        r_setup = time.perf_counter() - t0
+        s4 = stream_of(r4)
+        r4.iterate(1)  # graph capture and a first pass
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(s4)
+        for _ in range(args.recompute_iters):
+            r4.iterate(1)
+        b.record(s4)
+        b.synchronize()
+        r_ms = a.elapsed_time(b) / args.recompute_iters
+        r4st = r4.status()
+        r4.close()
+        recompute = {"ms_per_iteration": r_ms, "value": r4st["n_pairs"] / (r_ms / 1000.0), "unit": UNIT,
+                     "setup_s": r_setup, "iterations_timed": args.recompute_iters,
+                     "device_bytes": r4st["device_bytes"], "stored_ms_per_iteration": ms / args.steps,
+                     "stored_device_bytes": st["device_bytes"],
+                     "recompute_over_stored_time": r_ms / (ms / args.steps),
+                     "what": "no stored lists: every path walked in FP64 twice per iteration (sum, scatter)"}
+
+    # ---- PoCA on the same tracks (src/MutoPoCA.cpp:51-134) --------------------
+    poca = None
+    if args.poca and rank == 0:
+        pcfg = wl.poca_config()
+        times = []
+        for k in range(3):  # one warm-up
+            r5 = M.Reconstruction("poca", pcfg)
+            r5.load_tracks(None, on_device_ptr=d_rays.data_ptr(), n=n)
+            r5.set_profiling(True)
+            torch.cuda.synchronize()
+            r5.prepare()
+            c1, t1 = r5.kernel_stats("poca")
+            c2, t2 = r5.kernel_stats("poca_normalize")
+            pst = r5.status()
+            r5.close()
+            if k > 0:
+                times.append((t1, t2))
+        t_poca = statistics.mean(t for t, _ in times)
+        t_norm = statistics.mean(t for _, t in times)
+        pb = n * 112 + 2 * 8 * V  # every track read once; image and weight sums
+        poca = {"rays_per_s": n / ((t_poca + t_norm) / 1000.0), "kernel_ms": t_poca, "normalize_ms": t_norm,
+                "algorithmic_bytes": pb, "achieved": pb / (t_poca / 1000.0) / 1e9,
+                "frac": pb / (t_poca / 1000.0) / 1e9 / pk["hbm_gbs"], "peak": pk["hbm_gbs"],
+                "in_grid": pst["n_scat_in_grid"],
+                "what": "k_poca: FP64 closest approach, binning and the length-weighted Siddon weights of every "
+                        "track (integer fixed-point sums), then the normalisation"}
 
     # ---- time to lambda: mixed vs the plain FP64 form, same iteration count ---
     ttl = None
     if args.ttl_iters > 0 and rank == 0:
-        if host is None:
-            host = torch.empty((n, 14), dtype=torch.float64, pin_memory=True)
-            host.copy_(d_rays)
-            del d_rays
         res = {}
         for prec in ("fp64", "mixed"):
-            d = torch.empty((n, 14), dtype=torch.float64, device="cuda")
-            d.copy_(host)
             r3 = M.Reconstruction(method_of(args), em_config(wl, args, prec, args.ttl_iters))
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            r3.load_tracks(None, on_device_ptr=d.data_ptr(), n=n)
+            r3.load_tracks(None, on_device_ptr=d_rays.data_ptr(), n=n)
             r3.prepare()
             r3.iterate(args.ttl_iters)
             im = r3.image()
-            res[prec] = (time.perf_counter() - t0, im)
+            res[prec] = (time.perf_counter() - t0, im, r3.status()["device_bytes"])
             r3.close()
-            del d
-            torch.cuda.empty_cache()
         a64, b32 = res["fp64"][1].ravel(), res["mixed"][1].ravel()
         rel = float(np.linalg.norm(b32 - a64) / np.linalg.norm(a64))
         ttl = {"iterations": args.ttl_iters, "fp64_s": res["fp64"][0], "mixed_s": res["mixed"][0],
                "rel_l2_mixed_vs_fp64": rel, "speedup": res["fp64"][0] / res["mixed"][0],
-               "within_1e-4": rel < 1e-4}
+               "within_1e-4": rel < 1e-4, "fp64_device_bytes": res["fp64"][2],
+               "what": "set-up and iterations from device-resident tracks, wall clock; the FP64 GPU form stands "
+                       "in for the FP64 oracle at this size"}
 
     # ---- CPU baseline on this machine's host cores (rank 0 only) ----------------
     cpu = None
     if rank == 0 and args.cpu_sample > 0:
-        threads = os.cpu_count() or 1
-        r = cpu_port(wl, args, args.cpu_sample, 2, threads)
+        threads = host_cores()
+        ns = min(args.cpu_sample, n)
+        sample = d_rays[:ns].cpu().numpy()  # the first muons of the workload's stream
+        r = cpu_port(wl, args, sample, 2, threads)
         cval = r["pairs"] * len(r["times"]) / sum(r["times"])
         cpu = {"value": cval, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_sample} muons of the same workload, 2 EM iterations "
-                         f"({r['pairs']} pairs each), setup untimed"}
+               "sample": f"the first {ns} of the {n} muons of the same workload, 2 EM iterations "
+                         f"({r['pairs']} pairs each), set-up untimed"}
+    del d_rays
 
     if rank == 0:
         line = {
@@ -398,16 +520,22 @@ def run_ours(args) -> int:
                        "voxel_mm": wl.grid.dx, "muons": n,
                        "kept_muons": kept, "pairs_per_iteration": pairs, "mode": args.mode,
                        "precision": args.precision, "per_muon_2x2": "f64", "graph": True,
+                       "path_lists": {1: "voxel_major", 2: "muon_major", 3: "recompute"}.get(st["path_lists"]),
                        "parallelism": f"replicas x{world} (one scan per GPU)",
-                       "l2": "inputs larger than L2: pair lists and s_ij far exceed 126 MB, no flush",
-                                  "setup_s": t_setup, "setup_ms": setup_ms, "generate_s": t_gen, "muon_pass": {1: "tma_tiles", 2: "warp_batched"}.get(st["muon_pass"]),
-            "muon_group": st["muon_group"], "tile_pairs": st["tile_pairs"]},
+                       "l2": "inputs larger than L2: the pair lists read every iteration far exceed 126 MB, no flush",
+                       "device_bytes": st["device_bytes"], "setup_s": t_setup, "setup_ms": setup_ms,
+                       "generate_s": t_gen,
+                       "muon_pass": {1: "tma_tiles", 2: "warp_batched", 3: "one_pass_lists", 4: "recompute_walk",
+                                     5: "split_muon_pass_and_scatter"}.get(st["muon_pass"]),
+                       "muon_group": st["muon_group"], "held_pairs": st["tile_pairs"]},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": int(launches),
             "clocks": clk,
             "time_to_lambda": ttl,
+            "recompute": recompute,
+            "poca": poca,
         }
         print(json.dumps(line), flush=True)
     rep.close()
@@ -417,24 +545,35 @@ def run_ours(args) -> int:
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="cube100_20mm", choices=list(WORKLOADS))
+    ap.add_argument("--workload", default="grid256x256x128_10mm", choices=list(WORKLOADS))
     ap.add_argument("--n-muons", type=int, default=0)
-    ap.add_argument("--mode", choices=["median", "mean"], default="median")
+    ap.add_argument("--mode", choices=["median", "mean"], default=None,
+                    help="EM update (default: mean for the 256x256x128 scan, median otherwise)")
+    ap.add_argument("--lists", choices=["auto", "voxel_major", "muon_major", "recompute"], default="auto")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--e2e-iters", type=int, default=0, help="EM iterations per e2e call (0: the workload's)")
-    ap.add_argument("--ttl-iters", type=int, default=50)
-    ap.add_argument("--cpu-sample", type=int, default=150_000)
+    ap.add_argument("--ttl-iters", type=int, default=-1,
+                    help="iterations of the time-to-lambda runs (-1: the workload's)")
+    ap.add_argument("--recompute-iters", type=int, default=2)
+    ap.add_argument("--poca", type=int, default=1)
+    ap.add_argument("--cpu-sample", type=int, default=1_000_000)
+    ap.add_argument("--cpu-sample-fixed", action="store_true",
+                    help="reference leg: use --cpu-sample as it is instead of sizing it to the step count")
     ap.add_argument("--muon-pass", choices=["auto", "tile", "warp"], default="auto")
     ap.add_argument("--muon-layout", choices=["auto", "columns", "index"], default="auto")
     ap.add_argument("--voxel-stream-above", type=int, default=None,
                     help="segments longer than this are selected without holding their keys (-1: never)")
-    ap.add_argument("--ncu-traffic", type=float, default=None,
-                    help="DRAM bytes per voxel-pass iteration from an ncu capture of this workload")
     args = ap.parse_args()
+    if args.mode is None:
+        args.mode = DEFAULT_MODE.get(args.workload, "median")
+    if args.ttl_iters < 0:
+        from muontomography_gb300 import workloads as W
+
+        args.ttl_iters = WORKLOADS[args.workload](W)().n_iter
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     return run_reference(args) if args.impl == "reference" else run_ours(args)

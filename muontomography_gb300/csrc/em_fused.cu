@@ -27,9 +27,7 @@
 // per lane) writes every muon's coefficients; a second pass streams the lists
 // again and only adds g_ij to G_j.  Twice the list traffic from HBM, but
 // neither pass waits at a block barrier; the autotuner times it beside the
-// one-pass variants.  While a batch is worked on, the TMA engine prefetches the
-// CTA's next batch of pairs into L2 (cp.async.bulk.prefetch.L2), so the
-// loads at the start of a batch hit L2.
+// one-pass variants.
 //
 // Recompute pass (k_em_fused_walk).  The same sums without stored lists: a
 // thread per muon walks its merged path in FP64 (the bit-exact Siddon walk

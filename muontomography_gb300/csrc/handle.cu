@@ -617,6 +617,7 @@ void prepare_poca(muto_handle* h) {
     a.length_weighted = h->P.length_weighted;
     a.img = h->img64.as<double>();
     a.weight = h->weight.as<double>();
+    a.wscale = poca_weight_scale(nt, h->grid, h->P.length_weighted);
     a.assign = h->assign.as<long long>();
     a.ctr = h->ctr();
     a.vox = nullptr;
@@ -1194,11 +1195,29 @@ MuonPassArgs<Real> muon_args(muto_handle* h, const Real* lam, bool cost) {
     return a;
 }
 
+// Choices of the muon-pass tuner, kept for the process: scans of the same
+// shape (precision, device, muons to within a factor of 2, mean path to
+// within 8 voxels) reuse the choice instead of timing again.
+struct TuneShape {
+    int fp64, device, log2n, path8;
+    bool operator<(const TuneShape& o) const {
+        return std::tie(fp64, device, log2n, path8) < std::tie(o.fp64, o.device, o.log2n, o.path8);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneShape, std::pair<int, int>> g_tune_choice;
+
 // The mean-update pass over muon-major lists or recomputed paths: lambda
 // (voxel order) is copied to its bricked order first when the path indices
-// are bricked; the pass adds every g_ij to h->gsum.
+// are bricked; the pass adds every g_ij to h->gsum.  With `profiled` each
+// launch goes through run() under its own name (em_fused, em_walk, or the
+// split form's em_muon and em_scatter).
 template <typename Real>
-void launch_fused_pass(muto_handle* h, const Real* lam, bool cost, cudaStream_t s) {
+void launch_fused_pass(muto_handle* h, const Real* lam, bool cost, cudaStream_t s, bool profiled = false) {
+    auto launch = [&](const char* name, auto&& f) {
+        if (profiled) run(h, name, f);
+        else f();
+    };
     using R4 = typename Vec4<Real>::type;
     const Params& P = h->P;
     const double exy = P.error_xy, ezo = P.error_dz_outer, ezi = P.error_dz_inner;  // src/MutoMLSD.cpp:168-170
@@ -1213,7 +1232,10 @@ void launch_fused_pass(muto_handle* h, const Real* lam, bool cost, cudaStream_t 
     a.V = static_cast<uint32_t>(h->V());
     const bool split = h->lists == kListsMuonMajor && h->fused_variant == kFusedVariants;
     if (h->brick) {  // (the split form's muon pass refreshes the bricked copy itself)
-        if (!split) launch_brick_lambda<Real>(lam, static_cast<uint32_t>(h->V()), h->bdims, h->lam_b.as<Real>(), s);
+        if (!split)
+            launch("brick_lambda", [&] {
+                launch_brick_lambda<Real>(lam, static_cast<uint32_t>(h->V()), h->bdims, h->lam_b.as<Real>(), s);
+            });
         a.lam = h->lam_b.as<Real>();
         a.V = static_cast<uint32_t>(h->vb);
     }
@@ -1228,8 +1250,9 @@ void launch_fused_pass(muto_handle* h, const Real* lam, bool cost, cudaStream_t 
     if (h->lists == kListsMuonMajor && h->fused_variant == kFusedVariants) {
         // split form: the muon pass writes every muon's coefficients, the scatter adds g_ij
         const MuonPassArgs<Real> m = muon_args<Real>(h, lam, cost);
-        launch_muon_pass<Real>(h, m, s);
-        launch_em_scatter<Real>(a, h->kvec.as<R4>(), h->scatter_group, h->scatter_blocks, s);
+        launch("em_muon", [&] { launch_muon_pass<Real>(h, m, s); });
+        launch("em_scatter",
+               [&] { launch_em_scatter<Real>(a, h->kvec.as<R4>(), h->scatter_group, h->scatter_blocks, s); });
         return;
     }
     if (h->lists == kListsRecompute) {
@@ -1241,9 +1264,9 @@ void launch_fused_pass(muto_handle* h, const Real* lam, bool cost, cudaStream_t 
         a.straight = P.straight_line ? 1 : 0;
         a.bdims = h->bdims;
         a.brick = h->brick ? 1 : 0;
-        launch_em_fused_walk<Real>(a, h->num_sms, s);
+        launch("em_walk", [&] { launch_em_fused_walk<Real>(a, h->num_sms, s); });
     } else {
-        launch_em_fused<Real>(a, h->fused_variant, h->fused_blocks, s);
+        launch("em_fused", [&] { launch_em_fused<Real>(a, h->fused_variant, h->fused_blocks, s); });
     }
 }
 
@@ -1259,11 +1282,16 @@ void launch_fused_update(muto_handle* h, const Real* lam, OutT* out, double* gra
 // In-project autotuner of the stored-list pass: the variants whose held
 // pairs suit the scan's mean path, timed on the scan's own lists (one
 // warm-up and two timed launches each); the per-voxel sums are cleared after.
+std::map<TuneShape, int> g_fused_choice;  // the tuner's pick per scan shape (guarded by g_tune_mu)
+
 template <typename Real>
 void autotune_fused(muto_handle* h) {
     if (h->lists != kListsMuonMajor || h->N == 0) return;
     HostPhase ph(h, "autotune");
     const double avg = static_cast<double>(h->npairs) / static_cast<double>(h->N);
+    int log2n = 0;
+    while ((h->N >> log2n) > 1) ++log2n;
+    const TuneShape shape{h->fp64() ? 1 : 0, h->device, log2n, static_cast<int>(avg / 8.0)};
     std::vector<int> cands;
     const bool forced = h->P.fused_variant >= 0;
     if (forced) cands.push_back(h->P.fused_variant);
@@ -1292,6 +1320,14 @@ void autotune_fused(muto_handle* h) {
     if (cands.size() == 1) {
         apply(cands[0]);
         return;
+    }
+    {  // scans of the same shape reuse the choice instead of timing again
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        const auto it = g_fused_choice.find(shape);
+        if (it != g_fused_choice.end()) {
+            apply(it->second);
+            return;
+        }
     }
     cudaStream_t s = h->stream;
     Counters saved;
@@ -1323,23 +1359,16 @@ void autotune_fused(muto_handle* h) {
     cudaEventDestroy(e1);
     h->launches += 3 * cands.size() * (h->brick ? 2 : 1);
     apply(pick);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_fused_choice[shape] = pick;
+    }
     const uint64_t ng = h->brick ? h->vb : h->V();
     CK(cudaMemsetAsync(h->gsum.as<void>(), 0, (ng + kPad) * sizeof(Real), s));
     CK(cudaMemcpyAsync(h->ctr(), &saved, sizeof(Counters), cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
 }
 
-// Choices of the muon-pass tuner, kept for the process: scans of the same
-// shape (precision, device, muons to within a factor of 2, mean path to
-// within 8 voxels) reuse the choice instead of timing again.
-struct TuneShape {
-    int fp64, device, log2n, path8;
-    bool operator<(const TuneShape& o) const {
-        return std::tie(fp64, device, log2n, path8) < std::tie(o.fp64, o.device, o.log2n, o.path8);
-    }
-};
-std::mutex g_tune_mu;
-std::map<TuneShape, std::pair<int, int>> g_tune_choice;
 
 // In-project autotuner: time the candidate muon-pass variants on this scan's
 // own lists (one warm-up and two timed launches each) and keep the fastest.
@@ -1466,7 +1495,7 @@ void enqueue_iteration(muto_handle* h) {
     cudaStream_t s = h->stream;
     const uint32_t cap = static_cast<uint32_t>(h->cost_hist.bytes() / sizeof(double));
     if (h->lists != kListsVoxelMajor) {  // the mean update over muon-major lists or recomputed paths
-        run(h, "em_fused", [&] { launch_fused_pass<Real>(h, h->lam.as<Real>(), h->want_cost(), s); });
+        launch_fused_pass<Real>(h, h->lam.as<Real>(), h->want_cost(), s, true);
         if (h->method == kMap) {  // ML step into lambda_ML, then the MAP step (src/MutoMAP.cpp:138-184)
             run(h, "em_update", [&] {
                 launch_fused_update<Real, double>(h, h->lam.as<Real>(), h->lam_ml.as<double>(), nullptr, nullptr, s);
@@ -1613,7 +1642,7 @@ double nll_eval(muto_handle* h, const double* loglam_host, double* grad_host) {
     if (h->lists != kListsVoxelMajor) {
         // one pass over the muon-major lists (or the paths walked again): the
         // cost and the per-voxel sums of g_ij; d NLL / d log l_j = -l_j sum_i g_ij
-        run(h, grad_host ? "nll_backward" : "nll_forward", [&] { launch_fused_pass<Real>(h, lam_r, true, s); });
+        launch_fused_pass<Real>(h, lam_r, true, s, true);
         run(h, "em_update_grad", [&] {
             launch_fused_update<Real, Real>(h, lam_r, nullptr, h->grad.as<double>(), h->lam64.as<double>(), s);
         });

@@ -10,13 +10,21 @@
 // floor(M * cut) summed in ascending order from 0.0, as std::accumulate over
 // the sorted vector does (:113-117) — so the numerator is bit-exact and only
 // the weights carry the atomics' rounding.
+#include <cmath>
+
 #include "common.cuh"
 
 namespace muto {
 namespace {
 
+// The weights are summed in 64-bit fixed point (value * wscale rounded to an
+// integer, wscale a power of two chosen by the host so that no voxel's sum
+// can overflow): integer reductions are native to L2 where FP64 ones are
+// slow, and the integer sums are exact and independent of the order in which
+// the rays add them.  They are turned into doubles once all rays are done.
 struct WeightSink {
-    double* weight;
+    unsigned long long* wfix;
+    double wscale;
     uint32_t nx, ny, nz;
     double dz;
     int length_weighted;
@@ -26,9 +34,18 @@ struct WeightSink {
         if (x >= nx || y >= ny || z >= nz) return;  // never for an in-grid walk
         if (skip_scat && x == sx && y == sy && z == sz) return;
         const uint64_t j = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * (y + static_cast<uint64_t>(ny) * z);
-        atomicAdd(weight + j, length_weighted ? l : dz);
+        atomicAdd(wfix + j, __double2ull_rn((length_weighted ? l : dz) * wscale));
     }
 };
+
+// the fixed-point weight sums to doubles, in place
+__global__ void k_weight_from_fixed(double* __restrict__ weight, uint64_t V, double inv_scale) {
+    const uint64_t j = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (j < V) {
+        const unsigned long long w = reinterpret_cast<const unsigned long long*>(weight)[j];
+        weight[j] = static_cast<double>(w) * inv_scale;
+    }
+}
 
 __global__ void k_poca(PocaArgs a) {
     const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -59,7 +76,8 @@ __global__ void k_poca(PocaArgs a) {
             } else {
                 atomicAdd(a.img + js, v);
             }
-            WeightSink sink{a.weight, g.n[0], g.n[1], g.n[2], g.w[2], a.length_weighted, 0, xs, ys, zs};
+            WeightSink sink{reinterpret_cast<unsigned long long*>(a.weight), a.wscale, g.n[0], g.n[1], g.n[2],
+                            g.w[2], a.length_weighted, 0, xs, ys, zs};
             if (a.straight) {
                 siddon_walk(g, r.pin, r.pout, sink);
             } else {
@@ -184,9 +202,24 @@ __global__ void k_poca_normalize(double* __restrict__ img, const double* __restr
 }  // namespace
 
 void launch_poca(const PocaArgs& a, cudaStream_t s) {
-    if (a.n == 0) return;
+    if (a.n == 0) return;  // the weights stay all-zero bits, which is 0.0
     const unsigned nb = static_cast<unsigned>((a.n + 127) / 128);
-    k_poca<<<nb, 128, 0, s>>>(a); count_launches(1);
+    k_poca<<<nb, 128, 0, s>>>(a);
+    const uint64_t V = static_cast<uint64_t>(a.g.nx) * a.g.ny * a.g.nz;
+    k_weight_from_fixed<<<static_cast<unsigned>((V + 255) / 256), 256, 0, s>>>(a.weight, V, 1.0 / a.wscale);
+    count_launches(2);
+}
+
+double poca_weight_scale(uint64_t n_rays, const muto_grid& g, int length_weighted) {
+    // a ray adds at most twice (in and out half) the longest in-voxel length
+    // (or dz) to a voxel; the sum over all rays must stay below 2^62
+    const double wmax = length_weighted ? std::sqrt(g.dx * g.dx + g.dy * g.dy + g.dz * g.dz) : g.dz;
+    const double worst = 2.0 * static_cast<double>(n_rays > 0 ? n_rays : 1) * (wmax > 0 ? wmax : 1.0);
+    int e = 0;
+    std::frexp(4.611686018427387904e18 / worst, &e);  // 2^62 / worst = f * 2^e, f in [0.5, 1)
+    e -= 1;                                           // 2^e <= 2^62 / worst
+    e = e < -60 ? -60 : (e > 60 ? 60 : e);
+    return std::ldexp(1.0, e);
 }
 
 void launch_pocut_hist(const uint32_t* vox, uint64_t n, uint32_t* counts, cudaStream_t s) {

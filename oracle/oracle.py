@@ -3,7 +3,8 @@
 TEST INFRASTRUCTURE ONLY: imported by tests/, ``__graft_entry__.smoke()`` and
 the CPU-baseline / reference leg of ``bench.py`` -- to check results, never as
 the product path.  ``build()`` compiles the oracle into ``oracle/_build`` with
-``g++ -O3 -fopenmp -ffp-contract=off``.  ``fit_records`` (the raw-hit line
+``g++ -O3 -fopenmp -ffp-contract=off`` (with ``synthetic.cpp``, the tracks of
+the CPU-baseline legs).  ``fit_records`` (the raw-hit line
 fit, with numpy's SVD) is restated here in Python.
 """
 from __future__ import annotations
@@ -16,6 +17,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 SRC = HERE / "muto_oracle.cpp"
+SRCS = [SRC, HERE / "synthetic.cpp"]  # synthetic.cpp: the tracks of the CPU-baseline legs
 BUILD = HERE / "_build"
 LIB = BUILD / "libmuto_oracle.so"
 FLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math"]
@@ -38,8 +40,9 @@ class Cfg(C.Structure):  # == oracle_cfg
 
 def build(force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
-    if force or not LIB.exists() or SRC.stat().st_mtime > LIB.stat().st_mtime:
-        subprocess.run(["g++", *FLAGS, str(SRC), "-o", str(LIB)], check=True)
+    gen_h = HERE.parent / "muontomography_gb300" / "csrc" / "gen.h"
+    if force or not LIB.exists() or any(p.stat().st_mtime > LIB.stat().st_mtime for p in [*SRCS, gen_h]):
+        subprocess.run(["g++", *FLAGS, *map(str, SRCS), "-o", str(LIB)], check=True)
     return LIB
 
 
@@ -71,6 +74,8 @@ def lib() -> C.CDLL:
         L.oracle_mlsd_ml_step.argtypes = [P, D, U32]
         L.oracle_mlsd_nll.restype = C.c_double
         L.oracle_mlsd_nll.argtypes = [P, D, D]
+        L.oracle_generate.restype = C.c_int
+        L.oracle_generate.argtypes = [C.POINTER(Grid), D, P, C.c_uint64, C.c_uint64, P]
         L.oracle_cubic.restype = C.c_int
         L.oracle_cubic.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, D]
         _lib = L

@@ -133,9 +133,10 @@ def test_reference_arm_prints_one_contract_line():
     assert line["impl"] == "reference"
     assert line["metric"] == "EM-iter muon\u00b7voxel updates/s" and line["higher_is_better"] is True
     assert line["value"] > 0 and line["steps"] == 1 and line["n_gpus"] == 1
-    assert line["config"]["workload"] == "cube100_20mm_10M"
+    assert line["config"]["workload"] == "grid256x256x128_10mm_100M" and line["config"]["mode"] == "mean"
     cb = line["cpu_baseline"]
-    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and "3000 muons" in cb["sample"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"]
+    assert "the first 3000 of the 100000000 muons" in cb["sample"]
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
 
@@ -148,8 +149,29 @@ def test_reference_arm_other_ranks_exit_without_work():
 
 @pytest.mark.parametrize("argv,method,mode", [
     (("--workload", "map128x128x64_15mm"), "map", "median"),
-    (("--mode", "mean"), "mlsd", "mean"),
+    (("--workload", "cube100_20mm"), "mlsd", "median"),
+    (("--workload", "cube100_20mm", "--mode", "mean"), "mlsd", "mean"),
 ])
 def test_reference_arm_other_workloads(argv, method, mode):
     (line,) = _bench("--impl", "reference", "--steps", "1", "--warmup", "0", "--cpu-sample", "2000", *argv)
     assert line["config"]["method"] == method and line["config"]["mode"] == mode and line["value"] > 0
+
+
+def test_reference_arm_loads_no_product_library():
+    # the reference leg times the CPU port on tracks it makes itself: the
+    # product's CUDA library must not be in its process
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parents[1]
+    code = ("import atexit, runpy, sys\n"
+            "def libs():\n"
+            "    print('LIBS', sorted({l.split()[-1] for l in open('/proc/self/maps') if '.so' in l}))\n"
+            "atexit.register(libs)\n"
+            "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0', '--cpu-sample', '2000']\n"
+            "runpy.run_path('bench.py', run_name='__main__')\n")
+    out = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    libs = [ln for ln in out.stdout.splitlines() if ln.startswith("LIBS")][0]
+    assert "libmuto_oracle.so" in libs and "libmuto_gb300" not in libs and "libmuto_facade" not in libs

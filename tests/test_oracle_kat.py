@@ -176,3 +176,18 @@ def test_slr_iter_level_schedule_is_exact(oracle, lw, iters):
     # a schedule that breaks a voxel's order does change the result
     perm = np.random.default_rng(0).permutation(rays.shape[0])
     assert not np.array_equal(oracle.slr(g, cfg, rays[perm], iterative=True).view(np.uint64), want.view(np.uint64))
+
+
+def test_oracle_synthetic_tracks_equal_the_library_generator(oracle):
+    # the CPU-baseline legs make their tracks without the product library;
+    # they must be the workload's own tracks, bit for bit
+    import muontomography_gb300 as M
+    from muontomography_gb300 import workloads as W
+    from oracle import synthetic as S
+
+    for wl in (W.small(n_muons=2000, seed=5), W.grid256x256x128_10mm(n_muons=1500)):
+        lam = S.phantom(wl.grid, wl.blocks, M.X0_MM["air"], 3.0)
+        assert np.array_equal(lam, wl.lam())
+        a = S.generate(wl.grid, lam, wl.n_muons, wl.seed, first=11)
+        b = M.generate(wl.grid, wl.lam(), wl.n_muons, wl.seed, first=11)
+        assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
