@@ -1303,16 +1303,19 @@ void autotune_fused(muto_handle* h) {
         const bool fit = avg < 48.0 ? g <= 8 && held <= 64 : avg < 160.0 ? g >= 8 && held <= 128 : g == 16;
         if (fit) cands.push_back(v);
     }
-    if (!forced) cands.push_back(kFusedVariants);  // the split form
+    if (!forced) {  // the split form, its scatter with 32 and 16 lanes per muon
+        cands.push_back(kFusedVariants);
+        cands.push_back(kFusedVariants + 1);
+    }
     auto apply = [&](int v) {
-        h->fused_variant = v;
-        if (v == kFusedVariants) {  // split: the warp-batched muon pass and the scatter pass
+        h->fused_variant = v >= kFusedVariants ? kFusedVariants : v;
+        if (v >= kFusedVariants) {  // split: the warp-batched muon pass and the scatter pass
             const int g = avg <= 32 ? 8 : (avg <= 64 ? 16 : 32);
             h->muon_kind = 2;
             h->muon_group = g;
             h->warp_blocks = em_muon_warp_blocks<Real>(g) * h->num_sms;
-            h->scatter_group = g;
-            h->scatter_blocks = em_scatter_blocks<Real>(g) * h->num_sms;
+            h->scatter_group = v == kFusedVariants ? g : std::max(8, g / 2);
+            h->scatter_blocks = em_scatter_blocks<Real>(h->scatter_group) * h->num_sms;
         } else {
             h->fused_blocks = em_fused_blocks<Real>(v) * h->num_sms;
         }
