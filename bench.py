@@ -473,7 +473,7 @@ def run_ours(args) -> int:
                 "frac": pb / (t_poca / 1000.0) / 1e9 / pk["hbm_gbs"], "peak": pk["hbm_gbs"],
                 "in_grid": pst["n_scat_in_grid"],
                 "what": "k_poca: FP64 closest approach, binning and the length-weighted Siddon weights of every "
-                        "track (integer fixed-point sums), then the normalisation"}
+                        "track (FP64 atomics, a thread per kept track), then the normalisation"}
 
     # ---- time to lambda: mixed vs the plain FP64 form, same iteration count ---
     ttl = None

@@ -3,9 +3,9 @@
  *
  * The library replaces the reconstruction path of LasDes/MuonTomography:
  *   MutoVReconstruction::reconstruct   include/MutoVReconstruction.h:16
- *   MutoPoCA(json)  / reconstruct      include/MutoPoCA.h:23,28   src/MutoPoCA.cpp:74-134
+ *   MutoPoCA(json)  / reconstruct      include/MutoPoCA.h:23,28   src/MutoPoCA.cpp:24, :51-134
  *   MutoMLSD(json)  / reconstruct      include/MutoMLSD.h:33,38   src/MutoMLSD.cpp:47-220
- *   MutoMAP(json)   / reconstruct      include/MutoMAP.h:22,27    src/MutoMAP.cpp:75-268
+ *   MutoMAP(json)   / reconstruct      include/MutoMAP.h:22,27    src/MutoMAP.cpp:12, :39-205
  *   MutoSiddon::getVoxelPath           include/MutoSiddon.h:24    src/MutoSiddon.cpp:9-141
  *   MutoFile::saveImage / loadImage    include/MutoFile.h:49,59   src/MutoFile.cpp:85-211
  *
@@ -92,11 +92,11 @@ typedef struct muto_handle muto_handle;
 /* Create a reconstruction: method is "poca", "pocut", "slr", "slr_iter",
  * "mlsd" or "map"; config_json is the JSON object of that method (the value
  * of the key of the same name, as passed to the constructors MutoPoCA(json)
- * src/MutoPoCA.cpp:74, MutoPoCut(json) src/MutoPoCut.cpp:12 (PoCA's keys
+ * src/MutoPoCA.cpp:24, MutoPoCut(json) src/MutoPoCut.cpp:12 (PoCA's keys
  * plus "cut_percentile", 1.0; straight_line is always off), MutoSLR(json)
- * src/MutoSLR.cpp:21, MutoSLRIter(json) src/MutoSLRIter.cpp:8 (plus
+ * src/MutoSLR.cpp:21, MutoSLRIter(json) src/MutoSLRIter.cpp:9 (plus
  * "num_iteration", 1), MutoMLSD(json) src/MutoMLSD.cpp:47, MutoMAP(json)
- * src/MutoMAP.cpp:75).  poca, pocut, slr and slr_iter compute their image in
+ * src/MutoMAP.cpp:12).  poca, pocut, slr and slr_iter compute their image in
  * muto_prepare.
  * The reference's keys and defaults apply; extra keys: "precision"
  * ("mixed" default, or "fp64"), "use_graph" (true), "random_seed",
@@ -182,17 +182,21 @@ int muto_siddon_batch(const muto_grid* g, const double* p1, const double* p2, ui
  * has none left to give, and a loop that keeps other streams of the device
  * busy (data acquisition, online monitoring) cannot take the device-wide
  * synchronisation that cudaFree performs.  Inputs, outputs and errors are
- * those of muto_siddon_batch.
+ * those of muto_siddon_batch, plus MUTO_ERR_CAPACITY for cap; this call
+ * keeps no handle, so a failure is reported by its return code alone.
  * The work runs on `stream` (a cudaStream_t; NULL is the legacy default
- * stream) and the call returns when it is done.
+ * stream) and the call returns when it is done, also when it fails after
+ * queuing work (it then waits for the queued work before returning).
  *
  * Instead of allocating, the call stages rays and voxel lists, a chunk of
  * rays at a time, through one fixed device array of
  * MUTO_NOALLOC_SCRATCH_BYTES compiled into the library.  n is unbounded;
  * cap above MUTO_NOALLOC_MAX_CAP returns MUTO_ERR_CAPACITY before the
  * device is touched.  The first call on a device looks up the array's
- * address on that device (the current one); make that first call before
- * any stream capture begins.  All calls on one device share the array:
+ * address on that device (the current one) and keeps it for the rest of
+ * the process; make that first call before any stream capture begins.  The
+ * kept address is not valid after cudaDeviceReset, so do not use this call
+ * in a process that resets a device it has called it on.  All calls on one device share the array:
  * calls that overlap in time (several host threads, or several streams)
  * race on it, so the caller must serialise them. */
 #define MUTO_NOALLOC_SCRATCH_BYTES (16u << 20)

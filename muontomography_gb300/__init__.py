@@ -285,7 +285,7 @@ class Reconstruction:
 
 
 class MutoPoCA(Reconstruction):
-    """MutoPoCA(json) / reconstruct (src/MutoPoCA.cpp:74-134)."""
+    """MutoPoCA(json) / reconstruct (src/MutoPoCA.cpp:24, :51-134)."""
 
     def __init__(self, config: dict | None = None):
         super().__init__("poca", config)
@@ -308,7 +308,7 @@ class MutoSLR(Reconstruction):
 
 
 class MutoSLRIter(Reconstruction):
-    """MutoSLRIter(json) / reconstruct (src/MutoSLRIter.cpp:8-83): SLR repeated
+    """MutoSLRIter(json) / reconstruct (src/MutoSLRIter.cpp:9-83): SLR repeated
     ``num_iteration`` times (default 1), later passes in place and in muon order."""
 
     def __init__(self, config: dict | None = None):
@@ -324,7 +324,7 @@ class MutoMLSD(Reconstruction):
 
 
 class MutoMAP(Reconstruction):
-    """MutoMAP(json) / reconstruct (src/MutoMAP.cpp:75-268)."""
+    """MutoMAP(json) / reconstruct (src/MutoMAP.cpp:12-205)."""
 
     def __init__(self, config: dict | None = None):
         super().__init__("map", config)

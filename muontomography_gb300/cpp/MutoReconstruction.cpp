@@ -72,14 +72,18 @@ MutoPoCA::MutoPoCA(const char* method, json config) : MutoGpuReconstruction(meth
 MutoPoCut::MutoPoCut() : MutoPoCA("pocut", empty_object()) {}
 MutoPoCut::MutoPoCut(json config) : MutoPoCA("pocut", config) {}
 
-MutoSLR::MutoSLR() : MutoPoCA("slr", empty_object()) {}
-MutoSLR::MutoSLR(json config) : MutoPoCA("slr", config) {}
-MutoSLR::MutoSLR(const char* method, json config) : MutoPoCA(method, config) {}
+MutoSLR::MutoSLR() : MutoGpuReconstruction("slr", empty_object()) {}
+MutoSLR::MutoSLR(json config) : MutoGpuReconstruction("slr", config) {}
+MutoSLR::MutoSLR(const char* method, json config) : MutoGpuReconstruction(method, config) {}
 
 MutoSLRIter::MutoSLRIter() : MutoSLR("slr_iter", empty_object()) {}
 MutoSLRIter::MutoSLRIter(json config) : MutoSLR("slr_iter", config) {}
 
-Image MutoPoCA::reconstruct(const MutoMuonData& rays) {
+Image MutoPoCA::reconstruct(const MutoMuonData& rays) { return reconstructOnce(rays); }
+Image MutoSLR::reconstruct(const MutoMuonData& rays) { return reconstructOnce(rays); }
+
+// the one-shot methods (PoCA, PoCut, SLR, SLRIter): the image comes out of prepare
+Image MutoGpuReconstruction::reconstructOnce(const MutoMuonData& rays) {
     if (!fHandle) return Image{};
     fTimeStart = std::chrono::steady_clock::now();
     const muto_ray* r = rays.empty() ? nullptr : reinterpret_cast<const muto_ray*>(rays.data());

@@ -39,6 +39,7 @@ public:
 
 protected:
     MutoGpuReconstruction(const char* method, const json& config);
+    Image reconstructOnce(const MutoMuonData& rays);  // load, prepare (the whole method), image
     Image fetchImage();
     bool check(int rc, const char* what);
     void logMessage(const std::string& msg, bool printTime = false);
@@ -68,10 +69,12 @@ public:
 };
 
 // straight-line back-projection between the grid's top and bottom planes
-class MutoSLR : public MutoPoCA {
+// (a MutoVReconstruction of its own, as include/MutoSLR.h:13 declares it)
+class MutoSLR : public MutoGpuReconstruction {
 public:
     MutoSLR();
     explicit MutoSLR(json config);
+    Image reconstruct(const MutoMuonData& rays) override;
 
 protected:
     MutoSLR(const char* method, json config);

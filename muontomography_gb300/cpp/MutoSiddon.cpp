@@ -56,17 +56,30 @@ std::vector<std::vector<VoxelData>> MutoSiddon::getVoxelPaths(const std::vector<
             return out;
         }
         for (size_t i = 0; i < n; ++i) {
-            std::vector<VoxelData>& v = out[s0 + i];
-            const uint32_t k = std::min(cnt[i], cap);
-            v.resize(k);
-            for (uint32_t j = 0; j < k; ++j) {
-                const size_t q = i * cap + j;
-                v[j].x = xyz[3 * q];
-                v[j].y = xyz[3 * q + 1];
-                v[j].z = xyz[3 * q + 2];
-                v[j].length = len[q];
-            }
+            bool failed = false;
+            out[s0 + i] = unpackPath(cnt[i], cap, xyz.data() + 3 * i * cap, len.data() + i * cap, &failed);
+            if (failed)
+                std::cout << "MutoSiddon: the walk of segment " << s0 + i
+                          << " stopped at its step bound; its path is left empty. " << std::endl;
         }
     }
     return out;
+}
+
+std::vector<VoxelData> MutoSiddon::unpackPath(uint32_t count, uint32_t cap, const uint32_t* xyz, const double* len,
+                                              bool* failed) {
+    std::vector<VoxelData> v;
+    if (count == 0xffffffffu) {  // the device marks a walk that hit its step bound
+        if (failed) *failed = true;
+        return v;
+    }
+    const uint32_t k = std::min(count, cap);
+    v.resize(k);
+    for (uint32_t j = 0; j < k; ++j) {
+        v[j].x = xyz[3 * j];
+        v[j].y = xyz[3 * j + 1];
+        v[j].z = xyz[3 * j + 2];
+        v[j].length = len[j];
+    }
+    return v;
 }

@@ -6,6 +6,7 @@
 // belong in getVoxelPaths.
 #pragma once
 
+#include <cstdint>
 #include <vector>
 
 #include "MutoTypes.h"
@@ -21,6 +22,13 @@ public:
 
     // Segment i runs from p1[i] to p2[i]; out[i] is its path.
     std::vector<std::vector<VoxelData>> getVoxelPaths(const std::vector<Vector3>& p1, const std::vector<Vector3>& p2);
+
+    // One segment's path from muto_siddon_batch's slots: count voxels (at
+    // most cap kept) from xyz (3 per voxel) and len.  A count of 0xffffffff
+    // marks a walk stopped by its step bound: the path is then empty and
+    // *failed is set (it is never set otherwise).
+    static std::vector<VoxelData> unpackPath(uint32_t count, uint32_t cap, const uint32_t* xyz, const double* len,
+                                             bool* failed);
 
 private:
     VoxelGrid fGrid;

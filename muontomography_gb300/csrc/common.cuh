@@ -156,17 +156,15 @@ struct PocaArgs {
     double eps, mag;
     int has_energy, straight, length_weighted;
     double* img;        // PoCA: the summed values (null for PoCut)
-    double* weight;     // V doubles, zero on entry: summed in fixed point (x wscale), converted before return
-    double wscale;      // poca_weight_scale of the launch
+    double* weight;
+    uint32_t* walk;                  // n slots: the kept rays, listed by the first kernel for the walks
+    unsigned long long* walk_count;  // their number (device)
     long long* assign;  // 3 per ray, optional
     Counters* ctr;
     uint32_t* vox;      // PoCut: per ray its voxel, 0xffffffff when rejected (null for PoCA)
     double* value;      // PoCut: per ray its value (angle^2, times p^2 with momentum)
 };
-void launch_poca(const PocaArgs& a, cudaStream_t s);
-// the power of two the weights are scaled by for their fixed-point sums: the
-// largest for which n_rays rays cannot overflow a voxel's 63-bit sum
-double poca_weight_scale(uint64_t n_rays, const muto_grid& g, int length_weighted);
+void launch_poca(const PocaArgs& a, int num_sms, cudaStream_t s);
 void launch_poca_normalize(double* img, const double* weight, uint64_t V, double eps, cudaStream_t s);
 // slr.cu: straight-line reconstruction (src/MutoSLR.cpp:47-103) and the
 // iterative form's passes (src/MutoSLRIter.cpp:15-83)

@@ -124,7 +124,7 @@ enum Method { kPoca, kMlsd, kMap };
 
 struct Params {
     muto_grid grid{};
-    // MLSD / MAP keys, src/MutoMLSD.cpp:47-84 and src/MutoMAP.cpp:75-82
+    // MLSD / MAP keys, src/MutoMLSD.cpp:47-84 and src/MutoMAP.cpp:12-19
     bool update_with_mean = false;
     int mean_percentile = 100;
     bool straight_line = false, has_energy = false, early_stop = false, log_results = false;
@@ -137,11 +137,11 @@ struct Params {
     double angle_unit_mag = 1.0, eps = 1.0e-8;
     double beta = 1.0, p = 1.0, delta = 0.1;
     bool add_object_prior = false, all_neighbours = false;
-    // PoCA, src/MutoPoCA.cpp:74-97; PoCut, src/MutoPoCut.cpp:12-15
+    // PoCA, src/MutoPoCA.cpp:24-47; PoCut, src/MutoPoCut.cpp:12-15
     bool length_weighted = false;
     bool pocut = false;          // PoCut: the PoCA handle keeps a percentile of the values per voxel
     double cut_percentile = 1.0;
-    // SLR, src/MutoSLR.cpp:21-45; SLRIter, src/MutoSLRIter.cpp:8-11
+    // SLR, src/MutoSLR.cpp:21-45; SLRIter, src/MutoSLRIter.cpp:9-11
     int slr = 0;                 // 1 straight-line reconstruction, 2 its iterative form
     int slr_iterations = 1;
     // this library
@@ -617,7 +617,6 @@ void prepare_poca(muto_handle* h) {
     a.length_weighted = h->P.length_weighted;
     a.img = h->img64.as<double>();
     a.weight = h->weight.as<double>();
-    a.wscale = poca_weight_scale(nt, h->grid, h->P.length_weighted);
     a.assign = h->assign.as<long long>();
     a.ctr = h->ctr();
     a.vox = nullptr;
@@ -626,8 +625,12 @@ void prepare_poca(muto_handle* h) {
         prepare_slr(h, nt);
         return;
     }
+    DevMem walk;  // the kept rays' list for the walk kernel, and its length
+    walk.alloc((std::max<uint64_t>(nt, 1) + 2) * sizeof(uint32_t) + sizeof(unsigned long long), &h->dev_bytes);
+    a.walk_count = walk.as<unsigned long long>();
+    a.walk = reinterpret_cast<uint32_t*>(walk.as<unsigned long long>() + 1);
     if (!h->P.pocut) {
-        run(h, "poca", [&] { launch_poca(a, h->stream); });
+        run(h, "poca", [&] { launch_poca(a, h->num_sms, h->stream); });
         run(h, "poca_normalize", [&] { launch_poca_normalize(h->img64.as<double>(), h->weight.as<double>(), V, h->P.eps, h->stream); });
         return;
     }
@@ -646,7 +649,7 @@ void prepare_poca(muto_handle* h) {
     a.img = nullptr;
     a.vox = vox.as<uint32_t>();
     a.value = value.as<double>();
-    run(h, "poca", [&] { launch_poca(a, s); });
+    run(h, "poca", [&] { launch_poca(a, h->num_sms, s); });
     run(h, "pocut_group", [&] {
         launch_pocut_hist(vox.as<uint32_t>(), nt, counts.as<uint32_t>(), s);
         scan_u32_to_u64(counts.as<uint32_t>(), off.as<uint64_t>(), V, scan_scr.as<void>(), s);

@@ -133,9 +133,15 @@ extern "C" int muto_siddon_batch_noalloc(const muto_grid* g, const double* p1, c
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const Layout l = layout_for(cap);
     const DevGrid dg = make_dev_grid(*g);
-#define NOALLOC_CK(call)                                  \
-    do {                                                  \
-        if ((call) != cudaSuccess) return MUTO_ERR_CUDA;  \
+    // A failure after work was queued drains the stream before returning:
+    // copies still queued would otherwise land in the caller's buffers (and
+    // the next call could reuse the scratch array) after this call returned.
+#define NOALLOC_CK(call)                              \
+    do {                                              \
+        if ((call) != cudaSuccess) {                  \
+            (void)cudaStreamSynchronize(s);           \
+            return MUTO_ERR_CUDA;                     \
+        }                                             \
     } while (0)
     for (uint64_t r0 = 0; r0 < n; r0 += l.rays) {
         const uint32_t c = static_cast<uint32_t>(std::min<uint64_t>(l.rays, n - r0));

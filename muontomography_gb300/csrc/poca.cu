@@ -1,8 +1,9 @@
-// PoCA reconstruction (MutoPoCA::reconstruct, src/MutoPoCA.cpp:51-134), one
-// thread per ray: PoCA point, mean squared angle, unsigned-cast binning with
-// the reference's reject test, then the Siddon weights of the in and out
-// halves (or the straight line).  Sums are FP64 atomics; the voxel each ray
-// is binned to is bit-exact with the reference.
+// PoCA reconstruction (MutoPoCA::reconstruct, src/MutoPoCA.cpp:51-134): a
+// thread per ray for the PoCA point, mean squared angle, unsigned-cast binning
+// with the reference's reject test and the image sum; then a thread per kept
+// ray for the Siddon weights of the in and out halves (or the straight line).
+// Sums are FP64 atomics; the voxel each ray is binned to is bit-exact with
+// the reference.
 //
 // PoCut (MutoPoCut::reconstruct, src/MutoPoCut.cpp:19-121) runs the same ray
 // kernel, keeping each ray's value and voxel instead of summing it, then a
@@ -10,21 +11,13 @@
 // floor(M * cut) summed in ascending order from 0.0, as std::accumulate over
 // the sorted vector does (:113-117) — so the numerator is bit-exact and only
 // the weights carry the atomics' rounding.
-#include <cmath>
-
 #include "common.cuh"
 
 namespace muto {
 namespace {
 
-// The weights are summed in 64-bit fixed point (value * wscale rounded to an
-// integer, wscale a power of two chosen by the host so that no voxel's sum
-// can overflow): integer reductions are native to L2 where FP64 ones are
-// slow, and the integer sums are exact and independent of the order in which
-// the rays add them.  They are turned into doubles once all rays are done.
 struct WeightSink {
-    unsigned long long* wfix;
-    double wscale;
+    double* weight;
     uint32_t nx, ny, nz;
     double dz;
     int length_weighted;
@@ -34,17 +27,22 @@ struct WeightSink {
         if (x >= nx || y >= ny || z >= nz) return;  // never for an in-grid walk
         if (skip_scat && x == sx && y == sy && z == sz) return;
         const uint64_t j = static_cast<uint64_t>(x) + static_cast<uint64_t>(nx) * (y + static_cast<uint64_t>(ny) * z);
-        atomicAdd(wfix + j, __double2ull_rn((length_weighted ? l : dz) * wscale));
+        atomicAdd(weight + j, length_weighted ? l : dz);
     }
 };
 
-// the fixed-point weight sums to doubles, in place
-__global__ void k_weight_from_fixed(double* __restrict__ weight, uint64_t V, double inv_scale) {
-    const uint64_t j = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (j < V) {
-        const unsigned long long w = reinterpret_cast<const unsigned long long*>(weight)[j];
-        weight[j] = static_cast<double>(w) * inv_scale;
-    }
+// Per ray: PoCA point, value and binning; the image sum (or PoCut's value
+// and voxel); kept rays are appended to a.walk (warp-aggregated) for the
+// walk kernel, so that the FP64 walks run on full warps (a warp of rays
+// usually keeps fewer than half of them, and an FP64 instruction takes the
+// same pipe time however few of its lanes are active).
+__device__ __forceinline__ bool poca_bin(const DevGrid& g, const muto_ray& r, double eps, double zmin, double zmax,
+                                         double* ps, uint32_t* xyz, bool* parallel_ok) {
+    *parallel_ok = poca_point(r, eps, ps);
+    xyz[0] = u32_cast_x86(ddiv(dsub(ps[0], g.lo[0]), g.w[0]));  // :121-123
+    xyz[1] = u32_cast_x86(ddiv(dsub(ps[1], g.lo[1]), g.w[1]));
+    xyz[2] = u32_cast_x86(ddiv(dsub(ps[2], g.lo[2]), g.w[2]));
+    return !(g.n[0] <= xyz[0] || g.n[1] <= xyz[1] || g.n[2] <= xyz[2] || ps[2] < zmin || zmax < ps[2]);  // :125-129
 }
 
 __global__ void k_poca(PocaArgs a) {
@@ -55,20 +53,18 @@ __global__ void k_poca(PocaArgs a) {
         const muto_ray r = a.rays[i];
         const double zmin = a.rays[0].pout[2], zmax = a.rays[0].pin[2];  // :111-112
         double ps[3];
-        parallel_ok = poca_point(r, a.eps, ps);
-        const double a2 = scat_angle_square(r.din, r.dout, a.mag);
-        const uint32_t xs = u32_cast_x86(ddiv(dsub(ps[0], g.lo[0]), g.w[0]));  // :121-123
-        const uint32_t ys = u32_cast_x86(ddiv(dsub(ps[1], g.lo[1]), g.w[1]));
-        const uint32_t zs = u32_cast_x86(ddiv(dsub(ps[2], g.lo[2]), g.w[2]));
-        kept = !(g.n[0] <= xs || g.n[1] <= ys || g.n[2] <= zs || ps[2] < zmin || zmax < ps[2]);  // :125-129
+        uint32_t xyz[3];
+        kept = poca_bin(g, r, a.eps, zmin, zmax, ps, xyz, &parallel_ok);
         if (a.assign) {
-            a.assign[3 * i + 0] = kept ? static_cast<long long>(xs) : -1;
-            a.assign[3 * i + 1] = kept ? static_cast<long long>(ys) : -1;
-            a.assign[3 * i + 2] = kept ? static_cast<long long>(zs) : -1;
+            a.assign[3 * i + 0] = kept ? static_cast<long long>(xyz[0]) : -1;
+            a.assign[3 * i + 1] = kept ? static_cast<long long>(xyz[1]) : -1;
+            a.assign[3 * i + 2] = kept ? static_cast<long long>(xyz[2]) : -1;
         }
         if (a.vox) a.vox[i] = 0xffffffffu;
         if (kept) {
-            const uint64_t js = static_cast<uint64_t>(xs) + static_cast<uint64_t>(g.n[0]) * (ys + static_cast<uint64_t>(g.n[1]) * zs);
+            const uint64_t js = static_cast<uint64_t>(xyz[0]) +
+                                static_cast<uint64_t>(g.n[0]) * (xyz[1] + static_cast<uint64_t>(g.n[1]) * xyz[2]);
+            const double a2 = scat_angle_square(r.din, r.dout, a.mag);
             const double v = a.has_energy ? dmul(dmul(a2, r.ein), r.ein) : a2;  // :134-138 (PoCut :60-64)
             if (a.vox) {
                 a.vox[i] = static_cast<uint32_t>(js);
@@ -76,19 +72,40 @@ __global__ void k_poca(PocaArgs a) {
             } else {
                 atomicAdd(a.img + js, v);
             }
-            WeightSink sink{reinterpret_cast<unsigned long long*>(a.weight), a.wscale, g.n[0], g.n[1], g.n[2],
-                            g.w[2], a.length_weighted, 0, xs, ys, zs};
-            if (a.straight) {
-                siddon_walk(g, r.pin, r.pout, sink);
-            } else {
-                siddon_walk(g, r.pin, ps, sink);
-                sink.skip_scat = !a.length_weighted;
-                siddon_walk(g, ps, r.pout, sink);
-            }
         }
     }
+    // kept rays to the walk list, one atomic per warp
+    const unsigned act = __activemask(), b = __ballot_sync(act, kept);
+    const int lane = threadIdx.x & 31, lead = __ffs(act) - 1;
+    unsigned long long base = 0;
+    if (lane == lead && b) base = atomicAdd(a.walk_count, static_cast<unsigned long long>(__popc(b)));
+    base = __shfl_sync(act, base, lead);
+    if (kept) a.walk[base + __popc(b & ((1u << lane) - 1u))] = static_cast<uint32_t>(i);
     warp_count(&a.ctr->not_parallel, parallel_ok);
     warp_count(&a.ctr->in_grid, kept);
+}
+
+// The Siddon weights of the kept rays (:100-121), a thread per listed ray.
+__global__ void k_poca_walk(PocaArgs a) {
+    const uint64_t n = *a.walk_count;
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    const DevGrid g = make_dev_grid(a.g);
+    const double zmin = a.rays[0].pout[2], zmax = a.rays[0].pin[2];
+    for (uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const muto_ray r = a.rays[a.walk[t]];
+        double ps[3];
+        uint32_t xyz[3];
+        bool parallel_ok;
+        poca_bin(g, r, a.eps, zmin, zmax, ps, xyz, &parallel_ok);  // the kernel above kept it
+        WeightSink sink{a.weight, g.n[0], g.n[1], g.n[2], g.w[2], a.length_weighted, 0, xyz[0], xyz[1], xyz[2]};
+        if (a.straight) {
+            siddon_walk(g, r.pin, r.pout, sink);
+        } else {
+            siddon_walk(g, r.pin, ps, sink);
+            sink.skip_scat = !a.length_weighted;
+            siddon_walk(g, ps, r.pout, sink);
+        }
+    }
 }
 
 __global__ void k_pocut_hist(const uint32_t* __restrict__ vox, uint64_t n, uint32_t* __restrict__ counts) {
@@ -201,25 +218,17 @@ __global__ void k_poca_normalize(double* __restrict__ img, const double* __restr
 
 }  // namespace
 
-void launch_poca(const PocaArgs& a, cudaStream_t s) {
-    if (a.n == 0) return;  // the weights stay all-zero bits, which is 0.0
+void launch_poca(const PocaArgs& a, int num_sms, cudaStream_t s) {
+    if (a.n == 0) return;
+    cudaMemsetAsync(a.walk_count, 0, sizeof(unsigned long long), s);
     const unsigned nb = static_cast<unsigned>((a.n + 127) / 128);
     k_poca<<<nb, 128, 0, s>>>(a);
-    const uint64_t V = static_cast<uint64_t>(a.g.nx) * a.g.ny * a.g.nz;
-    k_weight_from_fixed<<<static_cast<unsigned>((V + 255) / 256), 256, 0, s>>>(a.weight, V, 1.0 / a.wscale);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_poca_walk, 128, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const uint64_t need = (a.n + 127) / 128, cap = static_cast<uint64_t>(per_sm) * num_sms;
+    k_poca_walk<<<static_cast<unsigned>(need < cap ? need : cap), 128, 0, s>>>(a);
     count_launches(2);
-}
-
-double poca_weight_scale(uint64_t n_rays, const muto_grid& g, int length_weighted) {
-    // a ray adds at most twice (in and out half) the longest in-voxel length
-    // (or dz) to a voxel; the sum over all rays must stay below 2^62
-    const double wmax = length_weighted ? std::sqrt(g.dx * g.dx + g.dy * g.dy + g.dz * g.dz) : g.dz;
-    const double worst = 2.0 * static_cast<double>(n_rays > 0 ? n_rays : 1) * (wmax > 0 ? wmax : 1.0);
-    int e = 0;
-    std::frexp(4.611686018427387904e18 / worst, &e);  // 2^62 / worst = f * 2^e, f in [0.5, 1)
-    e -= 1;                                           // 2^e <= 2^62 / worst
-    e = e < -60 ? -60 : (e > 60 ? 60 : e);
-    return std::ldexp(1.0, e);
 }
 
 void launch_pocut_hist(const uint32_t* vox, uint64_t n, uint32_t* counts, cudaStream_t s) {

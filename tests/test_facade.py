@@ -272,3 +272,35 @@ def test_fit_tracks_host_checks():
     assert M.fit_tracks(np.zeros((0, 14)), Z, N_MIDDLE).shape == (0, 14)
     with pytest.raises(ValueError):
         M.fit_tracks(np.zeros((3, 13)), Z, N_MIDDLE)
+
+
+UNPACK_PROGRAM = r"""
+#include <cstdio>
+#include "MutoSiddon.h"
+int main() {
+    const uint32_t xyz[9] = {1, 2, 3, 4, 5, 6, 7, 8, 9};
+    const double len[3] = {0.5, 1.5, 2.5};
+    bool failed = false;
+    std::vector<VoxelData> a = MutoSiddon::unpackPath(2, 3, xyz, len, &failed);
+    std::printf("%zu %d %u %u %u %.1f\n", a.size(), failed ? 1 : 0, a[1].x, a[1].y, a[1].z, a[1].length);
+    std::vector<VoxelData> b = MutoSiddon::unpackPath(0xffffffffu, 3, xyz, len, &failed);
+    std::printf("%zu %d\n", b.size(), failed ? 1 : 0);
+    return 0;
+}
+"""
+
+
+def test_siddon_facade_reports_a_walk_stopped_by_its_bound(facade, tmp_path):
+    # a count of 0xffffffff from the device is a failed walk: an empty path
+    # and a failure flag, not cap zero-filled voxels
+    src = tmp_path / "unpack.cpp"
+    src.write_text(UNPACK_PROGRAM)
+    exe = tmp_path / "unpack"
+    lib = B.facade_lib_path().parent
+    root = lib.parent
+    subprocess.run(["g++", "-std=c++17", "-I", str(root.parent / "include"), "-I", str(root / "cpp"), "-I",
+                    str(root / "csrc"), str(src), "-o", str(exe), "-L", str(lib), "-lmuto_facade", "-lmuto_gb300",
+                    f"-Wl,-rpath,{lib}"], check=True, capture_output=True, timeout=120)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.split("\n")[:2] == ["2 0 4 5 6 1.5", "0 1"]
