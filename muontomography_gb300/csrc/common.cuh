@@ -164,7 +164,7 @@ struct PocaArgs {
     uint32_t* vox;      // PoCut: per ray its voxel, 0xffffffff when rejected (null for PoCA)
     double* value;      // PoCut: per ray its value (angle^2, times p^2 with momentum)
 };
-void launch_poca(const PocaArgs& a, int num_sms, cudaStream_t s);
+void launch_poca(const PocaArgs& a, cudaStream_t s);
 void launch_poca_normalize(double* img, const double* weight, uint64_t V, double eps, cudaStream_t s);
 // slr.cu: straight-line reconstruction (src/MutoSLR.cpp:47-103) and the
 // iterative form's passes (src/MutoSLRIter.cpp:15-83)

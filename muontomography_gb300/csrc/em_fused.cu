@@ -30,7 +30,8 @@
 // one-pass variants.
 //
 // Recompute pass (k_em_fused_walk).  The same sums without stored lists: a
-// thread per muon walks its merged path in FP64 (the bit-exact Siddon walk
+// thread per muon (one muon each, so that a warp's lanes walk in step) walks
+// its merged path in FP64 (the bit-exact Siddon walk
 // of the set-up) once to sum Sigma, does the 2x2 algebra (a muon per lane),
 // and walks it again to add g_ij to G_j.  T_ij comes from the muon's total
 // in-grid length (kept per muon at set-up) minus the running length.
@@ -356,9 +357,10 @@ struct PlainSink {  // straight_line: the segment pin -> pout as it is
 
 // Walks the muon's path as the set-up does and hands every pair to emit;
 // false when a walk hit its step bound (the set-up drops such a muon).
+// `lanes`: the warp's lanes making this walk (walk_lanes), synced between the halves.
 template <class Emit>
 __device__ __forceinline__ bool walk_path(const DevGrid& g, const muto_ray& r, const double* ps, int straight,
-                                          Emit& emit) {
+                                          Emit& emit, unsigned lanes) {
     if (straight) {
         PlainSink<Emit> s{&emit};
         return siddon_walk(g, r.pin, r.pout, s) >= 0;
@@ -366,6 +368,7 @@ __device__ __forceinline__ bool walk_path(const DevGrid& g, const muto_ray& r, c
     MergedSink<Emit> s{&emit};
     const int ci = siddon_walk(g, r.pin, ps, s);
     s.phase = 1;
+    __syncwarp(lanes);
     const int co = siddon_walk(g, ps, r.pout, s);
     s.finish();
     return ci >= 0 && co >= 0;
@@ -431,20 +434,23 @@ __global__ void __launch_bounds__(128) k_em_fused_walk(FusedArgs<Real> a) {
     unsigned long long singular_local = 0;
     const VoxelIndexer ix{a.g.n[0], a.g.n[0] * a.g.n[1], a.bdims, a.brick};
     const uint64_t keep = l2_keep_policy();
-    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-    for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < a.N; i += stride) {
+    // a thread per muon (not a grid-stride loop, whose lanes would drift out of step)
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    // (ltot < 0: a walk the set-up dropped at its step bound: no pairs)
+    const double ltot = i < a.N ? a.ltot[i] : -1.0;
+    const unsigned lanes = walk_lanes(ltot >= 0.0);
+    if (ltot >= 0.0) {
         const muto_ray r = a.rays[a.kept[i]];
         const double ps[3] = {a.scat[3 * i], a.scat[3 * i + 1], a.scat[3 * i + 2]};
-        const double ltot = a.ltot[i];
-        if (ltot < 0.0) continue;  // a walk the set-up dropped (step bound): no pairs
         SumEmit<Real> se{a.lam, ix, keep, ltot};
-        walk_path(a.g, r, ps, a.straight, se);
+        walk_path(a.g, r, ps, a.straight, se, lanes);
         se.drain();
         Real k0, k1, k2;
-        muon_coefficients<Real>(se.c0, se.c1, se.c2, a.pr2[i], a.sd[i], a.E00, a.E01, a.E11, a.compute_cost != 0, k0,
-                                k1, k2, cost_local, singular_local);
+        muon_coefficients<Real>(se.c0, se.c1, se.c2, a.pr2[i], a.sd[i], a.E00, a.E01, a.E11, a.compute_cost != 0,
+                                k0, k1, k2, cost_local, singular_local);
         ScatterEmit<Real> ce{a.G, ix, keep, ltot, 0.0, k0, k1, k2};
-        walk_path(a.g, r, ps, a.straight, ce);
+        __syncwarp(lanes);
+        walk_path(a.g, r, ps, a.straight, ce, lanes);
     }
     flush_counters<128>(cost_local, singular_local, a.compute_cost, a.ctr);
 }
@@ -465,11 +471,12 @@ __global__ void k_path_stats(const muto_ray* __restrict__ rays, const uint32_t* 
                              const double* __restrict__ scat, uint64_t n, DevGrid g, int straight,
                              double* __restrict__ ltot, uint32_t* __restrict__ mult, Counters* ctr) {
     const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const unsigned lanes = walk_lanes(i < n);
     if (i >= n) return;
     const muto_ray r = rays[kept[i]];
     const double ps[3] = {scat[3 * i], scat[3 * i + 1], scat[3 * i + 2]};
     StatEmit e{mult, g.n[0], g.n[0] * g.n[1]};
-    if (!walk_path(g, r, ps, straight, e)) {
+    if (!walk_path(g, r, ps, straight, e, lanes)) {
         // dropped like the set-up's fill walk drops it; its voxels were counted
         // as they were walked, so count the same walk again with -1
         atomicAdd(&ctr->overflow, 1ull);
@@ -488,11 +495,13 @@ __global__ void k_path_uncount(const muto_ray* __restrict__ rays, const uint32_t
                                const double* __restrict__ scat, uint64_t n, DevGrid g, int straight,
                                const double* __restrict__ ltot, uint32_t* __restrict__ mult) {
     const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n || ltot[i] >= 0.0) return;
+    const bool again = i < n && ltot[i] < 0.0;
+    const unsigned lanes = walk_lanes(again);
+    if (!again) return;
     const muto_ray r = rays[kept[i]];
     const double ps[3] = {scat[3 * i], scat[3 * i + 1], scat[3 * i + 2]};
     UncountEmit e{mult, g.n[0], g.n[0] * g.n[1]};
-    walk_path(g, r, ps, straight, e);
+    walk_path(g, r, ps, straight, e, lanes);
 }
 
 // The voxel side: lambda_j + lambda_j^2 G_j / (2 M_j) (0 when M_j = 0), or the
@@ -629,13 +638,8 @@ template void launch_em_fused<double>(const FusedArgs<double>&, int, int, cudaSt
 template <typename Real>
 void launch_em_fused_walk(const FusedArgs<Real>& a, int num_sms, cudaStream_t s) {
     if (a.N == 0) return;
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_em_fused_walk<Real>, 128, 0) != cudaSuccess ||
-        per_sm < 1)
-        per_sm = 1;
-    const uint64_t need = (static_cast<uint64_t>(a.N) + 127) / 128;
-    const uint64_t cap = static_cast<uint64_t>(per_sm) * num_sms;
-    k_em_fused_walk<Real><<<static_cast<unsigned>(need < cap ? need : cap), 128, 0, s>>>(a);
+    (void)num_sms;
+    k_em_fused_walk<Real><<<static_cast<unsigned>((static_cast<uint64_t>(a.N) + 127) / 128), 128, 0, s>>>(a);
     count_launches(1);
 }
 template void launch_em_fused_walk<float>(const FusedArgs<float>&, int, cudaStream_t);

@@ -60,6 +60,14 @@ __device__ __forceinline__ int siddon_step_bound(const DevGrid& g) {
     return static_cast<int>(g.n[0] + g.n[1] + g.n[2]) + 8;
 }
 
+// The lanes of a warp that walk paths, for __syncwarp between consecutive
+// walks: a thread-per-path kernel calls this once at its start, with every
+// lane of the warp present (no lane has returned yet) and `walks` true on the
+// lanes that will make every one of the walks.  Without the sync, lanes that
+// finish a walk early start the next one on their own and the warp's lanes
+// no longer step together.
+__device__ __forceinline__ unsigned walk_lanes(bool walks) { return __ballot_sync(0xffffffffu, walks); }
+
 // Voxel walk of the segment p1 -> p2 (src/MutoSiddon.cpp:9-141).  For every
 // voxel with a recorded length the sink is called as sink(ix, iy, iz, len).
 // Returns the number of voxels, or -1 if the step bound was hit (never for a
@@ -119,10 +127,20 @@ __device__ __forceinline__ int siddon_walk(const DevGrid& g, const double* p1, c
     // integer compares need finite values (then every later crossing is finite too)
     const bool fast = isfinite(alpha) && isfinite(amax) && isfinite(an[0]) && isfinite(an[1]) && isfinite(an[2]);
     const long long amax_b = fast ? dbits(amax) : -1, eps_b = dbits(eps);
+    // The lanes of a warp that walk together step together: every iteration
+    // starts with a ballot over the lanes still walking, which makes it a
+    // reconvergence point (the three-way step below would otherwise let the
+    // lanes drift apart for the rest of the walk, each then issuing its own
+    // FP64 instructions).
+    unsigned live = __activemask();
     for (;;) {  // :108-138
         const long long alpha_b = fast ? dbits(alpha) : -1;
-        if (!((alpha_b | amax_b) >= 0 ? alpha_b < amax_b : alpha < amax)) break;
-        if (++steps > bound) return -1;
+        const bool more = (alpha_b | amax_b) >= 0 ? alpha_b < amax_b : alpha < amax;
+        const bool over = more && steps >= bound;  // the step bound: never for a walk that ends
+        live = __ballot_sync(live, more && !over);
+        if (!more) break;
+        if (over) return -1;
+        ++steps;
         const uint32_t vx = idx[0], vy = idx[1], vz = idx[2];
         // min of the three next crossings, reference tie-break order
         const long long b0 = fast ? dbits(an[0]) : -1, b1 = dbits(an[1]), b2 = dbits(an[2]);

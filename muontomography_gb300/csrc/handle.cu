@@ -630,7 +630,7 @@ void prepare_poca(muto_handle* h) {
     a.walk_count = walk.as<unsigned long long>();
     a.walk = reinterpret_cast<uint32_t*>(walk.as<unsigned long long>() + 1);
     if (!h->P.pocut) {
-        run(h, "poca", [&] { launch_poca(a, h->num_sms, h->stream); });
+        run(h, "poca", [&] { launch_poca(a, h->stream); });
         run(h, "poca_normalize", [&] { launch_poca_normalize(h->img64.as<double>(), h->weight.as<double>(), V, h->P.eps, h->stream); });
         return;
     }
@@ -649,7 +649,7 @@ void prepare_poca(muto_handle* h) {
     a.img = nullptr;
     a.vox = vox.as<uint32_t>();
     a.value = value.as<double>();
-    run(h, "poca", [&] { launch_poca(a, h->num_sms, s); });
+    run(h, "poca", [&] { launch_poca(a, s); });
     run(h, "pocut_group", [&] {
         launch_pocut_hist(vox.as<uint32_t>(), nt, counts.as<uint32_t>(), s);
         scan_u32_to_u64(counts.as<uint32_t>(), off.as<uint64_t>(), V, scan_scr.as<void>(), s);

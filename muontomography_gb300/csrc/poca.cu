@@ -85,13 +85,17 @@ __global__ void k_poca(PocaArgs a) {
     warp_count(&a.ctr->in_grid, kept);
 }
 
-// The Siddon weights of the kept rays (:100-121), a thread per listed ray.
+// The Siddon weights of the kept rays (:100-121), a thread per listed ray
+// (not a grid-stride loop: lanes that finished a ray would start their next
+// one while the others still walk, and the warp would not step together
+// again).
 __global__ void k_poca_walk(PocaArgs a) {
     const uint64_t n = *a.walk_count;
-    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
     const DevGrid g = make_dev_grid(a.g);
     const double zmin = a.rays[0].pout[2], zmax = a.rays[0].pin[2];
-    for (uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; t < n; t += stride) {
+    const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const unsigned lanes = walk_lanes(t < n);
+    if (t < n) {
         const muto_ray r = a.rays[a.walk[t]];
         double ps[3];
         uint32_t xyz[3];
@@ -103,6 +107,7 @@ __global__ void k_poca_walk(PocaArgs a) {
         } else {
             siddon_walk(g, r.pin, ps, sink);
             sink.skip_scat = !a.length_weighted;
+            __syncwarp(lanes);
             siddon_walk(g, ps, r.pout, sink);
         }
     }
@@ -218,16 +223,12 @@ __global__ void k_poca_normalize(double* __restrict__ img, const double* __restr
 
 }  // namespace
 
-void launch_poca(const PocaArgs& a, int num_sms, cudaStream_t s) {
+void launch_poca(const PocaArgs& a, cudaStream_t s) {
     if (a.n == 0) return;
     cudaMemsetAsync(a.walk_count, 0, sizeof(unsigned long long), s);
     const unsigned nb = static_cast<unsigned>((a.n + 127) / 128);
     k_poca<<<nb, 128, 0, s>>>(a);
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_poca_walk, 128, 0) != cudaSuccess || per_sm < 1)
-        per_sm = 1;
-    const uint64_t need = (a.n + 127) / 128, cap = static_cast<uint64_t>(per_sm) * num_sms;
-    k_poca_walk<<<static_cast<unsigned>(need < cap ? need : cap), 128, 0, s>>>(a);
+    k_poca_walk<<<nb, 128, 0, s>>>(a);  // one thread per ray that can have been kept
     count_launches(2);
 }
 

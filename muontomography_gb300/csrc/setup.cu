@@ -221,6 +221,7 @@ __global__ void k_path_fill_bounded(const muto_ray* __restrict__ rays, const uin
                                     Real* __restrict__ L, Real* __restrict__ T, uint32_t* __restrict__ counts,
                                     Counters* ctr, uint64_t slot_base) {
     const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const unsigned lanes = walk_lanes(i < n);
     if (i >= n) return;
     const uint64_t b = boff[i] - slot_base, e = boff[i + 1] - slot_base;
     const muto_ray& r = rays[kept[i]];
@@ -236,6 +237,7 @@ __global__ void k_path_fill_bounded(const muto_ray* __restrict__ rays, const uin
         FillSink s{vidx, l64, b, e, nx, nxy};
         const int ci = siddon_walk(g, r.pin, ps, s);
         s.phase = 1;
+        __syncwarp(lanes);
         const int co = siddon_walk(g, ps, r.pout, s);
         if (s.pending) s.emit(s.pj, dadd(s.pl, 0.0));  // out-half empty: length += 0.0
         overflow = ci < 0 || co < 0;
