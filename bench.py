@@ -186,7 +186,7 @@ def wl_lambda(wl) -> np.ndarray:
 
 def em_config(wl, args, precision: str, n_iter: int, lists: str | None = None) -> dict:
     over = {"precision": precision, "num_iteration": n_iter, "muon_pass": args.muon_pass,
-            "muon_layout": args.muon_layout, "path_lists": lists or args.lists}
+            "muon_layout": args.muon_layout, "path_lists": lists or args.lists, "fused_variant": args.fused_variant}
     if method_of(args) == "map":  # beta 0.01, p = 1, the 26-neighbour stencil, delta = 0.1 median(lambda) 1e7
         over.update(beta=0.01, p=1.0, all_neighbours=True, delta=0.1 * float(np.median(wl_lambda(wl))) * 1e7)
     if getattr(args, "voxel_stream_above", None) is not None:
@@ -564,6 +564,8 @@ def main() -> int:
     ap.add_argument("--cpu-sample-fixed", action="store_true",
                     help="reference leg: use --cpu-sample as it is instead of sizing it to the step count")
     ap.add_argument("--muon-pass", choices=["auto", "tile", "warp"], default="auto")
+    ap.add_argument("--fused-variant", choices=["auto", "4x8", "8x4", "8x8", "8x16", "16x8", "16x16", "split"],
+                    default="auto", help="the mean update's pass over muon-major lists (auto: timed at set-up)")
     ap.add_argument("--muon-layout", choices=["auto", "columns", "index"], default="auto")
     ap.add_argument("--voxel-stream-above", type=int, default=None,
                     help="segments longer than this are selected without holding their keys (-1: never)")

@@ -6,7 +6,8 @@
 # Only possible where the reference tree is mounted; test infrastructure only.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${MUTO_REFERENCE:-/root/reference}
+# the reference's source tree: $MUTO_REFERENCE, else "reference" beside this repository
+REF=${MUTO_REFERENCE:-$(cd "$HERE/../.." && pwd)/reference}
 [ -d "$REF/src" ] || { echo "reference sources not found at $REF" >&2; exit 2; }
 mkdir -p "$HERE/_ref"
 g++ -O2 -std=c++14 -fPIC -shared -fopenmp -ffp-contract=off -fno-fast-math -w \

@@ -21,7 +21,9 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_ref" / "libmuto_ref.so"
 FILE_LIB = HERE / "_ref" / "libmuto_ref_file.so"
 CLI = HERE / "_ref" / "muto_ref_cli"
-REF = Path(os.environ.get("MUTO_REFERENCE", "/root/reference"))
+# the reference's source tree: $MUTO_REFERENCE, else a directory named
+# "reference" beside this repository's root
+REF = Path(os.environ.get("MUTO_REFERENCE", str(HERE.parent.parent / "reference")))
 
 
 def available() -> bool:
