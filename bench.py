@@ -47,6 +47,7 @@ WORKLOADS = {
     "cube50_40mm": lambda W: W.cube50_40mm,  # the same scene on 50^3 voxels of 40 mm, 2.5 M muons
     "cube20_50mm": lambda W: W.cube20_50mm,  # 20^3 voxels of 50 mm, 100 k muons
     "map128x128x64_15mm": lambda W: W.map128x128x64_15mm,  # 128x128x64 voxels of 15 mm, 20 M muons
+    "batch64": None,  # 64 scans of 32^3..128^3 voxels of 20 mm, 50 k..5 M muons each, in one batch handle
 }
 # the EM update each workload is benchmarked with: the throughput scan with
 # the mean update (its per-voxel lists do not fit next to the muon-major
@@ -162,6 +163,9 @@ def workload(args, rank: int):
     from muontomography_gb300 import workloads as W
     from muontomography_gb300.replicas import replica_seed
 
+    if args.workload == "batch64":  # the CPU legs sample the batch's first scan
+        wl = W.batch64(seed=replica_seed(4, rank))[0]
+        return wl
     fn = WORKLOADS[args.workload](W)
     kw = {}
     if args.n_muons:
@@ -542,6 +546,190 @@ def run_ours(args) -> int:
     return 0
 
 
+def run_batch(args) -> int:
+    """The 64-scan batch: every pass of an EM iteration is one launch over all scans."""
+    import torch
+
+    from muontomography_gb300.replicas import Replicas, replica_seed
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    rep = Replicas("nccl")
+    import muontomography_gb300 as M
+    from muontomography_gb300 import _lib
+    from muontomography_gb300 import workloads as W
+
+    lib = M.library()
+    wls = W.batch64(scale=args.batch_scale, seed=replica_seed(4, rank))
+    grids = [w.grid for w in wls]
+    t0 = time.perf_counter()
+    tracks = []
+    for w in wls:
+        lam = torch.tensor(w.lam(), dtype=torch.float64, device="cuda")
+        d = torch.empty((w.n_muons, 14), dtype=torch.float64, device="cuda")
+        prm = _lib.muto_gen_params(w.seed, np.pi / 3, 1.0, 10.0, 3.0, 500.0, 3, 0, 1.0)
+        g = w.grid.c()
+        _lib.check(lib.muto_generate_device(C.byref(g), C.c_void_p(lam.data_ptr()), C.byref(prm), 0, w.n_muons,
+                                            C.c_void_p(d.data_ptr()),
+                                            C.c_void_p(torch.cuda.current_stream().cuda_stream)), "generate")
+        tracks.append(d)
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    n_all = sum(w.n_muons for w in wls)
+    sp = C.c_void_p()
+
+    def batch_cfg(precision, n_iter):
+        cfg = em_config(wls[0], args, precision, n_iter)
+        cfg.pop("grid")
+        cfg.update(initialize_method=2, voxel_stream_above="auto")
+        return cfg
+
+    def loaded(precision, n_iter):
+        b = M.Batch(batch_cfg(precision, n_iter), grids)
+        for k, d in enumerate(tracks):
+            b.load_scan(k, on_device_ptr=d.data_ptr(), n=d.shape[0])
+        return b
+
+    b = loaded(args.precision, args.warmup + args.steps)
+    b.set_profiling(True)
+    t0 = time.perf_counter()
+    b.prepare()
+    t_setup = time.perf_counter() - t0
+    st = b.status()
+    pairs, kept, V = st["n_pairs"], st["n_scat_in_grid"], sum(g.nvox for g in grids)
+    lib.muto_get_stream(b._h, C.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value)
+    for _ in range(args.warmup):
+        b.iterate(1)
+    b.reset_kernel_stats()
+    l0 = b.launch_count()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    rep.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        b.iterate(1)
+    e1.record(stream)
+    e1.synchronize()
+    rep.barrier()
+    ms = rep.max(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    launches = b.launch_count() - l0
+    value = rep.sum(float(pairs)) * args.steps / (ms / 1000.0)
+    kern = {}
+    for k in ITER_KERNELS:
+        c, t = b.kernel_stats(k)
+        if c:
+            kern[k] = t / args.steps
+    b.set_profiling(False)
+    img_mixed = [b.scan_image(k) for k in range(len(wls))] if args.precision == "mixed" else None
+    b.close()
+
+    rb = 4 if args.precision == "mixed" else 8
+    pk = peaks()
+    per_kernel = {}
+    for k, kms in kern.items():
+        nb = algorithmic_bytes(k, rb, pairs, kept, V)
+        if nb:
+            ach = nb / (kms / 1000.0) / 1e9
+            per_kernel[k] = {"kernel_ms": kms, "algorithmic_bytes": nb, "achieved": ach, "frac": ach / pk["hbm_gbs"],
+                             "traffic": None}
+    dom = max(per_kernel, key=lambda k: per_kernel[k]["kernel_ms"]) if per_kernel else None
+    roofline = {"bound": "hbm", "peak": pk["hbm_gbs"], "unit": "GB/s", "peak_source": pk["source"],
+                "kernels": per_kernel}
+    if dom:
+        d = per_kernel[dom]
+        roofline.update(kernel=dom, achieved=d["achieved"], frac=d["frac"], traffic=None, kernel_ms=d["kernel_ms"],
+                        algorithmic_bytes=d["algorithmic_bytes"])
+
+    # per-scan lambda of the mixed form against the plain FP64 form after the same iterations
+    errors = None
+    if img_mixed is not None and args.ttl_iters > 0:
+        b64 = loaded("fp64", args.warmup + args.steps)
+        t0 = time.perf_counter()
+        b64.prepare()
+        b64.iterate(args.warmup + args.steps)
+        ref = [b64.scan_image(k) for k in range(len(wls))]
+        t64 = time.perf_counter() - t0
+        b64.close()
+        rel = [float(np.linalg.norm(a.ravel() - r.ravel()) / max(np.linalg.norm(r.ravel()), 1e-300))
+               for a, r in zip(img_mixed, ref)]
+        errors = {"iterations": args.warmup + args.steps, "max_rel_l2": max(rel), "median_rel_l2": statistics.median(rel),
+                  "all_within_1e-4": max(rel) < 1e-4, "per_scan_rel_l2": [round(x, 10) for x in rel],
+                  "fp64_form_s": t64, "what": "per scan, the mixed form's lambda against the plain FP64 GPU form "
+                                             "after the same iterations (set-up and iterations of the FP64 form timed)"}
+
+    # e2e: load every scan from pinned host memory, set up, iterate, read every image
+    e2e = None
+    if args.e2e_steps > 0:
+        hosts = []
+        for d in tracks:
+            h = torch.empty(tuple(d.shape), dtype=torch.float64, pin_memory=True)
+            h.copy_(d)
+            hosts.append(h)
+        e_iters = args.e2e_iters if args.e2e_iters > 0 else wls[0].n_iter
+        times = []
+        for rnd in range(args.e2e_steps + 1):  # the first round is a warm-up
+            bb = M.Batch(batch_cfg(args.precision, e_iters), grids)
+            lib.muto_get_stream(bb._h, C.byref(sp))
+            s2 = torch.cuda.ExternalStream(sp.value)
+            a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(s2)
+            for k, h in enumerate(hosts):
+                _lib.check(lib.muto_batch_load_tracks(bb._h, k, C.c_void_p(h.data_ptr()), h.shape[0], 0), "load")
+            bb.prepare()
+            bb.iterate(e_iters)
+            out = [bb.scan_image(k) for k in range(len(wls))]
+            z.record(s2)
+            z.synchronize()
+            if rnd > 0:
+                times.append(a.elapsed_time(z))
+            bb.close()
+        e_ms = rep.max(statistics.mean(times))
+        e2e = {"value": rep.sum(float(pairs)) * e_iters / (e_ms / 1000.0), "unit": UNIT,
+               "h2d_bytes_per_step": int(n_all * 14 * 8), "d2h_bytes_per_step": int(V * 8), "ms_per_step": e_ms,
+               "em_iterations_per_step": e_iters,
+               "what": f"64 scans: H2D of pinned tracks, set-up, {e_iters} EM iterations, D2H of every image"}
+        del hosts, out
+
+    cpu = None
+    if rank == 0 and args.cpu_sample > 0:
+        ns = min(args.cpu_sample, tracks[0].shape[0])
+        sample = tracks[0][:ns].cpu().numpy()
+        r = cpu_port(wls[0], args, sample, 2, host_cores())
+        cval = r["pairs"] * len(r["times"]) / sum(r["times"])
+        cpu = {"value": cval, "unit": UNIT, "cores": host_cores(), "kind": "port",
+               "sample": f"the first {ns} muons of scan 0 ({wls[0].grid.nx}^3 voxels), 2 EM iterations "
+                         f"({r['pairs']} pairs each), set-up untimed"}
+    del tracks
+    if rank == 0:
+        sides = [g.nx for g in grids]
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "config": {"workload": "batch64", "scans": len(wls), "muons": n_all, "kept_muons": kept,
+                       "pairs_per_iteration": pairs, "voxels": V, "mode": args.mode, "precision": args.precision,
+                       "grids": {str(n): sides.count(n) for n in (32, 64, 96, 128)},
+                       "muons_per_scan": [min(w.n_muons for w in wls), max(w.n_muons for w in wls)],
+                       "graph": True, "one_launch_per_pass": True, "setup_s": t_setup, "generate_s": t_gen,
+                       "device_bytes": st["device_bytes"],
+                       "autotuner": {"muon_pass": {1: "tma_tiles", 2: "warp_batched"}.get(st["muon_pass"]),
+                                     "muon_group": st["muon_group"],
+                                     "voxel_stream_above": st["voxel_stream_above"]},
+                       "parallelism": f"replicas x{world} (one batch per GPU)",
+                       "l2": "inputs larger than L2: the batch's pair lists far exceed 126 MB, no flush"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+            "lambda_errors": errors,
+        }
+        print(json.dumps(line), flush=True)
+    rep.close()
+    return 0
+
+
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -561,6 +749,7 @@ def main() -> int:
     ap.add_argument("--recompute-iters", type=int, default=2)
     ap.add_argument("--poca", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=1_000_000)
+    ap.add_argument("--batch-scale", type=float, default=1.0, help="batch64: muons per scan times this")
     ap.add_argument("--cpu-sample-fixed", action="store_true",
                     help="reference leg: use --cpu-sample as it is instead of sizing it to the step count")
     ap.add_argument("--muon-pass", choices=["auto", "tile", "warp"], default="auto")
@@ -575,10 +764,12 @@ def main() -> int:
     if args.ttl_iters < 0:
         from muontomography_gb300 import workloads as W
 
-        args.ttl_iters = WORKLOADS[args.workload](W)().n_iter
+        args.ttl_iters = 20 if args.workload == "batch64" else WORKLOADS[args.workload](W)().n_iter
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
-    return run_reference(args) if args.impl == "reference" else run_ours(args)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_batch(args) if args.workload == "batch64" else run_ours(args)
 
 
 if __name__ == "__main__":

@@ -79,7 +79,8 @@ typedef struct muto_status {
     int32_t path_lists;         /* how the pairs are kept: 1 muon-major lists and their voxel-major copy,
                                    2 muon-major lists only, 3 none (paths walked every iteration);
                                    0 for the one-shot methods */
-    int32_t reserved;
+    int32_t voxel_stream_above; /* voxel pass in use: segments longer than this are selected from the
+                                   key array instead of registers (-1: none); "auto" picks it */
     char message[256];          /* text of the last error */
 } muto_status;
 
@@ -110,7 +111,9 @@ typedef struct muto_handle muto_handle;
  * in muon order; "columns" or "index" force one),
  * "voxel_stream_above" (-1: every segment up to 1536 pairs (768 in fp64)
  * is selected from registers; n >= 256: segments longer than n are
- * selected without holding their keys),
+ * selected without holding their keys; "auto": -1 or 512, whichever is
+ * faster on the scan's own lists, timed at prepare and reused for later
+ * scans of the same shape in the process),
  * "path_lists" (how the muon-voxel pairs are kept: "voxel_major" -- the
  * muon-major lists plus a voxel-major copy, which the median and
  * percentile updates need; "muon_major" -- the muon-major lists alone

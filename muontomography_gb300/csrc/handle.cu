@@ -153,7 +153,7 @@ struct Params {
     int newton_max_iter = 200;
     int tile_pairs = 0;
     int muon_pass = 0;  // 0 autotune, 1 tile (TMA), 2 warp-batched
-    long long voxel_stream_above = -1;  // segments longer than this are selected without registers (-1: none)
+    long long voxel_stream_above = -1;  // segments longer than this are selected without registers (-1: none, -2: tuned)
     int muon_layout = 0;  // coefficient rows: 0 auto (column order when the table outgrows L2), 1 columns, 2 index
     int path_lists = 0;   // 0 auto, 1 voxel-major copy, 2 muon-major lists only, 3 recomputed every iteration
     long long setup_chunk_pairs = 0;  // bounded pairs per set-up chunk (0: sized from free device memory)
@@ -249,7 +249,14 @@ Params parse_params(Method m, const std::string& text, int variant = 0) {
         else if (mp == "tile") P.muon_pass = 1;
         else if (mp == "warp") P.muon_pass = 2;
         else throw Error(MUTO_ERR_CONFIG, "muon_pass must be \"auto\", \"tile\" or \"warp\"");
-        P.voxel_stream_above = cfg.value("voxel_stream_above", static_cast<int64_t>(-1));
+        if (cfg.contains("voxel_stream_above") && cfg.at("voxel_stream_above").is_string()) {
+            if (cfg.value("voxel_stream_above", "") != "auto")
+                throw Error(MUTO_ERR_CONFIG, "voxel_stream_above must be an integer or \"auto\"");
+            P.voxel_stream_above = -2;  // chosen by timing at prepare
+        } else {
+            P.voxel_stream_above = cfg.value("voxel_stream_above", static_cast<int64_t>(-1));
+            if (P.voxel_stream_above < -1) throw Error(MUTO_ERR_CONFIG, "voxel_stream_above must be >= -1");
+        }
         const std::string ml = cfg.value("muon_layout", "auto");
         if (ml == "auto") P.muon_layout = 0;
         else if (ml == "columns") P.muon_layout = 1;
@@ -386,6 +393,7 @@ struct muto_handle {
     uint32_t vclass_n[kVoxClasses] = {};
     int vox_blocks_real[2 * kVoxClasses] = {}, vox_blocks_f64[2 * kVoxClasses] = {};  // resident blocks per class kernel
     uint32_t vox_streamed = 0;  // classes selected by the streamed path
+    long long vox_stream_above = -1;  // the threshold vox_streamed stands for (-1: none)
     uint64_t vclass_off[kVoxClasses] = {};
     DevMem kslot;                     // per kept muon: its row of kvec (empty: its own index)
     DevMem mult, start, kvec, keys;   // keys: the voxel pass's order key of every pair
@@ -1068,6 +1076,7 @@ void prepare_em(muto_handle* h) {
             }
             // the voxel pass's key array (kPad past the end: the class kernels'
             // L2 prefetches round out to 16 bytes)
+            h->vox_stream_above = P.voxel_stream_above == -2 ? -1 : P.voxel_stream_above;
             h->vox_streamed = P.voxel_stream_above < 0 ? 0u
                               : vox_streamed_mask(static_cast<uint32_t>(std::min<long long>(P.voxel_stream_above, 0xffffffffLL)));
             h->keys.alloc((Pn + kPad) * sizeof(typename KeyOf<Real>::type), &h->dev_bytes);
@@ -1451,6 +1460,83 @@ void autotune_muon_pass(muto_handle* h) {
     if (h->P.muon_pass == 0) {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         g_tune_choice[shape] = {pick.kind, pick.group};
+    }
+    CK(cudaMemcpyAsync(h->ctr(), &saved, sizeof(Counters), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+}
+
+std::map<std::pair<TuneShape, int>, long long> g_voxel_choice;  // per shape and log2(V) (guarded by g_tune_mu)
+
+template <typename Real, typename OutT>
+VoxelPassArgs<Real, OutT> voxel_args(muto_handle* h, const Real* lam, int mode, OutT* out);
+template <typename Real, typename OutT>
+void launch_voxel_pass(muto_handle* h, const VoxelPassArgs<Real, OutT>& v, cudaStream_t s);
+int voxel_mode(const Params& P);
+
+// In-project autotuner of the voxel pass's launch shape ("voxel_stream_above"
+// "auto"): the class kernels holding a voxel's keys in registers for every
+// segment up to the register budget, or streaming the classes beyond 512
+// pairs from the key array, timed on the scan's own lists after one muon
+// pass (one warm-up and two timed voxel passes each, into scratch, without
+// selection windows so that the iterations start as untuned ones do).
+template <typename Real>
+void autotune_voxel_pass(muto_handle* h) {
+    if (h->lists != kListsVoxelMajor || h->N == 0 || h->P.voxel_stream_above != -2) return;
+    HostPhase ph(h, "autotune");
+    int log2n = 0, log2v = 0;
+    while ((h->N >> log2n) > 1) ++log2n;
+    while ((h->V() >> log2v) > 1) ++log2v;
+    const std::pair<TuneShape, int> shape{TuneShape{h->fp64() ? 1 : 0, h->device, log2n,
+                                                    static_cast<int>(static_cast<double>(h->npairs) / h->N / 8.0)},
+                                          log2v};
+    auto apply = [&](long long above) {
+        h->vox_stream_above = above;
+        h->vox_streamed = above < 0 ? 0u : vox_streamed_mask(static_cast<uint32_t>(above));
+    };
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        const auto it = g_voxel_choice.find(shape);
+        if (it != g_voxel_choice.end()) {
+            apply(it->second);
+            return;
+        }
+    }
+    cudaStream_t s = h->stream;
+    Counters saved;
+    CK(cudaMemcpyAsync(&saved, h->ctr(), sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    launch_muon_pass<Real>(h, muon_args<Real>(h, h->lam.as<Real>(), false), s);  // the coefficients the pass reads
+    DevMem out;
+    out.alloc(h->V() * sizeof(Real), nullptr);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const long long cands[2] = {-1, 512};
+    float best = 1e30f;
+    long long pick = -1;
+    for (long long above : cands) {
+        apply(above);
+        auto v = voxel_args<Real, Real>(h, h->lam.as<Real>(), voxel_mode(h->P), out.as<Real>());
+        v.win = nullptr;
+        launch_voxel_pass<Real, Real>(h, v, s);
+        CK(cudaEventRecord(e0, s));
+        for (int r = 0; r < 2; ++r) launch_voxel_pass<Real, Real>(h, v, s);
+        CK(cudaEventRecord(e1, s));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaGetLastError());
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            pick = above;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    apply(pick);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_voxel_choice[shape] = pick;
     }
     CK(cudaMemcpyAsync(h->ctr(), &saved, sizeof(Counters), cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
@@ -1868,6 +1954,8 @@ int muto_get_status(const muto_handle* hc, muto_status* out) {
     out->tile_pairs = h->tile_pairs;
     out->tile_muons = h->tile_muons;
     out->path_lists = h->method == kPoca ? 0 : h->lists;
+    out->voxel_stream_above = h->method == kPoca || h->lists != kListsVoxelMajor
+                                  ? -1 : static_cast<int32_t>(std::min<long long>(h->vox_stream_above, 0x7fffffffLL));
     if (h->method != kPoca && h->lists == kListsMuonMajor && h->fused_variant == kFusedVariants) {
         out->muon_pass = 5;
         out->muon_group = h->scatter_group;
@@ -1939,12 +2027,20 @@ int muto_prepare(muto_handle* h) {
             prepare_poca(h);
         } else if (h->fp64()) {
             prepare_em<double>(h);
-            if (h->lists == kListsVoxelMajor) autotune_muon_pass<double>(h);
-            else autotune_fused<double>(h);
+            if (h->lists == kListsVoxelMajor) {
+                autotune_muon_pass<double>(h);
+                autotune_voxel_pass<double>(h);
+            } else {
+                autotune_fused<double>(h);
+            }
         } else {
             prepare_em<float>(h);
-            if (h->lists == kListsVoxelMajor) autotune_muon_pass<float>(h);
-            else autotune_fused<float>(h);
+            if (h->lists == kListsVoxelMajor) {
+                autotune_muon_pass<float>(h);
+                autotune_voxel_pass<float>(h);
+            } else {
+                autotune_fused<float>(h);
+            }
         }
         sync_and_harvest(h, pf);
         h->prepared = true;

@@ -106,3 +106,22 @@ def small(n_muons: int = 4000, seed: int = 11, n: int = 12) -> Workload:
     blocks = [Block((-100.0, -100.0, -100.0), (100.0, 100.0, 100.0), X0_MM["iron"]),
               Block((120.0, -60.0, -60.0), (240.0, 60.0, 60.0), X0_MM["lead"])]
     return Workload(f"small_{n}cube_{n_muons}", g, blocks, n_muons, seed, True, 5)
+
+
+def batch64(scale: float = 1.0, seed: int = 4) -> list[Workload]:
+    """64 independent scans of uneven sizes: cubic grids of 32, 64, 96 or 128
+    voxels a side at 20 mm, muon counts log-uniform between 50 k and 5 M (times
+    `scale`), each scan with its own seeded random phantom of three blocks of
+    iron, lead, aluminium or concrete."""
+    rng = np.random.default_rng(seed)
+    sides = rng.choice([32, 64, 96, 128], size=64)
+    muons = np.exp(rng.uniform(np.log(50_000), np.log(5_000_000), size=64))
+    mats = ["iron", "lead", "aluminium", "concrete"]
+    out = []
+    for k, (nside, nm) in enumerate(zip(sides, muons)):
+        half = float(nside) * 20.0 / 2
+        g = Grid(int(nside), int(nside), int(nside), -half, -half, -half, 20.0, 20.0, 20.0)
+        ext = float(nside) * 20.0
+        blocks = _random_blocks(rng, g, list(rng.choice(mats, size=3)), 0.1 * ext, 0.3 * ext)
+        out.append(Workload(f"batch64_scan{k:02d}", g, blocks, max(1000, int(nm * scale)), 400 + k, True, 20))
+    return out

@@ -141,3 +141,28 @@ def test_grid256_mixed_against_fp64(gpu):
         with M.MutoMLSD(wl.em_config(precision=prec, num_iteration=5)) as rec:
             out[prec] = rec.reconstruct(rays).reshape(-1, order="F")
     assert rel_l2(out["mixed"], out["fp64"]) < 1e-4
+
+
+def test_batch64_scans_match_the_oracle(gpu, oracle):
+    # the 64-scan batch at 1/100 of its muons, one handle, the voxel pass's
+    # launch shape chosen by the autotuner: per scan against the FP64 oracle
+    wls = W.batch64(scale=0.01)
+    tracks = [w.tracks() for w in wls]
+    out = {}
+    for prec in ("fp64", "mixed"):
+        cfg = wls[0].em_config(precision=prec, num_iteration=4, initialize_method=2, voxel_stream_above="auto")
+        cfg.pop("grid")
+        with M.Batch(cfg, [w.grid for w in wls]) as b:
+            out[prec] = b.reconstruct_all(tracks)
+            st = b.status()
+        assert st["voxel_stream_above"] in (-1, 512) and st["iterations_done"] == 4
+    small = sorted(range(64), key=lambda k: wls[k].n_muons)[:3]
+    for k in small:
+        cfg = wls[k].em_config(precision="fp64", num_iteration=4)
+        ref = oracle.Mlsd(wls[k].grid, cfg, tracks[k], np.full(wls[k].grid.nvox, 1e-7))
+        ref.iterate(4)
+        want = ref.image()
+        assert rel_l2(out["fp64"][k].reshape(-1, order="F"), want) < 1e-10, k
+        assert rel_l2(out["mixed"][k].reshape(-1, order="F"), want) < 1e-4, k
+    for k in range(64):
+        assert rel_l2(out["mixed"][k], out["fp64"][k]) < 1e-4, k
