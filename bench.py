@@ -502,6 +502,43 @@ def run_ours(args) -> int:
                "what": "set-up and iterations from device-resident tracks, wall clock; the FP64 GPU form stands "
                        "in for the FP64 oracle at this size"}
 
+    # ---- the gradient MAP solver against the MAP EM, to the same objective ---
+    grad_vs_em = None
+    if method_of(args) == "map" and args.grad_vs_em > 0 and rank == 0:
+        K = args.grad_vs_em
+        delta = 0.1 * float(np.median(wl_lambda(wl))) * 1e7
+        grad_vs_em = []
+        for beta in (1e-3, 1e-2):
+            for p in (2.0, 1.0):
+                gcfg = em_config(wl, args, args.precision, K)
+                gcfg.update(update_with_mean=True, mean_percentile=100, beta=beta, p=p, all_neighbours=True,
+                            delta=delta)
+                ra = M.Reconstruction("map", gcfg)
+                ra.load_tracks(None, on_device_ptr=d_rays.data_ptr(), n=n)
+                ra.prepare()
+                sa = stream_of(ra)
+                a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                a.record(sa)
+                ra.iterate(K)
+                z.record(sa)
+                z.synchronize()
+                mult = ra.multiplicity()
+                img = ra.image().reshape(-1, order="F")
+                f_em = ra.nll(np.log(np.where(mult > 0, np.maximum(img, 1e-300), 1.0)))
+                ra.close()
+                rg = M.Reconstruction("map", dict(gcfg, num_iteration=0))
+                rg.load_tracks(None, on_device_ptr=d_rays.data_ptr(), n=n)
+                rg.prepare()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                f_g, it = rg.gradient_solve_until(f_em, 200)
+                t_g = time.perf_counter() - t0
+                rg.close()
+                grad_vs_em.append({"beta": beta, "p": p, "em_iterations": K, "em_s": a.elapsed_time(z) / 1000.0,
+                                   "F_em": f_em, "gradient_iterations": it, "gradient_s": t_g, "F_gradient": f_g,
+                                   "reached": bool(f_g <= f_em)})
+
     # ---- CPU baseline on this machine's host cores (rank 0 only) ----------------
     cpu = None
     if rank == 0 and args.cpu_sample > 0:
@@ -542,6 +579,12 @@ def run_ours(args) -> int:
             "recompute": recompute,
             "poca": poca,
         }
+        if grad_vs_em is not None:
+            line["gradient_vs_em"] = {"runs": grad_vs_em, "what": (
+                "F = NLL + MAP prior (26 neighbours, delta 0.1 median lambda); the MAP EM with the mean ML step "
+                "(a scaled gradient step) for em_iterations, graph-captured, timed on the device; then the "
+                "gradient solver (preconditioned descent in log lambda with backtracking) from the same start "
+                "until F <= F_em, wall clock, its F and gradient from the same passes")}
         print(json.dumps(line), flush=True)
     rep.close()
     return 0
@@ -753,6 +796,8 @@ def main() -> int:
     ap.add_argument("--poca", type=int, default=1)
     ap.add_argument("--cpu-sample", type=int, default=1_000_000)
     ap.add_argument("--batch-scale", type=float, default=1.0, help="batch64: muons per scan times this")
+    ap.add_argument("--grad-vs-em", type=int, default=20,
+                    help="MAP workload: EM iterations the gradient solver is run to match (0: skip)")
     ap.add_argument("--cpu-sample-fixed", action="store_true",
                     help="reference leg: use --cpu-sample as it is instead of sizing it to the step count")
     ap.add_argument("--muon-pass", choices=["auto", "tile", "warp"], default="auto")

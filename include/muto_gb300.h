@@ -258,6 +258,11 @@ int muto_nll_backward(muto_handle* h, const double* log_lambda, double* out_valu
  * starting from the current image.  Leaves the result as the image and the
  * final F in *out_value. */
 int muto_gradient_solve(muto_handle* h, int n_iter, double* out_value);
+/* The same solver stopped as soon as F <= target (or after max_iter
+ * iterations, or when no step lowers F): *out_value is the F reached and
+ * *out_iters (may be NULL) the iterations taken.  Used to run the solver
+ * to the objective value an EM run reached. */
+int muto_gradient_solve_until(muto_handle* h, int max_iter, double target, double* out_value, int* out_iters);
 
 /* ---------------------------------------------------------------------------
  * Batches: many independent scans (each its own grid and tracks) in one

@@ -265,6 +265,13 @@ class Reconstruction:
         self._check(self._lib.muto_gradient_solve(self._h, int(n_iter), C.byref(v)), "muto_gradient_solve")
         return v.value
 
+    def gradient_solve_until(self, target: float, max_iter: int) -> tuple[float, int]:
+        """The gradient solver run until F <= target: (F reached, iterations taken)."""
+        v, it = C.c_double(), C.c_int()
+        self._check(self._lib.muto_gradient_solve_until(self._h, int(max_iter), float(target), C.byref(v),
+                                                         C.byref(it)), "muto_gradient_solve_until")
+        return v.value, it.value
+
     # --- profiling -------------------------------------------------------
     def set_profiling(self, on: bool) -> None:
         self._check(self._lib.muto_set_profiling(self._h, 1 if on else 0), "muto_set_profiling")

@@ -81,6 +81,7 @@ SIGNATURES = {
     "muto_nll_forward": (C.c_int, [_P, _D, _D]),
     "muto_nll_backward": (C.c_int, [_P, _D, _D, _D]),
     "muto_gradient_solve": (C.c_int, [_P, C.c_int, _D]),
+    "muto_gradient_solve_until": (C.c_int, [_P, C.c_int, C.c_double, _D, C.POINTER(C.c_int)]),
     "muto_get_multiplicity": (C.c_int, [_P, _U32, C.c_uint64]),
     "muto_set_profiling": (C.c_int, [_P, C.c_int]),
     "muto_kernel_stats": (C.c_int, [_P, C.c_char_p, _U64, _D]),

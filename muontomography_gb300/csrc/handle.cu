@@ -2251,7 +2251,13 @@ int muto_nll_backward(muto_handle* h, const double* log_lambda, double* out_valu
 }
 
 int muto_gradient_solve(muto_handle* h, int n_iter, double* out_value) {
+    return muto_gradient_solve_until(h, n_iter, -HUGE_VAL, out_value, nullptr);
+}
+
+int muto_gradient_solve_until(muto_handle* h, int max_iter, double target, double* out_value, int* out_iters) {
     if (!h) return MUTO_ERR_ARG;
+    const int n_iter = max_iter;
+    if (out_iters) *out_iters = 0;
     return guarded(h, [&] {
         n_prepared_check(h);
         if (h->method == kPoca) throw Error(MUTO_ERR_STATE, "PoCA has no likelihood");
@@ -2269,7 +2275,8 @@ int muto_gradient_solve(muto_handle* h, int n_iter, double* out_value) {
         };
         double f = F(x, &g);
         double step = 1.0;
-        for (int it = 0; it < n_iter; ++it) {
+        int done = 0;
+        for (int it = 0; it < n_iter && !(f <= target); ++it) {
             // step preconditioned by 1/(2 M_j): at step 1 it is the mean-mode EM move in log space
             double slope = 0.0;
             for (uint64_t j = 0; j < V; ++j) {
@@ -2293,7 +2300,9 @@ int muto_gradient_solve(muto_handle* h, int n_iter, double* out_value) {
             x.swap(xt);
             f = F(x, &g);
             step = std::min(step * 2.0, 4.0);
+            done = it + 1;
         }
+        if (out_iters) *out_iters = done;
         for (uint64_t j = 0; j < V; ++j) lam[j] = M[j] ? std::exp(x[j]) : 0.0;
         if (h->fp64()) upload_image<double>(h, lam.data());
         else upload_image<float>(h, lam.data());

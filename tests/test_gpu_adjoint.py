@@ -95,3 +95,26 @@ def test_gradient_solve_lowers_the_objective(gpu):
     assert f1 < f0 and f2 <= f1
     assert abs(f_img - f2) <= 1e-9 * abs(f2)
     assert np.all(img[mult > 0] > 0)
+
+
+@pytest.mark.parametrize("beta", [1e-3, 1e-2])
+@pytest.mark.parametrize("p", [2.0, 1.0])
+def test_gradient_solver_reaches_the_em_objective(gpu, beta, p):
+    # the 128x128x64 grid of 15 mm voxels (300 k muons): 20 MAP EM iterations
+    # (mean ML step), then the gradient solver from the same start to the
+    # objective value EM reached (src/MutoMAP.cpp:129-198 is the EM side)
+    wl = W.map128x128x64_15mm(n_muons=300_000)
+    rays = wl.tracks()
+    cfg = wl.em_config(precision="fp64", num_iteration=20, update_with_mean=True, beta=beta, p=p,
+                       all_neighbours=True, delta=0.1 * float(np.median(wl.lam())) * 1e7)
+    with M.MutoMAP(cfg) as a:
+        img = a.reconstruct(rays).reshape(-1, order="F")
+        mult = a.multiplicity()
+        f_em = a.nll(np.log(np.where(mult > 0, np.maximum(img, 1e-300), 1.0)))
+    with M.MutoMAP(dict(cfg, num_iteration=0)) as b:
+        b.load_tracks(rays)
+        b.prepare()
+        f0 = b.nll(np.log(np.where(mult > 0, 1e-7, 1.0)))
+        f_g, it = b.gradient_solve_until(f_em, 50)
+    assert f_em < f0  # EM lowered the objective
+    assert f_g <= f_em and 1 <= it <= 50
