@@ -18,6 +18,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -141,6 +142,25 @@ public:
     std::string dump() const {
         std::string out;
         dump_to(out);
+        return out;
+    }
+
+    // Implicit conversions (nlohmann's `operator ValueType()`): a number to
+    // any arithmetic type (truncated towards zero for integers), a boolean to
+    // bool, a string to std::string, an array to std::vector of any of these;
+    // a value of another kind throws type_error.  They let code written for
+    // nlohmann::json, such as `int n = config.get("detector_middle");` in the
+    // reference's driver, compile against this type unchanged.
+    template <typename T, typename std::enable_if<std::is_arithmetic<T>::value, int>::type = 0>
+    operator T() const {
+        if (std::is_same<T, bool>::value) return static_cast<T>(get_bool());
+        return static_cast<T>(get_double());
+    }
+    operator std::string() const { return get_string(); }
+    template <typename T>
+    operator std::vector<T>() const {
+        std::vector<T> out;
+        for (const json& e : items()) out.push_back(static_cast<T>(e));
         return out;
     }
 

@@ -304,3 +304,22 @@ def test_siddon_facade_reports_a_walk_stopped_by_its_bound(facade, tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stderr
     assert r.stdout.split("\n")[:2] == ["2 0 4 5 6 1.5", "0 1"]
+
+
+def test_reference_driver_compiles_unchanged(facade, tmp_path):
+    # the reference's own command-line program, its source as it is, built
+    # against this library's C++ headers and linked to its libraries: the
+    # drop-in for the reconstruction classes, MutoConfig and MutoFile
+    from oracle import reference as R
+
+    if not R.available():
+        pytest.skip("the reference's sources are not mounted here")
+    lib = B.facade_lib_path().parent
+    root = lib.parent
+    exe = tmp_path / "muto_test"
+    r = subprocess.run(["g++", "-std=c++17", "-I", str(root / "cpp"), "-I", str(root.parent / "include"), "-I",
+                        str(root / "csrc"), str(R.REF / "MuToTest.cpp"), "-o", str(exe), "-L", str(lib),
+                        "-lmuto_facade", "-lmuto_gb300", f"-Wl,-rpath,{lib}"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert exe.exists()

@@ -249,3 +249,34 @@ def test_gpu_em_matches_golden(gpu, name, precision, tol):
         rec._n_iter = cfg["num_iteration"]
         img = rec.reconstruct(T["rays"]).reshape(-1, order="F")
     assert rel_l2(img, T[name]) < tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", list(CLI_N_ITER))
+def test_library_cli_reproduces_reference_program_files(gpu, tmp_path, method):
+    # The library's command-line program (lib/muto, the reference's
+    # MuToTest.cpp on this library's classes) on the configurations the
+    # reference's own program was run with: the same raw-hit file in, the
+    # image file out, against the reference program's file.  MLSD and MAP
+    # start from the reference program's PoCA file, as their configurations
+    # say, and run in the fp64 form; the files hold float32 images.
+    import subprocess
+
+    from muontomography_gb300 import build as B
+
+    (tmp_path / "hits.bin").write_bytes(CLI["records"].tobytes())
+    (tmp_path / "poca.bin").write_bytes(CLI["out_poca"].tobytes())
+    cfg = json.loads(json.dumps(CLI_CFG[method]).replace("{dir}", str(tmp_path)))
+    if method in ("mlsd", "map"):
+        cfg[method]["precision"] = "fp64"
+    cfg["output_file"] = str(tmp_path / "out.bin")
+    (tmp_path / "cfg.json").write_text(json.dumps(cfg))
+    r = subprocess.run([str(B.cli_path()), str(tmp_path / "cfg.json")], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    want_hdr, want = image_file(CLI[f"out_{method}"].tobytes())
+    got_hdr, got = image_file((tmp_path / "out.bin").read_bytes())
+    for k in ("length", "version", "method", "n_ray", "n_iter", "precision", "n", "f", "pad"):
+        assert got_hdr[k] == want_hdr[k], k
+    assert np.array_equal(got > 0, want > 0)
+    a, b = got.astype(np.float64), want.astype(np.float64)
+    assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(b)
