@@ -201,6 +201,44 @@ def em_config(wl, args, precision: str, n_iter: int, lists: str | None = None) -
     return wl.em_config(**over)
 
 
+def map_conditioning(wl, args, d_rays, n: int, img64: np.ndarray, img32: np.ndarray) -> dict:
+    """How far the MAP EM moves under a rounding-sized change of its input.
+
+    With p = 1 the prior's surrogate picks among up to three roots per voxel,
+    and a change at the level of one rounding can switch the pick; the
+    iteration then amplifies it.  The FP64 form run again from an initial
+    image perturbed by 1e-7 (relative, uniform) shows that spread; the mixed
+    form is judged against it and by the objective F (NLL + prior, evaluated
+    in FP64) that each image reaches."""
+    cfg = em_config(wl, args, "fp64", args.ttl_iters)
+    r = M.Reconstruction(method_of(args), cfg)
+    r.load_tracks(None, on_device_ptr=d_rays.data_ptr(), n=n)
+    r.prepare()
+    init = np.full(wl.grid.nvox, cfg["initialize_value"])
+    r.set_image(init * (1.0 + 1e-7 * np.random.default_rng(12345).uniform(-1.0, 1.0, init.size)))
+    r.iterate(args.ttl_iters)
+    imgp = r.image()
+    mult = r.multiplicity()
+    r.close()
+    rf = M.Reconstruction(method_of(args), dict(cfg, num_iteration=0))
+    rf.load_tracks(None, on_device_ptr=d_rays.data_ptr(), n=n)
+    rf.prepare()
+
+    def objective(img):
+        flat = img.reshape(-1, order="F")
+        return rf.nll(np.log(np.where(mult > 0, np.maximum(flat, 1e-300), 1.0)))
+
+    def rel(x, y):
+        return float(np.linalg.norm(x - y) / np.linalg.norm(y))
+
+    spread = rel(imgp, img64)
+    out = {"rel_l2_fp64_perturbed_vs_fp64": spread, "perturbation": "initial image x (1 + 1e-7 u), u ~ U(-1, 1)",
+           "F_fp64": objective(img64), "F_fp64_perturbed": objective(imgp), "F_mixed": objective(img32),
+           "within_fp64_spread": bool(rel(img32, img64) <= 2.0 * spread)}
+    rf.close()
+    return out
+
+
 def cpu_port(wl, args, rays: np.ndarray, n_iter: int, threads: int) -> dict:
     """Time the CPU restatement of the reference path on a sample of the workload's tracks."""
     os.environ["OMP_NUM_THREADS"] = str(threads)
@@ -501,7 +539,8 @@ def run_ours(args) -> int:
                "within_1e-4": rel < 1e-4, "fp64_device_bytes": res["fp64"][2],
                "what": "set-up and iterations from device-resident tracks, wall clock; the FP64 GPU form stands "
                        "in for the FP64 oracle at this size"}
-
+        if method_of(args) == "map":
+            ttl.update(map_conditioning(wl, args, d_rays, n, res["fp64"][1], res["mixed"][1]))
     # ---- the gradient MAP solver against the MAP EM, to the same objective ---
     grad_vs_em = None
     if method_of(args) == "map" and args.grad_vs_em > 0 and rank == 0:

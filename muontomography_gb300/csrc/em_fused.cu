@@ -514,15 +514,26 @@ __global__ void k_mean_update(const Real* __restrict__ lam, Real* __restrict__ G
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= V) return;
     const uint32_t jb = brick ? brick_of(j, bd) : j;
-    const double gsum = static_cast<double>(G[jb]);
+    const Real gj = G[jb];
     G[jb] = Real(0);
     const uint32_t M = mult[j];
     if (grad) {
-        grad[j] = M ? -lam64[j] * gsum : 0.0;
+        grad[j] = M ? -lam64[j] * static_cast<double>(gj) : 0.0;
         return;
     }
-    const double l = static_cast<double>(lam[j]);
-    out[j] = M ? static_cast<OutT>(l + l * l * gsum / (2.0 * static_cast<double>(M))) : OutT(0);
+    if constexpr (sizeof(Real) == sizeof(float)) {
+        // the mixed form: lambda is stored in FP32, so its increment is formed
+        // in FP32 too.  GB300 issues FP64 at a sixty-fourth of the FP32 rate,
+        // and an FP64 division per voxel made this pass arithmetic bound at
+        // about ten times its memory time.
+        const float l = lam[j];
+        const float inc = l * l * gj / (2.0f * static_cast<float>(M));
+        if constexpr (sizeof(OutT) == sizeof(float)) out[j] = M ? l + inc : 0.0f;
+        else out[j] = M ? static_cast<double>(l) + static_cast<double>(inc) : 0.0;
+    } else {
+        const double l = static_cast<double>(lam[j]);
+        out[j] = M ? static_cast<OutT>(l + l * l * static_cast<double>(gj) / (2.0 * static_cast<double>(M))) : OutT(0);
+    }
 }
 
 template <typename Real, int GROUP, int RC>

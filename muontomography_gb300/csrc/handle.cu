@@ -1353,26 +1353,33 @@ void autotune_fused(muto_handle* h) {
     CK(cudaEventCreate(&e1));
     float best = 1e30f;
     int pick = cands[0];
+    // a scan of more than 2^30 pairs takes tens of milliseconds per pass:
+    // one timed pass per candidate, no warm-up, is then well above the noise
+    const bool big = h->npairs > (uint64_t(1) << 30);
+    const int reps = big ? 1 : 2;
     for (size_t i = 0; i < cands.size(); ++i) {
         apply(cands[i]);
-        launch_fused_pass<Real>(h, h->lam.as<Real>(), false, s);
+        if (!big) launch_fused_pass<Real>(h, h->lam.as<Real>(), false, s);
         CK(cudaEventRecord(e0, s));
-        for (int r = 0; r < 2; ++r) launch_fused_pass<Real>(h, h->lam.as<Real>(), false, s);
+        for (int r = 0; r < reps; ++r) launch_fused_pass<Real>(h, h->lam.as<Real>(), false, s);
         CK(cudaEventRecord(e1, s));
         CK(cudaEventSynchronize(e1));
         CK(cudaGetLastError());
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, e0, e1));
-        ms /= 2.f;
+        ms /= static_cast<float>(reps);
         if (i < 4) h->tune_ms[i] = ms;
-        if (ms < best) {
-            best = ms;
+        // a one-pass variant must beat the split form by 5 %: where the two
+        // are that close, run to run noise would otherwise flip the pick
+        const float score = cands[i] >= kFusedVariants ? ms : 1.05f * ms;
+        if (score < best) {
+            best = score;
             pick = cands[i];
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    h->launches += 3 * cands.size() * (h->brick ? 2 : 1);
+    h->launches += (big ? 1 : 3) * cands.size() * (h->brick ? 2 : 1);
     apply(pick);
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
