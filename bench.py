@@ -210,6 +210,8 @@ def map_conditioning(wl, args, d_rays, n: int, img64: np.ndarray, img32: np.ndar
     image perturbed by 1e-7 (relative, uniform) shows that spread; the mixed
     form is judged against it and by the objective F (NLL + prior, evaluated
     in FP64) that each image reaches."""
+    import muontomography_gb300 as M
+
     cfg = em_config(wl, args, "fp64", args.ttl_iters)
     r = M.Reconstruction(method_of(args), cfg)
     r.load_tracks(None, on_device_ptr=d_rays.data_ptr(), n=n)

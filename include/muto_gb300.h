@@ -81,6 +81,9 @@ typedef struct muto_status {
                                    0 for the one-shot methods */
     int32_t voxel_stream_above; /* voxel pass in use: segments longer than this are selected from the
                                    key array instead of registers (-1: none); "auto" picks it */
+    int32_t slr_levels;         /* slr_iter: levels of the later passes' schedule (muons of one level
+                                   share no voxel); 0 when they run muon after muon or not at all */
+    int32_t reserved;
     char message[256];          /* text of the last error */
 } muto_status;
 

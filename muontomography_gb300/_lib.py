@@ -38,7 +38,7 @@ class muto_status(C.Structure):
                 ("cost", C.c_double), ("cost_prev", C.c_double), ("device_bytes", C.c_uint64),
                 ("muon_pass", C.c_int32), ("muon_group", C.c_int32), ("tile_pairs", C.c_int32),
                 ("tile_muons", C.c_int32), ("path_lists", C.c_int32), ("voxel_stream_above", C.c_int32),
-                ("message", C.c_char * 256)]
+                ("slr_levels", C.c_int32), ("reserved", C.c_int32), ("message", C.c_char * 256)]
 
 
 class muto_block(C.Structure):

@@ -186,6 +186,10 @@ void launch_slr_paths(const SlrArgs& a, const uint64_t* off, uint32_t* counts, u
 // one later, in-place pass over the walked lines, muon after muon
 void launch_slr_iter_pass(const SlrArgs& a, const uint64_t* off, const uint32_t* vox, const double* len,
                           cudaStream_t s);
+// the same pass level by level: order[] lists the muons by level, level l's
+// muons at order[lstart[l] .. lstart[l+1])
+void launch_slr_iter_levels(const SlrArgs& a, const uint64_t* off, const uint32_t* vox, const double* len,
+                            const uint32_t* order, const uint32_t* lstart, uint32_t levels, cudaStream_t s);
 
 // PoCut's per-voxel step (src/MutoPoCut.cpp:113-118), after launch_poca:
 // the kept values grouped by voxel (counts, then offsets, then a scatter of

@@ -144,6 +144,7 @@ struct Params {
     // SLR, src/MutoSLR.cpp:21-45; SLRIter, src/MutoSLRIter.cpp:9-11
     int slr = 0;                 // 1 straight-line reconstruction, 2 its iterative form
     int slr_iterations = 1;
+    bool slr_sequential = false;  // later passes muon after muon instead of level by level
     // this library
     int precision = 0;  // 0 mixed, 1 fp64
     bool use_graph = true;
@@ -210,6 +211,10 @@ Params parse_params(Method m, const std::string& text, int variant = 0) {
                 P.slr = variant - 1;
                 if (P.slr == 2) P.slr_iterations = cfg.value("num_iteration", 1);
                 if (P.slr_iterations < 0) throw Error(MUTO_ERR_CONFIG, "num_iteration must be >= 0");
+                const std::string sch = cfg.value("slr_iter_schedule", std::string("levels"));
+                if (sch != "levels" && sch != "sequential")
+                    throw Error(MUTO_ERR_CONFIG, "slr_iter_schedule must be \"levels\" or \"sequential\"");
+                P.slr_sequential = sch == "sequential";
             }
         } else {
             P.update_with_mean = cfg.value("update_with_mean", false);
@@ -394,6 +399,7 @@ struct muto_handle {
     int vox_blocks_real[2 * kVoxClasses] = {}, vox_blocks_f64[2 * kVoxClasses] = {};  // resident blocks per class kernel
     uint32_t vox_streamed = 0;  // classes selected by the streamed path
     long long vox_stream_above = -1;  // the threshold vox_streamed stands for (-1: none)
+    uint32_t slr_levels = 0;          // levels of the SLRIter schedule (0: none or sequential)
     uint64_t vclass_off[kVoxClasses] = {};
     DevMem kslot;                     // per kept muon: its row of kvec (empty: its own index)
     DevMem mult, start, kvec, keys;   // keys: the voxel pass's order key of every pair
@@ -563,6 +569,58 @@ void alloc_counters(muto_handle* h) {
 // SLR (src/MutoSLR.cpp:47-103) and SLRIter (src/MutoSLRIter.cpp:15-83): the
 // first pass over every ray at once; the iterative form's later passes, in
 // place and in muon order, over the walked straight lines kept on the device
+// The level schedule of SLRIter's later passes (src/MutoSLRIter.cpp:40-71),
+// made once from the walked paths, which do not change between passes: muon
+// i's level is one more than the highest level that an earlier muon left on
+// any voxel of i's path.  A voxel's muons then have strictly increasing
+// levels in index order, and muons of one level share no voxel.  One ordered
+// sweep over the pairs on the host (the recurrence is sequential in i); the
+// muons are then grouped by level (index order inside a level) for the
+// device.
+void slr_level_schedule(muto_handle* h, const DevMem& off, const DevMem& vox, uint64_t nt, uint64_t np, DevMem& order,
+                        DevMem& lstart) {
+    const uint64_t V = h->V();
+    cudaStream_t s = h->stream;
+    if (nt >= 0xffffffffull) throw Error(MUTO_ERR_CAPACITY, "slr_iter: more than 2^32-1 rays");
+    std::vector<uint64_t> off_h(nt + 1);
+    std::vector<uint32_t> vox_h(np);
+    CK(cudaMemcpyAsync(off_h.data(), off.as<uint64_t>(), (nt + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+    if (np > 0) CK(cudaMemcpyAsync(vox_h.data(), vox.as<uint32_t>(), np * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::vector<uint32_t> last(V, 0), level(nt);
+    uint32_t levels = 0;
+    for (uint64_t i = 0; i < nt; ++i) {
+        uint32_t lv = 0;
+        for (uint64_t k = off_h[i]; k < off_h[i + 1]; ++k)
+            if (vox_h[k] < V) lv = std::max(lv, last[vox_h[k]]);
+        ++lv;
+        for (uint64_t k = off_h[i]; k < off_h[i + 1]; ++k)
+            if (vox_h[k] < V) last[vox_h[k]] = lv;
+        level[i] = lv;
+        levels = std::max(levels, lv);
+    }
+    std::vector<uint32_t> start(static_cast<size_t>(levels) + 1, 0), order_h(nt);
+    for (uint64_t i = 0; i < nt; ++i) ++start[level[i]];  // level l (1-based) counted at start[l]
+    uint32_t acc = 0;
+    for (uint32_t l = 0; l <= levels; ++l) {
+        const uint32_t c = start[l];
+        start[l] = acc;
+        acc += c;
+    }
+    // start[l] is now where level l begins (level 0 is empty); the device
+    // reads level l (0-based) at start[l + 1] .. start[l + 2]
+    std::vector<uint32_t> cur(start.begin(), start.end());
+    for (uint64_t i = 0; i < nt; ++i) order_h[cur[level[i]]++] = static_cast<uint32_t>(i);
+    start.push_back(static_cast<uint32_t>(nt));
+    order.alloc(std::max<uint64_t>(nt, 1) * sizeof(uint32_t), &h->dev_bytes);
+    lstart.alloc(start.size() * sizeof(uint32_t), &h->dev_bytes);
+    CK(cudaMemcpyAsync(order.as<uint32_t>(), order_h.data(), nt * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(lstart.as<uint32_t>(), start.data() + 1, (start.size() - 1) * sizeof(uint32_t),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));  // the host vectors go out of scope
+    h->slr_levels = levels;
+}
+
 void prepare_slr(muto_handle* h, uint64_t nt) {
     const uint64_t V = h->V();
     cudaStream_t s = h->stream;
@@ -594,9 +652,18 @@ void prepare_slr(muto_handle* h, uint64_t nt) {
         run(h, "slr_paths", [&] {
             launch_slr_paths(a, off.as<uint64_t>(), nullptr, vox.as<uint32_t>(), len.as<double>(), s);
         });
+        DevMem order, lstart;
+        if (!h->P.slr_sequential) {
+            HostPhase ph(h, "slr_levels");
+            slr_level_schedule(h, off, vox, nt, np, order, lstart);
+        }
         for (int p = 1; p < passes; ++p)
             run(h, "slr_iter_pass", [&] {
-                launch_slr_iter_pass(a, off.as<uint64_t>(), vox.as<uint32_t>(), len.as<double>(), s);
+                if (h->P.slr_sequential)
+                    launch_slr_iter_pass(a, off.as<uint64_t>(), vox.as<uint32_t>(), len.as<double>(), s);
+                else
+                    launch_slr_iter_levels(a, off.as<uint64_t>(), vox.as<uint32_t>(), len.as<double>(),
+                                           order.as<uint32_t>(), lstart.as<uint32_t>(), h->slr_levels, s);
             });
         CK(cudaStreamSynchronize(s));  // the path arrays go out of scope
     }
@@ -1961,6 +2028,8 @@ int muto_get_status(const muto_handle* hc, muto_status* out) {
     out->tile_pairs = h->tile_pairs;
     out->tile_muons = h->tile_muons;
     out->path_lists = h->method == kPoca ? 0 : h->lists;
+    out->slr_levels = static_cast<int32_t>(std::min<uint32_t>(h->slr_levels, 0x7fffffffu));
+    out->reserved = 0;
     out->voxel_stream_above = h->method == kPoca || h->lists != kListsVoxelMajor
                                   ? -1 : static_cast<int32_t>(std::min<long long>(h->vox_stream_above, 0x7fffffffLL));
     if (h->method != kPoca && h->lists == kListsMuonMajor && h->fused_variant == kFusedVariants) {

@@ -5,8 +5,9 @@
 // the two points (bit-exact, as for the other methods), and per voxel the
 // mean squared projected angle shared by length^2 or equally.  Sums are FP64
 // atomics.  The later passes of the iterative form are order-dependent (each
-// muon sees the image the muons before it left): they run muon after muon on
-// one warp over the walked paths (k_slr_iter_pass).
+// muon sees the image the muons before it left): they run over the walked
+// paths level by level (k_slr_iter_levels: muons of one level share no
+// voxel), or muon after muon on one warp (k_slr_iter_pass).
 #include "common.cuh"
 #include "geometry.cuh"
 
@@ -116,11 +117,43 @@ __global__ void k_slr_paths(SlrArgs a, const uint64_t* __restrict__ off, uint32_
     if (!off) counts[i] = p.k;
 }
 
-// One later pass of the iterative form (src/MutoSLRIter.cpp:40-71 with
-// iter != 0), muon after muon on a single warp: the warp reads the image on
-// the muon's path, sums it, and adds to each voxel its share times the
-// voxel's part of that sum.  A muon's stores are ordered before the next
-// muon's loads by __syncwarp; no other warp touches the image.
+// One muon of a later pass of the iterative form (src/MutoSLRIter.cpp:40-71
+// with iter != 0), on one warp: the warp reads the image on the muon's path,
+// sums it (lane partials, then the warp's sum), and adds to each voxel its
+// share times the voxel's part of that sum.
+__device__ __forceinline__ void slr_iter_muon(const SlrArgs& a, const DevGrid& g, double z_lo, double z_hi,
+                                              uint64_t i, const uint64_t* __restrict__ off,
+                                              const uint32_t* __restrict__ vox, const double* __restrict__ len,
+                                              int lane) {
+    const muto_ray r = a.rays[i];
+    const SlrRay s = slr_ray(r, g, z_lo, z_hi, a.mag);
+    const uint64_t p0 = off[i];
+    const uint32_t n = static_cast<uint32_t>(off[i + 1] - p0);
+    double part = 0.0;  // :49-52
+    for (uint32_t k = lane; k < n; k += 32) part = dadd(part, a.img[vox[p0 + k]]);
+    const double total = warp_sum(part);
+    const double share = ddiv(dmul(s.a2, 0.5), static_cast<double>(static_cast<uint64_t>(n) * n));
+    const double e2 = dmul(r.ein, r.ein);
+    for (uint32_t k = lane; k < n; k += 32) {
+        const uint32_t j = vox[p0 + k];
+        const double l = len[p0 + k];
+        double iv;
+        if (a.length_weighted) {
+            a.weight[j] = dadd(a.weight[j], ddiv(l, a.g.dz));
+            const double f = ddiv(l, s.l_total);
+            iv = dmul(dmul(dmul(s.a2, 0.5), f), f);
+        } else {
+            a.weight[j] = dadd(a.weight[j], 1.0);
+            iv = share;
+        }
+        iv = dmul(iv, ddiv(a.img[j], total));  // :64-66
+        if (a.has_energy) iv = dmul(iv, e2);
+        a.img[j] = dadd(a.img[j], iv);
+    }
+}
+
+// A later pass muon after muon on a single warp: a muon's stores are ordered
+// before the next muon's loads by __syncwarp; no other warp touches the image.
 __global__ void k_slr_iter_pass(SlrArgs a, const uint64_t* __restrict__ off, const uint32_t* __restrict__ vox,
                                 const double* __restrict__ len) {
     const int lane = threadIdx.x & 31;
@@ -129,32 +162,32 @@ __global__ void k_slr_iter_pass(SlrArgs a, const uint64_t* __restrict__ off, con
     const double z_lo = a.g.z_min;
     const double z_hi = dadd(a.g.z_min, dmul(a.g.dz, static_cast<double>(a.g.nz)));
     for (uint64_t i = 0; i < a.n; ++i) {
-        const muto_ray r = a.rays[i];
-        const SlrRay s = slr_ray(r, g, z_lo, z_hi, a.mag);
-        const uint64_t p0 = off[i];
-        const uint32_t n = static_cast<uint32_t>(off[i + 1] - p0);
-        double part = 0.0;  // :49-52, lanes' partial sums, then the warp's
-        for (uint32_t k = lane; k < n; k += 32) part = dadd(part, a.img[vox[p0 + k]]);
-        const double total = warp_sum(part);
-        const double share = ddiv(dmul(s.a2, 0.5), static_cast<double>(static_cast<uint64_t>(n) * n));
-        const double e2 = dmul(r.ein, r.ein);
-        for (uint32_t k = lane; k < n; k += 32) {
-            const uint32_t j = vox[p0 + k];
-            const double l = len[p0 + k];
-            double iv;
-            if (a.length_weighted) {
-                a.weight[j] = dadd(a.weight[j], ddiv(l, a.g.dz));
-                const double f = ddiv(l, s.l_total);
-                iv = dmul(dmul(dmul(s.a2, 0.5), f), f);
-            } else {
-                a.weight[j] = dadd(a.weight[j], 1.0);
-                iv = share;
-            }
-            iv = dmul(iv, ddiv(a.img[j], total));  // :64-66
-            if (a.has_energy) iv = dmul(iv, e2);
-            a.img[j] = dadd(a.img[j], iv);
-        }
+        slr_iter_muon(a, g, z_lo, z_hi, i, off, vox, len, lane);
         __syncwarp();
+    }
+}
+
+// A later pass level by level.  A muon's level is one more than the highest
+// level among the earlier muons that share a voxel with it, so two muons of
+// one level share no voxel, and every voxel meets its muons in index order:
+// each muon reads and writes the image state it would see in the sequential
+// loop, whatever the order inside a level.  One block: its warps take the
+// muons of a level, and the block barrier orders the levels (global stores
+// before it are visible to the whole block after it).
+__global__ void __launch_bounds__(1024) k_slr_iter_levels(SlrArgs a, const uint64_t* __restrict__ off,
+                                                          const uint32_t* __restrict__ vox,
+                                                          const double* __restrict__ len,
+                                                          const uint32_t* __restrict__ order,
+                                                          const uint32_t* __restrict__ lstart, uint32_t levels) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const DevGrid g = make_dev_grid(a.g);
+    const double z_lo = a.g.z_min;
+    const double z_hi = dadd(a.g.z_min, dmul(a.g.dz, static_cast<double>(a.g.nz)));
+    for (uint32_t l = 0; l < levels; ++l) {
+        const uint32_t e = lstart[l + 1];
+        for (uint32_t q = lstart[l] + warp; q < e; q += nw) slr_iter_muon(a, g, z_lo, z_hi, order[q], off, vox, len, lane);
+        __syncthreads();
     }
 }
 
@@ -177,6 +210,13 @@ void launch_slr_iter_pass(const SlrArgs& a, const uint64_t* off, const uint32_t*
                           cudaStream_t s) {
     if (a.n == 0) return;
     k_slr_iter_pass<<<1, 32, 0, s>>>(a, off, vox, len);
+    count_launches(1);
+}
+
+void launch_slr_iter_levels(const SlrArgs& a, const uint64_t* off, const uint32_t* vox, const double* len,
+                            const uint32_t* order, const uint32_t* lstart, uint32_t levels, cudaStream_t s) {
+    if (a.n == 0 || levels == 0) return;
+    k_slr_iter_levels<<<1, 1024, 0, s>>>(a, off, vox, len, order, lstart, levels);
     count_launches(1);
 }
 
