@@ -609,7 +609,8 @@ def run_ours(args) -> int:
                        "device_bytes": st["device_bytes"], "setup_s": t_setup, "setup_ms": setup_ms,
                        "generate_s": t_gen,
                        "muon_pass": {1: "tma_tiles", 2: "warp_batched", 3: "one_pass_lists", 4: "recompute_walk",
-                                     5: "split_muon_pass_and_scatter"}.get(st["muon_pass"]),
+                                     5: "split_muon_pass_and_scatter",
+                                     6: "one_pass_staged_in_shared_memory"}.get(st["muon_pass"]),
                        "muon_group": st["muon_group"], "held_pairs": st["tile_pairs"]},
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -804,7 +805,8 @@ def run_batch(args) -> int:
                        "device_bytes": st["device_bytes"],
                        "path_lists": {1: "voxel_major", 2: "muon_major", 3: "recompute"}.get(st["path_lists"]),
                        "autotuner": {"pass": {1: "tma_tiles", 2: "warp_batched", 3: "one_pass_lists",
-                                              5: "split_muon_pass_and_scatter"}.get(st["muon_pass"]),
+                                              5: "split_muon_pass_and_scatter",
+                                              6: "one_pass_staged_in_shared_memory"}.get(st["muon_pass"]),
                                      "lanes_per_muon": st["muon_group"], "held_pairs": st["tile_pairs"],
                                      "voxel_stream_above": st["voxel_stream_above"]},
                        "parallelism": f"replicas x{world} (one batch per GPU)",
@@ -842,7 +844,7 @@ def main() -> int:
     ap.add_argument("--cpu-sample-fixed", action="store_true",
                     help="reference leg: use --cpu-sample as it is instead of sizing it to the step count")
     ap.add_argument("--muon-pass", choices=["auto", "tile", "warp"], default="auto")
-    ap.add_argument("--fused-variant", choices=["auto", "4x8", "8x4", "8x8", "8x16", "16x8", "16x16", "split"],
+    ap.add_argument("--fused-variant", choices=["auto", "4x8", "8x4", "8x8", "8x16", "16x8", "16x16", "staged", "split"],
                     default="auto", help="the mean update's pass over muon-major lists (auto: timed at set-up)")
     ap.add_argument("--muon-layout", choices=["auto", "columns", "index"], default="auto")
     ap.add_argument("--voxel-stream-above", type=int, default=None,

@@ -71,10 +71,12 @@ typedef struct muto_status {
     uint64_t device_bytes;      /* device memory held by the handle */
     int32_t muon_pass;          /* muon-pass variant in use: 1 TMA tiles, 2 warp-batched, 3 the mean
                                    update's one-pass form over stored lists, 4 its pass over recomputed
-                                   paths, 5 its split form (warp-batched muon pass, then a scatter pass) */
+                                   paths, 5 its split form (warp-batched muon pass, then a scatter pass),
+                                   6 its one-pass form with each batch's pairs staged in shared memory */
     int32_t muon_group;         /* lanes per muon in its covariance sums */
     int32_t tile_pairs;         /* pairs per tile (TMA variant), pairs per muon held in registers
-                                   (fused stored-list pass); 0 otherwise */
+                                   (fused stored-list pass), pairs staged per batch (staged pass);
+                                   0 otherwise */
     int32_t tile_muons;         /* muons per tile (TMA variant), muons per CTA batch (fused pass) */
     int32_t path_lists;         /* how the pairs are kept: 1 muon-major lists and their voxel-major copy,
                                    2 muon-major lists only, 3 none (paths walked every iteration);
@@ -128,9 +130,11 @@ typedef struct muto_handle muto_handle;
  * "muon_major" and "recompute" require the mean update),
  * "fused_variant" ("auto": the mean update's pass over muon-major lists
  * takes the lanes per muon and pairs held per lane by timing the variants
- * that suit the scan's mean path and the split form (the muon pass, then a
- * second pass over the lists adding the terms) at prepare; "4x8", "8x4",
- * "8x8", "8x16", "16x8", "16x16" or "split" force one), "fused_prefetch"
+ * that suit the scan's mean path, the staged variant (each batch's pairs
+ * copied to shared memory once, read back there for the second step) and
+ * the split form (the muon pass, then a second pass over the lists adding
+ * the terms) at prepare; "4x8", "8x4", "8x8", "8x16", "16x8", "16x16",
+ * "staged" or "split" force one), "fused_prefetch"
  * (false; true: the one-pass form
  * prefetches every CTA's next batch of pairs into L2),
  * "setup_chunk_pairs" (0: the set-up walks the paths in chunks of muons

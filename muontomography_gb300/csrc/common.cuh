@@ -382,7 +382,8 @@ struct FusedArgs {
     int brick;
 };
 // stored-list variants: lanes per muon and pairs held in registers per muon
-constexpr int kFusedVariants = 6;
+constexpr int kFusedVariants = 7;
+constexpr int kFusedStaged = 6;  // the variant whose batches are staged in shared memory
 int fused_variant_group(int v);
 int fused_variant_held(int v);
 template <typename Real>

@@ -313,6 +313,147 @@ __global__ void __launch_bounds__(32 * GROUP, fused_min_blocks(GROUP, RC)) k_em_
 }
 
 // ---------------------------------------------------------------------------
+// Staged one-pass variant: a CTA batch's pairs copied to shared memory.
+// ---------------------------------------------------------------------------
+// The 32 muons of a batch own one contiguous range of the muon-major lists.
+// The CTA copies that range (up to kStagedPairs pairs) into shared memory
+// with 16-byte cp.async copies, so the lists leave HBM once and the scatter
+// reads them back from shared memory instead of from L2/HBM; pairs of a batch
+// beyond the staged ones are read from global memory in both steps.  Two
+// CTAs are resident per SM, so one copies its batch while the other works.
+template <typename Real>
+struct Staged {
+    static constexpr int kPairs = sizeof(Real) == sizeof(float) ? 8192 : 4096;
+    static constexpr int kSlots = kPairs + 8;  // room for the 16-byte widening at both ends
+    static constexpr size_t kSmem = static_cast<size_t>(kSlots) * (sizeof(uint32_t) + 2 * sizeof(Real));
+};
+constexpr int kStagedGroup = 16;
+
+template <typename Real>
+__global__ void __launch_bounds__(32 * kStagedGroup, 2) k_em_staged(FusedArgs<Real> a) {
+    using R4 = typename Vec4<Real>::type;
+    using S = Staged<Real>;
+    constexpr int GROUP = kStagedGroup;
+    constexpr int kThreads = 32 * GROUP;
+    constexpr int U = 4;                       // gathers in flight per lane
+    constexpr int EJ = 16 / sizeof(uint32_t);  // elements per 16-byte copy
+    constexpr int ER = 16 / sizeof(Real);
+    extern __shared__ __align__(16) unsigned char staged_smem[];
+    uint32_t* s_j = reinterpret_cast<uint32_t*>(staged_smem);
+    Real* s_L = reinterpret_cast<Real*>(staged_smem + static_cast<size_t>(S::kSlots) * sizeof(uint32_t));
+    Real* s_T = s_L + S::kSlots;
+    __shared__ Real s_sum[3][kBatch];
+    __shared__ Real s_k[3][kBatch];
+    __shared__ __align__(16) R4 s_sd[kBatch];
+    __shared__ Real s_pr2[kBatch];
+    __shared__ uint32_t s_off[kBatch + 1];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int ms = tid / GROUP, glane = tid % GROUP;
+    const unsigned gmask = ((1u << GROUP) - 1u) << (lane & ~(GROUP - 1));
+    const uint32_t V = a.V;
+    const uint64_t nbatch = (static_cast<uint64_t>(a.N) + kBatch - 1) / kBatch;
+    const uint64_t keep = l2_keep_policy();
+    double cost_local = 0.0;
+    unsigned long long singular_local = 0;
+
+    for (uint64_t b = blockIdx.x; b < nbatch; b += gridDim.x) {
+        const uint64_t mfirst = b * kBatch;
+        const uint64_t mend = min(mfirst + kBatch, static_cast<uint64_t>(a.N));
+        const uint64_t p0 = a.off[mfirst], p1 = a.off[mend];
+        const uint32_t nst = static_cast<uint32_t>(min(p1 - p0, static_cast<uint64_t>(S::kPairs)));  // staged
+        // ---- the batch's pairs into shared memory ------------------------------
+        // each array's copy starts at the 16-byte boundary at or below p0; the
+        // arrays are padded past their last pair, so the widened end stays inside
+        const uint64_t aj = p0 & ~static_cast<uint64_t>(EJ - 1), ar = p0 & ~static_cast<uint64_t>(ER - 1);
+        const uint32_t sj = static_cast<uint32_t>(p0 - aj), sr = static_cast<uint32_t>(p0 - ar);
+        const uint32_t cj = (sj + nst + EJ - 1) / EJ, cr = (sr + nst + ER - 1) / ER;
+        for (uint32_t c = tid; c < cj; c += kThreads) cp_async_16(s_j + c * EJ, a.vidx + aj + c * EJ);
+        for (uint32_t c = tid; c < cr; c += kThreads) {
+            cp_async_16(s_L + c * ER, a.L + ar + c * ER);
+            cp_async_16(s_T + c * ER, a.T + ar + c * ER);
+        }
+        if (tid < kBatch && mfirst + tid < mend) stage_muon(&s_sd[tid], &s_pr2[tid], a.sd + mfirst + tid, a.pr2 + mfirst + tid);
+        if (tid <= kBatch) s_off[tid] = static_cast<uint32_t>(a.off[min(mfirst + tid, mend)] - p0);
+        cp_async_wait_all();
+        __syncthreads();
+        // pair k of the batch (0-based): from shared memory, or global beyond the staged ones
+        auto pair = [&](uint32_t k, uint32_t& j, Real& L, Real& T) {
+            if (k < nst) {
+                j = s_j[sj + k];
+                L = s_L[sr + k];
+                T = s_T[sr + k];
+            } else {
+                j = __ldg(a.vidx + p0 + k);
+                L = __ldg(a.L + p0 + k);
+                T = __ldg(a.T + p0 + k);
+            }
+        };
+        uint32_t kb = 0, ke = 0;
+        if (mfirst + ms < mend) {
+            kb = s_off[ms];
+            ke = s_off[ms + 1];
+        }
+        // ---- the covariance sums: GROUP lanes per muon, U gathers in flight ----
+        Real c0 = 0, c1 = 0, c2 = 0;
+        for (uint32_t k0 = kb + glane; k0 < ke; k0 += GROUP * U) {
+            uint32_t jj[U];
+            Real ll[U], tt[U], lv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t k = k0 + u * GROUP;
+                jj[u] = 0xffffffffu;
+                ll[u] = tt[u] = Real(0);
+                if (k < ke) pair(k, jj[u], ll[u], tt[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) lv[u] = jj[u] < V ? ld_keep(a.lam + jj[u], keep) : Real(0);
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (jj[u] != 0xffffffffu) add_sigma(lv[u], ll[u], tt[u], c0, c1, c2);
+        }
+#pragma unroll
+        for (int o = GROUP / 2; o > 0; o >>= 1) {
+            c0 += __shfl_xor_sync(gmask, c0, o, GROUP);
+            c1 += __shfl_xor_sync(gmask, c1, o, GROUP);
+            c2 += __shfl_xor_sync(gmask, c2, o, GROUP);
+        }
+        if (glane == 0) {
+            s_sum[0][ms] = c0;
+            s_sum[1][ms] = c1;
+            s_sum[2][ms] = c2;
+        }
+        __syncthreads();
+        // ---- FP64 2x2 algebra of the batch, a muon per lane of warp 0 --------
+        if (tid < kBatch) {
+            Real k0 = 0, k1 = 0, k2 = 0;
+            if (mfirst + tid < mend)
+                muon_coefficients<Real>(s_sum[0][tid], s_sum[1][tid], s_sum[2][tid], s_pr2[tid], s_sd[tid], a.E00,
+                                        a.E01, a.E11, a.compute_cost != 0, k0, k1, k2, cost_local, singular_local);
+            s_k[0][tid] = k0;
+            s_k[1][tid] = k1;
+            s_k[2][tid] = k2;
+        }
+        __syncthreads();
+        // ---- g_ij of every pair added to G_j, the pairs read back -------------
+        const Real k0 = s_k[0][ms], k1 = s_k[1][ms], k2 = s_k[2][ms];
+        for (uint32_t q0 = kb + glane; q0 < ke; q0 += GROUP * U) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t k = q0 + u * GROUP;
+                if (k < ke) {
+                    uint32_t j;
+                    Real L, T;
+                    pair(k, j, L, T);
+                    if (j < V) red_add(a.G + j, g_term(k0, k1, k2, L, T), keep);
+                }
+            }
+        }
+        __syncthreads();  // the staging buffers are refilled by the next batch
+    }
+    flush_counters<kThreads>(cost_local, singular_local, a.compute_cost, a.ctr);
+}
+
+// ---------------------------------------------------------------------------
 // Recompute pass: the merged path walked in FP64 twice per iteration.
 // ---------------------------------------------------------------------------
 // The merged split path of getMuonPathAndTail (src/MutoMLSD.cpp:382-415): the
@@ -580,15 +721,30 @@ __global__ void __launch_bounds__(256) k_em_scatter(FusedArgs<Real> a, const typ
 
 }  // namespace
 
-// (GROUP, RC) of each stored-list variant
-static constexpr int kFusedGroup[kFusedVariants] = {4, 8, 8, 16, 16, 8};
-static constexpr int kFusedHeld[kFusedVariants] = {8, 8, 16, 8, 16, 4};
+// (GROUP, RC) of each stored-list variant; the last is the staged one (GROUP
+// lanes per muon, its batch's pairs in shared memory)
+static constexpr int kFusedGroup[kFusedVariants] = {4, 8, 8, 16, 16, 8, kStagedGroup};
+static constexpr int kFusedHeld[kFusedVariants] = {8, 8, 16, 8, 16, 4, 0};
 int fused_variant_group(int v) { return kFusedGroup[v]; }
-int fused_variant_held(int v) { return kFusedGroup[v] * kFusedHeld[v]; }
+int fused_variant_held(int v) {
+    return v == kFusedStaged ? Staged<float>::kPairs / kBatch : kFusedGroup[v] * kFusedHeld[v];
+}
+
+template <typename Real>
+int staged_blocks_per_sm() {
+    int n = 0;
+    if (cudaFuncSetAttribute(k_em_staged<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(Staged<Real>::kSmem)) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_em_staged<Real>, 32 * kStagedGroup, Staged<Real>::kSmem) !=
+            cudaSuccess)
+        n = 0;
+    return n > 0 ? n : 1;
+}
 
 template <typename Real>
 int em_fused_blocks(int variant) {
     switch (variant) {
+        case kFusedStaged: return staged_blocks_per_sm<Real>();
         case 0: return fused_blocks_per_sm<Real, 4, 8>();
         case 1: return fused_blocks_per_sm<Real, 8, 8>();
         case 2: return fused_blocks_per_sm<Real, 8, 16>();
@@ -607,6 +763,9 @@ void launch_em_fused(const FusedArgs<Real>& a, int variant, int blocks, cudaStre
     const unsigned nb = static_cast<unsigned>(batches < static_cast<uint64_t>(blocks) ? batches : blocks);
 #define MUTO_FUSED_LAUNCH(G, RC) k_em_fused_lists<Real, G, RC><<<nb, 32 * G, 0, s>>>(a)
     switch (variant) {
+        case kFusedStaged:
+            k_em_staged<Real><<<nb, 32 * kStagedGroup, Staged<Real>::kSmem, s>>>(a);
+            break;
         case 0: MUTO_FUSED_LAUNCH(4, 8); break;
         case 1: MUTO_FUSED_LAUNCH(8, 8); break;
         case 2: MUTO_FUSED_LAUNCH(8, 16); break;

@@ -276,9 +276,10 @@ Params parse_params(Method m, const std::string& text, int variant = 0) {
         else if (fv == "16x8") P.fused_variant = 3;
         else if (fv == "16x16") P.fused_variant = 4;
         else if (fv == "8x4") P.fused_variant = 5;
+        else if (fv == "staged") P.fused_variant = kFusedStaged;
         else if (fv == "split") P.fused_variant = kFusedVariants;
         else throw Error(MUTO_ERR_CONFIG, "fused_variant must be \"auto\", \"4x8\", \"8x4\", \"8x8\", \"8x16\", "
-                                          "\"16x8\", \"16x16\" or \"split\"");
+                                          "\"16x8\", \"16x16\", \"staged\" or \"split\"");
         P.fused_prefetch = cfg.value("fused_prefetch", false);
         P.setup_chunk_pairs = cfg.value("setup_chunk_pairs", static_cast<int64_t>(0));
         if (P.setup_chunk_pairs < 0) throw Error(MUTO_ERR_CONFIG, "setup_chunk_pairs must be >= 0");
@@ -1380,7 +1381,7 @@ void autotune_fused(muto_handle* h) {
         // mean path: 4 or 8 lanes below 48 pairs, 8 or 16 up to 160, 16 beyond
         const int g = fused_variant_group(v);
         const bool fit = avg < 48.0 ? g <= 8 && held <= 64 : avg < 160.0 ? g >= 8 && held <= 128 : g == 16;
-        if (fit) cands.push_back(v);
+        if (fit || v == kFusedStaged) cands.push_back(v);
     }
     if (!forced) {  // the split form, its scatter with 32 and 16 lanes per muon
         cands.push_back(kFusedVariants);
@@ -2038,9 +2039,10 @@ int muto_get_status(const muto_handle* hc, muto_status* out) {
         out->tile_pairs = 0;
         out->tile_muons = 0;
     } else if (h->method != kPoca && h->lists == kListsMuonMajor) {
-        out->muon_pass = 3;
+        const bool staged = h->fused_variant == kFusedStaged;
+        out->muon_pass = staged ? 6 : 3;
         out->muon_group = fused_variant_group(h->fused_variant);
-        out->tile_pairs = fused_variant_held(h->fused_variant);
+        out->tile_pairs = staged ? 32 * fused_variant_held(h->fused_variant) : fused_variant_held(h->fused_variant);
         out->tile_muons = 32;
     } else if (h->method != kPoca && h->lists == kListsRecompute) {
         out->muon_pass = 4;

@@ -155,22 +155,28 @@ def test_slr_matches_oracle(gpu, oracle, n, n_muons, seed, lw, energy, iters):
 
 @pytest.mark.parametrize("n,n_muons,seed", [(12, 5000, 83), (30, 20000, 84), (2, 3000, 85)])
 @pytest.mark.parametrize("lw,energy,iters", [(True, False, 2), (False, True, 3)])
-def test_slr_iter_levels_equal_sequential_passes(gpu, n, n_muons, seed, lw, energy, iters):
+def test_slr_iter_levels_equal_sequential_passes(gpu, oracle, n, n_muons, seed, lw, energy, iters):
     # src/MutoSLRIter.cpp:40-71: the later passes in place, each muon on the
     # image the earlier muons left.  Run level by level (muons of one level
-    # share no voxel) they must give the sequential loop's image bit for bit;
-    # the 2-voxel grid puts most muons on a voxel they share (a level each).
+    # share no voxel) they give the sequential loop's image; the 2-voxel grid
+    # puts most muons on a voxel they share (a level each).  The first pass's
+    # FP64 atomics sum in a different order from run to run, so the two
+    # schedules (and the oracle) agree to rounding, not bit for bit; the
+    # schedule itself is exact on the CPU (test_oracle_kat).
     wl = W.small(n_muons=n_muons, seed=seed, n=n)
     rays = wl.tracks()
     cfg = wl.poca_config(length_weighted=lw, has_energy=energy)
     cfg["num_iteration"] = iters
+    ref = oracle.slr(wl.grid, cfg, rays, iterative=True)
     out = {}
     for sch in ("levels", "sequential"):
         with M.MutoSLRIter(dict(cfg, slr_iter_schedule=sch)) as rec:
             out[sch] = rec.reconstruct(rays)
             out[sch + "_levels"] = rec.status()["slr_levels"]
     assert np.any(out["levels"])
-    assert np.array_equal(out["levels"], out["sequential"])
+    assert rel_l2(out["levels"], out["sequential"]) < 1e-12
+    assert rel_l2(out["levels"].reshape(-1, order="F"), ref) < 1e-12
+    assert np.array_equal(out["levels"] > 0, out["sequential"] > 0)
     assert out["sequential_levels"] == 0
     assert 1 <= out["levels_levels"] <= n_muons
     if n == 2:
