@@ -130,11 +130,11 @@ typedef struct muto_handle muto_handle;
  * "muon_major" and "recompute" require the mean update),
  * "fused_variant" ("auto": the mean update's pass over muon-major lists
  * takes the lanes per muon and pairs held per lane by timing the variants
- * that suit the scan's mean path, the staged variant (each batch's pairs
- * copied to shared memory once, read back there for the second step) and
- * the split form (the muon pass, then a second pass over the lists adding
- * the terms) at prepare; "4x8", "8x4", "8x8", "8x16", "16x8", "16x16",
- * "staged" or "split" force one), "fused_prefetch"
+ * that suit the scan's mean path and the split form (the muon pass, then a
+ * second pass over the lists adding the terms) at prepare; "4x8", "8x4",
+ * "8x8", "8x16", "16x8", "16x16", "split" or "staged" (each batch's pairs
+ * copied to shared memory once and read back there for the second step)
+ * force one), "fused_prefetch"
  * (false; true: the one-pass form
  * prefetches every CTA's next batch of pairs into L2),
  * "setup_chunk_pairs" (0: the set-up walks the paths in chunks of muons

@@ -183,13 +183,24 @@ void launch_slr(const SlrArgs& a, cudaStream_t s);
 // ray i's voxels (x + nx (y + ny z)) and lengths at vox/len + off[i]
 void launch_slr_paths(const SlrArgs& a, const uint64_t* off, uint32_t* counts, uint32_t* vox, double* len,
                       cudaStream_t s);
-// one later, in-place pass over the walked lines, muon after muon
-void launch_slr_iter_pass(const SlrArgs& a, const uint64_t* off, const uint32_t* vox, const double* len,
-                          cudaStream_t s);
+// the later, in-place passes over the walked lines: per pair its voxel, its
+// weight increment and its image increment before the path's scaling; per
+// muon ein^2
+struct SlrPass {
+    const uint64_t* off;
+    const uint32_t* vox;
+    const double* len;
+    double* iv0;
+    double* winc;
+    double* e2;
+};
+void launch_slr_pair_terms(const SlrArgs& a, const SlrPass& p, cudaStream_t s);
+// one later pass, muon after muon
+void launch_slr_iter_pass(const SlrArgs& a, const SlrPass& p, cudaStream_t s);
 // the same pass level by level: order[] lists the muons by level, level l's
 // muons at order[lstart[l] .. lstart[l+1])
-void launch_slr_iter_levels(const SlrArgs& a, const uint64_t* off, const uint32_t* vox, const double* len,
-                            const uint32_t* order, const uint32_t* lstart, uint32_t levels, cudaStream_t s);
+void launch_slr_iter_levels(const SlrArgs& a, const SlrPass& p, const uint32_t* order, const uint32_t* lstart,
+                            uint32_t levels, cudaStream_t s);
 
 // PoCut's per-voxel step (src/MutoPoCut.cpp:113-118), after launch_poca:
 // the kept values grouped by voxel (counts, then offsets, then a scatter of

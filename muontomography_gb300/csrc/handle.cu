@@ -653,6 +653,14 @@ void prepare_slr(muto_handle* h, uint64_t nt) {
         run(h, "slr_paths", [&] {
             launch_slr_paths(a, off.as<uint64_t>(), nullptr, vox.as<uint32_t>(), len.as<double>(), s);
         });
+        // the pass-independent terms of every pair, once
+        DevMem iv0, winc, e2;
+        iv0.alloc(std::max<uint64_t>(np, 1) * sizeof(double), &h->dev_bytes);
+        winc.alloc(std::max<uint64_t>(np, 1) * sizeof(double), &h->dev_bytes);
+        e2.alloc(nt * sizeof(double), &h->dev_bytes);
+        const SlrPass sp{off.as<uint64_t>(), vox.as<uint32_t>(), len.as<double>(), iv0.as<double>(), winc.as<double>(),
+                         e2.as<double>()};
+        run(h, "slr_paths", [&] { launch_slr_pair_terms(a, sp, s); });
         DevMem order, lstart;
         if (!h->P.slr_sequential) {
             HostPhase ph(h, "slr_levels");
@@ -661,10 +669,9 @@ void prepare_slr(muto_handle* h, uint64_t nt) {
         for (int p = 1; p < passes; ++p)
             run(h, "slr_iter_pass", [&] {
                 if (h->P.slr_sequential)
-                    launch_slr_iter_pass(a, off.as<uint64_t>(), vox.as<uint32_t>(), len.as<double>(), s);
+                    launch_slr_iter_pass(a, sp, s);
                 else
-                    launch_slr_iter_levels(a, off.as<uint64_t>(), vox.as<uint32_t>(), len.as<double>(),
-                                           order.as<uint32_t>(), lstart.as<uint32_t>(), h->slr_levels, s);
+                    launch_slr_iter_levels(a, sp, order.as<uint32_t>(), lstart.as<uint32_t>(), h->slr_levels, s);
             });
         CK(cudaStreamSynchronize(s));  // the path arrays go out of scope
     }
@@ -1381,7 +1388,10 @@ void autotune_fused(muto_handle* h) {
         // mean path: 4 or 8 lanes below 48 pairs, 8 or 16 up to 160, 16 beyond
         const int g = fused_variant_group(v);
         const bool fit = avg < 48.0 ? g <= 8 && held <= 64 : avg < 160.0 ? g >= 8 && held <= 128 : g == 16;
-        if (fit || v == kFusedStaged) cands.push_back(v);
+        // the staged variant runs only when asked for: slower than the split
+        // form on every workload measured (its fixed batches of 32 muons wait
+        // on their longest path)
+        if (fit && v != kFusedStaged) cands.push_back(v);
     }
     if (!forced) {  // the split form, its scatter with 32 and 16 lanes per muon
         cands.push_back(kFusedVariants);

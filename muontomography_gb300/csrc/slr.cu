@@ -117,52 +117,63 @@ __global__ void k_slr_paths(SlrArgs a, const uint64_t* __restrict__ off, uint32_
     if (!off) counts[i] = p.k;
 }
 
+// The pass-independent terms of every pair, once at set-up: the weight
+// increment (length / dz, or 1) and the image increment before it is scaled
+// by the voxel's part of the path's sum (a^2 / 2 (length / l_total)^2, or the
+// equal share a^2 / 2 / n^2), with the arithmetic of :80-89; and ein^2 per
+// muon.  A thread per muon.
+__global__ void k_slr_pair_terms(SlrArgs a, SlrPass p) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const DevGrid g = make_dev_grid(a.g);
+    const double z_lo = a.g.z_min;
+    const double z_hi = dadd(a.g.z_min, dmul(a.g.dz, static_cast<double>(a.g.nz)));
+    const muto_ray r = a.rays[i];
+    const SlrRay s = slr_ray(r, g, z_lo, z_hi, a.mag);
+    const uint64_t p0 = p.off[i];
+    const uint32_t n = static_cast<uint32_t>(p.off[i + 1] - p0);
+    const double share = ddiv(dmul(s.a2, 0.5), static_cast<double>(static_cast<uint64_t>(n) * n));
+    for (uint32_t k = 0; k < n; ++k) {
+        const double l = p.len[p0 + k];
+        if (a.length_weighted) {
+            p.winc[p0 + k] = ddiv(l, a.g.dz);
+            const double f = ddiv(l, s.l_total);
+            p.iv0[p0 + k] = dmul(dmul(dmul(s.a2, 0.5), f), f);
+        } else {
+            p.winc[p0 + k] = 1.0;
+            p.iv0[p0 + k] = share;
+        }
+    }
+    p.e2[i] = dmul(r.ein, r.ein);
+}
+
 // One muon of a later pass of the iterative form (src/MutoSLRIter.cpp:40-71
 // with iter != 0), on one warp: the warp reads the image on the muon's path,
 // sums it (lane partials, then the warp's sum), and adds to each voxel its
-// share times the voxel's part of that sum.
-__device__ __forceinline__ void slr_iter_muon(const SlrArgs& a, const DevGrid& g, double z_lo, double z_hi,
-                                              uint64_t i, const uint64_t* __restrict__ off,
-                                              const uint32_t* __restrict__ vox, const double* __restrict__ len,
-                                              int lane) {
-    const muto_ray r = a.rays[i];
-    const SlrRay s = slr_ray(r, g, z_lo, z_hi, a.mag);
-    const uint64_t p0 = off[i];
-    const uint32_t n = static_cast<uint32_t>(off[i + 1] - p0);
+// increment times the voxel's part of that sum (:64-66).
+__device__ __forceinline__ void slr_iter_muon(const SlrArgs& a, const SlrPass& p, uint64_t i, int lane) {
+    const uint64_t p0 = p.off[i];
+    const uint32_t n = static_cast<uint32_t>(p.off[i + 1] - p0);
     double part = 0.0;  // :49-52
-    for (uint32_t k = lane; k < n; k += 32) part = dadd(part, a.img[vox[p0 + k]]);
+    for (uint32_t k = lane; k < n; k += 32) part = dadd(part, a.img[p.vox[p0 + k]]);
     const double total = warp_sum(part);
-    const double share = ddiv(dmul(s.a2, 0.5), static_cast<double>(static_cast<uint64_t>(n) * n));
-    const double e2 = dmul(r.ein, r.ein);
+    const double e2 = a.has_energy ? p.e2[i] : 0.0;
     for (uint32_t k = lane; k < n; k += 32) {
-        const uint32_t j = vox[p0 + k];
-        const double l = len[p0 + k];
-        double iv;
-        if (a.length_weighted) {
-            a.weight[j] = dadd(a.weight[j], ddiv(l, a.g.dz));
-            const double f = ddiv(l, s.l_total);
-            iv = dmul(dmul(dmul(s.a2, 0.5), f), f);
-        } else {
-            a.weight[j] = dadd(a.weight[j], 1.0);
-            iv = share;
-        }
-        iv = dmul(iv, ddiv(a.img[j], total));  // :64-66
-        if (a.has_energy) iv = dmul(iv, e2);
+        const uint32_t j = p.vox[p0 + k];
+        a.weight[j] = dadd(a.weight[j], p.winc[p0 + k]);
+        double iv = dmul(p.iv0[p0 + k], ddiv(a.img[j], total));
+        if (a.has_energy) iv = dmul(iv, e2);  // :87-89
         a.img[j] = dadd(a.img[j], iv);
     }
 }
 
 // A later pass muon after muon on a single warp: a muon's stores are ordered
 // before the next muon's loads by __syncwarp; no other warp touches the image.
-__global__ void k_slr_iter_pass(SlrArgs a, const uint64_t* __restrict__ off, const uint32_t* __restrict__ vox,
-                                const double* __restrict__ len) {
+__global__ void k_slr_iter_pass(SlrArgs a, SlrPass p) {
     const int lane = threadIdx.x & 31;
     if (threadIdx.x >= 32) return;
-    const DevGrid g = make_dev_grid(a.g);
-    const double z_lo = a.g.z_min;
-    const double z_hi = dadd(a.g.z_min, dmul(a.g.dz, static_cast<double>(a.g.nz)));
     for (uint64_t i = 0; i < a.n; ++i) {
-        slr_iter_muon(a, g, z_lo, z_hi, i, off, vox, len, lane);
+        slr_iter_muon(a, p, i, lane);
         __syncwarp();
     }
 }
@@ -174,19 +185,13 @@ __global__ void k_slr_iter_pass(SlrArgs a, const uint64_t* __restrict__ off, con
 // loop, whatever the order inside a level.  One block: its warps take the
 // muons of a level, and the block barrier orders the levels (global stores
 // before it are visible to the whole block after it).
-__global__ void __launch_bounds__(1024) k_slr_iter_levels(SlrArgs a, const uint64_t* __restrict__ off,
-                                                          const uint32_t* __restrict__ vox,
-                                                          const double* __restrict__ len,
-                                                          const uint32_t* __restrict__ order,
+__global__ void __launch_bounds__(1024) k_slr_iter_levels(SlrArgs a, SlrPass p, const uint32_t* __restrict__ order,
                                                           const uint32_t* __restrict__ lstart, uint32_t levels) {
     const int lane = threadIdx.x & 31;
     const uint32_t warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const DevGrid g = make_dev_grid(a.g);
-    const double z_lo = a.g.z_min;
-    const double z_hi = dadd(a.g.z_min, dmul(a.g.dz, static_cast<double>(a.g.nz)));
     for (uint32_t l = 0; l < levels; ++l) {
         const uint32_t e = lstart[l + 1];
-        for (uint32_t q = lstart[l] + warp; q < e; q += nw) slr_iter_muon(a, g, z_lo, z_hi, order[q], off, vox, len, lane);
+        for (uint32_t q = lstart[l] + warp; q < e; q += nw) slr_iter_muon(a, p, order[q], lane);
         __syncthreads();
     }
 }
@@ -206,17 +211,22 @@ void launch_slr_paths(const SlrArgs& a, const uint64_t* off, uint32_t* counts, u
     count_launches(1);
 }
 
-void launch_slr_iter_pass(const SlrArgs& a, const uint64_t* off, const uint32_t* vox, const double* len,
-                          cudaStream_t s) {
+void launch_slr_pair_terms(const SlrArgs& a, const SlrPass& p, cudaStream_t s) {
     if (a.n == 0) return;
-    k_slr_iter_pass<<<1, 32, 0, s>>>(a, off, vox, len);
+    k_slr_pair_terms<<<static_cast<unsigned>((a.n + 127) / 128), 128, 0, s>>>(a, p);
     count_launches(1);
 }
 
-void launch_slr_iter_levels(const SlrArgs& a, const uint64_t* off, const uint32_t* vox, const double* len,
-                            const uint32_t* order, const uint32_t* lstart, uint32_t levels, cudaStream_t s) {
+void launch_slr_iter_pass(const SlrArgs& a, const SlrPass& p, cudaStream_t s) {
+    if (a.n == 0) return;
+    k_slr_iter_pass<<<1, 32, 0, s>>>(a, p);
+    count_launches(1);
+}
+
+void launch_slr_iter_levels(const SlrArgs& a, const SlrPass& p, const uint32_t* order, const uint32_t* lstart,
+                            uint32_t levels, cudaStream_t s) {
     if (a.n == 0 || levels == 0) return;
-    k_slr_iter_levels<<<1, 1024, 0, s>>>(a, off, vox, len, order, lstart, levels);
+    k_slr_iter_levels<<<1, 1024, 0, s>>>(a, p, order, lstart, levels);
     count_launches(1);
 }
 
