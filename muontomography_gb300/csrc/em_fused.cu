@@ -318,12 +318,8 @@ __global__ void __launch_bounds__(32 * GROUP, fused_min_blocks(GROUP, RC)) k_em_
 // The 32 muons of a batch own one contiguous range of the muon-major lists.
 // The CTA copies that range (up to kStagedPairs pairs) into shared memory
 // with 16-byte cp.async copies, so the lists leave HBM once and the scatter
-// reads them back from shared memory; pairs of a batch beyond the staged ones
-// are read from global memory in both steps.  The batch's pairs are split
-// evenly over the CTA's threads, whatever the muons' lengths: thread t takes
-// the C consecutive pairs from t*C (C odd, so a warp's shared-memory reads
-// fall in distinct banks), keeps running sums while its pairs stay on one
-// muon and adds them to that muon's shared sums where the muon ends.  Two
+// reads them back from shared memory instead of from L2/HBM; pairs of a batch
+// beyond the staged ones are read from global memory in both steps.  Two
 // CTAs are resident per SM, so one copies its batch while the other works.
 template <typename Real>
 struct Staged {
@@ -331,14 +327,15 @@ struct Staged {
     static constexpr int kSlots = kPairs + 8;  // room for the 16-byte widening at both ends
     static constexpr size_t kSmem = static_cast<size_t>(kSlots) * (sizeof(uint32_t) + 2 * sizeof(Real));
 };
-constexpr int kStagedGroup = 16;  // the launch is 32 * kStagedGroup threads
+constexpr int kStagedGroup = 16;
 
 template <typename Real>
 __global__ void __launch_bounds__(32 * kStagedGroup, 2) k_em_staged(FusedArgs<Real> a) {
     using R4 = typename Vec4<Real>::type;
     using S = Staged<Real>;
-    constexpr int kThreads = 32 * kStagedGroup;
-    constexpr int U = 8;                       // gathers in flight per thread
+    constexpr int GROUP = kStagedGroup;
+    constexpr int kThreads = 32 * GROUP;
+    constexpr int U = 4;                       // gathers in flight per lane
     constexpr int EJ = 16 / sizeof(uint32_t);  // elements per 16-byte copy
     constexpr int ER = 16 / sizeof(Real);
     extern __shared__ __align__(16) unsigned char staged_smem[];
@@ -350,7 +347,9 @@ __global__ void __launch_bounds__(32 * kStagedGroup, 2) k_em_staged(FusedArgs<Re
     __shared__ __align__(16) R4 s_sd[kBatch];
     __shared__ Real s_pr2[kBatch];
     __shared__ uint32_t s_off[kBatch + 1];
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int ms = tid / GROUP, glane = tid % GROUP;
+    const unsigned gmask = ((1u << GROUP) - 1u) << (lane & ~(GROUP - 1));
     const uint32_t V = a.V;
     const uint64_t nbatch = (static_cast<uint64_t>(a.N) + kBatch - 1) / kBatch;
     const uint64_t keep = l2_keep_policy();
@@ -360,10 +359,8 @@ __global__ void __launch_bounds__(32 * kStagedGroup, 2) k_em_staged(FusedArgs<Re
     for (uint64_t b = blockIdx.x; b < nbatch; b += gridDim.x) {
         const uint64_t mfirst = b * kBatch;
         const uint64_t mend = min(mfirst + kBatch, static_cast<uint64_t>(a.N));
-        const uint32_t nm = static_cast<uint32_t>(mend - mfirst);
         const uint64_t p0 = a.off[mfirst], p1 = a.off[mend];
-        const uint32_t np = static_cast<uint32_t>(p1 - p0);
-        const uint32_t nst = min(np, static_cast<uint32_t>(S::kPairs));  // staged
+        const uint32_t nst = static_cast<uint32_t>(min(p1 - p0, static_cast<uint64_t>(S::kPairs)));  // staged
         // ---- the batch's pairs into shared memory ------------------------------
         // each array's copy starts at the 16-byte boundary at or below p0; the
         // arrays are padded past their last pair, so the widened end stays inside
@@ -375,95 +372,79 @@ __global__ void __launch_bounds__(32 * kStagedGroup, 2) k_em_staged(FusedArgs<Re
             cp_async_16(s_L + c * ER, a.L + ar + c * ER);
             cp_async_16(s_T + c * ER, a.T + ar + c * ER);
         }
-        if (tid < static_cast<int>(nm)) stage_muon(&s_sd[tid], &s_pr2[tid], a.sd + mfirst + tid, a.pr2 + mfirst + tid);
+        if (tid < kBatch && mfirst + tid < mend) stage_muon(&s_sd[tid], &s_pr2[tid], a.sd + mfirst + tid, a.pr2 + mfirst + tid);
         if (tid <= kBatch) s_off[tid] = static_cast<uint32_t>(a.off[min(mfirst + tid, mend)] - p0);
-        if (tid < kBatch) s_sum[0][tid] = s_sum[1][tid] = s_sum[2][tid] = Real(0);
         cp_async_wait_all();
         __syncthreads();
         // pair k of the batch (0-based): from shared memory, or global beyond the staged ones
-        auto pair_j = [&](uint32_t k) { return k < nst ? s_j[sj + k] : __ldg(a.vidx + p0 + k); };
-        auto pair_lt = [&](uint32_t k, Real& L, Real& T) {
+        auto pair = [&](uint32_t k, uint32_t& j, Real& L, Real& T) {
             if (k < nst) {
+                j = s_j[sj + k];
                 L = s_L[sr + k];
                 T = s_T[sr + k];
             } else {
+                j = __ldg(a.vidx + p0 + k);
                 L = __ldg(a.L + p0 + k);
                 T = __ldg(a.T + p0 + k);
             }
         };
-        // this thread's pairs [k0, k1), and the muon of its first pair
-        const uint32_t C = ((np + kThreads - 1) / kThreads) | 1u;
-        const uint32_t k0 = min(static_cast<uint32_t>(tid) * C, np), k1 = min(k0 + C, np);
-        uint32_t mu0 = 0;
-        for (uint32_t step = kBatch / 2; step > 0; step >>= 1)  // last muon whose pairs start at or before k0
-            if (mu0 + step < nm && s_off[mu0 + step] <= k0) mu0 += step;
-        // ---- the covariance sums ------------------------------------------------
-        {
-            uint32_t mu = mu0, next = s_off[mu0 + 1];
-            Real c0 = 0, c1 = 0, c2 = 0;
-            for (uint32_t kb = k0; kb < k1; kb += U) {
-                uint32_t jj[U];
-                Real lv[U];
+        uint32_t kb = 0, ke = 0;
+        if (mfirst + ms < mend) {
+            kb = s_off[ms];
+            ke = s_off[ms + 1];
+        }
+        // ---- the covariance sums: GROUP lanes per muon, U gathers in flight ----
+        Real c0 = 0, c1 = 0, c2 = 0;
+        for (uint32_t k0 = kb + glane; k0 < ke; k0 += GROUP * U) {
+            uint32_t jj[U];
+            Real ll[U], tt[U], lv[U];
 #pragma unroll
-                for (int u = 0; u < U; ++u) jj[u] = kb + u < k1 ? pair_j(kb + u) : 0xffffffffu;
-#pragma unroll
-                for (int u = 0; u < U; ++u) lv[u] = jj[u] < V ? ld_keep(a.lam + jj[u], keep) : Real(0);
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const uint32_t k = kb + u;
-                    if (k >= k1) break;
-                    while (k >= next) {  // the muon ended: its share of the sums to shared memory
-                        if (c0 != Real(0) || c1 != Real(0) || c2 != Real(0)) {
-                            atomicAdd(&s_sum[0][mu], c0);
-                            atomicAdd(&s_sum[1][mu], c1);
-                            atomicAdd(&s_sum[2][mu], c2);
-                        }
-                        c0 = c1 = c2 = Real(0);
-                        ++mu;
-                        next = s_off[mu + 1];
-                    }
-                    if (jj[u] != 0xffffffffu) {
-                        Real L, T;
-                        pair_lt(k, L, T);
-                        add_sigma(lv[u], L, T, c0, c1, c2);
-                    }
-                }
+            for (int u = 0; u < U; ++u) {
+                const uint32_t k = k0 + u * GROUP;
+                jj[u] = 0xffffffffu;
+                ll[u] = tt[u] = Real(0);
+                if (k < ke) pair(k, jj[u], ll[u], tt[u]);
             }
-            if (k0 < k1 && (c0 != Real(0) || c1 != Real(0) || c2 != Real(0))) {
-                atomicAdd(&s_sum[0][mu], c0);
-                atomicAdd(&s_sum[1][mu], c1);
-                atomicAdd(&s_sum[2][mu], c2);
-            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) lv[u] = jj[u] < V ? ld_keep(a.lam + jj[u], keep) : Real(0);
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (jj[u] != 0xffffffffu) add_sigma(lv[u], ll[u], tt[u], c0, c1, c2);
+        }
+#pragma unroll
+        for (int o = GROUP / 2; o > 0; o >>= 1) {
+            c0 += __shfl_xor_sync(gmask, c0, o, GROUP);
+            c1 += __shfl_xor_sync(gmask, c1, o, GROUP);
+            c2 += __shfl_xor_sync(gmask, c2, o, GROUP);
+        }
+        if (glane == 0) {
+            s_sum[0][ms] = c0;
+            s_sum[1][ms] = c1;
+            s_sum[2][ms] = c2;
         }
         __syncthreads();
         // ---- FP64 2x2 algebra of the batch, a muon per lane of warp 0 --------
         if (tid < kBatch) {
-            Real k0c = 0, k1c = 0, k2c = 0;
-            if (tid < static_cast<int>(nm))
+            Real k0 = 0, k1 = 0, k2 = 0;
+            if (mfirst + tid < mend)
                 muon_coefficients<Real>(s_sum[0][tid], s_sum[1][tid], s_sum[2][tid], s_pr2[tid], s_sd[tid], a.E00,
-                                        a.E01, a.E11, a.compute_cost != 0, k0c, k1c, k2c, cost_local, singular_local);
-            s_k[0][tid] = k0c;
-            s_k[1][tid] = k1c;
-            s_k[2][tid] = k2c;
+                                        a.E01, a.E11, a.compute_cost != 0, k0, k1, k2, cost_local, singular_local);
+            s_k[0][tid] = k0;
+            s_k[1][tid] = k1;
+            s_k[2][tid] = k2;
         }
         __syncthreads();
         // ---- g_ij of every pair added to G_j, the pairs read back -------------
-        {
-            uint32_t mu = mu0, next = s_off[mu0 + 1];
-            Real q0 = s_k[0][mu], q1 = s_k[1][mu], q2 = s_k[2][mu];
-            for (uint32_t k = k0; k < k1; ++k) {
-                while (k >= next) {
-                    ++mu;
-                    next = s_off[mu + 1];
-                    q0 = s_k[0][mu];
-                    q1 = s_k[1][mu];
-                    q2 = s_k[2][mu];
-                }
-                const uint32_t j = pair_j(k);
-                if (j < V) {
+        const Real k0 = s_k[0][ms], k1 = s_k[1][ms], k2 = s_k[2][ms];
+        for (uint32_t q0 = kb + glane; q0 < ke; q0 += GROUP * U) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const uint32_t k = q0 + u * GROUP;
+                if (k < ke) {
+                    uint32_t j;
                     Real L, T;
-                    pair_lt(k, L, T);
-                    red_add(a.G + j, g_term(q0, q1, q2, L, T), keep);
+                    pair(k, j, L, T);
+                    if (j < V) red_add(a.G + j, g_term(k0, k1, k2, L, T), keep);
                 }
             }
         }
