@@ -75,8 +75,8 @@ TRAFFIC_PER_PAIR = {
 # set-up kernels and host phases reported by the library's profiler
 SETUP_KERNELS = ["keep_flags", "scan", "compact", "muon_info", "siddon_count", "siddon_fill", "voxel_offset",
                  "voxel_hist", "voxel_major", "voxel_classes", "path_bound", "path_compact", "path_stats"]
-SETUP_PHASES = ["gather", "info_count", "fill", "path_stats", "voxel_major", "classes", "tiles", "image",
-                "autotune"]
+SETUP_PHASES = ["load_alloc", "load_copy", "gather", "info_count", "fill", "path_stats", "voxel_major", "classes",
+                "tiles", "image", "autotune"]
 ITER_KERNELS = ["em_muon", "em_scatter", "em_fused", "em_walk", "em_voxel", "em_update", "brick_lambda", "map_voxel",
                 "map_copy", "cost"]
 

@@ -647,33 +647,55 @@ __global__ void k_path_uncount(const muto_ray* __restrict__ rays, const uint32_t
 
 // The voxel side: lambda_j + lambda_j^2 G_j / (2 M_j) (0 when M_j = 0), or the
 // gradient -lambda_j G_j of the NLL with respect to log(lambda_j); G_j is
-// cleared for the next pass.
+// cleared for the next pass.  Each thread takes kUpdateVox voxels a block's
+// width apart and issues all their loads before using any: the pass is bound
+// by load latency, not bandwidth, with one voxel per thread.
+constexpr int kUpdateVox = 4;
+constexpr int kUpdateThreads = 256;
+
 template <typename Real, typename OutT>
-__global__ void k_mean_update(const Real* __restrict__ lam, Real* __restrict__ G, const uint32_t* __restrict__ mult,
-                              uint32_t V, BrickDims bd, int brick, OutT* __restrict__ out, double* __restrict__ grad,
-                              const double* __restrict__ lam64) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= V) return;
-    const uint32_t jb = brick ? brick_of(j, bd) : j;
-    const Real gj = G[jb];
-    G[jb] = Real(0);
-    const uint32_t M = mult[j];
-    if (grad) {
-        grad[j] = M ? -lam64[j] * static_cast<double>(gj) : 0.0;
-        return;
+__global__ void __launch_bounds__(kUpdateThreads) k_mean_update(const Real* __restrict__ lam, Real* __restrict__ G,
+                                                                const uint32_t* __restrict__ mult, uint32_t V,
+                                                                BrickDims bd, int brick, OutT* __restrict__ out,
+                                                                double* __restrict__ grad,
+                                                                const double* __restrict__ lam64) {
+    const uint32_t base = blockIdx.x * (kUpdateThreads * kUpdateVox) + threadIdx.x;
+    uint32_t jb[kUpdateVox];
+    Real gj[kUpdateVox], lj[kUpdateVox];
+    uint32_t Mj[kUpdateVox];
+    double l64[kUpdateVox];
+#pragma unroll
+    for (int u = 0; u < kUpdateVox; ++u) {
+        const uint32_t j = base + u * kUpdateThreads;
+        jb[u] = j < V ? (brick ? brick_of(j, bd) : j) : 0xffffffffu;
+        gj[u] = jb[u] != 0xffffffffu ? G[jb[u]] : Real(0);
+        Mj[u] = j < V ? mult[j] : 0u;
+        if (grad) l64[u] = j < V ? lam64[j] : 0.0;
+        else lj[u] = j < V ? lam[j] : Real(0);
     }
-    if constexpr (sizeof(Real) == sizeof(float)) {
-        // the mixed form: lambda is stored in FP32, so its increment is formed
-        // in FP32 too.  GB300 issues FP64 at a sixty-fourth of the FP32 rate,
-        // and an FP64 division per voxel made this pass arithmetic bound at
-        // about ten times its memory time.
-        const float l = lam[j];
-        const float inc = l * l * gj / (2.0f * static_cast<float>(M));
-        if constexpr (sizeof(OutT) == sizeof(float)) out[j] = M ? l + inc : 0.0f;
-        else out[j] = M ? static_cast<double>(l) + static_cast<double>(inc) : 0.0;
-    } else {
-        const double l = static_cast<double>(lam[j]);
-        out[j] = M ? static_cast<OutT>(l + l * l * static_cast<double>(gj) / (2.0 * static_cast<double>(M))) : OutT(0);
+#pragma unroll
+    for (int u = 0; u < kUpdateVox; ++u) {
+        const uint32_t j = base + u * kUpdateThreads;
+        if (j >= V) break;
+        G[jb[u]] = Real(0);
+        const uint32_t M = Mj[u];
+        if (grad) {
+            grad[j] = M ? -l64[u] * static_cast<double>(gj[u]) : 0.0;
+            continue;
+        }
+        if constexpr (sizeof(Real) == sizeof(float)) {
+            // the mixed form: lambda is stored in FP32, so its increment is
+            // formed in FP32 too (GB300 issues FP64 at a sixty-fourth of the
+            // FP32 rate; an FP64 division per voxel cost more than the loads)
+            const float l = lj[u];
+            const float inc = l * l * gj[u] / (2.0f * static_cast<float>(M));
+            if constexpr (sizeof(OutT) == sizeof(float)) out[j] = M ? l + inc : 0.0f;
+            else out[j] = M ? static_cast<double>(l) + static_cast<double>(inc) : 0.0;
+        } else {
+            const double l = static_cast<double>(lj[u]);
+            out[j] = M ? static_cast<OutT>(l + l * l * static_cast<double>(gj[u]) / (2.0 * static_cast<double>(M)))
+                       : OutT(0);
+        }
     }
 }
 
@@ -828,8 +850,9 @@ template <typename Real, typename OutT>
 void launch_mean_update(const Real* lam, Real* G, const uint32_t* mult, uint32_t V, const BrickDims* brick, OutT* out,
                         double* grad, const double* lam64, cudaStream_t s) {
     if (V == 0) return;
-    k_mean_update<Real, OutT><<<(V + 255) / 256, 256, 0, s>>>(lam, G, mult, V, brick ? *brick : BrickDims{},
-                                                                brick ? 1 : 0, out, grad, lam64);
+    const uint32_t per_block = kUpdateThreads * kUpdateVox;
+    k_mean_update<Real, OutT><<<(V + per_block - 1) / per_block, kUpdateThreads, 0, s>>>(
+        lam, G, mult, V, brick ? *brick : BrickDims{}, brick ? 1 : 0, out, grad, lam64);
     count_launches(1);
 }
 template void launch_mean_update<float, float>(const float*, float*, const uint32_t*, uint32_t, const BrickDims*,

@@ -2090,7 +2090,11 @@ int muto_load_tracks(muto_handle* h, const muto_ray* rays, uint64_t n, int on_de
         h->drop_graph();
         h->prepared = false;
         h->n_rays = n;
-        h->rays.alloc(std::max<uint64_t>(n, 1) * sizeof(muto_ray), &h->dev_bytes);
+        {
+            HostPhase ph(h, "load_alloc");
+            h->rays.alloc(std::max<uint64_t>(n, 1) * sizeof(muto_ray), &h->dev_bytes);
+        }
+        HostPhase ph(h, "load_copy");
         if (n > 0)
             CK(cudaMemcpyAsync(h->rays.as<void>(), rays, n * sizeof(muto_ray),
                                on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
