@@ -611,7 +611,7 @@ def run_ours(args) -> int:
                        "muon_pass": {1: "tma_tiles", 2: "warp_batched", 3: "one_pass_lists", 4: "recompute_walk",
                                      5: "split_muon_pass_and_scatter",
                                      6: "one_pass_staged_in_shared_memory"}.get(st["muon_pass"]),
-                       "muon_group": st["muon_group"], "held_pairs": st["tile_pairs"]},
+                       "muon_group": st["muon_group"], "tile_pairs": st["tile_pairs"]},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
@@ -807,7 +807,7 @@ def run_batch(args) -> int:
                        "autotuner": {"pass": {1: "tma_tiles", 2: "warp_batched", 3: "one_pass_lists",
                                               5: "split_muon_pass_and_scatter",
                                               6: "one_pass_staged_in_shared_memory"}.get(st["muon_pass"]),
-                                     "lanes_per_muon": st["muon_group"], "held_pairs": st["tile_pairs"],
+                                     "lanes_per_muon": st["muon_group"], "tile_pairs": st["tile_pairs"],
                                      "voxel_stream_above": st["voxel_stream_above"]},
                        "parallelism": f"replicas x{world} (one batch per GPU)",
                        "l2": "inputs larger than L2: the batch's pair lists far exceed 126 MB, no flush"},
@@ -844,7 +844,7 @@ def main() -> int:
     ap.add_argument("--cpu-sample-fixed", action="store_true",
                     help="reference leg: use --cpu-sample as it is instead of sizing it to the step count")
     ap.add_argument("--muon-pass", choices=["auto", "tile", "warp"], default="auto")
-    ap.add_argument("--fused-variant", choices=["auto", "4x8", "8x4", "8x8", "8x16", "16x8", "16x16", "staged", "split"],
+    ap.add_argument("--fused-variant", choices=["auto", "4x8", "8x4", "8x8", "8x16", "16x8", "16x16", "staged", "split", "split8"],
                     default="auto", help="the mean update's pass over muon-major lists (auto: timed at set-up)")
     ap.add_argument("--muon-layout", choices=["auto", "columns", "index"], default="auto")
     ap.add_argument("--voxel-stream-above", type=int, default=None,

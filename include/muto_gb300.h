@@ -75,8 +75,8 @@ typedef struct muto_status {
                                    6 its one-pass form with each batch's pairs staged in shared memory */
     int32_t muon_group;         /* lanes per muon in its covariance sums */
     int32_t tile_pairs;         /* pairs per tile (TMA variant), pairs per muon held in registers
-                                   (fused stored-list pass), pairs staged per batch (staged pass);
-                                   0 otherwise */
+                                   (fused stored-list pass), pairs staged per batch (staged pass),
+                                   pairs in flight per lane (split form's scatter); 0 otherwise */
     int32_t tile_muons;         /* muons per tile (TMA variant), muons per CTA batch (fused pass) */
     int32_t path_lists;         /* how the pairs are kept: 1 muon-major lists and their voxel-major copy,
                                    2 muon-major lists only, 3 none (paths walked every iteration);
@@ -132,7 +132,8 @@ typedef struct muto_handle muto_handle;
  * takes the lanes per muon and pairs held per lane by timing the variants
  * that suit the scan's mean path and the split form (the muon pass, then a
  * second pass over the lists adding the terms) at prepare; "4x8", "8x4",
- * "8x8", "8x16", "16x8", "16x16", "split" or "staged" (each batch's pairs
+ * "8x8", "8x16", "16x8", "16x16", "split", "split8" (its scatter with 8
+ * pairs in flight per lane) or "staged" (each batch's pairs
  * copied to shared memory once and read back there for the second step)
  * force one), "fused_prefetch"
  * (false; true: the one-pass form

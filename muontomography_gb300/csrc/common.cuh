@@ -405,10 +405,10 @@ template <typename Real>
 void launch_em_fused_walk(const FusedArgs<Real>& a, int num_sms, cudaStream_t s);
 // split form: g_ij of every pair from the muon pass's coefficients kvec, added to G
 template <typename Real>
-int em_scatter_blocks(int group);  // resident 256-thread CTAs per SM
+int em_scatter_blocks(int group, int depth);  // resident 256-thread CTAs per SM (depth: pairs in flight per lane)
 template <typename Real>
-void launch_em_scatter(const FusedArgs<Real>& a, const typename Vec4<Real>::type* kvec, int group, int blocks,
-                       cudaStream_t s);
+void launch_em_scatter(const FusedArgs<Real>& a, const typename Vec4<Real>::type* kvec, int group, int depth,
+                       int blocks, cudaStream_t s);
 // recompute set-up: in-grid length per kept muon and pairs per voxel (mult zeroed by the caller)
 void launch_path_stats(const muto_ray* rays, const uint32_t* kept, const double* scat, uint64_t n, muto_grid g,
                        int straight, double* ltot, uint32_t* mult, Counters* ctr, cudaStream_t s);

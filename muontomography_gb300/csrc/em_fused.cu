@@ -708,19 +708,41 @@ int fused_blocks_per_sm() {
 
 // The scatter of the split form: the per-muon coefficients come from the
 // muon pass (em_muon.cu) in kvec; GROUP lanes per muon stream its pairs a
-// second time and add g_ij to G_j.  No block barrier and no FP64.
-template <typename Real, int GROUP>
+// second time and add g_ij to G_j.  No block barrier and no FP64.  U pairs
+// are in flight per lane; with AHEAD the next muon's offsets and
+// coefficients are loaded while the current muon's pairs are, so a muon's
+// pair loads do not wait on its offsets.
+template <typename Real, int GROUP, int U, bool AHEAD>
 __global__ void __launch_bounds__(256) k_em_scatter(FusedArgs<Real> a, const typename Vec4<Real>::type* __restrict__ kvec) {
     using R4 = typename Vec4<Real>::type;
-    constexpr int U = 4;
     const uint64_t gid = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) / GROUP;
     const uint64_t ngroups = (static_cast<uint64_t>(gridDim.x) * blockDim.x) / GROUP;
     const int glane = threadIdx.x % GROUP;
     const uint32_t V = a.V;
     const uint64_t keep = l2_keep_policy();
-    for (uint64_t m = gid; m < a.N; m += ngroups) {
-        const R4 kv = kvec[m];
-        const uint64_t pb = a.off[m], pe = a.off[m + 1];
+    uint64_t m = gid;
+    R4 kv{};
+    uint64_t pb = 0, pe = 0;
+    if (AHEAD && m < a.N) {
+        kv = kvec[m];
+        pb = a.off[m];
+        pe = a.off[m + 1];
+    }
+    for (; m < a.N; m += ngroups) {
+        R4 kn{};
+        uint64_t pbn = 0, pen = 0;
+        if (AHEAD) {
+            const uint64_t mn = m + ngroups;
+            if (mn < a.N) {
+                kn = kvec[mn];
+                pbn = a.off[mn];
+                pen = a.off[mn + 1];
+            }
+        } else {
+            kv = kvec[m];
+            pb = a.off[m];
+            pe = a.off[m + 1];
+        }
         for (uint64_t k0 = pb + glane; k0 < pe; k0 += static_cast<uint64_t>(GROUP) * U) {
             uint32_t jj[U];
             Real ll[U], tt[U];
@@ -737,6 +759,11 @@ __global__ void __launch_bounds__(256) k_em_scatter(FusedArgs<Real> a, const typ
 #pragma unroll
             for (int u = 0; u < U; ++u)
                 if (jj[u] < V) red_add(a.G + jj[u], g_term(kv.x, kv.y, kv.z, ll[u], tt[u]), keep);
+        }
+        if (AHEAD) {
+            kv = kn;
+            pb = pbn;
+            pe = pen;
         }
     }
 }
@@ -800,31 +827,47 @@ void launch_em_fused(const FusedArgs<Real>& a, int variant, int blocks, cudaStre
 }
 template void launch_em_fused<float>(const FusedArgs<float>&, int, int, cudaStream_t);
 
-template <typename Real>
-int em_scatter_blocks(int group) {
+template <typename Real, int GROUP, int U, bool AHEAD>
+int scatter_blocks_per_sm() {
     int n = 0;
-    cudaError_t e;
-    if (group <= 8) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_em_scatter<Real, 8>, 256, 0);
-    else if (group <= 16) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_em_scatter<Real, 16>, 256, 0);
-    else e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_em_scatter<Real, 32>, 256, 0);
+    const cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_em_scatter<Real, GROUP, U, AHEAD>, 256, 0);
     return (e == cudaSuccess && n > 0) ? n : 1;
 }
-template int em_scatter_blocks<float>(int);
-template int em_scatter_blocks<double>(int);
 
 template <typename Real>
-void launch_em_scatter(const FusedArgs<Real>& a, const typename Vec4<Real>::type* kvec, int group, int blocks,
-                       cudaStream_t s) {
+int em_scatter_blocks(int group, int depth) {
+    if (depth > 4) {
+        if (group <= 8) return scatter_blocks_per_sm<Real, 8, 8, true>();
+        if (group <= 16) return scatter_blocks_per_sm<Real, 16, 8, true>();
+        return scatter_blocks_per_sm<Real, 32, 8, true>();
+    }
+    if (group <= 8) return scatter_blocks_per_sm<Real, 8, 4, false>();
+    if (group <= 16) return scatter_blocks_per_sm<Real, 16, 4, false>();
+    return scatter_blocks_per_sm<Real, 32, 4, false>();
+}
+template int em_scatter_blocks<float>(int, int);
+template int em_scatter_blocks<double>(int, int);
+
+template <typename Real>
+void launch_em_scatter(const FusedArgs<Real>& a, const typename Vec4<Real>::type* kvec, int group, int depth,
+                       int blocks, cudaStream_t s) {
     if (a.N == 0) return;
     const uint64_t need = (static_cast<uint64_t>(a.N) * group + 255) / 256;
     const unsigned nb = static_cast<unsigned>(need < static_cast<uint64_t>(blocks) ? need : blocks);
-    if (group <= 8) k_em_scatter<Real, 8><<<nb, 256, 0, s>>>(a, kvec);
-    else if (group <= 16) k_em_scatter<Real, 16><<<nb, 256, 0, s>>>(a, kvec);
-    else k_em_scatter<Real, 32><<<nb, 256, 0, s>>>(a, kvec);
+    if (depth > 4) {
+        if (group <= 8) k_em_scatter<Real, 8, 8, true><<<nb, 256, 0, s>>>(a, kvec);
+        else if (group <= 16) k_em_scatter<Real, 16, 8, true><<<nb, 256, 0, s>>>(a, kvec);
+        else k_em_scatter<Real, 32, 8, true><<<nb, 256, 0, s>>>(a, kvec);
+    } else {
+        if (group <= 8) k_em_scatter<Real, 8, 4, false><<<nb, 256, 0, s>>>(a, kvec);
+        else if (group <= 16) k_em_scatter<Real, 16, 4, false><<<nb, 256, 0, s>>>(a, kvec);
+        else k_em_scatter<Real, 32, 4, false><<<nb, 256, 0, s>>>(a, kvec);
+    }
     count_launches(1);
 }
-template void launch_em_scatter<float>(const FusedArgs<float>&, const float4*, int, int, cudaStream_t);
-template void launch_em_scatter<double>(const FusedArgs<double>&, const double4*, int, int, cudaStream_t);
+template void launch_em_scatter<float>(const FusedArgs<float>&, const float4*, int, int, int, cudaStream_t);
+template void launch_em_scatter<double>(const FusedArgs<double>&, const double4*, int, int, int, cudaStream_t);
 template void launch_em_fused<double>(const FusedArgs<double>&, int, int, cudaStream_t);
 
 template <typename Real>

@@ -278,8 +278,9 @@ Params parse_params(Method m, const std::string& text, int variant = 0) {
         else if (fv == "8x4") P.fused_variant = 5;
         else if (fv == "staged") P.fused_variant = kFusedStaged;
         else if (fv == "split") P.fused_variant = kFusedVariants;
+        else if (fv == "split8") P.fused_variant = kFusedVariants + 2;  // its scatter 8 pairs deep per lane
         else throw Error(MUTO_ERR_CONFIG, "fused_variant must be \"auto\", \"4x8\", \"8x4\", \"8x8\", \"8x16\", "
-                                          "\"16x8\", \"16x16\", \"staged\" or \"split\"");
+                                          "\"16x8\", \"16x16\", \"staged\", \"split\" or \"split8\"");
         P.fused_prefetch = cfg.value("fused_prefetch", false);
         P.setup_chunk_pairs = cfg.value("setup_chunk_pairs", static_cast<int64_t>(0));
         if (P.setup_chunk_pairs < 0) throw Error(MUTO_ERR_CONFIG, "setup_chunk_pairs must be >= 0");
@@ -410,6 +411,7 @@ struct muto_handle {
     DevMem ltot;                      // recompute: in-grid path length per kept muon
     int fused_variant = 1, fused_blocks = 0;  // stored-list fused pass: variant and persistent grid
     int scatter_group = 32, scatter_blocks = 0;  // split form's scatter pass (fused_variant == kFusedVariants)
+    int scatter_depth = 4;                       // its pairs in flight per lane
     bool brick = false;               // path voxel indices are bricked (single scans), see lam_b
     BrickDims bdims{};
     uint64_t vb = 0;                  // bricked index space (>= V)
@@ -1339,7 +1341,7 @@ void launch_fused_pass(muto_handle* h, const Real* lam, bool cost, cudaStream_t 
         const MuonPassArgs<Real> m = muon_args<Real>(h, lam, cost);
         launch("em_muon", [&] { launch_muon_pass<Real>(h, m, s); });
         launch("em_scatter",
-               [&] { launch_em_scatter<Real>(a, h->kvec.as<R4>(), h->scatter_group, h->scatter_blocks, s); });
+               [&] { launch_em_scatter<Real>(a, h->kvec.as<R4>(), h->scatter_group, h->scatter_depth, h->scatter_blocks, s); });
         return;
     }
     if (h->lists == kListsRecompute) {
@@ -1393,19 +1395,19 @@ void autotune_fused(muto_handle* h) {
         // on their longest path)
         if (fit && v != kFusedStaged) cands.push_back(v);
     }
-    if (!forced) {  // the split form, its scatter with 32 and 16 lanes per muon
-        cands.push_back(kFusedVariants);
-        cands.push_back(kFusedVariants + 1);
-    }
+    if (!forced)  // the split form: its scatter with g and g/2 lanes per muon, 4 or 8 pairs in flight per lane
+        for (int c = 0; c < 4; ++c) cands.push_back(kFusedVariants + c);
     auto apply = [&](int v) {
         h->fused_variant = v >= kFusedVariants ? kFusedVariants : v;
         if (v >= kFusedVariants) {  // split: the warp-batched muon pass and the scatter pass
             const int g = avg <= 32 ? 8 : (avg <= 64 ? 16 : 32);
+            const int c = v - kFusedVariants;
             h->muon_kind = 2;
             h->muon_group = g;
             h->warp_blocks = em_muon_warp_blocks<Real>(g) * h->num_sms;
-            h->scatter_group = v == kFusedVariants ? g : std::max(8, g / 2);
-            h->scatter_blocks = em_scatter_blocks<Real>(h->scatter_group) * h->num_sms;
+            h->scatter_group = c % 2 == 0 ? g : std::max(8, g / 2);
+            h->scatter_depth = c >= 2 ? 8 : 4;
+            h->scatter_blocks = em_scatter_blocks<Real>(h->scatter_group, h->scatter_depth) * h->num_sms;
         } else {
             h->fused_blocks = em_fused_blocks<Real>(v) * h->num_sms;
         }
@@ -2046,7 +2048,7 @@ int muto_get_status(const muto_handle* hc, muto_status* out) {
     if (h->method != kPoca && h->lists == kListsMuonMajor && h->fused_variant == kFusedVariants) {
         out->muon_pass = 5;
         out->muon_group = h->scatter_group;
-        out->tile_pairs = 0;
+        out->tile_pairs = h->scatter_depth;
         out->tile_muons = 0;
     } else if (h->method != kPoca && h->lists == kListsMuonMajor) {
         const bool staged = h->fused_variant == kFusedStaged;
