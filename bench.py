@@ -66,8 +66,8 @@ UNIT = "muon·voxel updates/s"
 # profiles/em_passes_cube50_40mm_2.5M.md (the 100^3 scene on 50^3 voxels,
 # median update, 68 700 086 pairs).
 TRAFFIC_PER_PAIR = {
-    ("grid256", "em_muon"): (2.461415e9 + 7.902976e6) / 195962860,
-    ("grid256", "em_scatter"): (2.598490e9 + 10.157312e6) / 195962860,
+    ("grid256", "em_muon"): (2.461541e9 + 8.514816e6) / 195962860,
+    ("grid256", "em_scatter"): (2.511995e9 + 9.667328e6) / 195962860,  # the 8-deep scatter
     ("cube", "em_muon"): 868.4e6 / 68700086,
     ("cube", "em_voxel"): 1371.0e6 / 68700086,
 }
