@@ -77,7 +77,9 @@ typedef struct muto_status {
     int32_t tile_pairs;         /* pairs per tile (TMA variant), pairs per muon held in registers
                                    (fused stored-list pass), pairs staged per batch (staged pass),
                                    pairs in flight per lane (split form's scatter); 0 otherwise */
-    int32_t tile_muons;         /* muons per tile (TMA variant), muons per CTA batch (fused pass) */
+    int32_t tile_muons;         /* muons per tile (TMA variant), muons per CTA batch (fused pass),
+                                   chunks of muons whose muon pass and scatter overlap (split form;
+                                   0: not overlapped) */
     int32_t path_lists;         /* how the pairs are kept: 1 muon-major lists and their voxel-major copy,
                                    2 muon-major lists only, 3 none (paths walked every iteration);
                                    0 for the one-shot methods */
@@ -133,7 +135,9 @@ typedef struct muto_handle muto_handle;
  * that suit the scan's mean path and the split form (the muon pass, then a
  * second pass over the lists adding the terms) at prepare; "4x8", "8x4",
  * "8x8", "8x16", "16x8", "16x16", "split", "split8" (its scatter with 8
- * pairs in flight per lane) or "staged" (each batch's pairs
+ * pairs in flight per lane), "split8_overlap" (the same, the scatter of one
+ * chunk of muons running beside the muon pass of the next) or "staged"
+ * (each batch's pairs
  * copied to shared memory once and read back there for the second step)
  * force one), "fused_prefetch"
  * (false; true: the one-pass form

@@ -279,8 +279,9 @@ Params parse_params(Method m, const std::string& text, int variant = 0) {
         else if (fv == "staged") P.fused_variant = kFusedStaged;
         else if (fv == "split") P.fused_variant = kFusedVariants;
         else if (fv == "split8") P.fused_variant = kFusedVariants + 2;  // its scatter 8 pairs deep per lane
+        else if (fv == "split8_overlap") P.fused_variant = kFusedVariants + 4;  // and overlapped with the muon pass
         else throw Error(MUTO_ERR_CONFIG, "fused_variant must be \"auto\", \"4x8\", \"8x4\", \"8x8\", \"8x16\", "
-                                          "\"16x8\", \"16x16\", \"staged\", \"split\" or \"split8\"");
+                                          "\"16x8\", \"16x16\", \"staged\", \"split\", \"split8\" or \"split8_overlap\"");
         P.fused_prefetch = cfg.value("fused_prefetch", false);
         P.setup_chunk_pairs = cfg.value("setup_chunk_pairs", static_cast<int64_t>(0));
         if (P.setup_chunk_pairs < 0) throw Error(MUTO_ERR_CONFIG, "setup_chunk_pairs must be >= 0");
@@ -412,6 +413,12 @@ struct muto_handle {
     int fused_variant = 1, fused_blocks = 0;  // stored-list fused pass: variant and persistent grid
     int scatter_group = 32, scatter_blocks = 0;  // split form's scatter pass (fused_variant == kFusedVariants)
     int scatter_depth = 4;                       // its pairs in flight per lane
+    // the split form overlapped: muon pass and scatter on chunks of the muons,
+    // the scatter of chunk c on the side stream while the muon pass of c+1 runs
+    static constexpr int kOverlapChunks = 4;
+    bool overlap = false;
+    int warp_blocks_ov = 0, scatter_blocks_ov = 0;  // each kernel's grid when they share the GPU
+    cudaEvent_t ov_ev[kOverlapChunks + 1] = {};
     bool brick = false;               // path voxel indices are bricked (single scans), see lam_b
     BrickDims bdims{};
     uint64_t vb = 0;                  // bricked index space (>= V)
@@ -455,6 +462,8 @@ struct muto_handle {
             cudaEventDestroy(fan.join[k]);
         }
         if (fan.n) cudaEventDestroy(fan.fork);
+        for (cudaEvent_t e : ov_ev)
+            if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -1339,9 +1348,43 @@ void launch_fused_pass(muto_handle* h, const Real* lam, bool cost, cudaStream_t 
     if (h->lists == kListsMuonMajor && h->fused_variant == kFusedVariants) {
         // split form: the muon pass writes every muon's coefficients, the scatter adds g_ij
         const MuonPassArgs<Real> m = muon_args<Real>(h, lam, cost);
-        launch("em_muon", [&] { launch_muon_pass<Real>(h, m, s); });
-        launch("em_scatter",
-               [&] { launch_em_scatter<Real>(a, h->kvec.as<R4>(), h->scatter_group, h->scatter_depth, h->scatter_blocks, s); });
+        if (!h->overlap || profiled || h->N < static_cast<uint64_t>(muto_handle::kOverlapChunks)) {
+            // (profiled passes time each kernel alone)
+            launch("em_muon", [&] { launch_muon_pass<Real>(h, m, s); });
+            launch("em_scatter", [&] {
+                launch_em_scatter<Real>(a, h->kvec.as<R4>(), h->scatter_group, h->scatter_depth, h->scatter_blocks, s);
+            });
+            return;
+        }
+        // overlapped: chunk c's scatter on the side stream once chunk c's
+        // muon pass is done, while the muon pass of chunk c+1 runs; each
+        // kernel on a grid of about half the GPU
+        MuonPassArgs<Real> mb = m;
+        if (h->brick) {
+            launch_brick_lambda<Real>(lam, static_cast<uint32_t>(h->V()), h->bdims, h->lam_b.as<Real>(), s);
+            mb.lam = h->lam_b.as<Real>();
+            mb.V = static_cast<uint32_t>(h->vb);
+        }
+        cudaStream_t side = h->fan.side[0];
+        constexpr int C = muto_handle::kOverlapChunks;
+        for (int c = 0; c < C; ++c) {
+            const uint64_t m0 = h->N * c / C, m1 = h->N * (c + 1) / C;
+            MuonPassArgs<Real> mc = mb;
+            mc.off += m0;
+            mc.sd += m0;
+            mc.pr2 += m0;
+            mc.kout += m0;
+            launch_em_muon_warp<Real>(mc, static_cast<uint32_t>(m1 - m0), h->warp_blocks_ov, h->muon_group, s);
+            CK(cudaEventRecord(h->ov_ev[c], s));
+            CK(cudaStreamWaitEvent(side, h->ov_ev[c], 0));
+            FusedArgs<Real> ac = a;
+            ac.off += m0;
+            ac.N = static_cast<uint32_t>(m1 - m0);
+            launch_em_scatter<Real>(ac, h->kvec.as<R4>() + m0, h->scatter_group, h->scatter_depth,
+                                    h->scatter_blocks_ov, side);
+        }
+        CK(cudaEventRecord(h->ov_ev[C], side));
+        CK(cudaStreamWaitEvent(s, h->ov_ev[C], 0));
         return;
     }
     if (h->lists == kListsRecompute) {
@@ -1395,8 +1438,9 @@ void autotune_fused(muto_handle* h) {
         // on their longest path)
         if (fit && v != kFusedStaged) cands.push_back(v);
     }
-    if (!forced)  // the split form: its scatter with g and g/2 lanes per muon, 4 or 8 pairs in flight per lane
-        for (int c = 0; c < 4; ++c) cands.push_back(kFusedVariants + c);
+    if (!forced)  // the split form: its scatter with g and g/2 lanes per muon, 4 or 8 pairs in flight per
+                  // lane; and the 8-deep form overlapped with the muon pass on chunks of the muons
+        for (int c = 0; c < 5; ++c) cands.push_back(kFusedVariants + c);
     auto apply = [&](int v) {
         h->fused_variant = v >= kFusedVariants ? kFusedVariants : v;
         if (v >= kFusedVariants) {  // split: the warp-batched muon pass and the scatter pass
@@ -1408,8 +1452,12 @@ void autotune_fused(muto_handle* h) {
             h->scatter_group = c % 2 == 0 ? g : std::max(8, g / 2);
             h->scatter_depth = c >= 2 ? 8 : 4;
             h->scatter_blocks = em_scatter_blocks<Real>(h->scatter_group, h->scatter_depth) * h->num_sms;
+            h->overlap = c == 4;
+            h->warp_blocks_ov = std::max(1, em_muon_warp_blocks<Real>(g) / 2) * h->num_sms;
+            h->scatter_blocks_ov = std::max(1, em_scatter_blocks<Real>(h->scatter_group, h->scatter_depth) / 2) * h->num_sms;
         } else {
             h->fused_blocks = em_fused_blocks<Real>(v) * h->num_sms;
+            h->overlap = false;
         }
     };
     if (cands.size() == 1) {
@@ -1991,6 +2039,7 @@ int muto_create(const char* method, const char* config_json, muto_handle** out) 
             CK(cudaEventCreateWithFlags(&h->fan.join[k], cudaEventDisableTiming));
             h->fan.n = k + 1;
         }
+        for (cudaEvent_t& e : h->ov_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         alloc_counters(h.get());
         CK(cudaStreamSynchronize(h->stream));
     });
@@ -2049,7 +2098,7 @@ int muto_get_status(const muto_handle* hc, muto_status* out) {
         out->muon_pass = 5;
         out->muon_group = h->scatter_group;
         out->tile_pairs = h->scatter_depth;
-        out->tile_muons = 0;
+        out->tile_muons = h->overlap ? muto_handle::kOverlapChunks : 0;
     } else if (h->method != kPoca && h->lists == kListsMuonMajor) {
         const bool staged = h->fused_variant == kFusedStaged;
         out->muon_pass = staged ? 6 : 3;

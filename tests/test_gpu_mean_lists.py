@@ -61,7 +61,8 @@ def test_mean_update_matches_oracle(gpu, oracle, precision, lists, straight):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("variant", ["4x8", "8x4", "8x8", "8x16", "16x8", "16x16", "staged", "split", "split8"])
+@pytest.mark.parametrize("variant", ["4x8", "8x4", "8x8", "8x16", "16x8", "16x16", "staged", "split", "split8",
+                                     "split8_overlap"])
 @pytest.mark.parametrize("n,n_muons", [(12, 6000), (200, 1500)])
 def test_every_muon_major_variant_matches_oracle(gpu, oracle, precision, variant, n, n_muons):
     # every form of the stored-list pass, forced.  The 200^3 grid gives paths
@@ -79,9 +80,10 @@ def test_every_muon_major_variant_matches_oracle(gpu, oracle, precision, variant
     with M.MutoMLSD(cfg) as rec:
         img = rec.reconstruct(rays)
         st = rec.status()
-    assert st["muon_pass"] == {"staged": 6, "split": 5, "split8": 5}.get(variant, 3)
+    assert st["muon_pass"] == {"staged": 6, "split": 5, "split8": 5, "split8_overlap": 5}.get(variant, 3)
     if variant.startswith("split"):
-        assert st["tile_pairs"] == (8 if variant == "split8" else 4)
+        assert st["tile_pairs"] == (4 if variant == "split" else 8)
+        assert st["tile_muons"] == (4 if variant == "split8_overlap" else 0)
     if n == 200:
         assert st["n_pairs"] / st["n_scat_in_grid"] > (8192 if precision == "mixed" else 4096) / 32
     assert rel_l2(img.reshape(-1, order="F"), ref.image()) < TOL[precision]
