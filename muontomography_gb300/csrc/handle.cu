@@ -1438,9 +1438,12 @@ void autotune_fused(muto_handle* h) {
         // on their longest path)
         if (fit && v != kFusedStaged) cands.push_back(v);
     }
-    if (!forced)  // the split form: its scatter with g and g/2 lanes per muon, 4 or 8 pairs in flight per
-                  // lane; and the 8-deep form overlapped with the muon pass on chunks of the muons
-        for (int c = 0; c < 5; ++c) cands.push_back(kFusedVariants + c);
+    // the split form: its scatter with g and g/2 lanes per muon, 4 or 8 pairs in
+    // flight per lane.  (The overlapped form, kFusedVariants + 4, runs only
+    // when asked for: it measured no faster, the two kernels being bound by
+    // the same memory system.)
+    if (!forced)
+        for (int c = 0; c < 4; ++c) cands.push_back(kFusedVariants + c);
     auto apply = [&](int v) {
         h->fused_variant = v >= kFusedVariants ? kFusedVariants : v;
         if (v >= kFusedVariants) {  // split: the warp-batched muon pass and the scatter pass
