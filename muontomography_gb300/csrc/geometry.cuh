@@ -152,19 +152,20 @@ __device__ __forceinline__ int siddon_walk(const DevGrid& g, const double* p1, c
             t0 = an[0] < an[1] && an[0] < an[2];
             t1 = an[1] < an[2];
         }
-        if (t0) {
-            idx[0] += static_cast<uint32_t>(dir[0]);
-            alpha = an[0];
-            an[0] = dadd(an[0], da[0]);
-        } else if (t1) {
-            idx[1] += static_cast<uint32_t>(dir[1]);
-            alpha = an[1];
-            an[1] = dadd(an[1], da[1]);
-        } else {
-            idx[2] += static_cast<uint32_t>(dir[2]);
-            alpha = an[2];
-            an[2] = dadd(an[2], da[2]);
-        }
+        // the axis stepped, then one FP64 add for it: the lanes of a warp step
+        // along different axes, and a branch per axis would issue the add
+        // once per axis taken in the warp (selects are integer instructions)
+        const int k = t0 ? 0 : (t1 ? 1 : 2);
+        const double ak = k == 0 ? an[0] : (k == 1 ? an[1] : an[2]);
+        const double dk = k == 0 ? da[0] : (k == 1 ? da[1] : da[2]);
+        const double next = dadd(ak, dk);
+        alpha = ak;
+        an[0] = k == 0 ? next : an[0];
+        an[1] = k == 1 ? next : an[1];
+        an[2] = k == 2 ? next : an[2];
+        idx[0] += k == 0 ? static_cast<uint32_t>(dir[0]) : 0u;
+        idx[1] += k == 1 ? static_cast<uint32_t>(dir[1]) : 0u;
+        idx[2] += k == 2 ? static_cast<uint32_t>(dir[2]) : 0u;
         const long long ab = dbits(alpha);
         const double upto = (ab | amax_b) >= 0 ? (amax_b < ab ? amax : alpha) : smin(alpha, amax);
         const double dalpha = dsub(upto, alpha_last);
