@@ -120,11 +120,7 @@ void launch_path_bound(const muto_ray* rays, const uint32_t* kept, const double*
 template <typename Real>
 void launch_path_fill_bounded(const muto_ray* rays, const uint32_t* kept, const double* scat, const uint64_t* boff,
                               uint64_t slot_base, uint64_t n, muto_grid g, int straight, uint32_t* vidx, double* l64,
-                              Real* L, Real* T, uint32_t* counts, Counters* ctr, const uint32_t* order,
-                              cudaStream_t s);
-// order[0..n) = the muons 0..n-1 by decreasing bound boff[i+1] - boff[i] (in
-// buckets of 4 pairs; any order inside a bucket); work: 512 uint32 of scratch
-void launch_length_order(const uint64_t* boff, uint64_t n, uint32_t* order, uint32_t* work, cudaStream_t s);
+                              Real* L, Real* T, uint32_t* counts, Counters* ctr, cudaStream_t s);
 template <typename Real>
 void launch_path_compact(const uint64_t* boff, uint64_t slot_base, const uint64_t* off, uint64_t n,
                          const uint32_t* vidx_b, const Real* L_b, const Real* T_b, uint32_t* vidx, Real* L, Real* T,

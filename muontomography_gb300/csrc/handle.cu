@@ -844,10 +844,6 @@ void fill_lists(muto_handle* h, DevMem& counts, DevMem& scratch, std::vector<uin
     const double avg = N ? static_cast<double>(Pb) / static_cast<double>(N) : 1.0;
     const uint64_t chunk0 = std::max<uint64_t>(P.setup_chunk_pairs > 0 ? 1 : 1024,
                                                static_cast<uint64_t>(static_cast<double>(cap) / (1.25 * avg + 1.0)));
-    // each chunk's muons walked in order of decreasing path bound
-    DevMem order, order_work;
-    order.alloc(std::max<uint64_t>(std::min<uint64_t>(chunk0, N), 1) * sizeof(uint32_t), &h->dev_bytes);
-    order_work.alloc(512 * sizeof(uint32_t), &h->dev_bytes);
     uint64_t base = 0;
     for (size_t k = 0; k < S; ++k) {
         const auto& sc = h->scans[k];
@@ -863,14 +859,11 @@ void fill_lists(muto_handle* h, DevMem& counts, DevMem& scratch, std::vector<uin
                 nc = (nc + 1) / 2;
             }
             if (b[1] - b[0] > cap) throw Error(MUTO_ERR_CAPACITY, "a muon's path bound exceeds the set-up scratch");
-            run(h, "path_order", [&] {
-                launch_length_order(boff.as<uint64_t>() + m, nc, order.as<uint32_t>(), order_work.as<uint32_t>(), s);
-            });
             run(h, "siddon_fill", [&] {
                 launch_path_fill_bounded<Real>(h->scan_rays(k), h->kept.as<uint32_t>() + m, h->scat.as<double>() + 3 * m,
                                                boff.as<uint64_t>() + m, b[0], nc, sc.grid, P.straight_line,
                                                vidx_b.as<uint32_t>(), l64_b.as<double>(), Lb, T_b.as<Real>(),
-                                               counts.as<uint32_t>() + m, h->ctr(), order.as<uint32_t>(), s);
+                                               counts.as<uint32_t>() + m, h->ctr(), s);
             });
             run(h, "scan", [&] {
                 scan_u32_to_u64(counts.as<uint32_t>() + m, h->off.as<uint64_t>() + m, nc, scratch.as<void>(), s);
@@ -891,8 +884,6 @@ void fill_lists(muto_handle* h, DevMem& counts, DevMem& scratch, std::vector<uin
     L_b.release();
     T_b.release();
     boff.release();
-    order.release();
-    order_work.release();
     unsigned long long over_bound = 0;
     CK(cudaMemcpyAsync(&over_bound, &h->ctr()->over_bound, sizeof(over_bound), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));

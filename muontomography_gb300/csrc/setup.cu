@@ -212,80 +212,17 @@ __global__ void k_path_bound(const muto_ray* __restrict__ rays, const uint32_t* 
     }
 }
 
-// The muons of a chunk in order of decreasing path bound (buckets of 4
-// pairs): a warp's lanes then walk paths of about the same length, and the
-// warp does not idle behind its longest walk.  Block-local counts, one
-// global reservation per block and bucket, then each muon's place.
-constexpr int kOrderBuckets = 256;
-__device__ __forceinline__ uint32_t order_bucket(uint64_t len) {
-    const uint64_t b = len >> 2;
-    return kOrderBuckets - 1 - static_cast<uint32_t>(b < kOrderBuckets - 1 ? b : kOrderBuckets - 1);
-}
-constexpr int kOrderPerThread = 4;
-
-__global__ void k_order_hist(const uint64_t* __restrict__ boff, uint64_t n, uint32_t* __restrict__ hist) {
-    __shared__ uint32_t cnt[kOrderBuckets];
-    for (int t = threadIdx.x; t < kOrderBuckets; t += blockDim.x) cnt[t] = 0;
-    __syncthreads();
-    for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
-         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
-        atomicAdd(&cnt[order_bucket(boff[i + 1] - boff[i])], 1u);
-    __syncthreads();
-    for (int t = threadIdx.x; t < kOrderBuckets; t += blockDim.x)
-        if (cnt[t]) atomicAdd(&hist[t], cnt[t]);
-}
-
-// exclusive scan of the bucket counts into the cursors (one block of kOrderBuckets threads)
-__global__ void k_order_starts(const uint32_t* __restrict__ hist, uint32_t* __restrict__ cursor) {
-    __shared__ uint32_t v[kOrderBuckets];
-    const int t = threadIdx.x;
-    v[t] = hist[t];
-    __syncthreads();
-    for (int o = 1; o < kOrderBuckets; o <<= 1) {
-        const uint32_t x = t >= o ? v[t - o] : 0u;
-        __syncthreads();
-        v[t] += x;
-        __syncthreads();
-    }
-    cursor[t] = v[t] - hist[t];
-}
-
-__global__ void k_order_place(const uint64_t* __restrict__ boff, uint64_t n, uint32_t* __restrict__ cursor,
-                              uint32_t* __restrict__ order) {
-    __shared__ uint32_t cnt[kOrderBuckets], base[kOrderBuckets];
-    for (int t = threadIdx.x; t < kOrderBuckets; t += blockDim.x) cnt[t] = 0;
-    __syncthreads();
-    const uint64_t first = static_cast<uint64_t>(blockIdx.x) * blockDim.x * kOrderPerThread;
-    uint32_t bk[kOrderPerThread], rank[kOrderPerThread];
-#pragma unroll
-    for (int e = 0; e < kOrderPerThread; ++e) {
-        const uint64_t i = first + static_cast<uint64_t>(e) * blockDim.x + threadIdx.x;
-        bk[e] = i < n ? order_bucket(boff[i + 1] - boff[i]) : 0u;
-        rank[e] = i < n ? atomicAdd(&cnt[bk[e]], 1u) : 0u;
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < kOrderBuckets; t += blockDim.x) base[t] = cnt[t] ? atomicAdd(&cursor[t], cnt[t]) : 0u;
-    __syncthreads();
-#pragma unroll
-    for (int e = 0; e < kOrderPerThread; ++e) {
-        const uint64_t i = first + static_cast<uint64_t>(e) * blockDim.x + threadIdx.x;
-        if (i < n) order[base[bk[e]] + rank[e]] = static_cast<uint32_t>(i);
-    }
-}
-
 // the fill walk into bounded slots [boff[i], boff[i+1]) - slot_base; counts[i]
-// = the path's length (0 for a walk that hit its step guard, as in the count
-// walk).  Thread t walks muon order[t] (or muon t without an order).
+// = the path's length (0 for a walk that hit its step guard, as in the count walk)
 template <typename Real>
 __global__ void k_path_fill_bounded(const muto_ray* __restrict__ rays, const uint32_t* __restrict__ kept,
                                     const double* __restrict__ scat, const uint64_t* __restrict__ boff, uint64_t n,
                                     DevGrid g, int straight, uint32_t* __restrict__ vidx, double* __restrict__ l64,
                                     Real* __restrict__ L, Real* __restrict__ T, uint32_t* __restrict__ counts,
-                                    Counters* ctr, uint64_t slot_base, const uint32_t* __restrict__ order) {
-    const uint64_t slot = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const unsigned lanes = walk_lanes(slot < n);
-    if (slot >= n) return;
-    const uint64_t i = order ? order[slot] : slot;
+                                    Counters* ctr, uint64_t slot_base) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const unsigned lanes = walk_lanes(i < n);
+    if (i >= n) return;
     const uint64_t b = boff[i] - slot_base, e = boff[i + 1] - slot_base;
     const muto_ray& r = rays[kept[i]];
     const double ps[3] = {scat[3 * i], scat[3 * i + 1], scat[3 * i + 2]};
@@ -591,32 +528,18 @@ void launch_path_bound(const muto_ray* rays, const uint32_t* kept, const double*
 template <typename Real>
 void launch_path_fill_bounded(const muto_ray* rays, const uint32_t* kept, const double* scat, const uint64_t* boff,
                               uint64_t slot_base, uint64_t n, muto_grid g, int straight, uint32_t* vidx, double* l64,
-                              Real* L, Real* T, uint32_t* counts, Counters* ctr, const uint32_t* order,
-                              cudaStream_t s) {
+                              Real* L, Real* T, uint32_t* counts, Counters* ctr, cudaStream_t s) {
     if (n == 0) return;
     k_path_fill_bounded<Real><<<blocks_for(n, 128), 128, 0, s>>>(rays, kept, scat, boff, n, make_dev_grid(g), straight,
-                                                                  vidx, l64, L, T, counts, ctr, slot_base, order);
+                                                                  vidx, l64, L, T, counts, ctr, slot_base);
     count_launches(1);
-}
-
-void launch_length_order(const uint64_t* boff, uint64_t n, uint32_t* order, uint32_t* work, cudaStream_t s) {
-    if (n == 0) return;
-    uint32_t* hist = work;
-    uint32_t* cursor = work + kOrderBuckets;
-    (void)cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(uint32_t), s);  // an error surfaces at the caller's check
-    const uint64_t hb = (n + 255) / 256;
-    k_order_hist<<<static_cast<unsigned>(hb < 1024 ? hb : 1024), 256, 0, s>>>(boff, n, hist);
-    k_order_starts<<<1, kOrderBuckets, 0, s>>>(hist, cursor);
-    k_order_place<<<static_cast<unsigned>((n + 256 * kOrderPerThread - 1) / (256 * kOrderPerThread)), 256, 0, s>>>(
-        boff, n, cursor, order);
-    count_launches(3);
 }
 template void launch_path_fill_bounded<float>(const muto_ray*, const uint32_t*, const double*, const uint64_t*,
                                               uint64_t, uint64_t, muto_grid, int, uint32_t*, double*, float*, float*,
-                                              uint32_t*, Counters*, const uint32_t*, cudaStream_t);
+                                              uint32_t*, Counters*, cudaStream_t);
 template void launch_path_fill_bounded<double>(const muto_ray*, const uint32_t*, const double*, const uint64_t*,
                                                uint64_t, uint64_t, muto_grid, int, uint32_t*, double*, double*,
-                                               double*, uint32_t*, Counters*, const uint32_t*, cudaStream_t);
+                                               double*, uint32_t*, Counters*, cudaStream_t);
 
 template <typename Real>
 void launch_path_compact(const uint64_t* boff, uint64_t slot_base, const uint64_t* off, uint64_t n,
