@@ -241,6 +241,82 @@ def map_conditioning(wl, args, d_rays, n: int, img64: np.ndarray, img32: np.ndar
     return out
 
 
+def run_next_rows(wl, rays: np.ndarray) -> dict:
+    """PoCut (src/MutoPoCut.cpp:19-121), SLR (src/MutoSLR.cpp:47-103), SLRIter
+    (src/MutoSLRIter.cpp:15-83) and the reader's line fit
+    (src/MutoFile.cpp:248-304) on the same tracks: GPU time per call
+    (`reconstruct` from host tracks, copies included; the library's profiler
+    for the kernels), and the oracle on the host cores for the same call."""
+    import muontomography_gb300 as M
+    from oracle import oracle as O
+
+    n = rays.shape[0]
+    out = {"tracks": n, "what": "wall clock of one reconstruct call from host tracks (copies and set-up included), "
+                                "the best of three; the oracle on the same tracks, one call"}
+
+    def gpu_call(make):
+        best = None
+        for _ in range(3):
+            with make() as r:
+                t0 = time.perf_counter()
+                img = r.reconstruct(rays)
+                dt = time.perf_counter() - t0
+                st = r.status()
+            best = dt if best is None or dt < best else best
+        return best, img, st
+
+    def cpu_call(f):
+        t0 = time.perf_counter()
+        v = f()
+        return time.perf_counter() - t0, v
+
+    cfg = wl.poca_config(cut_percentile=0.5)
+    g_s, img, _ = gpu_call(lambda: M.MutoPoCut(cfg))
+    c_s, (ref, _, _) = cpu_call(lambda: O.pocut(wl.grid, cfg, rays))
+    out["pocut_cut_0.5"] = {"gpu_s": g_s, "cpu_s": c_s, "tracks_per_s": n / g_s,
+                            "rel_l2_vs_oracle": rel_l2(img.reshape(-1, order="F"), ref)}
+    cfg = wl.poca_config(length_weighted=True)
+    g_s, img, _ = gpu_call(lambda: M.MutoSLR(cfg))
+    c_s, ref = cpu_call(lambda: O.slr(wl.grid, cfg, rays))
+    out["slr"] = {"gpu_s": g_s, "cpu_s": c_s, "tracks_per_s": n / g_s,
+                  "rel_l2_vs_oracle": rel_l2(img.reshape(-1, order="F"), ref)}
+    for sch in ("levels", "sequential"):
+        cfg = dict(wl.poca_config(length_weighted=True), num_iteration=4, slr_iter_schedule=sch)
+        g_s, img, st = gpu_call(lambda: M.MutoSLRIter(cfg))
+        row = {"gpu_s": g_s, "levels": st["slr_levels"]}
+        if sch == "levels":
+            c_s, ref = cpu_call(lambda: O.slr(wl.grid, cfg, rays, iterative=True))
+            row.update(cpu_s=c_s, rel_l2_vs_oracle=rel_l2(img.reshape(-1, order="F"), ref))
+        out[f"slr_iter_4_passes_{sch}"] = row
+    # detector records of the same tracks: 3 + 3 planes 500 mm apart around the
+    # grid, hits on the fitted lines (input/example_mlsd.json:3-4 spacing)
+    zt, zb = wl.grid.z_min + wl.grid.nz * wl.grid.dz, wl.grid.z_min
+    z = np.array([zt + 1000.0, zt + 500.0, zt, zb, zb - 500.0, zb - 1000.0])
+    rec = np.empty((n, 14))
+    rec[:, 0], rec[:, -1] = rays[:, 0], rays[:, 1]
+    for k, zk in enumerate(z):
+        p, d = (rays[:, 2:5], rays[:, 8:11]) if k < 3 else (rays[:, 5:8], rays[:, 11:14])
+        t = (zk - p[:, 2]) / d[:, 2]
+        rec[:, 1 + 2 * k] = p[:, 0] + t * d[:, 0]
+        rec[:, 2 + 2 * k] = p[:, 1] + t * d[:, 1]
+    best = None
+    for _ in range(3):
+        t0 = time.perf_counter()
+        fit = M.fit_tracks(rec, z, 3)
+        dt = time.perf_counter() - t0
+        best = dt if best is None or dt < best else best
+    c_s, ref = cpu_call(lambda: O.fit_records(rec, z, 3))
+    out["line_fit"] = {"gpu_s": best, "cpu_s": c_s, "records_per_s": n / best,
+                       "max_abs_diff_vs_oracle": float(np.nanmax(np.abs(fit - ref))) if len(fit) == len(ref) else None}
+    return out
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
 def cpu_port(wl, args, rays: np.ndarray, n_iter: int, threads: int) -> dict:
     """Time the CPU restatement of the reference path on a sample of the workload's tracks."""
     os.environ["OMP_NUM_THREADS"] = str(threads)
@@ -524,6 +600,11 @@ def run_ours(args) -> int:
                 "what": "k_poca: FP64 closest approach, binning and the length-weighted Siddon weights of every "
                         "track (FP64 atomics, a thread per kept track), then the normalisation"}
 
+    # ---- the rows either side of the path: PoCut, SLR, SLRIter, the line fit ----
+    next_rows = None
+    if args.next_rows > 0 and rank == 0:
+        next_rows = run_next_rows(wl, d_rays[:min(args.next_rows, n)].cpu().numpy())
+
     # ---- time to lambda: mixed vs the plain FP64 form, same iteration count ---
     ttl = None
     if args.ttl_iters > 0 and rank == 0:
@@ -625,6 +706,7 @@ def run_ours(args) -> int:
             "time_to_lambda": ttl,
             "recompute": recompute,
             "poca": poca,
+            "next_rows": next_rows,
         }
         if grad_vs_em is not None:
             line["gradient_vs_em"] = {"runs": grad_vs_em, "what": (
@@ -842,6 +924,8 @@ def main() -> int:
                     help="iterations of the time-to-lambda runs (-1: the workload's)")
     ap.add_argument("--recompute-iters", type=int, default=2)
     ap.add_argument("--poca", type=int, default=1)
+    ap.add_argument("--next-rows", type=int, default=0,
+                    help="time PoCut, SLR, SLRIter and the line fit on the first N tracks (0: off)")
     ap.add_argument("--cpu-sample", type=int, default=1_000_000)
     ap.add_argument("--batch-scale", type=float, default=1.0, help="batch64: muons per scan times this")
     ap.add_argument("--grad-vs-em", type=int, default=20,
