@@ -198,9 +198,10 @@ void launch_slr_pair_terms(const SlrArgs& a, const SlrPass& p, cudaStream_t s);
 // one later pass, muon after muon
 void launch_slr_iter_pass(const SlrArgs& a, const SlrPass& p, cudaStream_t s);
 // the same pass level by level: order[] lists the muons by level, level l's
-// muons at order[lstart[l] .. lstart[l+1])
+// muons at order[lstart[l] .. lstart[l+1]); the image and weight sums are
+// kept in shared memory when 2 V doubles fit in smem_optin bytes
 void launch_slr_iter_levels(const SlrArgs& a, const SlrPass& p, const uint32_t* order, const uint32_t* lstart,
-                            uint32_t levels, cudaStream_t s);
+                            uint32_t levels, size_t smem_optin, cudaStream_t s);
 
 // PoCut's per-voxel step (src/MutoPoCut.cpp:113-118), after launch_poca:
 // the kept values grouped by voxel (counts, then offsets, then a scatter of

@@ -682,7 +682,8 @@ void prepare_slr(muto_handle* h, uint64_t nt) {
                 if (h->P.slr_sequential)
                     launch_slr_iter_pass(a, sp, s);
                 else
-                    launch_slr_iter_levels(a, sp, order.as<uint32_t>(), lstart.as<uint32_t>(), h->slr_levels, s);
+                    launch_slr_iter_levels(a, sp, order.as<uint32_t>(), lstart.as<uint32_t>(), h->slr_levels,
+                                           h->smem_optin, s);
             });
         CK(cudaStreamSynchronize(s));  // the path arrays go out of scope
     }

@@ -151,19 +151,22 @@ __global__ void k_slr_pair_terms(SlrArgs a, SlrPass p) {
 // with iter != 0), on one warp: the warp reads the image on the muon's path,
 // sums it (lane partials, then the warp's sum), and adds to each voxel its
 // increment times the voxel's part of that sum (:64-66).
-__device__ __forceinline__ void slr_iter_muon(const SlrArgs& a, const SlrPass& p, uint64_t i, int lane) {
+// img / weight: the image and weight sums (global memory, or a copy in
+// shared memory).
+__device__ __forceinline__ void slr_iter_muon(const SlrArgs& a, const SlrPass& p, uint64_t i, int lane, double* img,
+                                              double* weight) {
     const uint64_t p0 = p.off[i];
     const uint32_t n = static_cast<uint32_t>(p.off[i + 1] - p0);
     double part = 0.0;  // :49-52
-    for (uint32_t k = lane; k < n; k += 32) part = dadd(part, a.img[p.vox[p0 + k]]);
+    for (uint32_t k = lane; k < n; k += 32) part = dadd(part, img[p.vox[p0 + k]]);
     const double total = warp_sum(part);
     const double e2 = a.has_energy ? p.e2[i] : 0.0;
     for (uint32_t k = lane; k < n; k += 32) {
         const uint32_t j = p.vox[p0 + k];
-        a.weight[j] = dadd(a.weight[j], p.winc[p0 + k]);
-        double iv = dmul(p.iv0[p0 + k], ddiv(a.img[j], total));
+        weight[j] = dadd(weight[j], p.winc[p0 + k]);
+        double iv = dmul(p.iv0[p0 + k], ddiv(img[j], total));
         if (a.has_energy) iv = dmul(iv, e2);  // :87-89
-        a.img[j] = dadd(a.img[j], iv);
+        img[j] = dadd(img[j], iv);
     }
 }
 
@@ -173,7 +176,7 @@ __global__ void k_slr_iter_pass(SlrArgs a, SlrPass p) {
     const int lane = threadIdx.x & 31;
     if (threadIdx.x >= 32) return;
     for (uint64_t i = 0; i < a.n; ++i) {
-        slr_iter_muon(a, p, i, lane);
+        slr_iter_muon(a, p, i, lane, a.img, a.weight);
         __syncwarp();
     }
 }
@@ -184,15 +187,37 @@ __global__ void k_slr_iter_pass(SlrArgs a, SlrPass p) {
 // each muon reads and writes the image state it would see in the sequential
 // loop, whatever the order inside a level.  One block: its warps take the
 // muons of a level, and the block barrier orders the levels (global stores
-// before it are visible to the whole block after it).
+// before it are visible to the whole block after it).  With SMEM the image
+// and weight sums (2 V doubles) are copied into shared memory for the pass
+// and back after it: every level then reads and writes them there.
+template <bool SMEM>
 __global__ void __launch_bounds__(1024) k_slr_iter_levels(SlrArgs a, SlrPass p, const uint32_t* __restrict__ order,
                                                           const uint32_t* __restrict__ lstart, uint32_t levels) {
+    extern __shared__ double slr_smem[];
     const int lane = threadIdx.x & 31;
     const uint32_t warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t V = a.g.nx * a.g.ny * a.g.nz;
+    double* img = a.img;
+    double* weight = a.weight;
+    if (SMEM) {
+        img = slr_smem;
+        weight = slr_smem + V;
+        for (uint32_t j = threadIdx.x; j < V; j += blockDim.x) {
+            img[j] = a.img[j];
+            weight[j] = a.weight[j];
+        }
+        __syncthreads();
+    }
     for (uint32_t l = 0; l < levels; ++l) {
         const uint32_t e = lstart[l + 1];
-        for (uint32_t q = lstart[l] + warp; q < e; q += nw) slr_iter_muon(a, p, order[q], lane);
+        for (uint32_t q = lstart[l] + warp; q < e; q += nw) slr_iter_muon(a, p, order[q], lane, img, weight);
         __syncthreads();
+    }
+    if (SMEM) {
+        for (uint32_t j = threadIdx.x; j < V; j += blockDim.x) {
+            a.img[j] = img[j];
+            a.weight[j] = weight[j];
+        }
     }
 }
 
@@ -224,9 +249,17 @@ void launch_slr_iter_pass(const SlrArgs& a, const SlrPass& p, cudaStream_t s) {
 }
 
 void launch_slr_iter_levels(const SlrArgs& a, const SlrPass& p, const uint32_t* order, const uint32_t* lstart,
-                            uint32_t levels, cudaStream_t s) {
+                            uint32_t levels, size_t smem_optin, cudaStream_t s) {
     if (a.n == 0 || levels == 0) return;
-    k_slr_iter_levels<<<1, 1024, 0, s>>>(a, p, order, lstart, levels);
+    const size_t bytes = 2 * sizeof(double) * static_cast<size_t>(a.g.nx) * a.g.ny * a.g.nz;
+    if (bytes <= smem_optin &&
+        cudaFuncSetAttribute(k_slr_iter_levels<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(bytes)) == cudaSuccess) {
+        k_slr_iter_levels<true><<<1, 1024, bytes, s>>>(a, p, order, lstart, levels);
+    } else {
+        (void)cudaGetLastError();  // a refused attribute: the pass stays in global memory
+        k_slr_iter_levels<false><<<1, 1024, 0, s>>>(a, p, order, lstart, levels);
+    }
     count_launches(1);
 }
 
