@@ -356,8 +356,6 @@ __host__ __device__ inline uint32_t unbrick(uint32_t jb, const BrickDims& b) {
     const uint32_t z = bz * 4 + (((in >> 5) & 1u) << 1) + ((in >> 2) & 1u);
     return x + b.nx * (y + b.ny * z);
 }
-// drops the L2 lines of [p, p + bytes) without writing them back (a buffer about to be freed)
-void launch_l2_discard(void* p, uint64_t bytes, cudaStream_t s);
 // voxel indices to bricked ones in place (indices >= V are left alone)
 void launch_brick_indices(uint32_t* vidx, uint64_t n, BrickDims b, uint32_t V, cudaStream_t s);
 // bricked indices back to voxel indices

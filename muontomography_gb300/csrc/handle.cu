@@ -457,12 +457,6 @@ struct muto_handle {
     }
     ~muto_handle() {
         drop_graph();
-        // the arrays gathered and reduced with the L2 evict_last policy: their
-        // lines leave L2 with the handle
-        if (stream) {
-            for (DevMem* m : {&gsum, &lam_b, &lam}) launch_l2_discard(m->as<void>(), m->bytes(), stream);
-            cudaStreamSynchronize(stream);
-        }
         for (int k = 0; k < fan.n; ++k) {
             cudaStreamDestroy(fan.side[k]);
             cudaEventDestroy(fan.join[k]);

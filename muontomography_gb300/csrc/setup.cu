@@ -688,27 +688,6 @@ void launch_unbrick_indices(const uint32_t* in, uint32_t* out, uint64_t n, Brick
     count_launches(1);
 }
 
-// Drops the L2 lines of a buffer that is about to be freed, without writing
-// them back: the per-voxel arrays that the EM passes read and reduce with an
-// L2 evict_last policy would otherwise stay in L2 after their handle is gone.
-__global__ void k_l2_discard(char* base, uint64_t lines) {
-    for (uint64_t l = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; l < lines;
-         l += static_cast<uint64_t>(gridDim.x) * blockDim.x)
-        asm volatile("discard.global.L2 [%0], 128;" ::"l"(base + l * 128) : "memory");
-}
-
-void launch_l2_discard(void* p, uint64_t bytes, cudaStream_t s) {
-    // whole 128-byte lines inside [p, p + bytes) only
-    char* const b = static_cast<char*>(p);
-    const uint64_t first = (reinterpret_cast<uintptr_t>(b) + 127) / 128 * 128 - reinterpret_cast<uintptr_t>(b);
-    if (!p || bytes <= first) return;
-    const uint64_t lines = (bytes - first) / 128;
-    if (lines == 0) return;
-    k_l2_discard<<<static_cast<unsigned>(lines < 152 * 8 * 256 ? (lines + 255) / 256 : 152 * 8), 256, 0, s>>>(
-        b + first, lines);
-    count_launches(1);
-}
-
 template <typename Real>
 void launch_brick_lambda(const Real* lam, uint32_t V, BrickDims b, Real* lam_b, cudaStream_t s) {
     if (V == 0) return;
