@@ -144,7 +144,11 @@ typedef struct muto_handle muto_handle;
  * prefetches every CTA's next batch of pairs into L2),
  * "setup_chunk_pairs" (0: the set-up walks the paths in chunks of muons
  * whose bounded slots take at most a quarter of the free device memory,
- * 12 GiB at most; n > 0: chunks of at most n bounded pairs). */
+ * 12 GiB at most; n > 0: chunks of at most n bounded pairs),
+ * "slr_iter_schedule" (slr_iter only: "levels", the default, runs the later
+ * passes level by level, muons that share no voxel at once, each voxel
+ * meeting its muons in index order; "sequential" runs them muon after
+ * muon). */
 int muto_create(const char* method, const char* config_json, muto_handle** out);
 int muto_destroy(muto_handle* h);
 
