@@ -43,6 +43,8 @@ def test_python_bindings_cover_the_header():
     ("slr_v2", "{}", 1),
     ("slr_iter", '{"num_iteration": -1}', 2),
     ("slr_iter", '{"slr_iter_schedule": "shuffled"}', 2),
+    ("mlsd", '{"update_with_mean": true, "fused_variant": "split9"}', 2),
+    ("mlsd", '{"path_lists": "sideways"}', 2),
     ("pocut", '{"cut_percentile": "most"}', 2),
     ("mlsd", '{"muon_layout": "spiral"}', 2),
     ("mlsd", '{"muon_pass": "fast"}', 2),
