@@ -197,11 +197,21 @@ struct SlrPass {
 void launch_slr_pair_terms(const SlrArgs& a, const SlrPass& p, cudaStream_t s);
 // one later pass, muon after muon
 void launch_slr_iter_pass(const SlrArgs& a, const SlrPass& p, cudaStream_t s);
-// the same pass level by level: order[] lists the muons by level, level l's
-// muons at order[lstart[l] .. lstart[l+1]); the image and weight sums are
-// kept in shared memory when 2 V doubles fit in smem_optin bytes
-void launch_slr_iter_levels(const SlrArgs& a, const SlrPass& p, const uint32_t* order, const uint32_t* lstart,
-                            uint32_t levels, size_t smem_optin, cudaStream_t s);
+// the same pairs in level order: muon q of the level order (order[q]) has
+// its pairs at fo[q] .. fo[q+1]
+struct SlrFlat {
+    const uint64_t* fo;
+    uint32_t* vox;
+    double* iv0;
+    double* winc;
+    double* e2;
+};
+void launch_slr_flatten(const SlrPass& p, const uint32_t* order, uint64_t nt, const SlrFlat& f, cudaStream_t s);
+// the same pass level by level: level l's muons are q = lstart[l] ..
+// lstart[l+1] of the level order; the image and weight sums are kept in
+// shared memory when 2 V doubles fit in smem_optin bytes
+void launch_slr_iter_levels(const SlrArgs& a, const SlrFlat& f, const uint32_t* lstart, uint32_t levels,
+                            size_t smem_optin, cudaStream_t s);
 
 // PoCut's per-voxel step (src/MutoPoCut.cpp:113-118), after launch_poca:
 // the kept values grouped by voxel (counts, then offsets, then a scatter of

@@ -590,7 +590,7 @@ void alloc_counters(muto_handle* h) {
 // muons are then grouped by level (index order inside a level) for the
 // device.
 void slr_level_schedule(muto_handle* h, const DevMem& off, const DevMem& vox, uint64_t nt, uint64_t np, DevMem& order,
-                        DevMem& lstart) {
+                        DevMem& lstart, DevMem& fo) {
     const uint64_t V = h->V();
     cudaStream_t s = h->stream;
     if (nt >= 0xffffffffull) throw Error(MUTO_ERR_CAPACITY, "slr_iter: more than 2^32-1 rays");
@@ -624,11 +624,16 @@ void slr_level_schedule(muto_handle* h, const DevMem& off, const DevMem& vox, ui
     std::vector<uint32_t> cur(start.begin(), start.end());
     for (uint64_t i = 0; i < nt; ++i) order_h[cur[level[i]]++] = static_cast<uint32_t>(i);
     start.push_back(static_cast<uint32_t>(nt));
+    // where each muon's pairs go in level order
+    std::vector<uint64_t> fo_h(nt + 1, 0);
+    for (uint64_t q = 0; q < nt; ++q) fo_h[q + 1] = fo_h[q] + (off_h[order_h[q] + 1] - off_h[order_h[q]]);
     order.alloc(std::max<uint64_t>(nt, 1) * sizeof(uint32_t), &h->dev_bytes);
     lstart.alloc(start.size() * sizeof(uint32_t), &h->dev_bytes);
+    fo.alloc((nt + 1) * sizeof(uint64_t), &h->dev_bytes);
     CK(cudaMemcpyAsync(order.as<uint32_t>(), order_h.data(), nt * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(lstart.as<uint32_t>(), start.data() + 1, (start.size() - 1) * sizeof(uint32_t),
                        cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(fo.as<uint64_t>(), fo_h.data(), (nt + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));  // the host vectors go out of scope
     h->slr_levels = levels;
 }
@@ -672,18 +677,27 @@ void prepare_slr(muto_handle* h, uint64_t nt) {
         const SlrPass sp{off.as<uint64_t>(), vox.as<uint32_t>(), len.as<double>(), iv0.as<double>(), winc.as<double>(),
                          e2.as<double>()};
         run(h, "slr_paths", [&] { launch_slr_pair_terms(a, sp, s); });
-        DevMem order, lstart;
+        DevMem order, lstart, fo, fvox, fiv0, fwinc, fe2;
+        SlrFlat fl{};
         if (!h->P.slr_sequential) {
-            HostPhase ph(h, "slr_levels");
-            slr_level_schedule(h, off, vox, nt, np, order, lstart);
+            {
+                HostPhase ph(h, "slr_levels");
+                slr_level_schedule(h, off, vox, nt, np, order, lstart, fo);
+            }
+            // the pairs copied into level order
+            fvox.alloc(std::max<uint64_t>(np, 1) * sizeof(uint32_t), &h->dev_bytes);
+            fiv0.alloc(std::max<uint64_t>(np, 1) * sizeof(double), &h->dev_bytes);
+            fwinc.alloc(std::max<uint64_t>(np, 1) * sizeof(double), &h->dev_bytes);
+            fe2.alloc(nt * sizeof(double), &h->dev_bytes);
+            fl = SlrFlat{fo.as<uint64_t>(), fvox.as<uint32_t>(), fiv0.as<double>(), fwinc.as<double>(), fe2.as<double>()};
+            run(h, "slr_paths", [&] { launch_slr_flatten(sp, order.as<uint32_t>(), nt, fl, s); });
         }
         for (int p = 1; p < passes; ++p)
             run(h, "slr_iter_pass", [&] {
                 if (h->P.slr_sequential)
                     launch_slr_iter_pass(a, sp, s);
                 else
-                    launch_slr_iter_levels(a, sp, order.as<uint32_t>(), lstart.as<uint32_t>(), h->slr_levels,
-                                           h->smem_optin, s);
+                    launch_slr_iter_levels(a, fl, lstart.as<uint32_t>(), h->slr_levels, h->smem_optin, s);
             });
         CK(cudaStreamSynchronize(s));  // the path arrays go out of scope
     }

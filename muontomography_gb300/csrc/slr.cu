@@ -181,6 +181,48 @@ __global__ void k_slr_iter_pass(SlrArgs a, SlrPass p) {
     }
 }
 
+// The pairs of every muon copied into level order: muon q of the level
+// order (order[q]) gets its pairs at fo[q] .. fo[q+1], so a level's data is
+// contiguous and found from the level's start alone.  A warp per muon.
+__global__ void k_slr_flatten(SlrPass p, const uint32_t* __restrict__ order, uint64_t nt, SlrFlat f) {
+    const uint64_t q = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (q >= nt) return;
+    const uint32_t i = order[q];
+    const uint64_t s0 = p.off[i], n = p.off[i + 1] - s0, d0 = f.fo[q];
+    for (uint64_t k = lane; k < n; k += 32) {
+        f.vox[d0 + k] = p.vox[s0 + k];
+        f.iv0[d0 + k] = p.iv0[s0 + k];
+        f.winc[d0 + k] = p.winc[s0 + k];
+    }
+    if (lane == 0) f.e2[q] = p.e2[i];
+}
+
+// One muon of the level order on one warp, the arithmetic of slr_iter_muon;
+// the first pair of each lane (k = lane) comes in already loaded (v0, i0,
+// w0; valid when lane < n), the rest is loaded here.
+__device__ __forceinline__ void slr_flat_muon(const SlrArgs& a, const SlrFlat& f, uint64_t p0, uint32_t n, double e2,
+                                              uint32_t v0, double i0, double w0, int lane, double* img,
+                                              double* weight) {
+    double part = 0.0;  // :49-52, the same order of additions as slr_iter_muon
+    if (static_cast<uint32_t>(lane) < n) part = dadd(part, img[v0]);
+    for (uint32_t k = lane + 32; k < n; k += 32) part = dadd(part, img[f.vox[p0 + k]]);
+    const double total = warp_sum(part);
+    if (static_cast<uint32_t>(lane) < n) {
+        weight[v0] = dadd(weight[v0], w0);
+        double iv = dmul(i0, ddiv(img[v0], total));
+        if (a.has_energy) iv = dmul(iv, e2);  // :87-89
+        img[v0] = dadd(img[v0], iv);
+    }
+    for (uint32_t k = lane + 32; k < n; k += 32) {
+        const uint32_t j = f.vox[p0 + k];
+        weight[j] = dadd(weight[j], f.winc[p0 + k]);
+        double iv = dmul(f.iv0[p0 + k], ddiv(img[j], total));
+        if (a.has_energy) iv = dmul(iv, e2);
+        img[j] = dadd(img[j], iv);
+    }
+}
+
 // A later pass level by level.  A muon's level is one more than the highest
 // level among the earlier muons that share a voxel with it, so two muons of
 // one level share no voxel, and every voxel meets its muons in index order:
@@ -189,10 +231,12 @@ __global__ void k_slr_iter_pass(SlrArgs a, SlrPass p) {
 // muons of a level, and the block barrier orders the levels (global stores
 // before it are visible to the whole block after it).  With SMEM the image
 // and weight sums (2 V doubles) are copied into shared memory for the pass
-// and back after it: every level then reads and writes them there.
+// and back after it.  The next level's muon offsets are loaded while the
+// current level runs, and its first pair per lane just before the barrier
+// (neither depends on the image).
 template <bool SMEM>
-__global__ void __launch_bounds__(1024) k_slr_iter_levels(SlrArgs a, SlrPass p, const uint32_t* __restrict__ order,
-                                                          const uint32_t* __restrict__ lstart, uint32_t levels) {
+__global__ void __launch_bounds__(1024) k_slr_iter_levels(SlrArgs a, SlrFlat f, const uint32_t* __restrict__ lstart,
+                                                          uint32_t levels) {
     extern __shared__ double slr_smem[];
     const int lane = threadIdx.x & 31;
     const uint32_t warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -208,11 +252,58 @@ __global__ void __launch_bounds__(1024) k_slr_iter_levels(SlrArgs a, SlrPass p, 
         }
         __syncthreads();
     }
+    // this warp's first muon of level 0 and its first pair per lane
+    uint32_t b = lstart[0], e = lstart[1];
+    uint32_t q = b + warp;
+    uint64_t p0 = 0;
+    uint32_t n = 0, v0 = 0;
+    double i0 = 0.0, w0 = 0.0, e2 = 0.0;
+    if (q < e) {
+        p0 = f.fo[q];
+        n = static_cast<uint32_t>(f.fo[q + 1] - p0);
+        e2 = f.e2[q];
+        if (static_cast<uint32_t>(lane) < n) {
+            v0 = f.vox[p0 + lane];
+            i0 = f.iv0[p0 + lane];
+            w0 = f.winc[p0 + lane];
+        }
+    }
     for (uint32_t l = 0; l < levels; ++l) {
-        const uint32_t e = lstart[l + 1];
-        for (uint32_t q = lstart[l] + warp; q < e; q += nw) slr_iter_muon(a, p, order[q], lane, img, weight);
+        // the next level's first muon for this warp: its offsets now
+        const uint32_t en = l + 1 < levels ? lstart[l + 2] : e;
+        const uint32_t qn = e + warp;
+        const bool has_next = l + 1 < levels && qn < en;
+        uint64_t p0n = 0, p1n = 0;
+        if (has_next) {
+            p0n = f.fo[qn];
+            p1n = f.fo[qn + 1];
+        }
+        if (q < e) slr_flat_muon(a, f, p0, n, e2, v0, i0, w0, lane, img, weight);
+        for (uint32_t q2 = q + nw; q2 < e; q2 += nw) {  // more muons than warps in this level
+            const uint64_t s0 = f.fo[q2];
+            const uint32_t m = static_cast<uint32_t>(f.fo[q2 + 1] - s0);
+            const bool in = static_cast<uint32_t>(lane) < m;
+            slr_flat_muon(a, f, s0, m, f.e2[q2], in ? f.vox[s0 + lane] : 0u, in ? f.iv0[s0 + lane] : 0.0,
+                          in ? f.winc[s0 + lane] : 0.0, lane, img, weight);
+        }
+        // the next level's first pair per lane, before the barrier
+        q = qn;
+        b = e;
+        e = en;
+        n = 0;
+        if (has_next) {
+            p0 = p0n;
+            n = static_cast<uint32_t>(p1n - p0n);
+            e2 = f.e2[qn];
+            if (static_cast<uint32_t>(lane) < n) {
+                v0 = f.vox[p0 + lane];
+                i0 = f.iv0[p0 + lane];
+                w0 = f.winc[p0 + lane];
+            }
+        }
         __syncthreads();
     }
+    (void)b;
     if (SMEM) {
         for (uint32_t j = threadIdx.x; j < V; j += blockDim.x) {
             a.img[j] = img[j];
@@ -248,17 +339,23 @@ void launch_slr_iter_pass(const SlrArgs& a, const SlrPass& p, cudaStream_t s) {
     count_launches(1);
 }
 
-void launch_slr_iter_levels(const SlrArgs& a, const SlrPass& p, const uint32_t* order, const uint32_t* lstart,
-                            uint32_t levels, size_t smem_optin, cudaStream_t s) {
+void launch_slr_flatten(const SlrPass& p, const uint32_t* order, uint64_t nt, const SlrFlat& f, cudaStream_t s) {
+    if (nt == 0) return;
+    k_slr_flatten<<<static_cast<unsigned>((nt * 32 + 255) / 256), 256, 0, s>>>(p, order, nt, f);
+    count_launches(1);
+}
+
+void launch_slr_iter_levels(const SlrArgs& a, const SlrFlat& f, const uint32_t* lstart, uint32_t levels,
+                            size_t smem_optin, cudaStream_t s) {
     if (a.n == 0 || levels == 0) return;
     const size_t bytes = 2 * sizeof(double) * static_cast<size_t>(a.g.nx) * a.g.ny * a.g.nz;
     if (bytes <= smem_optin &&
         cudaFuncSetAttribute(k_slr_iter_levels<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(bytes)) == cudaSuccess) {
-        k_slr_iter_levels<true><<<1, 1024, bytes, s>>>(a, p, order, lstart, levels);
+        k_slr_iter_levels<true><<<1, 1024, bytes, s>>>(a, f, lstart, levels);
     } else {
         (void)cudaGetLastError();  // a refused attribute: the pass stays in global memory
-        k_slr_iter_levels<false><<<1, 1024, 0, s>>>(a, p, order, lstart, levels);
+        k_slr_iter_levels<false><<<1, 1024, 0, s>>>(a, f, lstart, levels);
     }
     count_launches(1);
 }
