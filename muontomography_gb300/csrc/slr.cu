@@ -253,8 +253,8 @@ __global__ void __launch_bounds__(1024) k_slr_iter_levels(SlrArgs a, SlrFlat f, 
         __syncthreads();
     }
     // this warp's first muon of level 0 and its first pair per lane
-    uint32_t b = lstart[0], e = lstart[1];
-    uint32_t q = b + warp;
+    uint32_t e = lstart[1];
+    uint32_t q = lstart[0] + warp;
     uint64_t p0 = 0;
     uint32_t n = 0, v0 = 0;
     double i0 = 0.0, w0 = 0.0, e2 = 0.0;
@@ -288,7 +288,6 @@ __global__ void __launch_bounds__(1024) k_slr_iter_levels(SlrArgs a, SlrFlat f, 
         }
         // the next level's first pair per lane, before the barrier
         q = qn;
-        b = e;
         e = en;
         n = 0;
         if (has_next) {
@@ -303,7 +302,6 @@ __global__ void __launch_bounds__(1024) k_slr_iter_levels(SlrArgs a, SlrFlat f, 
         }
         __syncthreads();
     }
-    (void)b;
     if (SMEM) {
         for (uint32_t j = threadIdx.x; j < V; j += blockDim.x) {
             a.img[j] = img[j];
