@@ -159,6 +159,9 @@ struct PocaArgs {
     double* weight;
     uint32_t* walk;                  // n slots: the kept rays, listed by the first kernel for the walks
     unsigned long long* walk_count;  // their number (device)
+    uint32_t* walk_len;              // n slots (or null): a bound on each listed ray's walk
+    uint32_t* walk_order;            // n slots (or null): the list by decreasing bound, walked in that order
+    uint32_t* order_work;            // 512 words of scratch for the ordering
     long long* assign;  // 3 per ray, optional
     Counters* ctr;
     uint32_t* vox;      // PoCut: per ray its voxel, 0xffffffff when rejected (null for PoCA)

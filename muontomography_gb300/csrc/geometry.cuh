@@ -72,6 +72,22 @@ __device__ __forceinline__ unsigned walk_lanes(bool walks) { return __ballot_syn
 // voxel with a recorded length the sink is called as sink(ix, iy, iz, len).
 // Returns the number of voxels, or -1 if the step bound was hit (never for a
 // walk that ends, kept as a guard against a non-terminating loop).
+// voxels a walk of a -> b can record: 1 + the index span on each axis of
+// the endpoints clamped to the grid (the pieces on the grid lie between
+// them), +2 per axis for rounding at either end
+__device__ __forceinline__ uint32_t walk_bound(const DevGrid& g, const double* a, const double* b) {
+    uint32_t n = 1;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float lo = static_cast<float>(g.lo[k]), w = static_cast<float>(g.w[k]);
+        const float top = static_cast<float>(g.n[k] - 1);
+        const float ia = fminf(fmaxf(floorf((static_cast<float>(a[k]) - lo) / w), 0.f), top);
+        const float ib = fminf(fmaxf(floorf((static_cast<float>(b[k]) - lo) / w), 0.f), top);
+        n += static_cast<uint32_t>(fabsf(ia - ib)) + 2u;
+    }
+    return n;
+}
+
 template <class Sink>
 __device__ __forceinline__ int siddon_walk(const DevGrid& g, const double* p1, const double* p2, Sink& sink) {
     const double eps = 1.0e-6;  // :19

@@ -734,10 +734,16 @@ void prepare_poca(muto_handle* h) {
         prepare_slr(h, nt);
         return;
     }
-    DevMem walk;  // the kept rays' list for the walk kernel, and its length
+    DevMem walk, wlen, worder, owork;  // the kept rays' list for the walk kernel, its length, its order
     walk.alloc((std::max<uint64_t>(nt, 1) + 2) * sizeof(uint32_t) + sizeof(unsigned long long), &h->dev_bytes);
     a.walk_count = walk.as<unsigned long long>();
     a.walk = reinterpret_cast<uint32_t*>(walk.as<unsigned long long>() + 1);
+    wlen.alloc(std::max<uint64_t>(nt, 1) * sizeof(uint32_t), &h->dev_bytes);
+    worder.alloc(std::max<uint64_t>(nt, 1) * sizeof(uint32_t), &h->dev_bytes);
+    owork.alloc(512 * sizeof(uint32_t), &h->dev_bytes);
+    a.walk_len = wlen.as<uint32_t>();
+    a.walk_order = worder.as<uint32_t>();
+    a.order_work = owork.as<uint32_t>();
     if (!h->P.pocut) {
         run(h, "poca", [&] { launch_poca(a, h->stream); });
         run(h, "poca_normalize", [&] { launch_poca_normalize(h->img64.as<double>(), h->weight.as<double>(), V, h->P.eps, h->stream); });

@@ -48,6 +48,7 @@ __device__ __forceinline__ bool poca_bin(const DevGrid& g, const muto_ray& r, do
 __global__ void k_poca(PocaArgs a) {
     const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     bool parallel_ok = false, kept = false;
+    uint32_t wlen = 0;  // a bound on the kept ray's walk, for the walk list's order
     if (i < a.n) {
         const DevGrid g = make_dev_grid(a.g);
         const muto_ray r = a.rays[i];
@@ -55,6 +56,8 @@ __global__ void k_poca(PocaArgs a) {
         double ps[3];
         uint32_t xyz[3];
         kept = poca_bin(g, r, a.eps, zmin, zmax, ps, xyz, &parallel_ok);
+        if (kept && a.walk_len)
+            wlen = a.straight ? walk_bound(g, r.pin, r.pout) : walk_bound(g, r.pin, ps) + walk_bound(g, ps, r.pout);
         if (a.assign) {
             a.assign[3 * i + 0] = kept ? static_cast<long long>(xyz[0]) : -1;
             a.assign[3 * i + 1] = kept ? static_cast<long long>(xyz[1]) : -1;
@@ -80,9 +83,77 @@ __global__ void k_poca(PocaArgs a) {
     unsigned long long base = 0;
     if (lane == lead && b) base = atomicAdd(a.walk_count, static_cast<unsigned long long>(__popc(b)));
     base = __shfl_sync(act, base, lead);
-    if (kept) a.walk[base + __popc(b & ((1u << lane) - 1u))] = static_cast<uint32_t>(i);
+    if (kept) {
+        const uint64_t pos = base + __popc(b & ((1u << lane) - 1u));
+        a.walk[pos] = static_cast<uint32_t>(i);
+        if (a.walk_len) a.walk_len[pos] = wlen;
+    }
     warp_count(&a.ctr->not_parallel, parallel_ok);
     warp_count(&a.ctr->in_grid, kept);
+}
+
+// The listed rays by decreasing walk bound (buckets of 4 voxels), so that
+// the lanes of a warp walk paths of about the same length: block-local
+// counts, one global reservation per block and bucket, then each entry's
+// place.  The list's length is read on the device.
+constexpr int kOrderBuckets = 256;
+constexpr int kOrderPerThread = 4;
+__device__ __forceinline__ uint32_t order_bucket(uint32_t len) {
+    const uint32_t b = len >> 2;
+    return kOrderBuckets - 1 - (b < kOrderBuckets - 1 ? b : kOrderBuckets - 1);
+}
+
+__global__ void k_order_hist(const uint32_t* __restrict__ len, const unsigned long long* __restrict__ count,
+                             uint32_t* __restrict__ hist) {
+    __shared__ uint32_t cnt[kOrderBuckets];
+    const uint64_t n = *count;
+    for (int t = threadIdx.x; t < kOrderBuckets; t += blockDim.x) cnt[t] = 0;
+    __syncthreads();
+    for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        atomicAdd(&cnt[order_bucket(len[i])], 1u);
+    __syncthreads();
+    for (int t = threadIdx.x; t < kOrderBuckets; t += blockDim.x)
+        if (cnt[t]) atomicAdd(&hist[t], cnt[t]);
+}
+
+// exclusive scan of the bucket counts into cursors (one block of kOrderBuckets threads)
+__global__ void k_order_starts(const uint32_t* __restrict__ hist, uint32_t* __restrict__ cursor) {
+    __shared__ uint32_t v[kOrderBuckets];
+    const int t = threadIdx.x;
+    v[t] = hist[t];
+    __syncthreads();
+    for (int o = 1; o < kOrderBuckets; o <<= 1) {
+        const uint32_t x = t >= o ? v[t - o] : 0u;
+        __syncthreads();
+        v[t] += x;
+        __syncthreads();
+    }
+    cursor[t] = v[t] - hist[t];
+}
+
+__global__ void k_order_place(const uint32_t* __restrict__ len, const unsigned long long* __restrict__ count,
+                              uint32_t* __restrict__ cursor, uint32_t* __restrict__ order) {
+    __shared__ uint32_t cnt[kOrderBuckets], base[kOrderBuckets];
+    const uint64_t n = *count;
+    for (int t = threadIdx.x; t < kOrderBuckets; t += blockDim.x) cnt[t] = 0;
+    __syncthreads();
+    const uint64_t first = static_cast<uint64_t>(blockIdx.x) * blockDim.x * kOrderPerThread;
+    uint32_t bk[kOrderPerThread], rank[kOrderPerThread];
+#pragma unroll
+    for (int e = 0; e < kOrderPerThread; ++e) {
+        const uint64_t i = first + static_cast<uint64_t>(e) * blockDim.x + threadIdx.x;
+        bk[e] = i < n ? order_bucket(len[i]) : 0u;
+        rank[e] = i < n ? atomicAdd(&cnt[bk[e]], 1u) : 0u;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < kOrderBuckets; t += blockDim.x) base[t] = cnt[t] ? atomicAdd(&cursor[t], cnt[t]) : 0u;
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < kOrderPerThread; ++e) {
+        const uint64_t i = first + static_cast<uint64_t>(e) * blockDim.x + threadIdx.x;
+        if (i < n) order[base[bk[e]] + rank[e]] = static_cast<uint32_t>(i);
+    }
 }
 
 // The Siddon weights of the kept rays (:100-121), a thread per listed ray
@@ -96,7 +167,7 @@ __global__ void k_poca_walk(PocaArgs a) {
     const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     const unsigned lanes = walk_lanes(t < n);
     if (t < n) {
-        const muto_ray r = a.rays[a.walk[t]];
+        const muto_ray r = a.rays[a.walk[a.walk_order ? a.walk_order[t] : t]];
         double ps[3];
         uint32_t xyz[3];
         bool parallel_ok;
@@ -228,6 +299,16 @@ void launch_poca(const PocaArgs& a, cudaStream_t s) {
     cudaMemsetAsync(a.walk_count, 0, sizeof(unsigned long long), s);
     const unsigned nb = static_cast<unsigned>((a.n + 127) / 128);
     k_poca<<<nb, 128, 0, s>>>(a);
+    if (a.walk_len && a.walk_order && a.order_work) {  // the list by decreasing walk bound
+        cudaMemsetAsync(a.order_work, 0, kOrderBuckets * sizeof(uint32_t), s);
+        const uint64_t hb = (a.n + 255) / 256;
+        k_order_hist<<<static_cast<unsigned>(hb < 1024 ? hb : 1024), 256, 0, s>>>(a.walk_len, a.walk_count,
+                                                                                 a.order_work);
+        k_order_starts<<<1, kOrderBuckets, 0, s>>>(a.order_work, a.order_work + kOrderBuckets);
+        k_order_place<<<static_cast<unsigned>((a.n + 256 * kOrderPerThread - 1) / (256 * kOrderPerThread)), 256, 0,
+                        s>>>(a.walk_len, a.walk_count, a.order_work + kOrderBuckets, a.walk_order);
+        count_launches(3);
+    }
     k_poca_walk<<<nb, 128, 0, s>>>(a);  // one thread per ray that can have been kept
     count_launches(2);
 }

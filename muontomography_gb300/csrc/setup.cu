@@ -182,21 +182,6 @@ __global__ void k_path_fill(const muto_ray* __restrict__ rays, const uint32_t* _
     }
 }
 
-// voxels a walk of a -> b can record: 1 + the index span on each axis of
-// the endpoints clamped to the grid (the pieces on the grid lie between
-// them), +2 per axis for rounding at either end
-__device__ __forceinline__ uint32_t walk_bound(const DevGrid& g, const double* a, const double* b) {
-    uint32_t n = 1;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float lo = static_cast<float>(g.lo[k]), w = static_cast<float>(g.w[k]);
-        const float top = static_cast<float>(g.n[k] - 1);
-        const float ia = fminf(fmaxf(floorf((static_cast<float>(a[k]) - lo) / w), 0.f), top);
-        const float ib = fminf(fmaxf(floorf((static_cast<float>(b[k]) - lo) / w), 0.f), top);
-        n += static_cast<uint32_t>(fabsf(ia - ib)) + 2u;
-    }
-    return n;
-}
 
 __global__ void k_path_bound(const muto_ray* __restrict__ rays, const uint32_t* __restrict__ kept,
                              const double* __restrict__ scat, uint64_t n, DevGrid g, int straight,
