@@ -168,6 +168,11 @@ struct PocaArgs {
     double* value;      // PoCut: per ray its value (angle^2, times p^2 with momentum)
 };
 void launch_poca(const PocaArgs& a, cudaStream_t s);
+// order[0..n) = the entries 0..n-1 by decreasing len[] (buckets of 4; any
+// order inside a bucket); n is *count when count is given (at most n
+// entries), else n; work: 512 uint32 of scratch
+void launch_length_order(const uint32_t* len, const unsigned long long* count, uint64_t n, uint32_t* order,
+                         uint32_t* work, cudaStream_t s);
 void launch_poca_normalize(double* img, const double* weight, uint64_t V, double eps, cudaStream_t s);
 // slr.cu: straight-line reconstruction (src/MutoSLR.cpp:47-103) and the
 // iterative form's passes (src/MutoSLRIter.cpp:15-83)
@@ -401,6 +406,7 @@ struct FusedArgs {
     const uint32_t* kept;
     const double* scat;                       // 3N PoCA points
     const double* ltot;                       // N in-grid path lengths (-1: dropped walk)
+    const uint32_t* order;                    // N (or null): the muons in the order their walks run
     DevGrid g;
     int straight;
     BrickDims bdims;

@@ -575,8 +575,10 @@ __global__ void __launch_bounds__(128) k_em_fused_walk(FusedArgs<Real> a) {
     unsigned long long singular_local = 0;
     const VoxelIndexer ix{a.g.n[0], a.g.n[0] * a.g.n[1], a.bdims, a.brick};
     const uint64_t keep = l2_keep_policy();
-    // a thread per muon (not a grid-stride loop, whose lanes would drift out of step)
-    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    // a thread per muon (not a grid-stride loop, whose lanes would drift out
+    // of step), the muons in a.order (by decreasing path bound) when given
+    const uint64_t t = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const uint64_t i = (a.order && t < a.N) ? a.order[t] : t;
     // (ltot < 0: a walk the set-up dropped at its step bound: no pairs)
     const double ltot = i < a.N ? a.ltot[i] : -1.0;
     const unsigned lanes = walk_lanes(ltot >= 0.0);

@@ -405,6 +405,7 @@ struct muto_handle {
     uint32_t slr_levels = 0;          // levels of the SLRIter schedule (0: none or sequential)
     uint64_t vclass_off[kVoxClasses] = {};
     DevMem kslot;                     // per kept muon: its row of kvec (empty: its own index)
+    DevMem walk_order;                // recompute form: the kept muons by decreasing path bound
     DevMem mult, start, kvec, keys;   // keys: the voxel pass's order key of every pair
     DevMem win;                       // per voxel: the last selection window (center, half-width)
     int lists = kListsVoxelMajor;     // how the pair lists are kept (Lists)
@@ -1074,6 +1075,21 @@ void prepare_em(muto_handle* h) {
             launch_path_stats(h->scan_rays(0), h->kept.as<uint32_t>(), h->scat.as<double>(), sc.N, sc.grid,
                               P.straight_line, h->ltot.as<double>(), h->mult.as<uint32_t>(), h->ctr(), s);
         });
+        // the walks of every iteration run in order of decreasing path bound,
+        // so that a warp's lanes walk paths of about the same length
+        {
+            DevMem bounds, work;
+            bounds.alloc(std::max<uint64_t>(N, 1) * sizeof(uint32_t), &h->dev_bytes);
+            work.alloc(512 * sizeof(uint32_t), &h->dev_bytes);
+            h->walk_order.alloc(std::max<uint64_t>(N, 1) * sizeof(uint32_t), &h->dev_bytes);
+            run(h, "path_order", [&] {
+                launch_path_bound(h->scan_rays(0), h->kept.as<uint32_t>(), h->scat.as<double>(), sc.N, sc.grid,
+                                  P.straight_line, bounds.as<uint32_t>(), s);
+                launch_length_order(bounds.as<uint32_t>(), nullptr, N, h->walk_order.as<uint32_t>(),
+                                    work.as<uint32_t>(), s);
+            });
+            CK(cudaStreamSynchronize(s));  // the bounds go out of scope
+        }
         DevMem moff;
         moff.alloc((V + 1) * sizeof(uint64_t), &h->dev_bytes);
         run(h, "scan", [&] { scan_u32_to_u64(h->mult.as<uint32_t>(), moff.as<uint64_t>(), V, scratch.as<void>(), s); });
@@ -1417,6 +1433,7 @@ void launch_fused_pass(muto_handle* h, const Real* lam, bool cost, cudaStream_t 
         a.straight = P.straight_line ? 1 : 0;
         a.bdims = h->bdims;
         a.brick = h->brick ? 1 : 0;
+        a.order = h->walk_order.empty() ? nullptr : h->walk_order.as<uint32_t>();
         launch("em_walk", [&] { launch_em_fused_walk<Real>(a, h->num_sms, s); });
     } else {
         launch("em_fused", [&] { launch_em_fused<Real>(a, h->fused_variant, h->fused_blocks, s); });

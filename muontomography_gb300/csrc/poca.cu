@@ -92,10 +92,10 @@ __global__ void k_poca(PocaArgs a) {
     warp_count(&a.ctr->in_grid, kept);
 }
 
-// The listed rays by decreasing walk bound (buckets of 4 voxels), so that
-// the lanes of a warp walk paths of about the same length: block-local
-// counts, one global reservation per block and bucket, then each entry's
-// place.  The list's length is read on the device.
+// Entries by decreasing walk bound (buckets of 4 voxels), so that the lanes
+// of a warp walk paths of about the same length: block-local counts, one
+// global reservation per block and bucket, then each entry's place.  The
+// number of entries is read on the device (count) or given (n_fixed).
 constexpr int kOrderBuckets = 256;
 constexpr int kOrderPerThread = 4;
 __device__ __forceinline__ uint32_t order_bucket(uint32_t len) {
@@ -104,9 +104,9 @@ __device__ __forceinline__ uint32_t order_bucket(uint32_t len) {
 }
 
 __global__ void k_order_hist(const uint32_t* __restrict__ len, const unsigned long long* __restrict__ count,
-                             uint32_t* __restrict__ hist) {
+                             uint64_t n_fixed, uint32_t* __restrict__ hist) {
     __shared__ uint32_t cnt[kOrderBuckets];
-    const uint64_t n = *count;
+    const uint64_t n = count ? *count : n_fixed;
     for (int t = threadIdx.x; t < kOrderBuckets; t += blockDim.x) cnt[t] = 0;
     __syncthreads();
     for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
@@ -133,9 +133,9 @@ __global__ void k_order_starts(const uint32_t* __restrict__ hist, uint32_t* __re
 }
 
 __global__ void k_order_place(const uint32_t* __restrict__ len, const unsigned long long* __restrict__ count,
-                              uint32_t* __restrict__ cursor, uint32_t* __restrict__ order) {
+                              uint64_t n_fixed, uint32_t* __restrict__ cursor, uint32_t* __restrict__ order) {
     __shared__ uint32_t cnt[kOrderBuckets], base[kOrderBuckets];
-    const uint64_t n = *count;
+    const uint64_t n = count ? *count : n_fixed;
     for (int t = threadIdx.x; t < kOrderBuckets; t += blockDim.x) cnt[t] = 0;
     __syncthreads();
     const uint64_t first = static_cast<uint64_t>(blockIdx.x) * blockDim.x * kOrderPerThread;
@@ -294,21 +294,25 @@ __global__ void k_poca_normalize(double* __restrict__ img, const double* __restr
 
 }  // namespace
 
+void launch_length_order(const uint32_t* len, const unsigned long long* count, uint64_t n, uint32_t* order,
+                         uint32_t* work, cudaStream_t s) {
+    if (n == 0) return;
+    (void)cudaMemsetAsync(work, 0, kOrderBuckets * sizeof(uint32_t), s);  // an error surfaces at the caller's check
+    const uint64_t hb = (n + 255) / 256;
+    k_order_hist<<<static_cast<unsigned>(hb < 1024 ? hb : 1024), 256, 0, s>>>(len, count, n, work);
+    k_order_starts<<<1, kOrderBuckets, 0, s>>>(work, work + kOrderBuckets);
+    k_order_place<<<static_cast<unsigned>((n + 256 * kOrderPerThread - 1) / (256 * kOrderPerThread)), 256, 0, s>>>(
+        len, count, n, work + kOrderBuckets, order);
+    count_launches(3);
+}
+
 void launch_poca(const PocaArgs& a, cudaStream_t s) {
     if (a.n == 0) return;
     cudaMemsetAsync(a.walk_count, 0, sizeof(unsigned long long), s);
     const unsigned nb = static_cast<unsigned>((a.n + 127) / 128);
     k_poca<<<nb, 128, 0, s>>>(a);
-    if (a.walk_len && a.walk_order && a.order_work) {  // the list by decreasing walk bound
-        cudaMemsetAsync(a.order_work, 0, kOrderBuckets * sizeof(uint32_t), s);
-        const uint64_t hb = (a.n + 255) / 256;
-        k_order_hist<<<static_cast<unsigned>(hb < 1024 ? hb : 1024), 256, 0, s>>>(a.walk_len, a.walk_count,
-                                                                                 a.order_work);
-        k_order_starts<<<1, kOrderBuckets, 0, s>>>(a.order_work, a.order_work + kOrderBuckets);
-        k_order_place<<<static_cast<unsigned>((a.n + 256 * kOrderPerThread - 1) / (256 * kOrderPerThread)), 256, 0,
-                        s>>>(a.walk_len, a.walk_count, a.order_work + kOrderBuckets, a.walk_order);
-        count_launches(3);
-    }
+    if (a.walk_len && a.walk_order && a.order_work)  // the list by decreasing walk bound
+        launch_length_order(a.walk_len, a.walk_count, a.n, a.walk_order, a.order_work, s);
     k_poca_walk<<<nb, 128, 0, s>>>(a);  // one thread per ray that can have been kept
     count_launches(2);
 }
