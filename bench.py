@@ -597,6 +597,8 @@ def run_ours(args) -> int:
                 "algorithmic_bytes": pb, "achieved": pb / (t_poca / 1000.0) / 1e9,
                 "frac": pb / (t_poca / 1000.0) / 1e9 / pk["hbm_gbs"], "peak": pk["hbm_gbs"],
                 "in_grid": pst["n_scat_in_grid"],
+                "bound": "the FP64 pipe, not HBM: the frac above is by bytes only (ncu: "
+                         "profiles/poca_walk_grid256x256x128_10mm_2M.md)",
                 "what": "k_poca: FP64 closest approach, binning and the length-weighted Siddon weights of every "
                         "track (FP64 atomics, a thread per kept track), then the normalisation"}
 
