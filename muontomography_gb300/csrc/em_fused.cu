@@ -1,5 +1,5 @@
-// Mean-update EM iteration in one pass over the muon-major lists
-// (update_with_mean with mean_percentile 100, src/MutoMLSD.cpp:497-499).
+// Mean-update EM iteration over the muon-major lists (update_with_mean with
+// mean_percentile 100, src/MutoMLSD.cpp:497-499).
 //
 // The mean of s_ij = 2 l_j + g_ij l_j^2 over the M_j pairs of voxel j is
 //     mean_j / 2 = l_j + l_j^2 G_j / (2 M_j),      G_j = sum_i g_ij,
@@ -20,21 +20,25 @@
 // instruction per 32 muons); finally every lane forms g_ij for the pairs it
 // holds and adds them to G_j.  Pairs beyond the RC held per lane are read a
 // second time, from L1 or L2: RC is kept small so that several CTAs (several
-// batches) are resident on an SM and the batches' latencies overlap.
+// batches) are resident on an SM and the batches' latencies overlap.  The
+// staged variant (k_em_staged, run when asked for) copies a batch's whole
+// pair range into shared memory instead.
 //
 // Split form (launch_em_scatter).  The muon pass of the median path
 // (em_muon.cu: warp-batched, no block barriers, its FP64 2x2 algebra a muon
 // per lane) writes every muon's coefficients; a second pass streams the lists
-// again and only adds g_ij to G_j.  Twice the list traffic from HBM, but
-// neither pass waits at a block barrier; the autotuner times it beside the
-// one-pass variants.
+// again and only adds g_ij to G_j, 4 or 8 pairs in flight per lane.  Twice
+// the list traffic from HBM, but neither pass waits at a block barrier; the
+// autotuner times it beside the one-pass variants, and on the largest scans
+// it is the one picked.
 //
 // Recompute pass (k_em_fused_walk).  The same sums without stored lists: a
-// thread per muon (one muon each, so that a warp's lanes walk in step) walks
-// its merged path in FP64 (the bit-exact Siddon walk
-// of the set-up) once to sum Sigma, does the 2x2 algebra (a muon per lane),
-// and walks it again to add g_ij to G_j.  T_ij comes from the muon's total
-// in-grid length (kept per muon at set-up) minus the running length.
+// thread per muon (one muon each, so that a warp's lanes walk in step; the
+// muons in order of decreasing path bound) walks its merged path in FP64 (the
+// bit-exact Siddon walk of the set-up) once to sum Sigma, does the 2x2
+// algebra (a muon per lane), and walks it again to add g_ij to G_j.  T_ij
+// comes from the muon's total in-grid length (kept per muon at set-up) minus
+// the running length.
 #include "common.cuh"
 
 namespace muto {
