@@ -35,7 +35,8 @@ struct WeightSink {
 // and voxel); kept rays are appended to a.walk (warp-aggregated) for the
 // walk kernel, so that the FP64 walks run on full warps (a warp of rays
 // usually keeps fewer than half of them, and an FP64 instruction takes the
-// same pipe time however few of its lanes are active).
+// same pipe time however few of its lanes are active), with a bound on each
+// walk by which the list is then ordered (a warp's walks of similar length).
 __device__ __forceinline__ bool poca_bin(const DevGrid& g, const muto_ray& r, double eps, double zmin, double zmax,
                                          double* ps, uint32_t* xyz, bool* parallel_ok) {
     *parallel_ok = poca_point(r, eps, ps);
