@@ -51,29 +51,25 @@ struct Error : std::runtime_error {
 // mapped, so the next handle (the next scan) reuses them instead of paying
 // for new mappings; the pool grows to the largest working set seen.  Frees
 // keep cudaFree's ordering: they wait for the device to be idle first.
-// Two pools per device: kind 0 for everything else, kind 1 for the loaded
-// tracks alone, so that a new handle's track buffer takes the block an
-// earlier track buffer left, not one of the blocks the lists used.
-cudaMemPool_t device_pool(int dev, int kind = 0) {
+cudaMemPool_t device_pool(int dev) {
     constexpr int kMaxDevices = 64;
-    static std::once_flag once[kMaxDevices][2];
-    static cudaMemPool_t pools[kMaxDevices][2];
-    static cudaError_t errs[kMaxDevices][2];
+    static std::once_flag once[kMaxDevices];
+    static cudaMemPool_t pools[kMaxDevices];
+    static cudaError_t errs[kMaxDevices];
     if (dev < 0 || dev >= kMaxDevices) throw Error(MUTO_ERR_CUDA, "device ordinal out of range");
-    kind = kind ? 1 : 0;
-    std::call_once(once[dev][kind], [dev, kind] {
+    std::call_once(once[dev], [dev] {
         cudaMemPoolProps props{};
         props.allocType = cudaMemAllocationTypePinned;
         props.location.type = cudaMemLocationTypeDevice;
         props.location.id = dev;
-        errs[dev][kind] = cudaMemPoolCreate(&pools[dev][kind], &props);
-        if (errs[dev][kind] == cudaSuccess) {
+        errs[dev] = cudaMemPoolCreate(&pools[dev], &props);
+        if (errs[dev] == cudaSuccess) {
             unsigned long long keep = ~0ull;
-            errs[dev][kind] = cudaMemPoolSetAttribute(pools[dev][kind], cudaMemPoolAttrReleaseThreshold, &keep);
+            errs[dev] = cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
         }
     });
-    CK(errs[dev][kind]);
-    return pools[dev][kind];
+    CK(errs[dev]);
+    return pools[dev];
 }
 
 // Owned device allocation.
@@ -83,12 +79,12 @@ public:
     DevMem(const DevMem&) = delete;
     DevMem& operator=(const DevMem&) = delete;
     ~DevMem() { release(); }
-    void alloc(size_t bytes, std::atomic<uint64_t>* tally, int pool_kind = 0) {
+    void alloc(size_t bytes, std::atomic<uint64_t>* tally) {
         release();
         if (bytes == 0) bytes = 16;
         int dev = 0;
         CK(cudaGetDevice(&dev));
-        CK(cudaMallocFromPoolAsync(&p_, bytes, device_pool(dev, pool_kind), 0));
+        CK(cudaMallocFromPoolAsync(&p_, bytes, device_pool(dev), 0));
         CK(cudaStreamSynchronize(0));  // usable from any stream once this returns
         bytes_ = bytes;
         tally_ = tally;
@@ -2188,7 +2184,7 @@ int muto_load_tracks(muto_handle* h, const muto_ray* rays, uint64_t n, int on_de
         h->n_rays = n;
         {
             HostPhase ph(h, "load_alloc");
-            h->rays.alloc(std::max<uint64_t>(n, 1) * sizeof(muto_ray), &h->dev_bytes, 1);
+            h->rays.alloc(std::max<uint64_t>(n, 1) * sizeof(muto_ray), &h->dev_bytes);
         }
         HostPhase ph(h, "load_copy");
         if (n > 0)
@@ -2573,7 +2569,7 @@ int muto_batch_load_tracks(muto_handle* h, uint32_t scan, const muto_ray* rays, 
         h->prepared = false;
         auto& slot = h->batch_rays[scan - 1];
         slot.reset(new DevMem());
-        slot->alloc(std::max<uint64_t>(n, 1) * sizeof(muto_ray), &h->dev_bytes, 1);
+        slot->alloc(std::max<uint64_t>(n, 1) * sizeof(muto_ray), &h->dev_bytes);
         if (n > 0)
             CK(cudaMemcpyAsync(slot->as<void>(), rays, n * sizeof(muto_ray),
                                on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
