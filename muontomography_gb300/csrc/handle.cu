@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/muto_gb300.h"
+#include "slr_levels.h"
 #include "common.cuh"
 #include "gen.h"
 #include "json.hpp"
@@ -582,14 +583,9 @@ void alloc_counters(muto_handle* h) {
 // SLR (src/MutoSLR.cpp:47-103) and SLRIter (src/MutoSLRIter.cpp:15-83): the
 // first pass over every ray at once; the iterative form's later passes, in
 // place and in muon order, over the walked straight lines kept on the device
-// The level schedule of SLRIter's later passes (src/MutoSLRIter.cpp:40-71),
-// made once from the walked paths, which do not change between passes: muon
-// i's level is one more than the highest level that an earlier muon left on
-// any voxel of i's path.  A voxel's muons then have strictly increasing
-// levels in index order, and muons of one level share no voxel.  One ordered
-// sweep over the pairs on the host (the recurrence is sequential in i); the
-// muons are then grouped by level (index order inside a level) for the
-// device.
+// The level schedule of SLRIter's later passes (slr_levels.h), made once
+// from the walked paths, which do not change between passes; the muons are
+// then grouped by level (index order inside a level) for the device.
 void slr_level_schedule(muto_handle* h, const DevMem& off, const DevMem& vox, uint64_t nt, uint64_t np, DevMem& order,
                         DevMem& lstart, DevMem& fo) {
     const uint64_t V = h->V();
@@ -600,18 +596,8 @@ void slr_level_schedule(muto_handle* h, const DevMem& off, const DevMem& vox, ui
     CK(cudaMemcpyAsync(off_h.data(), off.as<uint64_t>(), (nt + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
     if (np > 0) CK(cudaMemcpyAsync(vox_h.data(), vox.as<uint32_t>(), np * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    std::vector<uint32_t> last(V, 0), level(nt);
-    uint32_t levels = 0;
-    for (uint64_t i = 0; i < nt; ++i) {
-        uint32_t lv = 0;
-        for (uint64_t k = off_h[i]; k < off_h[i + 1]; ++k)
-            if (vox_h[k] < V) lv = std::max(lv, last[vox_h[k]]);
-        ++lv;
-        for (uint64_t k = off_h[i]; k < off_h[i + 1]; ++k)
-            if (vox_h[k] < V) last[vox_h[k]] = lv;
-        level[i] = lv;
-        levels = std::max(levels, lv);
-    }
+    std::vector<uint32_t> level(nt);
+    const uint32_t levels = slr_levels(off_h.data(), vox_h.data(), nt, V, level.data());
     std::vector<uint32_t> start(static_cast<size_t>(levels) + 1, 0), order_h(nt);
     for (uint64_t i = 0; i < nt; ++i) ++start[level[i]];  // level l (1-based) counted at start[l]
     uint32_t acc = 0;
