@@ -4,6 +4,7 @@ replacement) running the reconstruction classes on the GPU."""
 import ctypes as C
 import json
 import re
+import shutil
 import subprocess
 from pathlib import Path
 
@@ -265,6 +266,43 @@ def test_user_program_compiles_against_the_headers(facade, tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
     assert r.returncode == 0, r.stderr
     assert r.stdout.split("\n")[:3] == ["0", str(tmp_path), "0"]
+
+
+NLOHMANN_STYLE = r"""
+#include <cstdio>
+#include <string>
+#include <vector>
+#include "MutoConfig.h"
+int main() {
+    MutoConfig cfg;
+    if (!cfg.loadString("{\"detector_middle\": 3, \"detector_height\": [1500.5, -1500],"
+                        " \"output_file\": \"out.bin\", \"mlsd\": {\"early_stop\": true, \"eps\": 1e-8}}"))
+        return 2;
+    // the reference's driver reads its configuration this way (nlohmann's implicit conversions)
+    int middle = cfg.get("detector_middle");
+    std::vector<double> zs = cfg.get("detector_height");
+    std::string out = cfg.get("output_file");
+    bool stop = cfg.get("mlsd")["early_stop"];
+    double eps = cfg.get("mlsd")["eps"];
+    std::printf("%d %zu %.1f %.1f %s %d %.0e\n", middle, zs.size(), zs[0], zs[1], out.c_str(), stop ? 1 : 0, eps);
+    return 0;
+}
+"""
+
+
+def test_configuration_reads_like_nlohmann_json(tmp_path):
+    # the implicit conversions a driver written for nlohmann::json relies on
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    root = B.facade_lib_path().parent.parent
+    src = tmp_path / "cfg.cpp"
+    src.write_text(NLOHMANN_STYLE)
+    exe = tmp_path / "cfg"
+    subprocess.run(["g++", "-std=c++17", "-I", str(root / "cpp"), "-I", str(root / "csrc"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True, timeout=120)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.split() == ["3", "2", "1500.5", "-1500.0", "out.bin", "1", "1e-08"]
 
 
 def test_fit_tracks_host_checks():
