@@ -178,3 +178,25 @@ def test_reference_arm_loads_no_product_library():
     assert out.returncode == 0, out.stderr[-2000:]
     libs = [ln for ln in out.stdout.splitlines() if ln.startswith("LIBS")][0]
     assert "libmuto_oracle.so" in libs and "libmuto_gb300" not in libs and "libmuto_facade" not in libs
+
+
+@pytest.mark.parametrize("name", ["muto_grid", "muto_status", "muto_block", "muto_gen_params"])
+def test_ctypes_structs_match_the_c_header(tmp_path, name):
+    # the Python bindings' structures have the C header's size and field offsets
+    import shutil
+    import subprocess
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no gcc")
+    st = getattr(_lib, name)
+    fields = [f for f, _ in st._fields_]
+    body = "\n".join(f'    printf("%zu\\n", offsetof({name}, {f}));' for f in fields)
+    src = tmp_path / "layout.c"
+    src.write_text(f"#include <stddef.h>\n#include <stdio.h>\n#include \"muto_gb300.h\"\n"
+                   f"int main(void) {{\n    printf(\"%zu\\n\", sizeof({name}));\n{body}\n    return 0;\n}}\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", str(_lib.header_path().parent), str(src), "-o", str(exe)], check=True,
+                   capture_output=True, timeout=120)
+    out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert out[0] == C.sizeof(st)
+    assert out[1:] == [getattr(st, f).offset for f in fields]
