@@ -200,3 +200,22 @@ def test_ctypes_structs_match_the_c_header(tmp_path, name):
     out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert out[0] == C.sizeof(st)
     assert out[1:] == [getattr(st, f).offset for f in fields]
+
+
+def test_batch64_workload_matches_its_description():
+    # 64 scans, cubic grids of 32..128 voxels of 20 mm, 50 k..5 M muons each,
+    # seeded: the same scans every time
+    from muontomography_gb300 import workloads as W
+
+    wls = W.batch64()
+    assert len(wls) == 64
+    assert {w.grid.nx for w in wls} <= {32, 64, 96, 128}
+    assert all(w.grid.nx == w.grid.ny == w.grid.nz and w.grid.dx == 20.0 for w in wls)
+    counts = np.array([w.n_muons for w in wls])
+    assert counts.min() >= 50_000 and counts.max() <= 5_000_000
+    assert 40e6 < counts.sum() < 100e6
+    again = W.batch64()
+    assert [w.n_muons for w in again] == list(counts) and [w.grid for w in again] == [w.grid for w in wls]
+    assert len({w.seed for w in wls}) == 64
+    small = W.batch64(scale=0.01)  # the GPU test's 1/100 of the muons, at least 1 000 a scan
+    assert all(1000 <= s.n_muons <= max(1000, 0.01 * w.n_muons + 1) for s, w in zip(small, wls))
